@@ -1,0 +1,32 @@
+// Bordered-system helper kernels (border_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace rskel {
+
+template <class Real>
+void masked_cross(const Real* A, int lda, int na, const Real* B, int ldb, int nb,
+                  const unsigned char* mask, int D, double* out, int ldo, cudaStream_t st);
+template <class Real>
+void assemble_s(Real* S, int ns, int nb, const Real* root, const Real* mU, const Real* mP, int D,
+                const int* allskel, const double* G, cudaStream_t st);
+template <class Real>
+void border_rhs(Real* M, int ns, int nb, const Real* x, const int* allskel, const double* g1,
+                cudaStream_t st);
+template <class Real>
+void border_sub(Real* nv, const Real* x, const Real* mU, int D, int nb, const Real* alpha,
+                const unsigned char* red_mask, cudaStream_t st);
+template <class Real>
+void border_merge(Real* x, const Real* nv, const unsigned char* red_mask, int D, const int* allskel,
+                  const Real* y, int ns, cudaStream_t st);
+template <class Real>
+void transpose_to(const double* in, int rows, int cols, Real* out, cudaStream_t st);
+template <class Real>
+void convert_from_double(const double* in, Real* out, size_t n, cudaStream_t st);
+template <class Real>
+void convert_to_double(const Real* in, double* out, size_t n, cudaStream_t st);
+
+}  // namespace rskel

@@ -1,0 +1,192 @@
+// Kernels of the bordered (multiply connected) system, restating
+// SkelFactorization::skeletonize :188-305 and multiply_connected_solve
+// :596-777 (ie_solver/skel_factorization/skel_factorization.cpp).  The
+// redundant / skeleton partition is carried as a per-DOF mask instead of the
+// reference's gathered index maps.
+#include "border.hpp"
+#include "common.cuh"
+
+namespace rskel {
+
+// out(i, j) = sum_l mask[l] * A[l, i] * B[l, j]  (A: D x na, B: D x nb).
+template <class Real>
+__global__ void __launch_bounds__(256) masked_cross_kernel(const Real* A, int lda, int na,
+                                                           const Real* B, int ldb, int nb,
+                                                           const unsigned char* mask, int D,
+                                                           double* out, int ldo) {
+  const int i = blockIdx.x;
+  const int j0 = blockIdx.y * 8;
+  double acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+  for (int l = threadIdx.x; l < D; l += blockDim.x) {
+    if (!mask[l]) continue;
+    const double a = (double)A[l + (size_t)lda * i];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (j0 + q < nb) acc[q] += a * (double)B[l + (size_t)ldb * (j0 + q)];
+  }
+  __shared__ double red[8][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    double v = warp_sum(acc[q]);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 8 && j0 + threadIdx.x < nb) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+    out[i + (size_t)ldo * (j0 + threadIdx.x)] = s;
+  }
+}
+
+template <class Real>
+void masked_cross(const Real* A, int lda, int na, const Real* B, int ldb, int nb,
+                  const unsigned char* mask, int D, double* out, int ldo, cudaStream_t st) {
+  if (na <= 0 || nb <= 0) return;
+  dim3 grid(na, (nb + 7) / 8);
+  masked_cross_kernel<Real><<<grid, 256, 0, st>>>(A, lda, na, B, ldb, nb, mask, D, out, ldo);
+}
+template void masked_cross<double>(const double*, int, int, const double*, int, int,
+                                   const unsigned char*, int, double*, int, cudaStream_t);
+template void masked_cross<float>(const float*, int, int, const float*, int, int,
+                                  const unsigned char*, int, double*, int, cudaStream_t);
+
+// S = [Ktilde_root, mU(allskel, :); mP(allskel, :)^T, -I - G], SN = ns + nb.
+template <class Real>
+__global__ void assemble_s_kernel(Real* S, int ns, int nb, const Real* root, const Real* mU,
+                                  const Real* mP, int D, const int* allskel, const double* G) {
+  const int SN = ns + nb;
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)SN * SN) return;
+  const int i = (int)(e % SN), j = (int)(e / SN);
+  Real v;
+  if (i < ns && j < ns) v = root[i + (size_t)ns * j];
+  else if (i < ns) v = mU[allskel[i] + (size_t)D * (j - ns)];
+  else if (j < ns) v = mP[allskel[j] + (size_t)D * (i - ns)];
+  else v = (Real)((i == j ? -1.0 : 0.0) - G[(i - ns) + (size_t)nb * (j - ns)]);
+  S[e] = v;
+}
+
+template <class Real>
+void assemble_s(Real* S, int ns, int nb, const Real* root, const Real* mU, const Real* mP, int D,
+                const int* allskel, const double* G, cudaStream_t st) {
+  size_t tot = (size_t)(ns + nb) * (ns + nb);
+  assemble_s_kernel<Real><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(S, ns, nb, root, mU, mP,
+                                                                         D, allskel, G);
+}
+template void assemble_s<double>(double*, int, int, const double*, const double*, const double*,
+                                 int, const int*, const double*, cudaStream_t);
+template void assemble_s<float>(float*, int, int, const float*, const float*, const float*, int,
+                                const int*, const double*, cudaStream_t);
+
+// M[0:ns] = x[allskel]; M[ns + i] = -G1[i]  (G1 = masked_cross(mP, Dw))
+template <class Real>
+__global__ void border_rhs_kernel(Real* M, int ns, int nb, const Real* x, const int* allskel,
+                                  const double* g1) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ns) M[i] = x[allskel[i]];
+  else if (i < ns + nb) M[i] = (Real)(-g1[i - ns]);
+}
+
+template <class Real>
+void border_rhs(Real* M, int ns, int nb, const Real* x, const int* allskel, const double* g1,
+                cudaStream_t st) {
+  int tot = ns + nb;
+  if (tot > 0) border_rhs_kernel<Real><<<(tot + 255) / 256, 256, 0, st>>>(M, ns, nb, x, allskel, g1);
+}
+template void border_rhs<double>(double*, int, int, const double*, const int*, const double*,
+                                 cudaStream_t);
+template void border_rhs<float>(float*, int, int, const float*, const int*, const double*,
+                                cudaStream_t);
+
+// For redundant l: nv[l] = x[l] - sum_j mU[l, j] alpha[j]; skeleton rows copy x.
+template <class Real>
+__global__ void border_sub_kernel(Real* nv, const Real* x, const Real* mU, int D, int nb,
+                                  const Real* alpha, const unsigned char* red_mask) {
+  size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (l >= (size_t)D) return;
+  Real v = x[l];
+  if (red_mask[l]) {
+    double acc = 0.0;
+    for (int j = 0; j < nb; ++j) acc += (double)mU[l + (size_t)D * j] * (double)alpha[j];
+    v = (Real)((double)v - acc);
+  }
+  nv[l] = v;
+}
+
+template <class Real>
+void border_sub(Real* nv, const Real* x, const Real* mU, int D, int nb, const Real* alpha,
+                const unsigned char* red_mask, cudaStream_t st) {
+  if (D > 0)
+    border_sub_kernel<Real><<<(D + 255) / 256, 256, 0, st>>>(nv, x, mU, D, nb, alpha, red_mask);
+}
+template void border_sub<double>(double*, const double*, const double*, int, int, const double*,
+                                 const unsigned char*, cudaStream_t);
+template void border_sub<float>(float*, const float*, const float*, int, int, const float*,
+                                const unsigned char*, cudaStream_t);
+
+// x[l] = red ? nv[l] : x[l]; then x[allskel[i]] = y[i].
+template <class Real>
+__global__ void border_merge_kernel(Real* x, const Real* nv, const unsigned char* red_mask, int D) {
+  size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (l < (size_t)D && red_mask[l]) x[l] = nv[l];
+}
+template <class Real>
+__global__ void scatter_kernel(Real* x, const int* idx, const Real* y, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[idx[i]] = y[i];
+}
+
+template <class Real>
+void border_merge(Real* x, const Real* nv, const unsigned char* red_mask, int D, const int* allskel,
+                  const Real* y, int ns, cudaStream_t st) {
+  if (D > 0) border_merge_kernel<Real><<<(D + 255) / 256, 256, 0, st>>>(x, nv, red_mask, D);
+  if (ns > 0) scatter_kernel<Real><<<(ns + 255) / 256, 256, 0, st>>>(x, allskel, y, ns);
+}
+template void border_merge<double>(double*, const double*, const unsigned char*, int, const int*,
+                                   const double*, int, cudaStream_t);
+template void border_merge<float>(float*, const float*, const unsigned char*, int, const int*,
+                                  const float*, int, cudaStream_t);
+
+template <class Real>
+__global__ void transpose_kernel(const double* in, int rows, int cols, Real* out) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)rows * cols) return;
+  int i = (int)(e % rows), j = (int)(e / rows);
+  out[j + (size_t)cols * i] = (Real)in[e];
+}
+template <class Real>
+void transpose_to(const double* in, int rows, int cols, Real* out, cudaStream_t st) {
+  size_t tot = (size_t)rows * cols;
+  if (tot) transpose_kernel<Real><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(in, rows, cols, out);
+}
+template void transpose_to<double>(const double*, int, int, double*, cudaStream_t);
+template void transpose_to<float>(const double*, int, int, float*, cudaStream_t);
+
+template <class Real>
+__global__ void convert_kernel(const double* in, Real* out, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (Real)in[i];
+}
+template <class Real>
+void convert_from_double(const double* in, Real* out, size_t n, cudaStream_t st) {
+  if (n) convert_kernel<Real><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+}
+template void convert_from_double<double>(const double*, double*, size_t, cudaStream_t);
+template void convert_from_double<float>(const double*, float*, size_t, cudaStream_t);
+
+template <class Real>
+__global__ void to_double_kernel(const Real* in, double* out, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+template <class Real>
+void convert_to_double(const Real* in, double* out, size_t n, cudaStream_t st) {
+  if (n) to_double_kernel<Real><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+}
+template void convert_to_double<double>(const double*, double*, size_t, cudaStream_t);
+template void convert_to_double<float>(const float*, double*, size_t, cudaStream_t);
+
+}  // namespace rskel

@@ -1,0 +1,152 @@
+// Device helpers shared by the factorization and solve kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "plan.hpp"
+
+namespace rskel {
+
+constexpr int kThreads = 256;              // threads per box (8 warps)
+constexpr int kWarps = kThreads / 32;
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide argmax of val over [lo, hi) (ties -> smallest index), result in
+// *out_idx for every thread.  scratch needs 2 * kWarps entries.
+__device__ __forceinline__ int block_argmax(const double* val, int lo, int hi, double* sv,
+                                            int* si) {
+  double best = -1.0;
+  int bi = hi;
+  for (int c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+    double v = val[c];
+    if (v > best || (v == best && c < bi)) { best = v; bi = c; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_xor_sync(0xffffffffu, best, o);
+    int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sv[warp] = best; si[warp] = bi; }
+  __syncthreads();
+  if (warp == 0) {
+    int nw = blockDim.x >> 5;
+    best = lane < nw ? sv[lane] : -1.0;
+    bi = lane < nw ? si[lane] : hi;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (lane == 0) si[0] = bi;
+  }
+  __syncthreads();
+  int r = si[0];
+  __syncthreads();
+  return r;
+}
+
+// Per-DOF boundary data staged in shared memory (structure of arrays).
+template <class Real>
+struct DofSoA {
+  Real *x, *y, *nx, *ny, *w, *kap;
+  int* comp;
+};
+
+template <class Real>
+__device__ __forceinline__ Real* carve(unsigned char*& p, int count) {
+  Real* r = reinterpret_cast<Real*>(p);
+  size_t bytes = sizeof(Real) * (size_t)count;
+  p += (bytes + 15) & ~size_t(15);
+  return r;
+}
+
+template <class Real>
+__device__ __forceinline__ DofSoA<Real> carve_dofs(unsigned char*& p, int count) {
+  DofSoA<Real> d;
+  d.x = carve<Real>(p, count);
+  d.y = carve<Real>(p, count);
+  d.nx = carve<Real>(p, count);
+  d.ny = carve<Real>(p, count);
+  d.w = carve<Real>(p, count);
+  d.kap = carve<Real>(p, count);
+  d.comp = carve<int>(p, count);
+  return d;
+}
+
+template <class Real>
+__host__ __device__ constexpr size_t dofs_bytes(int count) {
+  return 6 * ((sizeof(Real) * (size_t)count + 15) & ~size_t(15)) +
+         ((sizeof(int) * (size_t)count + 15) & ~size_t(15));
+}
+
+// Loads DOF data for dofs[0..cnt) into slots [0..cnt) of d.  Coordinates are
+// shifted by (ox, oy) in double before rounding to Real.
+template <class Real>
+__device__ __forceinline__ void load_dof(const Geo<double>& g, int sd, int dof, double ox,
+                                         double oy, DofSoA<Real>& d, int slot) {
+  int p = sd == 1 ? dof : (dof >> 1);
+  d.x[slot] = (Real)(g.x[p] - ox);
+  d.y[slot] = (Real)(g.y[p] - oy);
+  d.nx[slot] = (Real)g.nx[p];
+  d.ny[slot] = (Real)g.ny[p];
+  d.w[slot] = (Real)g.w[p];
+  d.kap[slot] = (Real)g.kap[p];
+  d.comp[slot] = dof - p * sd;
+}
+
+// Double-layer kernel entries (ie_solver/kernel/kernel.cpp:29-91, 123-290).
+// Target (tx, ty, tn) component ta; source (sx, sy, sn, sw, skap) component sb.
+template <class Real>
+__device__ __forceinline__ Real kernel_entry(int pde, Real tx, Real ty, Real tnx, Real tny,
+                                             int ta, Real sx, Real sy, Real snx, Real sny,
+                                             Real sw, Real skap, int sb) {
+  if (pde == kLaplace) {
+    const Real scale = (Real)(1.0 / (2.0 * CUDART_PI));
+    if (tx == sx && ty == sy) return (Real)0.5 + (Real)0.5 * skap * sw * scale;
+    Real r0 = tx - sx, r1 = ty - sy;
+    return -sw * scale * (r0 * snx + r1 * sny) / (r0 * r0 + r1 * r1);
+  }
+  if (pde == kStokes) {
+    const Real scale = (Real)(1.0 / CUDART_PI);
+    Real tn_a = ta == 0 ? tnx : tny;
+    Real sn_b = sb == 0 ? snx : sny;
+    if (tx == sx && ty == sy) {
+      Real pot = (Real)-0.5 * skap * sw * scale;
+      // tangent t = (-sn_y, sn_x): -0.5 delta_ab + pot t_a t_b + w n_a n_b
+      Real t_a = ta == 0 ? -sny : snx;
+      Real t_b = sb == 0 ? -sny : snx;
+      Real v = pot * t_a * t_b + sw * tn_a * sn_b;
+      return ta == sb ? (Real)-0.5 + v : v;
+    }
+    Real r0 = tx - sx, r1 = ty - sy;
+    Real d = r0 * r0 + r1 * r1;
+    Real pot = sw * scale * (r0 * snx + r1 * sny) / (d * d);
+    Real ra = ta == 0 ? r0 : r1;
+    Real rb = sb == 0 ? r0 : r1;
+    return pot * ra * rb + sw * tn_a * sn_b;
+  }
+  // Laplace-Neumann (kernel.cpp:80-91)
+  const Real scale = (Real)(1.0 / (2.0 * CUDART_PI));
+  if (tx == sx && ty == sy) return sw - (Real)0.5 + (Real)0.5 * skap * sw * scale;
+  Real r0 = tx - sx, r1 = ty - sy;
+  return sw + sw * scale * (r0 * tnx + r1 * tny) / (r0 * r0 + r1 * r1);
+}
+
+template <class Real>
+__device__ __forceinline__ Real kernel_dofs(int pde, const DofSoA<Real>& t, int i,
+                                            const DofSoA<Real>& s, int j) {
+  return kernel_entry<Real>(pde, t.x[i], t.y[i], t.nx[i], t.ny[i], t.comp[i], s.x[j], s.y[j],
+                            s.nx[j], s.ny[j], s.w[j], s.kap[j], s.comp[j]);
+}
+
+}  // namespace rskel

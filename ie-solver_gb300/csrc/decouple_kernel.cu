@@ -1,0 +1,269 @@
+// Batched Schur-complement elimination of compressed boxes, one CTA per box.
+//
+// Restates SkelFactorization::decouple (ie_solver/skel_factorization/
+// skel_factorization.cpp:77-128) with the descendant updates of
+// get_all_schur_updates (:323-381) folded in differently: under weak
+// admissibility every Schur update of a box's descendants lives inside one
+// child's DOF set, so the updated matrix of a box is the kernel everywhere
+// except on the children's diagonal blocks, which are the children's own
+// Schur-complemented blocks E_child (k x k for a compressed child, its whole
+// assembled block otherwise).  Each box therefore assembles
+//     Ktilde = [E_c1  K(c1,c2) ...; K(c2,c1)  E_c2 ...; ...]
+// in shared memory directly in skeleton-first order (s = p[0:k], r = p[k:]),
+// and writes its own E = Ktilde(s,s) - L K_r_sn for its parent.  Boxes that
+// are not compressed write E = Ktilde.
+//
+// With T the ID interpolation matrix (k x r):
+//   K_r_sn = Ktilde(r,s) - T^T Ktilde(s,s)
+//   X_rr   = Ktilde(r,r) - T^T Ktilde(s,r) - K_r_sn T
+//   K_sn_r = Ktilde(s,r) - Ktilde(s,s) T
+//   X_rr = P^T L U (partial pivoting), U_f = X_rr^{-1} K_r_sn,
+//   L_f = K_sn_r X_rr^{-1},  E = Ktilde(s,s) - K_sn_r U_f  (= L_f K_r_sn).
+#include "common.cuh"
+#include "kernels.hpp"
+
+namespace rskel {
+
+template <class Real>
+__host__ __device__ size_t dec_smem_bytes(int n, bool tile_in_smem) {
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  size_t b = 0;
+  if (tile_in_smem) {
+    b += al(sizeof(Real) * (size_t)n * n);        // M
+    b += al(sizeof(Real) * (size_t)(n / 2 + 1) * (n - n / 2 + 1));  // T (k*r <= n^2/4)
+  }
+  b += dofs_bytes<Real>(n);
+  b += 3 * al(sizeof(int) * n);                   // child, idx, ld
+  b += al(sizeof(int64_t) * n);                   // e_base
+  b += 2 * al(sizeof(int) * n);                   // order, piv
+  b += al(sizeof(double) * 4);
+  return b;
+}
+
+size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem) {
+  return fp32 ? dec_smem_bytes<float>(n, tile_in_smem) : dec_smem_bytes<double>(n, tile_in_smem);
+}
+
+template <class Real>
+__global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
+  const DecoupleTask t = p.tasks[blockIdx.x];
+  const int n = t.n;
+  const int k = t.slot >= 0 ? p.ranks[t.slot] : 0;
+  const int r = n - k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* sp = smem;
+  Real *M, *T;
+  if (t.scratch_off < 0) {
+    M = carve<Real>(sp, n * n);
+    T = carve<Real>(sp, (n / 2 + 1) * (n - n / 2 + 1));
+  } else {
+    M = reinterpret_cast<Real*>(p.scratch) + t.scratch_off;
+    T = M + (size_t)n * n;
+  }
+  DofSoA<Real> act = carve_dofs<Real>(sp, n);
+  int* bchild = carve<int>(sp, n);
+  int* bidx = carve<int>(sp, n);
+  int* bld = carve<int>(sp, n);
+  int64_t* bbase = carve<int64_t>(sp, n);
+  int* order = carve<int>(sp, n);
+  int* piv = carve<int>(sp, n);
+  double* scal = carve<double>(sp, 4);
+
+  const Real* E_in = reinterpret_cast<const Real*>(p.epool);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], 0.0, 0.0, act, j);
+    const BlkRef b = p.blk[t.blk_off + j];
+    bchild[j] = b.child;
+    bidx[j] = b.idx;
+    bld[j] = b.ld;
+    bbase[j] = b.e_base;
+    order[j] = k > 0 ? p.perm[t.perm_off + j] : j;
+  }
+  __syncthreads();
+  // Assemble Ktilde in skeleton-first order.
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int a = e % n, b = e / n;
+    const int ia = order[a], ib = order[b];
+    Real val;
+    if (bchild[ia] == bchild[ib] && bbase[ia] >= 0) {
+      val = E_in[bbase[ia] + bidx[ia] + (int64_t)bld[ia] * bidx[ib]];
+    } else {
+      val = kernel_dofs<Real>(p.pde, act, ia, act, ib);
+    }
+    M[a + (size_t)n * b] = val;
+  }
+  __syncthreads();
+  Real* E_out = reinterpret_cast<Real*>(p.epool) + t.e_off;
+  if (k == 0) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) E_out[e] = M[e];
+    return;
+  }
+  Real* fac = reinterpret_cast<Real*>(p.fac) + t.fac_off;
+  for (int e = threadIdx.x; e < k * r; e += blockDim.x) T[e] = fac[fac_T(k, r) + e];
+  __syncthreads();
+  const size_t ld = n;
+  Real* Mss = M;
+  Real* Msr = M + ld * k;
+  Real* Mrs = M + k;
+  Real* Mrr = M + k + ld * k;
+  // 1) K_r_sn = Mrs - T^T Mss  (r x k), in place
+  for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
+    const int i = e % r, j = e / r;
+    Real acc = Mrs[i + ld * j];
+    for (int l = 0; l < k; ++l) acc -= T[l + (size_t)k * i] * Mss[l + ld * j];
+    Mrs[i + ld * j] = acc;
+  }
+  __syncthreads();
+  // 2) X_rr = Mrr - T^T Msr - K_r_sn T  (r x r), in place
+  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+    const int i = e % r, j = e / r;
+    Real a1 = 0, a2 = 0;
+    for (int l = 0; l < k; ++l) {
+      a1 += T[l + (size_t)k * i] * Msr[l + ld * j];
+      a2 += Mrs[i + ld * l] * T[l + (size_t)k * j];
+    }
+    Mrr[i + ld * j] = (Mrr[i + ld * j] - a1) - a2;
+  }
+  __syncthreads();
+  // 3) K_sn_r = Msr - Mss T  (k x r), in place
+  for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
+    const int i = e % k, j = e / k;
+    Real acc = Msr[i + ld * j];
+    for (int l = 0; l < k; ++l) acc -= Mss[i + ld * l] * T[l + (size_t)k * j];
+    Msr[i + ld * j] = acc;
+  }
+  __syncthreads();
+  // 4) LU of X_rr with partial pivoting (dgetrf), in place.
+  if (threadIdx.x == 0) scal[0] = 0.0;
+  for (int j = 0; j < r; ++j) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = r;
+      for (int i = j + lane; i < r; i += 32) {
+        double v = fabs((double)Mrr[i + ld * j]);
+        if (v > best || (v == best && i < bi)) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (lane == 0) {
+        piv[j] = bi;
+        if (!(best > 0.0) || !isfinite(best)) scal[0] = 1.0;
+      }
+    }
+    __syncthreads();
+    const int pj = piv[j];
+    if (pj != j) {
+      for (int c = threadIdx.x; c < r; c += blockDim.x) {
+        Real tmp = Mrr[j + ld * c];
+        Mrr[j + ld * c] = Mrr[pj + ld * c];
+        Mrr[pj + ld * c] = tmp;
+      }
+      __syncthreads();
+    }
+    const Real d = Mrr[j + ld * j];
+    if (d != (Real)0) {
+      const Real inv = (Real)1 / d;
+      for (int i = j + 1 + threadIdx.x; i < r; i += blockDim.x) Mrr[i + ld * j] *= inv;
+    }
+    __syncthreads();
+    const int rem = r - j - 1;
+    for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
+      const int i = j + 1 + e % rem, c = j + 1 + e / rem;
+      Mrr[i + ld * c] -= Mrr[i + ld * j] * Mrr[j + ld * c];
+    }
+    __syncthreads();
+  }
+  // 5) U_f = X^{-1} K_r_sn, in place over Mrs (one warp per column).
+  for (int c = warp; c < k; c += kWarps) {
+    Real* y = Mrs + ld * c;
+    if (lane == 0)
+      for (int j = 0; j < r; ++j)
+        if (piv[j] != j) { Real tmp = y[j]; y[j] = y[piv[j]]; y[piv[j]] = tmp; }
+    __syncwarp();
+    for (int j = 0; j < r; ++j) {
+      const Real yj = y[j];
+      __syncwarp();
+      for (int i = j + 1 + lane; i < r; i += 32) y[i] -= Mrr[i + ld * j] * yj;
+      __syncwarp();
+    }
+    for (int j = r - 1; j >= 0; --j) {
+      const Real yj = y[j] / Mrr[j + ld * j];
+      __syncwarp();
+      for (int i = lane; i < j; i += 32) y[i] -= Mrr[i + ld * j] * yj;
+      if (lane == 0) y[j] = yj;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // 6) E = Mss - K_sn_r U_f  (k x k), in place over Mss.
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e % k, j = e / k;
+    Real acc = 0;
+    for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrs[l + ld * j];
+    Mss[i + ld * j] -= acc;
+  }
+  __syncthreads();
+  // 7) L_f = K_sn_r X^{-1}: solve X^T y = K_sn_r(i,:)^T per row (one warp per row).
+  for (int i = warp; i < k; i += kWarps) {
+    Real* y = Msr + i;  // stride ld
+    for (int j = 0; j < r; ++j) {  // U^T z = b
+      const Real yj = y[ld * j] / Mrr[j + ld * j];
+      __syncwarp();
+      for (int q = j + 1 + lane; q < r; q += 32) y[ld * q] -= Mrr[j + ld * q] * yj;
+      if (lane == 0) y[ld * j] = yj;
+      __syncwarp();
+    }
+    for (int j = r - 1; j >= 0; --j) {  // L^T w = z (unit diagonal)
+      const Real yj = y[ld * j];
+      __syncwarp();
+      for (int q = lane; q < j; q += 32) y[ld * q] -= Mrr[j + ld * q] * yj;
+      __syncwarp();
+    }
+    if (lane == 0)
+      for (int j = r - 1; j >= 0; --j)
+        if (piv[j] != j) { Real tmp = y[ld * j]; y[ld * j] = y[ld * piv[j]]; y[ld * piv[j]] = tmp; }
+    __syncwarp();
+  }
+  __syncthreads();
+  // 8) write L_f (k x r), U_f (r x k), X_rr LU (r x r), pivots, E (k x k).
+  Real* Lo = fac + fac_L(k, r);
+  Real* Uo = fac + fac_U(k, r);
+  Real* Xo = fac + fac_X(k, r);
+  for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
+    const int i = e % k, j = e / k;
+    Lo[e] = Msr[i + ld * j];
+    const int i2 = e % r, j2 = e / r;
+    Uo[e] = Mrs[i2 + ld * j2];
+  }
+  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+    const int i = e % r, j = e / r;
+    Xo[e] = Mrr[i + ld * j];
+  }
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e % k, j = e / k;
+    E_out[e] = Mss[i + ld * j];
+  }
+  for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = piv[j];
+  if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
+}
+
+void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
+                     cudaStream_t st) {
+  if (num_tasks <= 0) return;
+  if (fp32) {
+    cudaFuncSetAttribute(decouple_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    decouple_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
+  } else {
+    cudaFuncSetAttribute(decouple_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    decouple_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
+  }
+}
+
+}  // namespace rskel

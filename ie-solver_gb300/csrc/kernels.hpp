@@ -1,0 +1,91 @@
+// Launch interfaces of the CUDA kernels (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "plan.hpp"
+
+namespace rskel {
+
+struct IdParams {
+  Geo<double> geo;
+  int pde, sd, npp;
+  double tol;
+  const IdTask* tasks;
+  const int* dofs;
+  const double* pxy_cos;
+  const double* pxy_sin;
+  int* ranks;      // per slot
+  int* perm;       // written at act_off (n entries per task)
+  void* fac;       // T output (Real)
+  void* scratch;   // global tiles for large boxes (Real)
+  const double* dense;  // matrices for rs_id_batched (column major)
+};
+
+struct DecoupleParams {
+  Geo<double> geo;
+  int pde, sd;
+  const DecoupleTask* tasks;
+  const int* dofs;
+  const BlkRef* blk;
+  const int* ranks;
+  const int* perm;
+  void* fac;       // T in, L/U/X_rr LU out (Real)
+  int* piv;
+  void* epool;     // E blocks in/out (Real)
+  void* scratch;
+  int* status;     // non-zero on singular pivot / non-finite value
+};
+
+// Sweep modes (solve_kernels.cu).
+enum SweepMode : int {
+  kUpSolve = 0,   // x_r -= T^T x_s; x_s -= L x_r; x_r = X_rr^{-1} x_r
+  kUpPlain = 1,   // x_r -= T^T x_s; x_s -= L x_r
+  kUpTransU = 2,  // x_r -= T^T x_s; x_s -= U^T x_r
+  kDiagOnly = 3,  // x_r = X_rr^{-1} x_r
+  kDown = 4       // x_r -= U x_s; x_s -= T x_r
+};
+
+struct SweepParams {
+  const SweepTask* tasks;
+  const int* dofs;
+  const void* fac;  // Real
+  const int* piv;
+  void* x;          // Real, D x nrhs, column major
+  int ld, nrhs;
+  int mode;
+};
+
+size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);
+size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
+
+void launch_id(const IdParams& p, int num_tasks, size_t smem, bool fp32, cudaStream_t st);
+void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
+                     cudaStream_t st);
+void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st);
+
+// Dense LU with partial pivoting of an n x n column-major matrix (one CTA),
+// and the corresponding solve on gathered rows of x.
+void launch_dense_lu(double* a, int n, int* piv, int* status, cudaStream_t st);
+void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st);
+// x[idx, :] = LU^{-1} x[idx, :] (idx == nullptr: rows 0..n-1); x is Real.
+void launch_dense_solve_gather(const void* lu, bool fp32, int n, const int* piv,
+                               const int* idx, void* x, int ld, int nrhs, cudaStream_t st);
+// Precision conversions and residual update for refinement.
+void launch_d2f(const double* in, float* out, size_t n, cudaStream_t st);
+void launch_add_f2d(double* acc, const float* inc, size_t n, cudaStream_t st);
+
+// Dense double-layer block K(I, J) (FP64), column major.
+void launch_kernel_block(const Geo<double>& g, int pde, int sd, const int* I, int nI,
+                         const int* J, int nJ, double* out, cudaStream_t st);
+// y = K x over all DOFs, FP64.
+void launch_matvec(const Geo<double>& g, int pde, int sd, int npts, const double* x,
+                   int nrhs, double* y, cudaStream_t st);
+
+// Elementwise helpers.
+void launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);
+
+}  // namespace rskel

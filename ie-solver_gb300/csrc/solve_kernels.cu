@@ -1,0 +1,413 @@
+// Solve sweeps, dense LU, kernel blocks and the dense matvec.
+//
+// Sweeps restate SkelFactorization::apply_sweep_matrix / apply_diag_inv_matrix
+// and the level loops of solve / multiply_connected_solve
+// (ie_solver/skel_factorization/skel_factorization.cpp:388-426, 507-777).
+// All compressed boxes of one tree level touch disjoint DOF sets, so a level
+// is one launch with one CTA per box; the per-box work is a gather of the
+// box's skeleton / redundant rows of x, a few small matrix products with the
+// box's factors and a scatter back.
+#include "common.cuh"
+#include "kernels.hpp"
+
+namespace rskel {
+
+constexpr int kRhsBlock = 8;
+
+// In-place solve of X y = b (LU with pivots) for up to kWarps columns of a
+// column-major r x cb block y (ld = r), one warp per column.
+template <class Real>
+__device__ void lu_solve_cols(const Real* X, const int* piv, int r, Real* y, int ldy, int cb) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = warp; c < cb; c += kWarps) {
+    Real* v = y + (size_t)ldy * c;
+    if (lane == 0)
+      for (int j = 0; j < r; ++j)
+        if (piv[j] != j) { Real t = v[j]; v[j] = v[piv[j]]; v[piv[j]] = t; }
+    __syncwarp();
+    for (int j = 0; j < r; ++j) {
+      const Real vj = v[j];
+      __syncwarp();
+      for (int i = j + 1 + lane; i < r; i += 32) v[i] -= X[i + (size_t)r * j] * vj;
+      __syncwarp();
+    }
+    for (int j = r - 1; j >= 0; --j) {
+      const Real vj = v[j] / X[j + (size_t)r * j];
+      __syncwarp();
+      for (int i = lane; i < j; i += 32) v[i] -= X[i + (size_t)r * j] * vj;
+      if (lane == 0) v[j] = vj;
+      __syncwarp();
+    }
+  }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(kThreads) sweep_kernel(SweepParams p) {
+  const SweepTask t = p.tasks[blockIdx.x];
+  const int k = t.k, r = t.r;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* sp = smem;
+  Real* xs = carve<Real>(sp, k * kRhsBlock);
+  Real* xr = carve<Real>(sp, r * kRhsBlock);
+  int* piv = carve<int>(sp, r);
+  const Real* fac = reinterpret_cast<const Real*>(p.fac) + t.fac_off;
+  const Real* T = fac + fac_T(k, r);
+  const Real* L = fac + fac_L(k, r);
+  const Real* U = fac + fac_U(k, r);
+  const Real* X = fac + fac_X(k, r);
+  Real* x = reinterpret_cast<Real*>(p.x);
+  const int* sk = p.dofs + t.skel_off;
+  const int* rd = p.dofs + t.red_off;
+  for (int j = threadIdx.x; j < r; j += blockDim.x) piv[j] = p.piv[t.piv_off + j];
+  for (int c0 = 0; c0 < p.nrhs; c0 += kRhsBlock) {
+    const int cb = p.nrhs - c0 < kRhsBlock ? p.nrhs - c0 : kRhsBlock;
+    for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {
+      int i = e % k, c = e / k;
+      xs[i + k * c] = x[sk[i] + (size_t)p.ld * (c0 + c)];
+    }
+    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {
+      int i = e % r, c = e / r;
+      xr[i + r * c] = x[rd[i] + (size_t)p.ld * (c0 + c)];
+    }
+    __syncthreads();
+    if (p.mode == kUpSolve || p.mode == kUpPlain || p.mode == kUpTransU) {
+      for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {  // x_r -= T^T x_s
+        int i = e % r, c = e / r;
+        Real acc = 0;
+        for (int l = 0; l < k; ++l) acc += T[l + (size_t)k * i] * xs[l + k * c];
+        xr[i + r * c] -= acc;
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {
+        int i = e % k, c = e / k;
+        Real acc = 0;
+        if (p.mode == kUpTransU)  // x_s -= U^T x_r
+          for (int l = 0; l < r; ++l) acc += U[l + (size_t)r * i] * xr[l + r * c];
+        else  // x_s -= L x_r
+          for (int l = 0; l < r; ++l) acc += L[i + (size_t)k * l] * xr[l + r * c];
+        xs[i + k * c] -= acc;
+      }
+      __syncthreads();
+      if (p.mode == kUpSolve) {
+        lu_solve_cols<Real>(X, piv, r, xr, r, cb);
+        __syncthreads();
+      }
+    } else if (p.mode == kDiagOnly) {
+      lu_solve_cols<Real>(X, piv, r, xr, r, cb);
+      __syncthreads();
+    } else {  // kDown
+      for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {  // x_r -= U x_s
+        int i = e % r, c = e / r;
+        Real acc = 0;
+        for (int l = 0; l < k; ++l) acc += U[i + (size_t)r * l] * xs[l + k * c];
+        xr[i + r * c] -= acc;
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {  // x_s -= T x_r
+        int i = e % k, c = e / k;
+        Real acc = 0;
+        for (int l = 0; l < r; ++l) acc += T[i + (size_t)k * l] * xr[l + r * c];
+        xs[i + k * c] -= acc;
+      }
+      __syncthreads();
+    }
+    if (p.mode != kDiagOnly)
+      for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {
+        int i = e % k, c = e / k;
+        x[sk[i] + (size_t)p.ld * (c0 + c)] = xs[i + k * c];
+      }
+    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {
+      int i = e % r, c = e / r;
+      x[rd[i] + (size_t)p.ld * (c0 + c)] = xr[i + r * c];
+    }
+    __syncthreads();
+  }
+}
+
+void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st) {
+  if (num_tasks <= 0) return;
+  size_t es = fp32 ? sizeof(float) : sizeof(double);
+  size_t smem = 2 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) + sizeof(int) * nmax + 64;
+  if (fp32) {
+    cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sweep_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
+  } else {
+    cudaFuncSetAttribute(sweep_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sweep_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dense LU (dgetrf with partial pivoting), one CTA, matrix in global memory.
+// ---------------------------------------------------------------------------
+template <class Real>
+__global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* A, int n, int* piv,
+                                                            int* status) {
+  __shared__ int s_piv;
+  __shared__ int s_bad;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_bad = 0;
+  for (int j = 0; j < n; ++j) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = n;
+      for (int i = j + lane; i < n; i += 32) {
+        double v = fabs((double)A[i + (size_t)n * j]);
+        if (v > best || (v == best && i < bi)) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (lane == 0) {
+        s_piv = bi;
+        piv[j] = bi;
+        if (!(best > 0.0) || !isfinite(best)) s_bad = 1;
+      }
+    }
+    __syncthreads();
+    const int pj = s_piv;
+    if (pj != j) {
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        Real t = A[j + (size_t)n * c];
+        A[j + (size_t)n * c] = A[pj + (size_t)n * c];
+        A[pj + (size_t)n * c] = t;
+      }
+      __syncthreads();
+    }
+    const Real d = A[j + (size_t)n * j];
+    if (d != (Real)0) {
+      const Real inv = (Real)1 / d;
+      for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)n * j] *= inv;
+    }
+    __syncthreads();
+    const int rem = n - j - 1;
+    for (int c = j + 1 + warp; c < n; c += kWarps) {
+      const Real ajc = A[j + (size_t)n * c];
+      for (int i = j + 1 + lane; i < n; i += 32) A[i + (size_t)n * c] -= A[i + (size_t)n * j] * ajc;
+    }
+    (void)rem;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && s_bad) atomicExch(status, 1);
+}
+
+void launch_dense_lu(double* a, int n, int* piv, int* status, cudaStream_t st) {
+  if (n > 0) dense_lu_kernel<double><<<1, kThreads, 0, st>>>(a, n, piv, status);
+}
+void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st) {
+  if (n > 0) dense_lu_kernel<float><<<1, kThreads, 0, st>>>(a, n, piv, status);
+}
+
+// x[idx, c] = LU^{-1} x[idx, c]: one CTA; the gathered block lives in global
+// scratch-free form by solving column by column directly on x (one warp per
+// column; rows are reached through idx).
+template <class Real>
+__global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LU, int n,
+                                                               const int* piv, const int* idx,
+                                                               Real* x, int ld, int nrhs) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = warp; c < nrhs; c += kWarps) {
+    Real* v = x + (size_t)ld * c;
+    auto at = [&](int i) -> Real& { return v[idx ? idx[i] : i]; };
+    if (lane == 0)
+      for (int j = 0; j < n; ++j)
+        if (piv[j] != j) { Real t = at(j); at(j) = at(piv[j]); at(piv[j]) = t; }
+    __syncwarp();
+    for (int j = 0; j < n; ++j) {
+      const Real vj = at(j);
+      __syncwarp();
+      for (int i = j + 1 + lane; i < n; i += 32) at(i) -= LU[i + (size_t)n * j] * vj;
+      __syncwarp();
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      const Real vj = at(j) / LU[j + (size_t)n * j];
+      __syncwarp();
+      for (int i = lane; i < j; i += 32) at(i) -= LU[i + (size_t)n * j] * vj;
+      if (lane == 0) at(j) = vj;
+      __syncwarp();
+    }
+  }
+}
+
+void launch_dense_solve_gather(const void* lu, bool fp32, int n, const int* piv,
+                               const int* idx, void* x, int ld, int nrhs, cudaStream_t st) {
+  if (n <= 0 || nrhs <= 0) return;
+  int blocks = (nrhs + kWarps - 1) / kWarps;
+  // Each CTA handles kWarps columns.
+  for (int b = 0; b < blocks; ++b) {
+    int cols = nrhs - b * kWarps < kWarps ? nrhs - b * kWarps : kWarps;
+    if (fp32)
+      dense_solve_kernel<float><<<1, kThreads, 0, st>>>(
+          (const float*)lu, n, piv, idx, (float*)x + (size_t)ld * b * kWarps, ld, cols);
+    else
+      dense_solve_kernel<double><<<1, kThreads, 0, st>>>(
+          (const double*)lu, n, piv, idx, (double*)x + (size_t)ld * b * kWarps, ld, cols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel blocks and the dense FP64 matvec
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double kernel_gdof(const Geo<double>& g, int pde, int sd, int ti,
+                                              int sj) {
+  int tp = sd == 1 ? ti : ti >> 1, spt = sd == 1 ? sj : sj >> 1;
+  return kernel_entry<double>(pde, g.x[tp], g.y[tp], g.nx[tp], g.ny[tp], ti - tp * sd, g.x[spt],
+                              g.y[spt], g.nx[spt], g.ny[spt], g.w[spt], g.kap[spt], sj - spt * sd);
+}
+
+__global__ void kernel_block_kernel(Geo<double> g, int pde, int sd, const int* I, int nI,
+                                    const int* J, int nJ, double* out) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nI * nJ) return;
+  int i = (int)(e % nI), j = (int)(e / nI);
+  out[e] = kernel_gdof(g, pde, sd, I[i], J[j]);
+}
+
+void launch_kernel_block(const Geo<double>& g, int pde, int sd, const int* I, int nI,
+                         const int* J, int nJ, double* out, cudaStream_t st) {
+  size_t tot = (size_t)nI * nJ;
+  if (!tot) return;
+  kernel_block_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g, pde, sd, I, nI, J, nJ, out);
+}
+
+constexpr int kMvTargets = 64;
+constexpr int kMvSplit = 4;
+constexpr int kMvTile = 256;
+
+// y = K x: CTA per 64 target DOFs, 4 source lanes per target, FP64.
+__global__ void __launch_bounds__(kMvTargets * kMvSplit) matvec_kernel(Geo<double> g, int pde,
+                                                                       int sd, int D,
+                                                                       const double* x, int nrhs,
+                                                                       double* y) {
+  __shared__ double sx[kMvTile], sy[kMvTile], snx[kMvTile], sny[kMvTile], sw[kMvTile],
+      sk[kMvTile];
+  __shared__ int sc[kMvTile];
+  __shared__ double part[kMvSplit][kMvTargets][kRhsBlock];
+  const int tl = threadIdx.x % kMvTargets, sl = threadIdx.x / kMvTargets;
+  const int ti = blockIdx.x * kMvTargets + tl;
+  const bool valid = ti < D;
+  int tp = 0, ta = 0;
+  double tx = 0, ty = 0, tnx = 0, tny = 0;
+  if (valid) {
+    tp = sd == 1 ? ti : ti >> 1;
+    ta = ti - tp * sd;
+    tx = g.x[tp]; ty = g.y[tp]; tnx = g.nx[tp]; tny = g.ny[tp];
+  }
+  for (int c0 = 0; c0 < nrhs; c0 += kRhsBlock) {
+    const int cb = nrhs - c0 < kRhsBlock ? nrhs - c0 : kRhsBlock;
+    double acc[kRhsBlock];
+#pragma unroll
+    for (int c = 0; c < kRhsBlock; ++c) acc[c] = 0.0;
+    for (int s0 = 0; s0 < D; s0 += kMvTile) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < kMvTile; q += blockDim.x) {
+        int sj = s0 + q;
+        if (sj < D) {
+          int spt = sd == 1 ? sj : sj >> 1;
+          sx[q] = g.x[spt]; sy[q] = g.y[spt]; snx[q] = g.nx[spt]; sny[q] = g.ny[spt];
+          sw[q] = g.w[spt]; sk[q] = g.kap[spt]; sc[q] = sj - spt * sd;
+        }
+      }
+      __syncthreads();
+      if (valid) {
+        const int lim = D - s0 < kMvTile ? D - s0 : kMvTile;
+        for (int q = sl; q < lim; q += kMvSplit) {
+          double kv = kernel_entry<double>(pde, tx, ty, tnx, tny, ta, sx[q], sy[q], snx[q],
+                                           sny[q], sw[q], sk[q], sc[q]);
+#pragma unroll
+          for (int c = 0; c < kRhsBlock; ++c)
+            if (c < cb) acc[c] += kv * x[s0 + q + (size_t)D * (c0 + c)];
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kRhsBlock; ++c) part[sl][tl][c] = acc[c];
+    __syncthreads();
+    if (sl == 0 && valid)
+      for (int c = 0; c < cb; ++c) {
+        double s = 0.0;
+        for (int q = 0; q < kMvSplit; ++q) s += part[q][tl][c];
+        y[ti + (size_t)D * (c0 + c)] = s;
+      }
+    __syncthreads();
+  }
+}
+
+void launch_matvec(const Geo<double>& g, int pde, int sd, int npts, const double* x, int nrhs,
+                   double* y, cudaStream_t st) {
+  int D = npts * sd;
+  if (D <= 0 || nrhs <= 0) return;
+  matvec_kernel<<<(D + kMvTargets - 1) / kMvTargets, kMvTargets * kMvSplit, 0, st>>>(g, pde, sd,
+                                                                                   D, x, nrhs, y);
+}
+
+// ---------------------------------------------------------------------------
+// elementwise
+// ---------------------------------------------------------------------------
+__global__ void d2f_kernel(const double* in, float* out, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+__global__ void add_f2d_kernel(double* acc, const float* inc, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) acc[i] += (double)inc[i];
+}
+__global__ void axpby_kernel(double* y, const double* x, double a, double b, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a * x[i] + b * y[i];
+}
+
+void launch_d2f(const double* in, float* out, size_t n, cudaStream_t st) {
+  if (n) d2f_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+}
+void launch_add_f2d(double* acc, const float* inc, size_t n, cudaStream_t st) {
+  if (n) add_f2d_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(acc, inc, n);
+}
+void launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st) {
+  if (n) axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, x, a, b, n);
+}
+
+}  // namespace rskel
+
+namespace rskel {
+
+// out[c] = || x[:, c] ||_2
+__global__ void col_norms_kernel(const double* x, int rows, double* out) {
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    double v = x[i + (size_t)rows * c];
+    s += v * v;
+  }
+  s = warp_sum(s);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[c] = sqrt(t);
+  }
+}
+
+void launch_col_norms(const double* x, int rows, int cols, double* out, cudaStream_t st) {
+  if (cols > 0) col_norms_kernel<<<cols, 256, 0, st>>>(x, rows, out);
+}
+
+// r[l] -= sum_j U[l, j] a[j]
+__global__ void gemv_sub_kernel(double* r, const double* U, const double* a, int D, int nb) {
+  size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (l >= (size_t)D) return;
+  double acc = 0.0;
+  for (int j = 0; j < nb; ++j) acc += U[l + (size_t)D * j] * a[j];
+  r[l] -= acc;
+}
+
+void launch_gemv_sub(double* r, const double* U, const double* a, int D, int nb, cudaStream_t st) {
+  if (D > 0) gemv_sub_kernel<<<(D + 255) / 256, 256, 0, st>>>(r, U, a, D, nb);
+}
+
+}  // namespace rskel

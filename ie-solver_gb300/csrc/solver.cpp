@@ -1,0 +1,1356 @@
+// Host orchestration of the GB300 recursive-skeletonization solver and the
+// C ABI declared in include/rskel.h.
+//
+// Factorization (SkelFactorization::skeletonize, ie_solver/skel_factorization/
+// skel_factorization.cpp:140-310) runs level by level from the leaves up.  For
+// each level the host
+//   1. forms every box's active DOF list from its children's skeletons
+//      (QuadTree::remove_inactive_dofs_at_level, quadtree.cpp:997-1074) and the
+//      row-source lists of the ID matrices (Kernel::get_id_mat, kernel.cpp:293-423);
+//   2. uploads one packed plan and launches two batched kernels over all boxes
+//      of the level (ID, then Schur elimination), binned by box size;
+//   3. reads back the ranks and pivots (a few KB) to plan the next level.
+// The device keeps the geometry, every factor block and every Schur-
+// complemented diagonal block; nothing is recomputed on the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rskel.h"
+#include "border.hpp"
+#include "devbuf.hpp"
+#include "kernels.hpp"
+#include "plan.hpp"
+#include "tree.hpp"
+
+using namespace rskel;
+
+namespace {
+
+constexpr size_t kSmemMax = 227 * 1024;
+
+struct NodeState {
+  int compressed = 0;
+  int k = 0, r = 0;
+  std::vector<int> active, skel, red, near_, perm;
+  int64_t fac_off = -1, piv_off = -1, e_off = -1;
+  int e_ld = 0;  // leading dimension of this box's block E (0: none, use the kernel)
+  int slot = -1;
+};
+
+template <class Real>
+struct Factor {
+  DevBuf<Real> fac, epool, scratch, x, tmp, mU, mP, S, M, nv;
+  size_t fac_used = 0, e_used = 0;
+};
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+}  // namespace
+
+struct rs_solver {
+  rs_config cfg;
+  std::string err;
+  int n = 0, D = 0, sd = 1, nh = 0;
+  std::vector<double> pts, nrm, w, kap, hc, hr;
+  QuadTree tree;
+  bool tree_built = false;
+  std::vector<NodeState> st;
+  bool factored = false;
+  bool fp32 = false;
+
+  bool dev_ready = false;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_a = nullptr, ev_b = nullptr;
+  cudaEvent_t ev_f0 = nullptr, ev_f1 = nullptr;
+  DevBuf<double> gx, gy, gnx, gny, gw, gk, pxy_c, pxy_s;
+  bool geo_on_dev = false;
+
+  std::vector<int> pool;  // host mirror of the device DOF pool
+  DevBuf<int> dofs, perm, ranks, piv, status;
+  DevBuf<IdTask> id_tasks;
+  DevBuf<DecoupleTask> dc_tasks;
+  DevBuf<BlkRef> blk;
+  HostBuf<int> h_ranks, h_perm, h_status;
+  size_t piv_used = 0;
+  Factor<double> F64;
+  Factor<float> F32;
+
+  std::vector<SweepTask> sweeps;
+  std::vector<int> sweep_off, sweep_cnt, sweep_nmax;  // per level
+  DevBuf<SweepTask> sweep_dev;
+  int ns = 0;
+  std::vector<int> allskel;
+  int allskel_off = -1;
+  int64_t root_e_off = -1;
+  DevBuf<int> root_piv;
+
+  // bordered system
+  int nb = 0;
+  std::vector<double> Uh, Psih;  // D x nb, nb x D (host)
+  DevBuf<double> U0, PsiT0, G, g1;
+  DevBuf<unsigned char> red_mask, skel_mask, ones_mask;
+  DevBuf<int> S_piv;
+
+  // solve buffers
+  DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev;
+  HostBuf<double> h_io;
+
+  rs_stats stats;
+  int launches = 0;
+};
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+namespace {
+
+rs_status fail(rs_solver* s, rs_status code, const std::string& msg) {
+  if (s) s->err = msg;
+  return code;
+}
+
+#define RSCHK(expr)                 \
+  do {                              \
+    rs_status rc_ = (expr);         \
+    if (rc_ != RS_OK) return rc_;   \
+  } while (0)
+
+#define CU(expr)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(s, RS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+rs_status ensure_device(rs_solver* s) {
+  if (s->dev_ready) return RS_OK;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0)
+    return fail(s, RS_ERR_NO_DEVICE, "no CUDA device available (there is no CPU fallback)");
+  if (s->cfg.device < 0 || s->cfg.device >= count) return fail(s, RS_ERR_ARG, "bad device ordinal");
+  CU(cudaSetDevice(s->cfg.device));
+  CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  CU(cudaEventCreate(&s->ev_t0));
+  CU(cudaEventCreate(&s->ev_t1));
+  CU(cudaEventCreate(&s->ev_a));
+  CU(cudaEventCreate(&s->ev_b));
+  CU(cudaEventCreate(&s->ev_f0));
+  CU(cudaEventCreate(&s->ev_f1));
+  CU(s->status.ensure(4));
+  CU(s->h_status.ensure(4));
+  s->dev_ready = true;
+  return RS_OK;
+}
+
+rs_status upload_geometry(rs_solver* s) {
+  if (s->geo_on_dev) return RS_OK;
+  const int n = s->n;
+  std::vector<double> x(n), y(n), nx(n), ny(n);
+  for (int i = 0; i < n; ++i) {
+    x[i] = s->pts[2 * i];
+    y[i] = s->pts[2 * i + 1];
+    nx[i] = s->nrm[2 * i];
+    ny[i] = s->nrm[2 * i + 1];
+  }
+  CU(s->gx.ensure(n));
+  CU(s->gy.ensure(n));
+  CU(s->gnx.ensure(n));
+  CU(s->gny.ensure(n));
+  CU(s->gw.ensure(n));
+  CU(s->gk.ensure(n));
+  CU(cudaMemcpy(s->gx.p, x.data(), n * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->gy.p, y.data(), n * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->gnx.p, nx.data(), n * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->gny.p, ny.data(), n * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->gw.p, s->w.data(), n * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->gk.p, s->kap.data(), n * 8, cudaMemcpyHostToDevice));
+  // proxy circle directions, kernel.cpp:432-441
+  const int npp = s->cfg.num_proxy_points;
+  std::vector<double> c(npp), sn(npp);
+  for (int i = 0; i < npp; ++i) {
+    double ang = 2 * M_PI * i * (1.0 / npp);
+    c[i] = std::cos(ang);
+    sn[i] = std::sin(ang);
+  }
+  CU(s->pxy_c.ensure(npp));
+  CU(s->pxy_s.ensure(npp));
+  CU(cudaMemcpy(s->pxy_c.p, c.data(), npp * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(s->pxy_s.p, sn.data(), npp * 8, cudaMemcpyHostToDevice));
+  s->geo_on_dev = true;
+  return RS_OK;
+}
+
+Geo<double> geo_of(const rs_solver* s) {
+  return Geo<double>{s->gx.p, s->gy.p, s->gnx.p, s->gny.p, s->gw.p, s->gk.p};
+}
+
+// Surviving DOFs of a box after its level: skeleton when compressed.
+const std::vector<int>& surviving(const NodeState& ns) {
+  return ns.compressed ? ns.skel : ns.active;
+}
+
+// QuadTree::remove_inactive_dofs_at_box (quadtree.cpp:1032-1055)
+void compute_active(rs_solver* s, int id) {
+  NodeState& S = s->st[id];
+  const TreeNode& nd = s->tree.nodes[id];
+  S.active.clear();
+  if (nd.is_leaf) {
+    S.active = nd.original;
+  } else {
+    for (int c = 0; c < 4; ++c) {
+      const std::vector<int>& v = surviving(s->st[nd.children[c]]);
+      S.active.insert(S.active.end(), v.begin(), v.end());
+    }
+  }
+}
+
+// near lists, quadtree.cpp:1005-1024
+void compute_near(rs_solver* s, int id) {
+  NodeState& S = s->st[id];
+  const TreeNode& nd = s->tree.nodes[id];
+  S.near_.clear();
+  for (int nb : nd.neighbors) {
+    const TreeNode& o = s->tree.nodes[nb];
+    if (o.level > nd.level) continue;
+    const std::vector<int>& v = o.is_leaf ? o.original : s->st[nb].active;
+    S.near_.insert(S.near_.end(), v.begin(), v.end());
+  }
+}
+
+// Row-source DOFs of a box's ID matrix (kernel.cpp:300-394).
+void id_rows(rs_solver* s, int id, std::vector<int>* rows, int* use_proxy) {
+  rows->clear();
+  const TreeNode& nd = s->tree.nodes[id];
+  const int lv = nd.level;
+  *use_proxy = 0;
+  if (lv == 1 || lv == 2) {
+    for (int o : s->tree.levels[lv])
+      if (o != id) {
+        const std::vector<int>& v = s->st[o].active;
+        rows->insert(rows->end(), v.begin(), v.end());
+      }
+    if (lv == 2)
+      for (int o : s->tree.levels[1])
+        if (s->tree.nodes[o].is_leaf) {
+          const std::vector<int>& v = s->tree.nodes[o].original;
+          rows->insert(rows->end(), v.begin(), v.end());
+        }
+    return;
+  }
+  const double cx = nd.corners[0] + nd.side / 2.0;
+  const double cy = nd.corners[1] + nd.side / 2.0;
+  const double lim = s->cfg.radius_ratio * nd.side;
+  for (int mi : s->st[id].near_) {
+    const int pv = (mi / s->sd) * 2;
+    const double dx = cx - s->pts[pv], dy = cy - s->pts[pv + 1];
+    if (std::sqrt(dx * dx + dy * dy) < lim) rows->push_back(mi);
+  }
+  *use_proxy = 1;
+}
+
+rs_status upload_pool(rs_solver* s, size_t from) {
+  size_t to = s->pool.size();
+  if (to == from) return RS_OK;
+  CU(s->dofs.ensure_keep(to, from, s->stream));
+  CU(s->perm.ensure_keep(to, from, s->stream));
+  CU(cudaMemcpyAsync(s->dofs.p + from, s->pool.data() + from, (to - from) * sizeof(int),
+                     cudaMemcpyHostToDevice, s->stream));
+  return RS_OK;
+}
+
+double id_flops(int m, int n, int k, int pde) {
+  const double per = pde == kStokes ? 20.0 : 10.0;
+  const double r = n - k;
+  return per * m * n + 4.0 * m * n * k - 2.0 * k * k * (m + n) + 4.0 * k * k * k / 3.0 +
+         (double)k * k * r;
+}
+double dec_flops(int k, int r) {
+  const double K = k, R = r;
+  return 2.0 * (R * K * K + 2 * R * R * K + R * K * K + K * K * R) + 2.0 / 3.0 * R * R * R +
+         4.0 * R * R * K + 2.0 * K * K * R;
+}
+
+template <class Real>
+Factor<Real>& factor_of(rs_solver* s);
+template <>
+Factor<double>& factor_of<double>(rs_solver* s) { return s->F64; }
+template <>
+Factor<float>& factor_of<float>(rs_solver* s) { return s->F32; }
+
+// Splits tasks into launches of similar size (so the shared-memory request of
+// a launch fits its boxes) and launches them.
+template <class Task, class Launch>
+void launch_binned(const std::vector<Task>& tasks, const Task* dev_tasks, Launch&& fn) {
+  // tasks are pre-sorted by n; group consecutive tasks with equal ceil(n/32)
+  size_t i = 0;
+  while (i < tasks.size()) {
+    int cls = (tasks[i].n + 31) / 32;
+    size_t j = i;
+    int nmax = 0;
+    while (j < tasks.size() && (tasks[j].n + 31) / 32 == cls) {
+      nmax = std::max(nmax, tasks[j].n);
+      ++j;
+    }
+    fn(dev_tasks + i, (int)(j - i), nmax);
+    i = j;
+  }
+}
+
+template <class Real>
+rs_status factor_border(rs_solver* s);
+
+template <class Real>
+rs_status factor_impl(rs_solver* s) {
+  constexpr bool f32 = sizeof(Real) == 4;
+  Factor<Real>& F = factor_of<Real>(s);
+  const int L = (int)s->tree.levels.size();
+  const double tol = f32 ? std::max(s->cfg.id_tol, s->cfg.fp32_id_tol) : s->cfg.id_tol;
+  s->st.assign(s->tree.nodes.size(), NodeState());
+  s->pool.clear();
+  F.fac_used = 0;
+  F.e_used = 0;
+  s->piv_used = 0;
+  s->stats.id_flops = 0;
+  s->stats.decouple_flops = 0;
+  s->stats.id_ms = 0;
+  s->stats.decouple_ms = 0;
+  s->launches = 0;
+  s->stats.max_active = 0;
+  s->stats.max_rank = 0;
+  s->stats.max_rows = 0;
+  CU(cudaMemsetAsync(s->status.p, 0, sizeof(int) * 4, s->stream));
+  std::vector<IdTask> idt;
+  std::vector<DecoupleTask> dct;
+  std::vector<BlkRef> blk;
+  std::vector<int> rows;
+  std::vector<int> cand_ids, dc_ids;
+  std::vector<int> m_of_slot;
+  // Contents below these marks are live and survive buffer growth.
+  size_t fac_prev = 0, e_prev = 0, piv_prev = 0;
+  for (int lv = L - 1; lv >= 1; --lv) {
+    const std::vector<int>& lvl = s->tree.levels[lv];
+    for (int id : lvl)
+      if (!s->st[id].compressed) compute_active(s, id);
+    for (int id : lvl) compute_near(s, id);
+    idt.clear();
+    dct.clear();
+    blk.clear();
+    cand_ids.clear();
+    dc_ids.clear();
+    m_of_slot.clear();
+    const size_t seg0 = s->pool.size();
+    const int npp = s->cfg.num_proxy_points;
+    const int prow = (s->cfg.pde == kStokes ? 2 : 1) * npp;
+    for (int id : lvl) {
+      NodeState& S = s->st[id];
+      const TreeNode& nd = s->tree.nodes[id];
+      const int n = (int)S.active.size();
+      const bool cand = !S.compressed && n >= s->cfg.min_dofs_to_compress;
+      if (!cand && nd.is_leaf) {
+        S.e_ld = 0;
+        continue;
+      }
+      const int act_off = (int)s->pool.size();
+      s->pool.insert(s->pool.end(), S.active.begin(), S.active.end());
+      S.fac_off = -1;
+      S.slot = -1;
+      if (cand) {
+        int use_proxy = 0;
+        id_rows(s, id, &rows, &use_proxy);
+        const int rows_off = (int)s->pool.size();
+        s->pool.insert(s->pool.end(), rows.begin(), rows.end());
+        IdTask t{};
+        t.n = n;
+        t.act_off = act_off;
+        t.q = (int)rows.size();
+        t.rows_off = rows_off;
+        t.use_proxy = use_proxy;
+        t.slot = (int)idt.size();
+        t.cx = nd.corners[0] + nd.side / 2.0;
+        t.cy = nd.corners[1] + nd.side / 2.0;
+        t.pr = nd.side * s->cfg.radius_ratio;
+        t.fac_off = (int64_t)F.fac_used;
+        t.scratch_off = -1;
+        t.dense_off = -1;
+        t.m_dense = 0;
+        F.fac_used += fac_reserve(n);
+        S.slot = t.slot;
+        S.fac_off = t.fac_off;
+        const int m = 2 * t.q + (use_proxy ? 2 * prow : 0);
+        m_of_slot.push_back(m);
+        s->stats.max_rows = std::max(s->stats.max_rows, m);
+        idt.push_back(t);
+        cand_ids.push_back(id);
+      }
+      DecoupleTask d{};
+      d.n = n;
+      d.act_off = act_off;
+      d.blk_off = (int)blk.size();
+      d.slot = S.slot;
+      d.perm_off = act_off;
+      d.fac_off = S.fac_off;
+      d.piv_off = (int64_t)s->piv_used;
+      s->piv_used += n;
+      d.e_off = (int64_t)F.e_used;
+      F.e_used += (size_t)n * n;
+      d.scratch_off = -1;
+      S.piv_off = d.piv_off;
+      S.e_off = d.e_off;
+      if (nd.is_leaf) {
+        for (int j = 0; j < n; ++j) blk.push_back(BlkRef{0, j, 0, 0, -1});
+      } else {
+        for (int c = 0; c < 4; ++c) {
+          const NodeState& C = s->st[nd.children[c]];
+          const std::vector<int>& v = surviving(C);
+          for (int j = 0; j < (int)v.size(); ++j)
+            blk.push_back(BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1});
+        }
+      }
+      dct.push_back(d);
+      dc_ids.push_back(id);
+      s->stats.max_active = std::max(s->stats.max_active, n);
+    }
+    if (dct.empty()) continue;
+    // sort by size for binned launches (slots keep their identity)
+    std::vector<size_t> oi(idt.size()), od(dct.size());
+    for (size_t i = 0; i < oi.size(); ++i) oi[i] = i;
+    for (size_t i = 0; i < od.size(); ++i) od[i] = i;
+    std::stable_sort(oi.begin(), oi.end(), [&](size_t a, size_t b) { return idt[a].n < idt[b].n; });
+    std::stable_sort(od.begin(), od.end(), [&](size_t a, size_t b) { return dct[a].n < dct[b].n; });
+    std::vector<IdTask> idt_s(idt.size());
+    std::vector<DecoupleTask> dct_s(dct.size());
+    for (size_t i = 0; i < oi.size(); ++i) idt_s[i] = idt[oi[i]];
+    for (size_t i = 0; i < od.size(); ++i) dct_s[i] = dct[od[i]];
+    // global-memory tiles for boxes whose tiles do not fit in shared memory
+    size_t scratch_need = 0;
+    for (IdTask& t : idt_s)
+      if (id_kernel_smem(t.n, f32, true) > kSmemMax) {
+        t.scratch_off = (int64_t)scratch_need;
+        scratch_need += (size_t)t.n * t.n + 64 * (size_t)t.n + 64;
+      }
+    for (DecoupleTask& t : dct_s)
+      if (decouple_kernel_smem(t.n, f32, true) > kSmemMax) {
+        t.scratch_off = (int64_t)scratch_need;
+        scratch_need += (size_t)(t.n + 1) * (t.n + 1) * 2;
+      }
+    // upload
+    RSCHK(upload_pool(s, seg0));
+    CU(F.fac.ensure_keep(F.fac_used, fac_prev, s->stream));
+    CU(F.epool.ensure_keep(F.e_used, e_prev, s->stream));
+    CU(s->piv.ensure_keep(s->piv_used, piv_prev, s->stream));
+    fac_prev = F.fac_used;
+    e_prev = F.e_used;
+    piv_prev = s->piv_used;
+    if (scratch_need) CU(F.scratch.ensure(scratch_need));
+    CU(s->id_tasks.ensure(std::max<size_t>(idt_s.size(), 1)));
+    CU(s->dc_tasks.ensure(dct_s.size()));
+    CU(s->blk.ensure(std::max<size_t>(blk.size(), 1)));
+    CU(s->ranks.ensure(std::max<size_t>(idt_s.size(), 1)));
+    if (!idt_s.empty())
+      CU(cudaMemcpyAsync(s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask),
+                         cudaMemcpyHostToDevice, s->stream));
+    CU(cudaMemcpyAsync(s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask),
+                       cudaMemcpyHostToDevice, s->stream));
+    if (!blk.empty())
+      CU(cudaMemcpyAsync(s->blk.p, blk.data(), blk.size() * sizeof(BlkRef),
+                         cudaMemcpyHostToDevice, s->stream));
+    // ID launches
+    IdParams ip{};
+    ip.geo = geo_of(s);
+    ip.pde = s->cfg.pde;
+    ip.sd = s->sd;
+    ip.npp = s->cfg.num_proxy_points;
+    ip.tol = tol;
+    ip.tasks = s->id_tasks.p;
+    ip.dofs = s->dofs.p;
+    ip.pxy_cos = s->pxy_c.p;
+    ip.pxy_sin = s->pxy_s.p;
+    ip.ranks = s->ranks.p;
+    ip.perm = s->perm.p;
+    ip.fac = F.fac.p;
+    ip.scratch = F.scratch.p;
+    ip.dense = nullptr;
+    CU(cudaEventRecord(s->ev_a, s->stream));
+    launch_binned(idt_s, s->id_tasks.p, [&](const IdTask* dt, int cnt, int nmax) {
+      IdParams q = ip;
+      q.tasks = dt;
+      bool in_smem = id_kernel_smem(nmax, f32, true) <= kSmemMax;
+      launch_id(q, cnt, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
+      ++s->launches;
+    });
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(s->ev_b, s->stream));
+    // decouple launches
+    DecoupleParams dp{};
+    dp.geo = geo_of(s);
+    dp.pde = s->cfg.pde;
+    dp.sd = s->sd;
+    dp.tasks = s->dc_tasks.p;
+    dp.dofs = s->dofs.p;
+    dp.blk = s->blk.p;
+    dp.ranks = s->ranks.p;
+    dp.perm = s->perm.p;
+    dp.fac = F.fac.p;
+    dp.piv = s->piv.p;
+    dp.epool = F.epool.p;
+    dp.scratch = F.scratch.p;
+    dp.status = s->status.p;
+    launch_binned(dct_s, s->dc_tasks.p, [&](const DecoupleTask* dt, int cnt, int nmax) {
+      DecoupleParams q = dp;
+      q.tasks = dt;
+      bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
+      launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream);
+      ++s->launches;
+    });
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(s->ev_f1, s->stream));
+    // read back ranks and pivots
+    const size_t seg1 = s->pool.size();
+    CU(s->h_ranks.ensure(std::max<size_t>(idt.size(), 1)));
+    CU(s->h_perm.ensure(seg1 - seg0 + 1));
+    if (!idt.empty())
+      CU(cudaMemcpyAsync(s->h_ranks.p, s->ranks.p, idt.size() * sizeof(int),
+                         cudaMemcpyDeviceToHost, s->stream));
+    CU(cudaMemcpyAsync(s->h_perm.p, s->perm.p + seg0, (seg1 - seg0) * sizeof(int),
+                       cudaMemcpyDeviceToHost, s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+    float ms_id = 0, ms_dc = 0;
+    cudaEventElapsedTime(&ms_id, s->ev_a, s->ev_b);
+    cudaEventElapsedTime(&ms_dc, s->ev_b, s->ev_f1);
+    s->stats.id_ms += ms_id;
+    s->stats.decouple_ms += ms_dc;
+    for (size_t c = 0; c < cand_ids.size(); ++c) {
+      const int id = cand_ids[c];
+      NodeState& S = s->st[id];
+      const int k = s->h_ranks.p[S.slot];
+      const int n = (int)S.active.size();
+      s->stats.id_flops += id_flops(m_of_slot[S.slot], n, k, s->cfg.pde);
+      if (k <= 0) {
+        S.e_ld = n;
+        continue;
+      }
+      const int act_off = idt[S.slot].act_off;
+      S.compressed = 1;
+      S.k = k;
+      S.r = n - k;
+      S.perm.assign(s->h_perm.p + (act_off - seg0), s->h_perm.p + (act_off - seg0) + n);
+      S.skel.clear();
+      S.red.clear();
+      for (int i = 0; i < k; ++i) S.skel.push_back(S.active[S.perm[i]]);
+      for (int i = k; i < n; ++i) S.red.push_back(S.active[S.perm[i]]);
+      S.e_ld = k;
+      s->stats.max_rank = std::max(s->stats.max_rank, k);
+      s->stats.decouple_flops += dec_flops(k, n - k);
+    }
+    for (int id : dc_ids) {
+      NodeState& S = s->st[id];
+      if (S.slot < 0) S.e_ld = (int)S.active.size();
+    }
+  }
+  // remove_inactive_dofs_at_all_boxes (quadtree.cpp:989-995): only the root
+  // (and level-0 bookkeeping) changes for a fresh factorization.
+  {
+    const int root = s->tree.root;
+    compute_active(s, root);
+    compute_near(s, root);
+  }
+  // root block (skel_factorization.cpp:174-186)
+  NodeState& R = s->st[s->tree.root];
+  s->allskel = R.active;
+  s->ns = (int)s->allskel.size();
+  const size_t seg0 = s->pool.size();
+  s->allskel_off = (int)seg0;
+  s->pool.insert(s->pool.end(), s->allskel.begin(), s->allskel.end());
+  std::vector<BlkRef> rblk;
+  const TreeNode& rn = s->tree.nodes[s->tree.root];
+  if (rn.is_leaf) {
+    for (int j = 0; j < s->ns; ++j) rblk.push_back(BlkRef{0, j, 0, 0, -1});
+  } else {
+    for (int c = 0; c < 4; ++c) {
+      const NodeState& C = s->st[rn.children[c]];
+      const std::vector<int>& v = surviving(C);
+      for (int j = 0; j < (int)v.size(); ++j)
+        rblk.push_back(BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1});
+    }
+  }
+  // solve plan: compressed boxes per level, skeleton / redundant lists
+  s->sweeps.clear();
+  s->sweep_off.assign(L, 0);
+  s->sweep_cnt.assign(L, 0);
+  s->sweep_nmax.assign(L, 0);
+  for (int lv = L - 1; lv >= 1; --lv) {
+    s->sweep_off[lv] = (int)s->sweeps.size();
+    for (int id : s->tree.levels[lv]) {
+      const NodeState& S = s->st[id];
+      if (!S.compressed) continue;
+      SweepTask t{};
+      t.k = S.k;
+      t.r = S.r;
+      t.skel_off = (int)s->pool.size();
+      s->pool.insert(s->pool.end(), S.skel.begin(), S.skel.end());
+      t.red_off = (int)s->pool.size();
+      s->pool.insert(s->pool.end(), S.red.begin(), S.red.end());
+      t.fac_off = S.fac_off;
+      t.piv_off = S.piv_off;
+      s->sweeps.push_back(t);
+      s->sweep_nmax[lv] = std::max(s->sweep_nmax[lv], S.k + S.r);
+    }
+    s->sweep_cnt[lv] = (int)s->sweeps.size() - s->sweep_off[lv];
+  }
+  RSCHK(upload_pool(s, seg0));
+  CU(s->sweep_dev.ensure(std::max<size_t>(s->sweeps.size(), 1)));
+  if (!s->sweeps.empty())
+    CU(cudaMemcpyAsync(s->sweep_dev.p, s->sweeps.data(), s->sweeps.size() * sizeof(SweepTask),
+                       cudaMemcpyHostToDevice, s->stream));
+  s->root_e_off = (int64_t)F.e_used;
+  F.e_used += (size_t)s->ns * s->ns;
+  CU(F.epool.ensure_keep(F.e_used, e_prev, s->stream));
+  if (s->ns > 0) {
+    DecoupleTask d{};
+    d.n = s->ns;
+    d.act_off = s->allskel_off;
+    d.blk_off = 0;
+    d.slot = -1;
+    d.perm_off = s->allskel_off;
+    d.fac_off = 0;
+    d.piv_off = 0;
+    d.e_off = s->root_e_off;
+    d.scratch_off = -1;
+    bool in_smem = decouple_kernel_smem(s->ns, f32, true) <= kSmemMax;
+    if (!in_smem) {
+      d.scratch_off = 0;
+      CU(F.scratch.ensure((size_t)(s->ns + 1) * (s->ns + 1) * 2));
+    }
+    CU(s->blk.ensure(rblk.size()));
+    CU(cudaMemcpyAsync(s->blk.p, rblk.data(), rblk.size() * sizeof(BlkRef),
+                       cudaMemcpyHostToDevice, s->stream));
+    CU(s->dc_tasks.ensure(1));
+    CU(cudaMemcpyAsync(s->dc_tasks.p, &d, sizeof(d), cudaMemcpyHostToDevice, s->stream));
+    DecoupleParams dp{};
+    dp.geo = geo_of(s);
+    dp.pde = s->cfg.pde;
+    dp.sd = s->sd;
+    dp.tasks = s->dc_tasks.p;
+    dp.dofs = s->dofs.p;
+    dp.blk = s->blk.p;
+    dp.ranks = s->ranks.p;
+    dp.perm = s->perm.p;
+    dp.fac = F.fac.p;
+    dp.piv = s->piv.p;
+    dp.epool = F.epool.p;
+    dp.scratch = F.scratch.p;
+    dp.status = s->status.p;
+    launch_decouple(dp, 1, decouple_kernel_smem(s->ns, f32, in_smem), f32, s->stream);
+    ++s->launches;
+    CU(cudaGetLastError());
+  }
+  s->nb = 0;
+  if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann) {
+    // bordered system, skel_factorization.cpp:188-305
+    rs_status rc = factor_border<Real>(s);
+    if (rc != RS_OK) return rc;
+  } else if (s->ns > 0) {
+    CU(s->root_piv.ensure(s->ns));
+    Real* a = F.epool.p + s->root_e_off;
+    if (f32) launch_dense_lu_f32((float*)a, s->ns, s->root_piv.p, s->status.p, s->stream);
+    else launch_dense_lu((double*)a, s->ns, s->root_piv.p, s->status.p, s->stream);
+    ++s->launches;
+  }
+  CU(cudaGetLastError());
+  return RS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// bordered system (holes): linear_solve.cpp:20-112 and
+// skel_factorization.cpp:188-305, 596-777
+// ---------------------------------------------------------------------------
+namespace {
+
+void build_border_host(rs_solver* s) {
+  const int h = s->nh, N = s->n, D = s->D;
+  s->nb = s->cfg.pde == kStokes ? 3 * h : h;
+  const int nb = s->nb;
+  s->Uh.assign((size_t)D * nb, 0.0);
+  s->Psih.assign((size_t)nb * D, 0.0);
+  for (int i = 0; i < N; ++i) {
+    const double x0 = s->pts[2 * i], x1 = s->pts[2 * i + 1];
+    for (int hi = 0; hi < h; ++hi) {
+      const double r0 = x0 - s->hc[2 * hi], r1 = x1 - s->hc[2 * hi + 1];
+      const double rn = std::sqrt(r0 * r0 + r1 * r1);
+      if (s->cfg.pde == kLaplace) {
+        s->Uh[i + (size_t)D * hi] = std::log(rn);
+      } else {
+        const double scale = 1.0 / (4 * M_PI);
+        const double r2 = rn * rn;
+        double* U = s->Uh.data();
+        U[2 * i + (size_t)D * (3 * hi)] = scale * (std::log(1 / rn) + (1.0 / r2) * r0 * r0);
+        U[2 * i + 1 + (size_t)D * (3 * hi)] = scale * ((1.0 / r2) * r1 * r0);
+        U[2 * i + (size_t)D * (3 * hi + 1)] = scale * ((1.0 / r2) * r0 * r1);
+        U[2 * i + 1 + (size_t)D * (3 * hi + 1)] = scale * (std::log(1 / rn) + (1.0 / r2) * r1 * r1);
+        U[2 * i + (size_t)D * (3 * hi + 2)] = r1 * (scale / r2);
+        U[2 * i + 1 + (size_t)D * (3 * hi + 2)] = -r0 * (scale / r2);
+      }
+    }
+    for (int hi = 0; hi < h; ++hi) {
+      const double r0 = x0 - s->hc[2 * hi], r1 = x1 - s->hc[2 * hi + 1];
+      if (std::sqrt(r0 * r0 + r1 * r1) < s->hr[hi] + 1e-8) {
+        const double wi = s->w[i];
+        if (s->cfg.pde == kLaplace) {
+          s->Psih[hi + (size_t)nb * i] = wi;
+        } else {
+          s->Psih[3 * hi + (size_t)nb * (2 * i)] = wi;
+          s->Psih[3 * hi + 1 + (size_t)nb * (2 * i + 1)] = wi;
+          s->Psih[3 * hi + 2 + (size_t)nb * (2 * i)] = wi * x1;
+          s->Psih[3 * hi + 2 + (size_t)nb * (2 * i + 1)] = -wi * x0;
+        }
+        break;
+      }
+    }
+  }
+}
+
+template <class Real>
+void sweep_levels(rs_solver* s, Real* x, int ld, int nrhs, int mode, bool up) {
+  Factor<Real>& F = factor_of<Real>(s);
+  const int L = (int)s->tree.levels.size();
+  SweepParams sp{};
+  sp.dofs = s->dofs.p;
+  sp.fac = F.fac.p;
+  sp.piv = s->piv.p;
+  sp.x = x;
+  sp.ld = ld;
+  sp.nrhs = nrhs;
+  sp.mode = mode;
+  for (int step = 0; step < L - 1; ++step) {
+    const int lv = up ? L - 1 - step : 1 + step;
+    if (!s->sweep_cnt[lv]) continue;
+    sp.tasks = s->sweep_dev.p + s->sweep_off[lv];
+    launch_sweep(sp, s->sweep_cnt[lv], s->sweep_nmax[lv], sizeof(Real) == 4, s->stream);
+    ++s->launches;
+  }
+}
+
+template <class Real>
+rs_status factor_border(rs_solver* s) {
+  Factor<Real>& F = factor_of<Real>(s);
+  build_border_host(s);
+  const int D = s->D, nb = s->nb, ns = s->ns;
+  std::vector<unsigned char> red(D, 1), sk(D, 0);
+  for (int i : s->allskel) {
+    red[i] = 0;
+    sk[i] = 1;
+  }
+  bool any_red = false;
+  for (unsigned char c : red) any_red |= c != 0;
+  if (!any_red) return fail(s, RS_ERR_NO_COMPRESSION, "No compression possible");
+  CU(s->red_mask.ensure(D));
+  CU(s->skel_mask.ensure(D));
+  CU(cudaMemcpyAsync(s->red_mask.p, red.data(), D, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemcpyAsync(s->skel_mask.p, sk.data(), D, cudaMemcpyHostToDevice, s->stream));
+  CU(s->U0.ensure((size_t)D * nb));
+  CU(s->PsiT0.ensure((size_t)D * nb));
+  CU(cudaMemcpyAsync(s->U0.p, s->Uh.data(), (size_t)D * nb * 8, cudaMemcpyHostToDevice,
+                     s->stream));
+  CU(F.mU.ensure((size_t)D * nb));
+  CU(F.mP.ensure((size_t)D * nb));
+  CU(F.tmp.ensure((size_t)D * nb));
+  convert_from_double<Real>(s->U0.p, F.mU.p, (size_t)D * nb, s->stream);
+  // Psi (nb x D) staged through tmp storage, stored transposed (D x nb)
+  {
+    DevBuf<double> psi;
+    CU(psi.ensure((size_t)D * nb));
+    CU(cudaMemcpyAsync(psi.p, s->Psih.data(), (size_t)D * nb * 8, cudaMemcpyHostToDevice,
+                       s->stream));
+    transpose_to<double>(psi.p, nb, D, s->PsiT0.p, s->stream);
+    convert_from_double<Real>(s->PsiT0.p, F.mP.p, (size_t)D * nb, s->stream);
+    CU(cudaStreamSynchronize(s->stream));
+  }
+  // sweeps on U (with L) and Psi^T (with U^T), skel_factorization.cpp:229-266
+  sweep_levels<Real>(s, F.mU.p, D, nb, kUpPlain, true);
+  sweep_levels<Real>(s, F.mP.p, D, nb, kUpTransU, true);
+  // D^{-1} C on a copy of the modified U (redundant rows), :268-285
+  CU(cudaMemcpyAsync(F.tmp.p, F.mU.p, (size_t)D * nb * sizeof(Real), cudaMemcpyDeviceToDevice,
+                     s->stream));
+  sweep_levels<Real>(s, F.tmp.p, D, nb, kDiagOnly, true);
+  CU(s->G.ensure((size_t)nb * nb));
+  masked_cross<Real>(F.mP.p, D, nb, F.tmp.p, D, nb, s->red_mask.p, D, s->G.p, nb, s->stream);
+  const int SN = ns + nb;
+  CU(F.S.ensure((size_t)SN * SN));
+  assemble_s<Real>(F.S.p, ns, nb, F.epool.p + s->root_e_off, F.mU.p, F.mP.p, D,
+                   s->dofs.p + s->allskel_off, s->G.p, s->stream);
+  CU(s->S_piv.ensure(SN));
+  if (sizeof(Real) == 4)
+    launch_dense_lu_f32((float*)F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+  else
+    launch_dense_lu((double*)F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+  s->launches += 4;
+  CU(cudaGetLastError());
+  return RS_OK;
+}
+
+// multiply_connected_solve (skel_factorization.cpp:596-777) for one column x
+// (device, Real, length D) with second-block right-hand side g (nb, may be
+// null = 0).  On return x = mu and alpha (device, Real, nb) is set.
+template <class Real>
+rs_status solve_border_col(rs_solver* s, Real* x, Real* alpha, const double* g) {
+  Factor<Real>& F = factor_of<Real>(s);
+  const int D = s->D, nb = s->nb, ns = s->ns, SN = ns + nb;
+  CU(F.nv.ensure(D));
+  CU(F.M.ensure(SN));
+  CU(s->g1.ensure(2 * (size_t)nb));
+  sweep_levels<Real>(s, x, D, 1, kUpPlain, true);
+  CU(cudaMemcpyAsync(F.nv.p, x, D * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
+  sweep_levels<Real>(s, F.nv.p, D, 1, kDiagOnly, true);
+  masked_cross<Real>(F.mP.p, D, nb, F.nv.p, D, 1, s->red_mask.p, D, s->g1.p, nb, s->stream);
+  if (g) launch_axpby(s->g1.p, g, -1.0, 1.0, nb, s->stream);  // g1 <- g1 - g
+  border_rhs<Real>(F.M.p, ns, nb, x, s->dofs.p + s->allskel_off, s->g1.p, s->stream);
+  launch_dense_solve_gather(F.S.p, sizeof(Real) == 4, SN, s->S_piv.p, nullptr, F.M.p, SN, 1,
+                            s->stream);
+  CU(cudaMemcpyAsync(alpha, F.M.p + ns, nb * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
+  border_sub<Real>(F.nv.p, x, F.mU.p, D, nb, alpha, s->red_mask.p, s->stream);
+  sweep_levels<Real>(s, F.nv.p, D, 1, kDiagOnly, true);
+  border_merge<Real>(x, F.nv.p, s->red_mask.p, D, s->dofs.p + s->allskel_off, F.M.p, ns,
+                     s->stream);
+  sweep_levels<Real>(s, x, D, 1, kDown, false);
+  s->launches += 8;
+  CU(cudaGetLastError());
+  return RS_OK;
+}
+
+// Applies the factorization inverse in place to x (device, Real, D x nrhs);
+// alpha (device, Real, nb x nrhs) for bordered systems; g (device, double,
+// nb x nrhs) is the second-block right-hand side (null = 0).
+template <class Real>
+rs_status apply_inverse(rs_solver* s, Real* x, int nrhs, Real* alpha, const double* g) {
+  Factor<Real>& F = factor_of<Real>(s);
+  if (s->nb == 0) {
+    sweep_levels<Real>(s, x, s->D, nrhs, kUpSolve, true);
+    if (s->ns > 0) {
+      launch_dense_solve_gather(F.epool.p + s->root_e_off, sizeof(Real) == 4, s->ns,
+                                s->root_piv.p, s->dofs.p + s->allskel_off, x, s->D, nrhs,
+                                s->stream);
+      ++s->launches;
+    }
+    sweep_levels<Real>(s, x, s->D, nrhs, kDown, false);
+    CU(cudaGetLastError());
+    return RS_OK;
+  }
+  for (int c = 0; c < nrhs; ++c) {
+    rs_status rc = solve_border_col<Real>(s, x + (size_t)s->D * c, alpha + (size_t)s->nb * c,
+                                          g ? g + (size_t)s->nb * c : nullptr);
+    if (rc != RS_OK) return rc;
+  }
+  return RS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// solves and FP64 refinement
+// ---------------------------------------------------------------------------
+namespace rskel {
+void launch_col_norms(const double* x, int rows, int cols, double* out, cudaStream_t st);
+void launch_gemv_sub(double* r, const double* U, const double* a, int D, int nb, cudaStream_t st);
+}  // namespace rskel
+
+namespace {
+
+// r = f - K mu - U alpha;  rg = alpha - Psi mu  (bordered operator of
+// ie_solver_test.cpp:43-83, [K U; Psi -I]).
+rs_status residual(rs_solver* s, const double* f, const double* mu, const double* alpha,
+                   int nrhs, double* r, double* rg) {
+  const int D = s->D;
+  launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, mu, nrhs, r, s->stream);
+  launch_axpby(r, f, 1.0, -1.0, (size_t)D * nrhs, s->stream);
+  s->launches += 2;
+  if (s->nb > 0) {
+    const int nb = s->nb;
+    for (int c = 0; c < nrhs; ++c) {
+      launch_gemv_sub(r + (size_t)D * c, s->U0.p, alpha + (size_t)nb * c, D, nb, s->stream);
+      masked_cross<double>(s->PsiT0.p, D, nb, mu + (size_t)D * c, D, 1, s->ones_mask.p, D,
+                           rg + (size_t)nb * c, nb, s->stream);
+      launch_axpby(rg + (size_t)nb * c, alpha + (size_t)nb * c, 1.0, -1.0, nb, s->stream);
+      s->launches += 3;
+    }
+  }
+  CU(cudaGetLastError());
+  return RS_OK;
+}
+
+rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu, double* alpha) {
+  const int D = s->D, nb = s->nb;
+  const size_t nd = (size_t)D * nrhs;
+  if (!s->fp32) {
+    Factor<double>& F = s->F64;
+    CU(F.x.ensure(nd));
+    CU(F.M.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
+    CU(cudaMemcpyAsync(F.x.p, f, nd * 8, cudaMemcpyDeviceToDevice, s->stream));
+    rs_status rc = apply_inverse<double>(s, F.x.p, nrhs, alpha, nullptr);
+    if (rc != RS_OK) return rc;
+    CU(cudaMemcpyAsync(mu, F.x.p, nd * 8, cudaMemcpyDeviceToDevice, s->stream));
+    s->stats.refine_iters = 0;
+    return RS_OK;
+  }
+  // FP32 factorization + FP64 iterative refinement
+  Factor<float>& F = s->F32;
+  CU(F.x.ensure(nd));
+  CU(F.tmp.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
+  CU(s->r64.ensure(nd));
+  CU(s->acc64.ensure(std::max<size_t>(2 * (size_t)nb * nrhs, 1)));
+  CU(s->nrm_dev.ensure(2 * (size_t)nrhs + 2));
+  CU(s->h_io.ensure(4 * (size_t)nrhs + 4));
+  double* rg = s->acc64.p;
+  double* a64 = alpha;
+  CU(cudaMemsetAsync(mu, 0, nd * 8, s->stream));
+  if (nb) CU(cudaMemsetAsync(a64, 0, (size_t)nb * nrhs * 8, s->stream));
+  CU(cudaMemcpyAsync(s->r64.p, f, nd * 8, cudaMemcpyDeviceToDevice, s->stream));
+  launch_col_norms(f, D, nrhs, s->nrm_dev.p, s->stream);
+  CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  std::vector<double> fn(s->h_io.p, s->h_io.p + nrhs);
+  int it = 0;
+  double worst = 0;
+  const int max_it = std::max(1, s->cfg.refine_max_iters);
+  for (it = 0; it < max_it; ++it) {
+    launch_d2f(s->r64.p, F.x.p, nd, s->stream);
+    rs_status rc = apply_inverse<float>(s, F.x.p, nrhs, F.tmp.p, it == 0 || !nb ? nullptr : rg);
+    if (rc != RS_OK) return rc;
+    launch_add_f2d(mu, F.x.p, nd, s->stream);
+    if (nb) launch_add_f2d(a64, F.tmp.p, (size_t)nb * nrhs, s->stream);
+    s->launches += 3;
+    rc = residual(s, f, mu, a64, nrhs, s->r64.p, rg);
+    if (rc != RS_OK) return rc;
+    launch_col_norms(s->r64.p, D, nrhs, s->nrm_dev.p, s->stream);
+    CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+    worst = 0;
+    for (int c = 0; c < nrhs; ++c) {
+      double rel = fn[c] > 0 ? s->h_io.p[c] / fn[c] : s->h_io.p[c];
+      worst = std::max(worst, rel);
+    }
+    if (worst <= s->cfg.refine_tol) { ++it; break; }
+  }
+  s->stats.refine_iters = it;
+  s->stats.refine_residual = worst;
+  return RS_OK;
+}
+
+rs_status check_solver(rs_solver* s) {
+  if (!s) return RS_ERR_ARG;
+  return RS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void rs_config_default(rs_config* c) {
+  if (!c) return;
+  c->pde = RS_LAPLACE;
+  c->solution_dimension = 1;
+  c->domain_dimension = 2;
+  c->id_tol = 1e-6;
+  c->max_leaf_dofs = 32;
+  c->num_proxy_points = 128;
+  c->radius_ratio = 1.5;
+  c->min_dofs_to_compress = 16;
+  c->is_strong_admissibility = 0;
+  c->precision = RS_FP64;
+  c->refine_tol = 1e-12;
+  c->refine_max_iters = 10;
+  c->fp32_id_tol = 1e-6;
+  c->device = 0;
+}
+
+rs_status rs_create(const rs_config* cfg, rs_solver** out) {
+  if (!cfg || !out) return RS_ERR_ARG;
+  *out = nullptr;
+  if (cfg->pde < 0 || cfg->pde > 2) return RS_ERR_ARG;
+  const int want_sd = cfg->pde == RS_STOKES ? 2 : 1;
+  if (cfg->solution_dimension != want_sd || cfg->domain_dimension != 2) return RS_ERR_ARG;
+  if (!(cfg->id_tol > 0) || cfg->max_leaf_dofs < 1 || cfg->num_proxy_points < 1 ||
+      !(cfg->radius_ratio > 0) || cfg->min_dofs_to_compress < 1)
+    return RS_ERR_ARG;
+  if (cfg->is_strong_admissibility) return RS_ERR_ARG;
+  if (cfg->precision != RS_FP64 && cfg->precision != RS_FP32_REFINE) return RS_ERR_ARG;
+  rs_solver* s = new rs_solver();
+  s->cfg = *cfg;
+  s->sd = want_sd;
+  s->fp32 = cfg->precision == RS_FP32_REFINE;
+  if (s->fp32 && !(s->cfg.fp32_id_tol > 0)) s->cfg.fp32_id_tol = 1e-6;
+  std::memset(&s->stats, 0, sizeof(s->stats));
+  *out = s;
+  return RS_OK;
+}
+
+rs_status rs_destroy(rs_solver* s) {
+  if (!s) return RS_ERR_ARG;
+  if (s->dev_ready) {
+    cudaSetDevice(s->cfg.device);
+    cudaStreamSynchronize(s->stream);
+    cudaEventDestroy(s->ev_t0);
+    cudaEventDestroy(s->ev_t1);
+    cudaEventDestroy(s->ev_a);
+    cudaEventDestroy(s->ev_b);
+    cudaEventDestroy(s->ev_f0);
+    cudaEventDestroy(s->ev_f1);
+  }
+  cudaStream_t st = s->stream;
+  delete s;  // device buffers free themselves
+  if (st) cudaStreamDestroy(st);
+  return RS_OK;
+}
+
+rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
+                          const double* normals, const double* weights, const double* curvatures,
+                          int num_holes, const double* hole_centers, const double* hole_radii) {
+  if (!s || num_points <= 0 || !points || !normals || !weights || !curvatures || num_holes < 0)
+    return fail(s, RS_ERR_ARG, "bad geometry arguments");
+  if (num_holes > 0 && (!hole_centers || !hole_radii))
+    return fail(s, RS_ERR_ARG, "holes need centres and radii");
+  for (int i = 0; i < 2 * num_points; ++i)
+    if (!std::isfinite(points[i]) || !std::isfinite(normals[i]))
+      return fail(s, RS_ERR_NUMERIC, "non-finite point or normal");
+  for (int i = 0; i < num_points; ++i)
+    if (!std::isfinite(weights[i]) || !std::isfinite(curvatures[i]))
+      return fail(s, RS_ERR_NUMERIC, "non-finite weight or curvature");
+  s->n = num_points;
+  s->D = num_points * s->sd;
+  s->pts.assign(points, points + 2 * (size_t)num_points);
+  s->nrm.assign(normals, normals + 2 * (size_t)num_points);
+  s->w.assign(weights, weights + num_points);
+  s->kap.assign(curvatures, curvatures + num_points);
+  s->nh = num_holes;
+  s->hc.assign(hole_centers ? hole_centers : points, hole_centers ? hole_centers + 2 * num_holes : points);
+  s->hr.assign(hole_radii ? hole_radii : points, hole_radii ? hole_radii + num_holes : points);
+  s->tree_built = false;
+  s->factored = false;
+  s->geo_on_dev = false;
+  return RS_OK;
+}
+
+rs_status rs_build_tree(rs_solver* s) {
+  if (!s) return RS_ERR_ARG;
+  if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
+  double t0 = now_ms();
+  if (!s->tree.build(s->pts.data(), s->n, s->sd, s->cfg.max_leaf_dofs))
+    return fail(s, RS_ERR_ARG, "tree build failed");
+  s->tree_built = true;
+  s->factored = false;
+  s->st.assign(s->tree.nodes.size(), NodeState());
+  s->stats.t_tree_ms = now_ms() - t0;
+  s->stats.num_levels = (int)s->tree.levels.size();
+  s->stats.num_nodes = (int)s->tree.nodes.size();
+  return RS_OK;
+}
+
+rs_status rs_factor(rs_solver* s) {
+  if (!s) return RS_ERR_ARG;
+  if (!s->tree_built) {
+    rs_status rc = rs_build_tree(s);
+    if (rc != RS_OK) return rc;
+  }
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  CU(cudaSetDevice(s->cfg.device));
+  rc = upload_geometry(s);
+  if (rc != RS_OK) return rc;
+  double t0 = now_ms();
+  CU(cudaEventRecord(s->ev_f0, s->stream));
+  s->factored = false;
+  rc = s->fp32 ? factor_impl<float>(s) : factor_impl<double>(s);
+  if (rc != RS_OK) return rc;
+  if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann && s->fp32) {
+    // refinement residual needs the FP64 border matrices and an all-ones mask
+    std::vector<unsigned char> ones(s->D, 1);
+    CU(s->ones_mask.ensure(s->D));
+    CU(cudaMemcpyAsync(s->ones_mask.p, ones.data(), s->D, cudaMemcpyHostToDevice, s->stream));
+  } else if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann) {
+    std::vector<unsigned char> ones(s->D, 1);
+    CU(s->ones_mask.ensure(s->D));
+    CU(cudaMemcpyAsync(s->ones_mask.p, ones.data(), s->D, cudaMemcpyHostToDevice, s->stream));
+  }
+  CU(cudaEventRecord(s->ev_f1, s->stream));
+  CU(cudaMemcpyAsync(s->h_status.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s->ev_f0, s->ev_f1);
+  s->stats.dev_factor_ms = ms;
+  s->stats.t_factor_ms = now_ms() - t0;
+  int nc = 0;
+  for (const NodeState& S : s->st) nc += S.compressed;
+  s->stats.num_compressed = nc;
+  s->stats.num_skel_root = s->ns;
+  if (s->h_status.p[0] != 0) return fail(s, RS_ERR_NUMERIC, "singular or non-finite pivot");
+  s->factored = true;
+  return RS_OK;
+}
+
+rs_status rs_solve_device(rs_solver* s, const double* d_f, int nrhs, double* d_mu,
+                          double* d_alpha) {
+  if (!s || !d_f || !d_mu || nrhs < 1) return fail(s, RS_ERR_ARG, "bad solve arguments");
+  if (!s->factored) return fail(s, RS_ERR_STATE, "solve before factor");
+  if (s->nb > 0 && !d_alpha) return fail(s, RS_ERR_ARG, "holes need an alpha output");
+  CU(cudaSetDevice(s->cfg.device));
+  CU(cudaEventRecord(s->ev_f0, s->stream));
+  rs_status rc = solve_device_impl(s, d_f, nrhs, d_mu, d_alpha);
+  if (rc != RS_OK) return rc;
+  CU(cudaEventRecord(s->ev_f1, s->stream));
+  return RS_OK;
+}
+
+rs_status rs_solve(rs_solver* s, const double* f, int nrhs, double* mu, double* alpha) {
+  if (!s || !f || !mu || nrhs < 1) return fail(s, RS_ERR_ARG, "bad solve arguments");
+  if (!s->factored) return fail(s, RS_ERR_STATE, "solve before factor");
+  if (s->nb > 0 && !alpha) return fail(s, RS_ERR_ARG, "holes need an alpha output");
+  double t0 = now_ms();
+  CU(cudaSetDevice(s->cfg.device));
+  const size_t nd = (size_t)s->D * nrhs;
+  const size_t na = (size_t)s->nb * nrhs;
+  CU(s->f_dev.ensure(nd));
+  CU(s->mu_dev.ensure(nd));
+  CU(s->alpha_dev.ensure(std::max<size_t>(na, 1)));
+  CU(cudaMemcpyAsync(s->f_dev.p, f, nd * 8, cudaMemcpyHostToDevice, s->stream));
+  rs_status rc = rs_solve_device(s, s->f_dev.p, nrhs, s->mu_dev.p, s->alpha_dev.p);
+  if (rc != RS_OK) return rc;
+  CU(cudaMemcpyAsync(mu, s->mu_dev.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
+  if (s->nb > 0) CU(cudaMemcpyAsync(alpha, s->alpha_dev.p, na * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s->ev_f0, s->ev_f1);
+  s->stats.dev_solve_ms = ms;
+  s->stats.t_solve_ms = now_ms() - t0;
+  return RS_OK;
+}
+
+rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int nJ, double* out) {
+  if (!s || nI < 0 || nJ < 0 || (nI && !I) || (nJ && !J) || (nI > 0 && nJ > 0 && !out))
+    return fail(s, RS_ERR_ARG, "bad kernel block arguments");
+  for (int i = 0; i < nI; ++i)
+    if (I[i] < 0 || I[i] >= s->D) return fail(s, RS_ERR_ARG, "row index out of range");
+  for (int j = 0; j < nJ; ++j)
+    if (J[j] < 0 || J[j] >= s->D) return fail(s, RS_ERR_ARG, "column index out of range");
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  rc = upload_geometry(s);
+  if (rc != RS_OK) return rc;
+  if (!nI || !nJ) return RS_OK;
+  DevBuf<int> dI, dJ;
+  DevBuf<double> dO;
+  CU(dI.ensure(nI));
+  CU(dJ.ensure(nJ));
+  CU(dO.ensure((size_t)nI * nJ));
+  CU(cudaMemcpyAsync(dI.p, I, nI * 4, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemcpyAsync(dJ.p, J, nJ * 4, cudaMemcpyHostToDevice, s->stream));
+  launch_kernel_block(geo_of(s), s->cfg.pde, s->sd, dI.p, nI, dJ.p, nJ, dO.p, s->stream);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out, dO.p, (size_t)nI * nJ * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y) {
+  if (!s || !x || !y || nrhs < 1) return fail(s, RS_ERR_ARG, "bad matvec arguments");
+  if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  rc = upload_geometry(s);
+  if (rc != RS_OK) return rc;
+  const size_t nd = (size_t)s->D * nrhs;
+  DevBuf<double> dx, dy;
+  CU(dx.ensure(nd));
+  CU(dy.ensure(nd));
+  CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
+  launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, dx.p, nrhs, dy.p, s->stream);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64_t* a_off,
+                        const int* m, const int* n, double tol, int* ranks, int* perm,
+                        const int64_t* p_off, double* Z, const int64_t* z_off) {
+  if (!s || count < 0 || (count && (!mats || !a_off || !m || !n || !ranks || !perm || !p_off ||
+                                    !Z || !z_off)) ||
+      !(tol > 0))
+    return fail(s, RS_ERR_ARG, "bad id arguments");
+  if (!count) return RS_OK;
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  int64_t a_tot = 0, p_tot = 0, z_tot = 0;
+  std::vector<IdTask> tasks(count);
+  size_t scratch = 0;
+  for (int i = 0; i < count; ++i) {
+    if (m[i] < 1 || n[i] < 1 || n[i] > 4096) return fail(s, RS_ERR_ARG, "bad matrix size");
+    a_tot = std::max<int64_t>(a_tot, a_off[i] + (int64_t)m[i] * n[i]);
+    p_tot = std::max<int64_t>(p_tot, p_off[i] + n[i]);
+    z_tot = std::max<int64_t>(z_tot, z_off[i] + (int64_t)n[i] * n[i]);
+    IdTask& t = tasks[i];
+    t = IdTask{};
+    t.n = n[i];
+    t.act_off = (int)p_off[i];
+    t.slot = i;
+    t.fac_off = z_off[i];
+    t.scratch_off = -1;
+    t.dense_off = a_off[i];
+    t.m_dense = m[i];
+  }
+  std::vector<size_t> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return tasks[a].n < tasks[b].n; });
+  std::vector<IdTask> sorted(count);
+  for (int i = 0; i < count; ++i) sorted[i] = tasks[order[i]];
+  for (IdTask& t : sorted)
+    if (id_kernel_smem(t.n, false, true) > kSmemMax) {
+      t.scratch_off = (int64_t)scratch;
+      scratch += (size_t)t.n * t.n + 64 * (size_t)t.n + 64;
+    }
+  DevBuf<double> dA, dZ, dS;
+  DevBuf<int> dP, dR;
+  DevBuf<IdTask> dT;
+  CU(dA.ensure(a_tot));
+  CU(dZ.ensure(z_tot));
+  CU(dS.ensure(std::max<size_t>(scratch, 1)));
+  CU(dP.ensure(p_tot));
+  CU(dR.ensure(count));
+  CU(dT.ensure(count));
+  CU(cudaMemcpyAsync(dA.p, mats, a_tot * 8, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemsetAsync(dZ.p, 0, z_tot * 8, s->stream));
+  CU(cudaMemcpyAsync(dT.p, sorted.data(), count * sizeof(IdTask), cudaMemcpyHostToDevice, s->stream));
+  IdParams ip{};
+  ip.tol = tol;
+  ip.ranks = dR.p;
+  ip.perm = dP.p;
+  ip.fac = dZ.p;
+  ip.scratch = dS.p;
+  ip.dense = dA.p;
+  ip.sd = 1;
+  ip.npp = 1;
+  launch_binned(sorted, dT.p, [&](const IdTask* dt, int cnt, int nmax) {
+    IdParams q = ip;
+    q.tasks = dt;
+    bool in_smem = id_kernel_smem(nmax, false, true) <= kSmemMax;
+    launch_id(q, cnt, id_kernel_smem(nmax, false, in_smem), false, s->stream);
+  });
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(ranks, dR.p, count * 4, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaMemcpyAsync(perm, dP.p, p_tot * 4, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaMemcpyAsync(Z, dZ.p, z_tot * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+rs_status rs_get_stats(const rs_solver* s, rs_stats* out) {
+  if (!s || !out) return RS_ERR_ARG;
+  *out = s->stats;
+  out->kernel_launches = s->launches;
+  return RS_OK;
+}
+
+rs_status rs_node_info(const rs_solver* s, int node, int* info, double* corners8, double* side) {
+  if (!s || !info || !s->tree_built) return RS_ERR_ARG;
+  if (node < 0 || node >= (int)s->tree.level_order.size()) return RS_ERR_ARG;
+  const int id = s->tree.level_order[node];
+  const TreeNode& nd = s->tree.nodes[id];
+  info[0] = nd.level;
+  info[1] = nd.is_leaf;
+  info[2] = nd.parent >= 0 ? s->tree.level_rank[nd.parent] : -1;
+  for (int c = 0; c < 4; ++c) info[3 + c] = nd.children[c] >= 0 ? s->tree.level_rank[nd.children[c]] : -1;
+  const bool have = id < (int)s->st.size();
+  info[7] = have ? s->st[id].compressed : 0;
+  info[8] = have ? (int)s->st[id].skel.size() : 0;
+  info[9] = have ? (int)s->st[id].red.size() : 0;
+  if (corners8) std::memcpy(corners8, nd.corners, sizeof(nd.corners));
+  if (side) *side = nd.side;
+  return RS_OK;
+}
+
+rs_status rs_node_list(const rs_solver* s, int node, int which, int* out, int cap, int* len) {
+  if (!s || !s->tree_built || !len) return RS_ERR_ARG;
+  if (node < 0 || node >= (int)s->tree.level_order.size()) return RS_ERR_ARG;
+  const int id = s->tree.level_order[node];
+  const TreeNode& nd = s->tree.nodes[id];
+  std::vector<int> tmp;
+  const std::vector<int>* src = nullptr;
+  const bool have = id < (int)s->st.size();
+  static const std::vector<int> empty;
+  switch (which) {
+    case 0: src = &nd.original; break;
+    case 1: src = have ? &s->st[id].active : &empty; break;
+    case 2: src = have ? &s->st[id].skel : &empty; break;
+    case 3: src = have ? &s->st[id].red : &empty; break;
+    case 4: src = have ? &s->st[id].near_ : &empty; break;
+    case 5:
+      for (int x : nd.neighbors) tmp.push_back(s->tree.level_rank[x]);
+      src = &tmp;
+      break;
+    case 6: src = have ? &s->st[id].perm : &empty; break;
+    default: return RS_ERR_ARG;
+  }
+  *len = (int)src->size();
+  if (out)
+    for (int i = 0; i < *len && i < cap; ++i) out[i] = (*src)[i];
+  return RS_OK;
+}
+
+rs_status rs_tree_bounds(const rs_solver* s, double* mn, double* mx) {
+  if (!s || !s->tree_built) return RS_ERR_ARG;
+  if (mn) *mn = s->tree.min;
+  if (mx) *mx = s->tree.max;
+  return RS_OK;
+}
+
+rs_status rs_allskel(const rs_solver* s, int* out, int cap, int* len) {
+  if (!s || !len) return RS_ERR_ARG;
+  *len = (int)s->allskel.size();
+  if (out)
+    for (int i = 0; i < *len && i < cap; ++i) out[i] = s->allskel[i];
+  return RS_OK;
+}
+
+rs_status rs_timer_start(rs_solver* s) {
+  if (!s) return RS_ERR_ARG;
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  CU(cudaEventRecord(s->ev_t0, s->stream));
+  return RS_OK;
+}
+
+rs_status rs_timer_stop(rs_solver* s, float* ms) {
+  if (!s || !ms || !s->dev_ready) return RS_ERR_ARG;
+  CU(cudaEventRecord(s->ev_t1, s->stream));
+  CU(cudaEventSynchronize(s->ev_t1));
+  CU(cudaEventElapsedTime(ms, s->ev_t0, s->ev_t1));
+  return RS_OK;
+}
+
+rs_status rs_synchronize(rs_solver* s) {
+  if (!s) return RS_ERR_ARG;
+  if (!s->dev_ready) return RS_OK;
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+const char* rs_last_error(const rs_solver* s) {
+  static const char* none = "";
+  return s ? s->err.c_str() : none;
+}
+
+}  // extern "C"

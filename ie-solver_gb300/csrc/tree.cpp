@@ -1,0 +1,185 @@
+// Host quadtree construction; see tree.hpp for the rules it reproduces.
+#include "tree.hpp"
+
+#include <cmath>
+
+namespace rskel {
+
+int QuadTree::new_node() {
+  nodes.emplace_back();
+  return static_cast<int>(nodes.size()) - 1;
+}
+
+void QuadTree::push_level(int level, int id) {
+  if (static_cast<int>(levels.size()) <= level) levels.resize(level + 1);
+  levels[level].push_back(id);
+}
+
+// quadtree.cpp:230-269
+void QuadTree::add(int id, double x, double y, int point) {
+  for (int c = 0; c < sd; ++c) nodes[id].original.push_back(sd * point + c);
+  const TreeNode& nd = nodes[id];
+  const double midx = ((nd.corners[6] - nd.corners[0]) / 2.0) + nd.corners[0];
+  const double midy = ((nd.corners[3] - nd.corners[1]) / 2.0) + nd.corners[1];
+  int child;
+  if (x < midx && y < midy) child = nd.bl;
+  else if (x < midx && y >= midy) child = nd.tl;
+  else if (x >= midx && y < midy) child = nd.br;
+  else child = nd.tr;
+  if (child >= 0) {
+    add(child, x, y, point);
+  } else if (nd.is_leaf && static_cast<int>(nd.original.size()) > leaf_) {
+    subdivide(id);
+  }
+}
+
+// quadtree.cpp:275-432
+void QuadTree::subdivide(int id) {
+  nodes[id].is_leaf = 0;
+  double c[8];
+  for (int i = 0; i < 8; ++i) c[i] = nodes[id].corners[i];
+  const double midx = ((c[6] - c[0]) / 2.0) + c[0];
+  const double midy = ((c[3] - c[1]) / 2.0) + c[1];
+  const int bl = new_node(), tl = new_node(), tr = new_node(), br = new_node();
+  const double cb[8] = {c[0], c[1], c[2], midy, midx, midy, midx, c[7]};
+  const double ct[8] = {c[0], midy, c[2], c[3], midx, c[5], midx, midy};
+  const double cr[8] = {midx, midy, midx, c[3], c[4], c[5], c[6], midy};
+  const double cq[8] = {midx, c[1], midx, midy, c[4], midy, c[6], c[7]};
+  for (int i = 0; i < 8; ++i) {
+    nodes[bl].corners[i] = cb[i];
+    nodes[tl].corners[i] = ct[i];
+    nodes[tr].corners[i] = cr[i];
+    nodes[br].corners[i] = cq[i];
+  }
+  const int kids[4] = {bl, tl, tr, br};
+  for (int k : kids) {
+    nodes[k].level = nodes[id].level + 1;
+    nodes[k].side = nodes[id].side / 2.0;
+    nodes[k].parent = id;
+  }
+  const int lv = nodes[id].level + 1;
+  push_level(lv, bl);
+  push_level(lv, br);
+  push_level(lv, tr);
+  push_level(lv, tl);
+  TreeNode& nd = nodes[id];
+  nd.bl = bl; nd.tl = tl; nd.tr = tr; nd.br = br;
+  nd.children[0] = bl; nd.children[1] = tl; nd.children[2] = tr; nd.children[3] = br;
+  const std::vector<int> parent_dofs = nd.original;
+  for (size_t idx = 0; idx < parent_dofs.size(); idx += sd) {
+    const int mi = parent_dofs[idx];
+    const int pv = (mi / sd) * 2;
+    const double x = pts_[pv], y = pts_[pv + 1];
+    int dst;
+    if (x < midx && y < midy) dst = bl;
+    else if (x < midx && y >= midy) dst = tl;
+    else if (x >= midx && y < midy) dst = br;
+    else dst = tr;
+    for (int q = 0; q < sd; ++q) nodes[dst].original.push_back(mi + q);
+  }
+  if (static_cast<int>(nodes[bl].original.size()) > leaf_) subdivide(bl);
+  if (static_cast<int>(nodes[tl].original.size()) > leaf_) subdivide(tl);
+  if (static_cast<int>(nodes[tr].original.size()) > leaf_) subdivide(tr);
+  if (static_cast<int>(nodes[br].original.size()) > leaf_) subdivide(br);
+}
+
+// quadtree.cpp:185-227
+void QuadTree::descendant_neighbors(int big, int small) {
+  const double top = nodes[big].corners[3];
+  const double bottom = nodes[big].corners[1];
+  const double left = nodes[big].corners[0];
+  const double right = nodes[big].corners[4];
+  for (int i = 0; i < 8; i += 2) {
+    const double x = nodes[small].corners[i];
+    const double y = nodes[small].corners[i + 1];
+    bool hit = false;
+    if (x > left && x < right) {
+      if (std::fabs(y - top) < 1e-14 || std::fabs(y - bottom) < 1e-14) hit = true;
+    }
+    // The reference tests `y < top && y < bottom` here (not y > bottom).
+    if (!hit && y < top && y < bottom) {
+      if (std::fabs(x - left) < 1e-14 || std::fabs(x - right) < 1e-14) hit = true;
+    }
+    if (hit) {
+      nodes[big].neighbors.push_back(small);
+      nodes[small].neighbors.push_back(big);
+      break;
+    }
+  }
+  for (int c = 0; c < 4; ++c) {
+    const int ch = nodes[small].children[c];
+    if (ch >= 0) descendant_neighbors(big, ch);
+  }
+}
+
+bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
+  nodes.clear();
+  levels.clear();
+  if (n <= 0 || points == nullptr) return false;
+  pts_ = points;
+  sd = sd_;
+  leaf_ = max_leaf_dofs;
+  nodes.reserve(static_cast<size_t>(8 * (n * sd_ / (max_leaf_dofs > 0 ? max_leaf_dofs : 1) + 1)));
+  double mn = points[0], mx = points[0];
+  for (int i = 0; i < 2 * n; ++i) {
+    if (points[i] < mn) mn = points[i];
+    if (points[i] > mx) mx = points[i];
+  }
+  min = mn;
+  max = mx;
+  const double lo = mn - 0.01, hi = mx + 0.01;
+  root = new_node();
+  TreeNode& r = nodes[root];
+  const double rc[8] = {lo, lo, lo, hi, hi, hi, hi, lo};
+  for (int i = 0; i < 8; ++i) r.corners[i] = rc[i];
+  r.side = hi - lo;
+  push_level(0, root);
+  for (int i = 0; i < n; ++i) add(root, points[2 * i], points[2 * i + 1], i);
+
+  // quadtree.cpp:131-175
+  const double sqrt2 = std::sqrt(2.0);
+  for (size_t lv = 0; lv < levels.size(); ++lv) {
+    for (size_t k = 0; k < levels[lv].size(); ++k) {
+      const int a = levels[lv][k];
+      const int par = nodes[a].parent;
+      if (par >= 0) {
+        for (int c = 0; c < 4; ++c) {
+          const int sib = nodes[par].children[c];
+          if (sib != a) nodes[a].neighbors.push_back(sib);
+        }
+        const std::vector<int>& pn = nodes[par].neighbors;
+        for (size_t q = 0; q < pn.size(); ++q) {
+          for (int c = 0; c < 4; ++c) {
+            const int cousin = nodes[pn[q]].children[c];
+            if (cousin < 0 || nodes[cousin].level != nodes[a].level) continue;
+            const double dx = nodes[a].corners[0] - nodes[cousin].corners[0];
+            const double dy = nodes[a].corners[1] - nodes[cousin].corners[1];
+            const double dist = std::sqrt(dx * dx + dy * dy);
+            if (dist < nodes[a].side * sqrt2 + 1e-5) nodes[a].neighbors.push_back(cousin);
+          }
+        }
+      }
+      if (nodes[a].is_leaf) {
+        for (size_t q = 0; q < nodes[a].neighbors.size(); ++q) {
+          const int nb = nodes[a].neighbors[q];
+          if (nodes[nb].level != nodes[a].level) continue;
+          for (int c = 0; c < 4; ++c) {
+            const int ch = nodes[nb].children[c];
+            if (ch >= 0) descendant_neighbors(a, ch);
+          }
+        }
+      }
+    }
+  }
+  level_order.clear();
+  level_rank.assign(nodes.size(), -1);
+  for (const auto& lvl : levels)
+    for (int id : lvl) {
+      level_rank[id] = static_cast<int>(level_order.size());
+      level_order.push_back(id);
+    }
+  pts_ = nullptr;
+  return true;
+}
+
+}  // namespace rskel

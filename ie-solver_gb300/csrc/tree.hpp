@@ -1,0 +1,54 @@
+// Host quadtree over the boundary nodes, bit-exact with the reference's
+// QuadTree::initialize_tree (ie_solver/quadtree/quadtree.cpp:39-432):
+//  * bounding square [min - 0.01, max + 0.01] with min/max pooled over x and y;
+//  * points inserted in index order, DOFs sd*i + c pushed along the path;
+//  * a leaf splits when its DOF count exceeds max_leaf_dofs; children are
+//    appended to their level as bl, br, tr, tl, while children[] is
+//    {bl, tl, tr, br}; the parent's DOFs are redistributed in parent order;
+//  * neighbour lists: siblings, parents' neighbours' children within
+//    s*sqrt(2) + 1e-5 (bottom-left corners), plus leaf <-> finer-box links
+//    including the reference's `y < top && y < bottom` condition.
+// Compiled with floating-point contraction off so x86-64 and aarch64 hosts
+// produce the same tree.
+#pragma once
+
+#include <vector>
+
+namespace rskel {
+
+struct TreeNode {
+  int level = 0;
+  int is_leaf = 1;
+  int parent = -1;
+  int children[4] = {-1, -1, -1, -1};  // bl, tl, tr, br
+  int bl = -1, tl = -1, tr = -1, br = -1;
+  double corners[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // {BL, TL, TR, BR} x,y pairs
+  double side = 0;
+  std::vector<int> neighbors;
+  std::vector<int> original;  // DOF indices
+};
+
+struct QuadTree {
+  std::vector<TreeNode> nodes;           // creation order
+  std::vector<std::vector<int>> levels;  // node ids per level, reference order
+  double min = 0, max = 0;
+  int root = -1;
+  int sd = 1;
+
+  // points: interleaved (2n). Returns false on empty input.
+  bool build(const double* points, int n, int sd, int max_leaf_dofs);
+  // level-order numbering (level 0 first) <-> creation ids
+  std::vector<int> level_order;   // level-order index -> node id
+  std::vector<int> level_rank;    // node id -> level-order index
+
+ private:
+  const double* pts_ = nullptr;
+  int leaf_ = 32;
+  int new_node();
+  void push_level(int level, int id);
+  void add(int id, double x, double y, int point);
+  void subdivide(int id);
+  void descendant_neighbors(int big, int small);
+};
+
+}  // namespace rskel

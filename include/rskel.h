@@ -1,0 +1,159 @@
+/* rskel: GB300-native recursive-skeletonization direct solver for 2D Laplace
+ * and Stokes double-layer boundary integral equations.  C ABI.
+ *
+ * This is the drop-in boundary for the factor + solve path of jpryan1/ie-solver.
+ * Each entry point replaces the reference interface cited beside it (paths
+ * within that project).  All entry points return an rs_status (0 = success);
+ * no call exits the process or asserts.  Pointers are plain host pointers
+ * unless an argument is documented as a device pointer.  A handle owns one
+ * CUDA stream; a handle is not thread-safe, distinct handles are independent.
+ */
+#ifndef RSKEL_H
+#define RSKEL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  RS_OK = 0,
+  RS_ERR_ARG = 1,          /* invalid argument (null pointer, bad size, bad enum) */
+  RS_ERR_STATE = 2,        /* call out of order (e.g. solve before factor) */
+  RS_ERR_CUDA = 3,         /* a CUDA runtime call failed; see rs_last_error */
+  RS_ERR_NO_DEVICE = 4,    /* no usable GPU; there is no CPU fallback */
+  RS_ERR_CAPACITY = 5,     /* a box exceeded the supported block size */
+  RS_ERR_NUMERIC = 6,      /* non-finite value or exactly singular pivot */
+  RS_ERR_NO_COMPRESSION = 7 /* bordered system with no redundant DOFs
+                               (skel_factorization.cpp:209-212 exits there) */
+} rs_status;
+
+/* ie_solver_config::Pde (io/io.h:20-24). */
+typedef enum { RS_LAPLACE = 0, RS_LAPLACE_NEUMANN = 1, RS_STOKES = 2 } rs_pde;
+
+/* Arithmetic of the factorization. */
+typedef enum {
+  RS_FP64 = 0,        /* plain FP64, the reference's arithmetic */
+  RS_FP32_REFINE = 1  /* FP32 factorization + FP64 iterative refinement */
+} rs_precision;
+
+/* ie_solver_config (io/io.h:18-38) plus the compile-time constants of the
+ * reference made runtime fields: MAX_LEAF_DOFS (quadtree/quadtree.h:10),
+ * NUM_PROXY_POINTS and RADIUS_RATIO (kernel/kernel.h:11-12),
+ * MIN_DOFS_TO_COMPRESS (skel_factorization/skel_factorization.h:11). */
+typedef struct {
+  int pde;                   /* rs_pde */
+  int solution_dimension;    /* 1 (Laplace) or 2 (Stokes) */
+  int domain_dimension;      /* must be 2 */
+  double id_tol;             /* ID tolerance, > 0 */
+  int max_leaf_dofs;         /* reference default 32 */
+  int num_proxy_points;      /* reference default 128 */
+  double radius_ratio;       /* reference default 1.5 */
+  int min_dofs_to_compress;  /* reference default 16 */
+  int is_strong_admissibility; /* must be 0 (weak admissibility only) */
+  int precision;             /* rs_precision */
+  double refine_tol;         /* RS_FP32_REFINE: target relative residual */
+  int refine_max_iters;      /* RS_FP32_REFINE: maximum refinement steps */
+  double fp32_id_tol;        /* RS_FP32_REFINE: ID tolerance of the FP32 factor
+                                (at least id_tol; FP32 cannot resolve below ~1e-6) */
+  int device;                /* CUDA device ordinal */
+} rs_config;
+
+typedef struct rs_solver rs_solver;
+
+/* Fills cfg with the reference defaults (io/io.h:11-14, 18-38). */
+void rs_config_default(rs_config* cfg);
+
+/* SkelFactorization(double id_tol, bool strong, int nt)
+ * (skel_factorization/skel_factorization.cpp:26-32) + Kernel(...)
+ * (kernel/kernel.h:28-35). */
+rs_status rs_create(const rs_config* cfg, rs_solver** out);
+rs_status rs_destroy(rs_solver* s);
+
+/* Boundary data vectors (boundaries/boundary.h:39-41): points and normals
+ * interleaved (2*num_points), weights and curvatures (num_points).  Holes
+ * (boundaries/boundary.h:11-15) are optional: centres interleaved (2*h) and
+ * radii (h).  The data are copied. */
+rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
+                          const double* normals, const double* weights,
+                          const double* curvatures, int num_holes,
+                          const double* hole_centers, const double* hole_radii);
+
+/* QuadTree::initialize_tree(boundary, {}, sd, 2) (quadtree/quadtree.cpp:39-180).
+ * Host-side; needs no GPU. */
+rs_status rs_build_tree(rs_solver* s);
+
+/* SkelFactorization::skeletonize (skel_factorization.cpp:140-310), including
+ * the bordered system for holes (initialize_U_mat / initialize_Psi_mat,
+ * linear_solve.cpp:20-112).  Builds the tree first when needed. */
+rs_status rs_factor(rs_solver* s);
+
+/* linear_solve (linear_solve.cpp:115-129) -> SkelFactorization::solve
+ * (skel_factorization.cpp:507-592) or multiply_connected_solve (:596-777).
+ * f and mu: (num_points*sd) x nrhs, column major, host memory.  alpha:
+ * (3h Stokes, h Laplace) x nrhs when holes exist, else may be NULL. */
+rs_status rs_solve(rs_solver* s, const double* f, int nrhs, double* mu, double* alpha);
+
+/* Same as rs_solve with device pointers (no host copies); work is ordered on
+ * the handle's stream and the call returns without synchronising. */
+rs_status rs_solve_device(rs_solver* s, const double* d_f, int nrhs, double* d_mu,
+                          double* d_alpha);
+
+/* Kernel::operator()(I, J) (kernel/kernel.cpp:105-120): dense block
+ * K(I, J), column major |I| x |J|, evaluated on the GPU. */
+rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int nJ,
+                          double* out);
+
+/* y = K x over all DOFs (dense, FP64 accurate, on the GPU), the operator whose
+ * inverse the factorization represents.  x, y: (num_points*sd) x nrhs. */
+rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
+
+/* ie_Mat::id (ie_mat.cpp:548-588) for a batch of matrices on the GPU.
+ * mats: concatenated column-major m_i x n_i blocks (offsets a_off, in
+ * doubles); ranks[i] gets k (0 = no compression); perm gets n_i 0-based
+ * column indices at p_off[i]; Z gets k x (n_i - k) at z_off[i] (caller
+ * reserves n_i*n_i doubles). */
+rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64_t* a_off,
+                        const int* m, const int* n, double tol, int* ranks, int* perm,
+                        const int64_t* p_off, double* Z, const int64_t* z_off);
+
+/* --- introspection (tree and factorization), for tests and tooling --- */
+typedef struct {
+  int num_levels, num_nodes, num_compressed, num_skel_root;
+  int max_active, max_rank, max_rows;
+  double t_tree_ms, t_factor_ms, t_solve_ms;   /* host wall clock of last calls */
+  double dev_factor_ms, dev_solve_ms;          /* CUDA-event time of last calls */
+  double id_flops, decouple_flops, solve_bytes; /* algorithmic work of last calls */
+  double id_ms, decouple_ms;                   /* CUDA-event time in those kernels */
+  int refine_iters;                            /* iterations of last solve */
+  double refine_residual;                      /* final relative residual */
+  int kernel_launches;                         /* kernels launched by last factor+solve */
+} rs_stats;
+rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
+
+/* Node numbering is level order (QuadTree::levels, quadtree.h:107): level 0,
+ * then each level's node list in order.  info gets {level, is_leaf, parent,
+ * child0..child3 (bl, tl, tr, br), compressed, num_skel, num_redundant}. */
+rs_status rs_node_info(const rs_solver* s, int node, int* info, double* corners8,
+                       double* side);
+/* which: 0 original_box, 1 active_box, 2 skel, 3 redundant, 4 near,
+ * 5 neighbors (node numbers), 6 permutation (InteractionLists, quadtree.h:16-49).
+ * Writes up to cap entries; *len gets the full length. */
+rs_status rs_node_list(const rs_solver* s, int node, int which, int* out, int cap, int* len);
+rs_status rs_tree_bounds(const rs_solver* s, double* min_coord, double* max_coord);
+rs_status rs_allskel(const rs_solver* s, int* out, int cap, int* len);
+
+/* Device-event timing on the handle's stream, for benchmarks. */
+rs_status rs_timer_start(rs_solver* s);
+rs_status rs_timer_stop(rs_solver* s, float* ms);
+rs_status rs_synchronize(rs_solver* s);
+
+/* Last error message of this handle (static storage for NULL handles). */
+const char* rs_last_error(const rs_solver* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

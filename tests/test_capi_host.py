@@ -1,0 +1,88 @@
+"""The C ABI library: loads, exports every entry point declared in
+include/rskel.h, validates arguments and orders calls without touching a GPU,
+and refuses to compute (no CPU fallback) when no GPU is present."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "rskel.h")).read()
+    names = set(re.findall(r"^\s*(?:rs_status|void|const char\s*\*)\s*(rs_\w+)\s*\(", text,
+                           re.MULTILINE))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(solver_lib):
+    lib = solver_lib.lib()
+    names = declared_symbols()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(solver_lib.EXPORTS) == set(names)
+
+
+def test_config_defaults_are_the_reference_defaults(solver_lib):
+    c = solver_lib.default_config()
+    assert c.id_tol == 1e-6 and c.max_leaf_dofs == 32 and c.num_proxy_points == 128
+    assert c.radius_ratio == 1.5 and c.min_dofs_to_compress == 16
+    assert c.is_strong_admissibility == 0 and c.solution_dimension == 1
+
+
+def test_argument_validation(solver_lib):
+    from rskel import geometry as g
+
+    lib = solver_lib.lib()
+    h = ctypes.c_void_p()
+    bad = solver_lib.default_config(pde=2, solution_dimension=1)  # Stokes needs sd = 2
+    assert lib.rs_create(ctypes.byref(bad), ctypes.byref(h)) == 1
+    bad = solver_lib.default_config(id_tol=0.0)
+    assert lib.rs_create(ctypes.byref(bad), ctypes.byref(h)) == 1
+    bad = solver_lib.default_config(is_strong_admissibility=1)
+    assert lib.rs_create(ctypes.byref(bad), ctypes.byref(h)) == 1
+    geo = g.unit_circle(64)
+    s = solver_lib.Solver(geo, solver_lib.RS_LAPLACE, 1e-6)
+    with pytest.raises(solver_lib.RsError) as e:
+        s.solve(np.ones(64))
+    assert e.value.code == 2  # solve before factor
+    with pytest.raises(solver_lib.RsError):
+        s.kernel_block([0, 64], [1])  # index out of range
+    # non-finite geometry is rejected before any compute
+    geo.points[3] = np.nan
+    with pytest.raises(solver_lib.RsError) as e:
+        solver_lib.Solver(geo, solver_lib.RS_LAPLACE, 1e-6)
+    assert e.value.code == 6
+
+
+def _has_gpu():
+    try:
+        lib = ctypes.CDLL("libcudart.so")
+    except OSError:
+        try:
+            import glob
+
+            cands = glob.glob("/usr/local/cuda/lib64/libcudart.so*")
+            lib = ctypes.CDLL(cands[0]) if cands else None
+        except OSError:
+            lib = None
+    if lib is None:
+        return False
+    n = ctypes.c_int(0)
+    return lib.cudaGetDeviceCount(ctypes.byref(n)) == 0 and n.value > 0
+
+
+def test_no_cpu_fallback_without_gpu(solver_lib):
+    if _has_gpu():
+        pytest.skip("a GPU is present")
+    from rskel import geometry as g
+
+    s = solver_lib.Solver(g.unit_circle(256), solver_lib.RS_LAPLACE, 1e-6)
+    s.build_tree()  # host-side, works without a GPU
+    with pytest.raises(solver_lib.RsError) as e:
+        s.factor()
+    assert e.value.code == 4  # RS_ERR_NO_DEVICE

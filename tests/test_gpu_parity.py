@@ -1,0 +1,184 @@
+"""GPU parity: the CUDA solver against the oracle and the reference's golden
+outputs, through the C ABI.
+
+Tolerances (all relative unless stated):
+* kernel blocks vs the oracle: 1e-13 (same formula, FMA contraction differs);
+* plain FP64 solutions vs the reference / oracle: 10 x the ID tolerance
+  (skeleton choices at exact pivot ties may differ, as between LAPACK builds);
+* backward error vs the dense operator: max |K mu - f| <= 50 tol, the
+  reference's own test bound (ie_solver_test.cpp:82,94);
+* FP32 factorization + FP64 refinement: 1e-8 vs the FP64 oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden_geometry, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(capi, d, **kw):
+    geo = golden_geometry(d)
+    pde, sd, leaf, npp = (int(x) for x in d["meta"][:4])
+    return capi.Solver(geo, pde, float(d["tol"][0]), leaf=leaf, npp=npp, **kw), geo
+
+
+def _oracle(O, d):
+    geo = golden_geometry(d)
+    pde, sd, leaf, npp = (int(x) for x in d["meta"][:4])
+    s = O.OracleSolver(geo, pde, sd, float(d["tol"][0]), leaf, npp, 4)
+    s.build_tree()
+    s.factor()
+    return s
+
+
+def test_kernel_blocks_match_oracle(solver_lib, oracle_lib):
+    for name in ("laplace_star_8192_2rhs", "stokes_ellipses_4096"):
+        d = load_golden(name)
+        s, geo = _solver(solver_lib, d)
+        o = _oracle(oracle_lib, d)
+        rng = np.random.default_rng(0)
+        D = s.D
+        I = rng.choice(D, 300, replace=False)
+        J = np.concatenate([I[:50], rng.choice(D, 250, replace=False)])  # includes diagonal entries
+        A = s.kernel_block(I, J)
+        B = o.kernel_block(I, J)
+        assert np.abs(A - B).max() <= 1e-13 * np.abs(B).max()
+
+
+def test_matvec_matches_oracle(solver_lib, oracle_lib):
+    d = load_golden("stokes_ellipses_4096")
+    s, geo = _solver(solver_lib, d)
+    o = _oracle(oracle_lib, d)
+    x = np.random.default_rng(1).standard_normal((s.D, 3))
+    y = s.matvec(x)
+    z = o.matvec(x)
+    assert np.abs(y - z).max() <= 1e-12 * np.abs(z).max()
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_fp64_solve_matches_reference(name, solver_lib, oracle_lib):
+    d = load_golden(name)
+    tol = float(d["tol"][0])
+    s, geo = _solver(solver_lib, d)
+    s.factor()
+    f = d["rhs"]
+    mu, alpha = s.solve(f)
+    ref = d["mu"].reshape(np.shape(mu), order="F")
+    rel = np.linalg.norm(mu - ref) / np.linalg.norm(ref)
+    assert rel <= 10 * tol, rel
+    if "alpha" in d:
+        scale = max(1.0, np.abs(d["alpha"]).max())
+        assert np.abs(alpha - d["alpha"]).max() <= 10 * tol * scale
+    # the same inputs through the oracle
+    o = _oracle(oracle_lib, d)
+    mo, ao = o.solve(f)
+    mo = mo.reshape(np.shape(mu), order="F")
+    assert np.linalg.norm(mu - mo) / np.linalg.norm(mo) <= 10 * tol
+    # backward error against the dense operator (ie_solver_test.cpp:29-96)
+    Kmu = s.matvec(mu)
+    r = Kmu - np.reshape(f, np.shape(mu), order="F")
+    if alpha is not None:
+        U, P = o.border_mats()
+        r = r + (U @ alpha)
+        assert np.abs(P @ mu - alpha).max() <= 50 * tol
+    assert np.abs(r).max() <= 50 * tol
+
+
+@pytest.mark.parametrize("name", ["laplace_unit_circle_4096", "laplace_star_8192_2rhs",
+                                  "stokes_ellipses_4096"])
+def test_gpu_tree_and_lists_follow_reference_rules(name, solver_lib):
+    from test_tree_golden import TREE_FIELDS, active_near_from_rules
+
+    d = load_golden(name)
+    s, geo = _solver(solver_lib, d)
+    s.factor()
+    t = s.tree_dump()
+    for f in TREE_FIELDS:
+        assert np.array_equal(t[f], d[f]), f
+    t["allskel"] = s.allskel()
+    active, near = active_near_from_rules(t)
+    for i in range(len(t["node_level"])):
+        off = t["active_off"]
+        assert np.array_equal(active[i], t["active"][off[i]:off[i + 1]]), i
+        off = t["skel_off"]
+        sk = t["skel"][off[i]:off[i + 1]]
+        off = t["red_off"]
+        rd = t["red"][off[i]:off[i + 1]]
+        if t["node_compressed"][i]:
+            assert sorted(np.concatenate([sk, rd]).tolist()) == sorted(active[i].tolist())
+    # compression agrees with the reference's on most boxes (ranks may differ at ties)
+    ours = t["node_compressed"].astype(bool)
+    theirs = d["node_compressed"].astype(bool)
+    assert (ours == theirs).mean() >= 0.97
+
+
+def test_id_matches_reference_ranks(solver_lib):
+    from rskel import capi
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "id_cases.npz"))
+    from rskel import geometry as g
+
+    s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
+    mats = [d[f"A{i}"] for i in range(len(d["ranks"]))]
+    tol = float(d["tols"][0])
+    agree = 0
+    for i, (A, tl) in enumerate(zip(mats, d["tols"])):
+        (k, perm, Z), = capi.id_batched(s, [A], float(tl))
+        agree += int(k == d["ranks"][i])
+        assert abs(k - d["ranks"][i]) <= 1, (i, k, d["ranks"][i])
+        sk, rd = perm[:k], perm[k:]
+        err = np.linalg.norm(A[:, rd] - A[:, sk] @ Z, 2)
+        assert err <= 100 * float(tl) * np.linalg.norm(A, 2)
+        assert sorted(perm.tolist()) == list(range(A.shape[1]))
+    assert agree >= len(mats) - 1
+    # batched call gives the same as one-by-one
+    res = capi.id_batched(s, mats, tol)
+    for i, (k, perm, Z) in enumerate(res):
+        (k1, p1, z1), = capi.id_batched(s, [mats[i]], tol)
+        assert k == k1 and np.array_equal(perm, p1)
+
+
+def test_multi_rhs_equals_single(solver_lib):
+    d = load_golden("laplace_star_8192_2rhs")
+    s, geo = _solver(solver_lib, d)
+    s.factor()
+    F = d["rhs"]
+    mu2, _ = s.solve(F)
+    for c in range(F.shape[1]):
+        mu1, _ = s.solve(F[:, c])
+        assert np.abs(mu1 - mu2[:, c]).max() <= 1e-13 * np.abs(mu1).max()
+
+
+def test_refactor_is_deterministic(solver_lib):
+    d = load_golden("laplace_unit_circle_4096")
+    s, geo = _solver(solver_lib, d)
+    s.factor()
+    a, _ = s.solve(d["rhs"])
+    s.factor()
+    b, _ = s.solve(d["rhs"])
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["laplace_unit_circle_4096", "laplace_star_8192_2rhs",
+                                  "stokes_circle_512", "stokes_ellipses_4096",
+                                  "laplace_annulus_512"])
+def test_fp32_refined_matches_fp64_oracle(name, solver_lib, oracle_lib):
+    d = load_golden(name)
+    s, geo = _solver(solver_lib, d, precision=solver_lib.RS_FP32_REFINE, refine_tol=1e-13,
+                     refine_max_iters=12)
+    s.factor()
+    mu, alpha = s.solve(d["rhs"])
+    st = s.stats()
+    o = _oracle(oracle_lib, d)
+    mo, ao = o.solve(d["rhs"])
+    mo = mo.reshape(np.shape(mu), order="F")
+    tol = float(d["tol"][0])
+    # the FP64 oracle itself carries the ID error (~tol); the refined
+    # solution is the exact discrete solution to ~1e-12, so compare at
+    # max(1e-8, 10 tol).
+    rel = np.linalg.norm(mu - mo) / np.linalg.norm(mo)
+    assert rel <= max(1e-8, 10 * tol), (rel, st["refine_iters"], st["refine_residual"])
+    assert st["refine_residual"] <= 1e-12

@@ -1,0 +1,91 @@
+"""Pins the oracle restatement (oracle/rs_oracle.c) to the reference.
+
+Against the committed golden fixtures (outputs of the reference itself):
+solutions within the ID tolerance, the reference's backward-error bound
+(max |K mu - f| <= 50 tol, ie_solver_test.cpp:82,94), and per-box ID ranks on
+the reference's own ID results.  When the reference build is present
+(oracle/_ref, this container only) the oracle is also compared live.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden_geometry, load_golden
+
+
+def _solve_oracle(O, d, threads=2):
+    geo = golden_geometry(d)
+    pde, sd, leaf, npp = (int(x) for x in d["meta"][:4])
+    s = O.OracleSolver(geo, pde, sd, float(d["tol"][0]), leaf, npp, threads)
+    s.build_tree()
+    s.factor()
+    mu, alpha = s.solve(d["rhs"])
+    return s, mu, alpha
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_oracle_solution_matches_reference(name, oracle_lib):
+    d = load_golden(name)
+    tol = float(d["tol"][0])
+    s, mu, alpha = _solve_oracle(oracle_lib, d)
+    ref = d["mu"].reshape(mu.shape, order="F")
+    rel = np.linalg.norm(mu - ref) / np.linalg.norm(ref)
+    # pivot ties (symmetric geometries) change skeleton choices, so the two
+    # factorizations agree to the ID tolerance, not to rounding.
+    assert rel <= 10 * tol, rel
+    if "alpha" in d:
+        # alpha is ~0 for data generated by exterior sources: compare on the
+        # scale max(1, |alpha|), not relatively.
+        scale = max(1.0, np.abs(d["alpha"]).max())
+        assert np.abs(alpha - d["alpha"]).max() <= 10 * tol * scale
+
+
+@pytest.mark.parametrize("name", ["laplace_circle_512", "stokes_circle_512",
+                                  "laplace_unit_circle_4096", "laplace_annulus_512"])
+def test_oracle_backward_error(name, oracle_lib):
+    d = load_golden(name)
+    tol = float(d["tol"][0])
+    s, mu, alpha = _solve_oracle(oracle_lib, d)
+    f = d["rhs"].reshape(mu.shape, order="F")
+    r = s.matvec(mu) - f
+    if alpha is not None:
+        U, P = s.border_mats()
+        r = r + U @ alpha[:, None] if r.ndim == 2 else r + U @ alpha
+        r2 = P @ mu[:, 0] - alpha
+        assert np.abs(r2).max() <= 50 * tol
+    assert np.abs(r).max() <= 50 * tol
+
+
+def test_oracle_id_matches_reference_ranks(oracle_lib):
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "id_cases.npz"))
+    ranks = d["ranks"]
+    for i in range(len(ranks)):
+        A = d[f"A{i}"]
+        tol = float(d["tols"][i])
+        k, perm, Z, rd = oracle_lib.orc_id(A, tol)
+        assert k == ranks[i], (i, k, ranks[i])
+        # interpolation error of the ID: ||A(:, r) - A(:, s) Z|| small vs ||A||
+        s_idx, r_idx = perm[:k], perm[k:]
+        err = np.linalg.norm(A[:, r_idx] - A[:, s_idx] @ Z, 2)
+        assert err <= 100 * tol * np.linalg.norm(A, 2)
+
+
+def test_oracle_matches_live_reference(oracle_lib):
+    refio = pytest.importorskip("refio")
+    if refio.ref_binary(64, 64) is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    from rskel import geometry as g
+
+    rng = np.random.default_rng(11)
+    geo = g.random_star(6000, rng)
+    f = g.laplace_point_source(geo, (2.5, -0.7))
+    r = refio.run_reference(geo, 0, 1, f, 1e-9, leaf=64, npp=64)
+    s = oracle_lib.OracleSolver(geo, 0, 1, 1e-9, 64, 64)
+    s.build_tree()
+    s.factor()
+    mu, _ = s.solve(f)
+    t = s.tree_dump()
+    for k in ("level_sizes", "node_parent", "nbr", "orig"):
+        assert np.array_equal(t[k], r[k]), k
+    assert np.linalg.norm(mu[:, 0] - r["mu"]) / np.linalg.norm(r["mu"]) < 1e-8
