@@ -1,0 +1,406 @@
+"""Benchmark: factor + solve DOFs/s on one GB300.
+
+Workload (the metric's configuration): Laplace double-layer on the star curve
+r(t) = 1 + 0.3 cos 5t with N = 65536 nodes, ID tolerance 1e-8, leaf 64 DOFs,
+64 proxy points, 8 right-hand sides from point sources at 8 seeded exterior
+points on the radius-2 circle (seed 2).  A step is one factorization plus one
+solve of all 8 right-hand sides; DOFs/s = N / (t_factor + t_solve), as in
+the reference's timing protocol (linear_solve.cpp:156-185: tree build
+excluded).  The headline arm is FP32 factorization + FP64 iterative
+refinement to a relative residual of 1e-12; the plain FP64 arm is reported
+beside it.  Accuracy: relative error of the 8 solutions against the FP64
+oracle restatement of the reference (oracle/), which must be <= 1e-8.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement, built for the host's cores, OpenMP over boxes as the
+reference does) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import glob
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "ie-solver_gb300"), os.path.join(ROOT, "oracle")]
+
+METRIC = ("factor+solve DOFs/s at rel err<=1e-8 vs FP64; mixed+learned vs plain FP64, "
+          "1 GB300")
+N_POINTS = 65536
+TOL = 1e-8
+NRHS = 8
+LEAF = 64
+NPP = 64
+
+
+def workload():
+    from rskel import geometry as g
+
+    geo = g.star(N_POINTS)
+    rng = np.random.default_rng(2)
+    th = rng.uniform(0.0, 2.0 * math.pi, NRHS)
+    F = np.stack([g.laplace_point_source(geo, (2.0 * math.cos(t), 2.0 * math.sin(t)))
+                  for t in th], 1)
+    return geo, np.asfortranarray(F)
+
+
+def config(n_gpus):
+    return {"workload": "laplace_dlp_star_r1+0.3cos5t_N65536_tol1e-8_8rhs",
+            "points": N_POINTS, "dofs": N_POINTS, "nrhs": NRHS, "id_tol": TOL,
+            "max_leaf_dofs": LEAF, "num_proxy_points": NPP, "parallelism": f"replicas{n_gpus}",
+            "l2": "256 MiB device buffer rewritten between timed steps"}
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (one process per GPU, independent replicas)
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# device helpers through the CUDA runtime (no framework on the timed path)
+# ---------------------------------------------------------------------------
+class Cudart:
+    def __init__(self):
+        cands = ["libcudart.so", "libcudart.so.13"] + sorted(
+            glob.glob("/usr/local/cuda/lib64/libcudart.so*"))
+        self.lib = None
+        for c in cands:
+            try:
+                self.lib = ctypes.CDLL(c)
+                break
+            except OSError:
+                continue
+        if self.lib is None:
+            raise RuntimeError("libcudart not found")
+        self.flush_buf = ctypes.c_void_p()
+        self.flush_bytes = 256 << 20
+
+    def set_device(self, d):
+        assert self.lib.cudaSetDevice(d) == 0
+
+    def malloc(self, nbytes):
+        p = ctypes.c_void_p()
+        assert self.lib.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(nbytes)) == 0
+        return p
+
+    def free(self, p):
+        self.lib.cudaFree(p)
+
+    def memcpy_htod(self, dst, src_np):
+        assert self.lib.cudaMemcpy(dst, src_np.ctypes.data_as(ctypes.c_void_p),
+                                   ctypes.c_size_t(src_np.nbytes), 1) == 0
+
+    def memcpy_dtoh(self, dst_np, src):
+        assert self.lib.cudaMemcpy(dst_np.ctypes.data_as(ctypes.c_void_p), src,
+                                   ctypes.c_size_t(dst_np.nbytes), 2) == 0
+
+    def flush_l2(self):
+        if not self.flush_buf.value:
+            self.flush_buf = self.malloc(self.flush_bytes)
+        self.lib.cudaMemset(self.flush_buf, ctypes.c_int(1), ctypes.c_size_t(self.flush_bytes))
+        self.lib.cudaDeviceSynchronize()
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def time_arm(capi, geo, F, precision, steps, warmup, cu, dist):
+    s = capi.Solver(geo, capi.RS_LAPLACE, TOL, leaf=LEAF, npp=NPP, precision=precision,
+                    refine_tol=1e-12, refine_max_iters=8, fp32_id_tol=1e-6, device=dist.local)
+    s.build_tree()
+    D = s.D
+    d_f = cu.malloc(F.nbytes)
+    d_mu = cu.malloc(F.nbytes)
+    cu.memcpy_htod(d_f, F)
+    for _ in range(warmup):
+        s.factor()
+        s.solve_device(d_f.value, NRHS, d_mu.value)
+        s.synchronize()
+    times = []
+    launches = 0
+    for _ in range(steps):
+        cu.flush_l2()
+        dist.barrier()
+        s.synchronize()
+        s.timer_start()
+        s.factor()
+        s.solve_device(d_f.value, NRHS, d_mu.value)
+        ms = s.timer_stop()
+        times.append(ms)
+        launches += s.stats()["kernel_launches"]
+    mu = np.zeros_like(F)
+    cu.memcpy_dtoh(mu, d_mu)
+    st = s.stats()
+    cu.free(d_f)
+    cu.free(d_mu)
+    return s, times, mu, st, launches
+
+
+def e2e_arm(capi, geo, F, precision, steps, dist):
+    """Through the C ABI with host buffers: geometry and right-hand sides go
+    host -> device and the solutions come back inside the timed region
+    (tree build included, as a user of the library pays it)."""
+    times = []
+    h2d = d2h = 0
+    for _ in range(steps):
+        dist.barrier()
+        t0 = time.perf_counter()
+        s = capi.Solver(geo, capi.RS_LAPLACE, TOL, leaf=LEAF, npp=NPP, precision=precision,
+                        refine_tol=1e-12, refine_max_iters=8, fp32_id_tol=1e-6,
+                        device=dist.local)
+        s.factor()
+        mu, _ = s.solve(F)
+        t1 = time.perf_counter()
+        s.close()
+        times.append((t1 - t0) * 1e3)
+        h2d = 6 * geo.n * 8 + F.nbytes
+        d2h = mu.nbytes
+    return times, h2d, d2h
+
+
+def oracle_reference(geo, F, threads):
+    import oracle as O
+
+    o = O.OracleSolver(geo, 0, 1, TOL, LEAF, NPP, threads)
+    o.build_tree()
+    tf = o.factor()
+    mu, _ = o.solve(F)
+    return mu, tf, o.solve_seconds
+
+
+def rel_err(mu, ref):
+    return max(np.linalg.norm(mu[:, c] - ref[:, c]) / np.linalg.norm(ref[:, c])
+               for c in range(ref.shape[1]))
+
+
+def run_gpu(args):
+    from rskel import capi
+
+    dist = Dist()
+    cu = Cudart()
+    cu.set_device(dist.local)
+    geo, F = workload()
+    cores = os.cpu_count() or 1
+    # plain FP64 arm
+    s64, t64, mu64, st64, _ = time_arm(capi, geo, F, capi.RS_FP64, args.steps, args.warmup, cu,
+                                       dist)
+    # FP32 + FP64 refinement arm (headline), clocks sampled during its timed region
+    clk = ClockSampler(dist.local)
+    clk.start()
+    s32, t32, mu32, st32, launches = time_arm(capi, geo, F, capi.RS_FP32_REFINE, args.steps,
+                                              args.warmup, cu, dist)
+    clocks = clk.stop()
+    e2e_t, h2d, d2h = e2e_arm(capi, geo, F, capi.RS_FP32_REFINE, max(1, min(args.steps, 3)), dist)
+    # accuracy against the FP64 oracle (CPU)
+    mu_ref, t_ref_f, t_ref_s = oracle_reference(geo, F, cores)
+    err32 = rel_err(mu32, mu_ref)
+    err64 = rel_err(mu64, mu_ref)
+    ms32 = dist.max(max(t32))
+    ms64 = dist.max(max(t64))
+    ms32_med = statistics.median(t32)
+    ms64_med = statistics.median(t64)
+    e2e_ms = dist.max(statistics.median(e2e_t))
+    dofs = N_POINTS
+    value = dist.sum(dofs) / (ms32 * 1e-3)
+    # roofline of the dominant kernel (batched ID) in the headline arm
+    id_ms_per_step = st32["id_ms"]
+    id_tflops = st32["id_flops"] / (id_ms_per_step * 1e-3) / 1e12 if id_ms_per_step > 0 else 0.0
+    peaks = {"fp32_fma_tflops": 69.8, "fp64_fma_tflops": 1.19}
+    id64_tflops = st64["id_flops"] / (st64["id_ms"] * 1e-3) / 1e12 if st64["id_ms"] > 0 else 0.0
+    cpu_sample = {"value": dofs / (t_ref_f + t_ref_s), "unit": "DOFs/s", "cores": cores,
+                  "kind": "port",
+                  "sample": "one factor + 8-RHS solve of the full workload by the oracle "
+                            "restatement (OpenMP over boxes, all host cores)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOFs/s", "n_gpus": dist.ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded star curve, exterior point-source data)",
+        "config": config(dist.ws),
+        "accuracy": {"rel_err_vs_fp64_oracle": err32, "plain_fp64_rel_err": err64,
+                     "refine_iters": st32["refine_iters"],
+                     "refine_residual": st32["refine_residual"]},
+        "plain_fp64": {"value": dofs / (ms64 * 1e-3), "ms_per_step": ms64,
+                       "ms_median": ms64_med, "dev_factor_ms": st64["dev_factor_ms"],
+                       "id_ms": st64["id_ms"], "decouple_ms": st64["decouple_ms"],
+                       "id_tflops": id64_tflops,
+                       "id_frac_of_fp64_fma_peak": id64_tflops / peaks["fp64_fma_tflops"]},
+        "speedup_vs_plain_fp64": ms64 / ms32,
+        "ms_median": ms32_med,
+        "e2e": {"value": dist.sum(dofs) / (e2e_ms * 1e-3), "unit": "DOFs/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp32_fma", "kernel": "id_kernel<float>", "achieved": id_tflops,
+                     "peak": peaks["fp32_fma_tflops"], "unit": "TFLOP/s",
+                     "frac": id_tflops / peaks["fp32_fma_tflops"], "traffic": None,
+                     "peak_source": "FMA microbenchmark on this pool (profiles/fma_peaks.md)"},
+        "cpu_baseline": cpu_sample,
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def run_reference(args):
+    dist = Dist()
+    if dist.rank != 0:
+        dist.close()
+        return
+    import oracle as O
+
+    geo, F = workload()
+    cores = os.cpu_count() or 1
+    o = O.OracleSolver(geo, 0, 1, TOL, LEAF, NPP, cores)
+    o.build_tree()
+    for _ in range(args.warmup):
+        o.factor()
+        o.solve(F)
+        o = O.OracleSolver(geo, 0, 1, TOL, LEAF, NPP, cores)
+        o.build_tree()
+    times = []
+    for _ in range(args.steps):
+        o = O.OracleSolver(geo, 0, 1, TOL, LEAF, NPP, cores)
+        o.build_tree()
+        t0 = time.perf_counter()
+        o.factor()
+        o.solve(F)
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = max(times)
+    v = N_POINTS / (ms * 1e-3)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "DOFs/s", "n_gpus": dist.ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded star curve, exterior point-source data)",
+            "config": config(dist.ws),
+            "cpu_baseline": {"value": v, "unit": "DOFs/s", "cores": cores, "kind": "port",
+                             "sample": "full workload per step (factor + 8-RHS solve)"},
+            "e2e": {"value": v, "unit": "DOFs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -104,6 +104,21 @@ __device__ __forceinline__ void load_dof(const Geo<double>& g, int sd, int dof, 
   d.comp[slot] = dof - p * sd;
 }
 
+// Reciprocal: correctly rounded single-precision reciprocal; for double, a
+// single-precision seed refined by two Newton-Raphson steps
+// y <- y + y (1 - d y) (quadratic convergence: 2^-23 -> 2^-46 -> below one
+// ulp), which costs four FP64 FMAs instead of a full-precision division.
+__device__ __forceinline__ float rcp(float d) { return __frcp_rn(d); }
+__device__ __forceinline__ double rcp(double d) {
+  const double ad = fabs(d);
+  if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+  double y = (double)__frcp_rn((float)d);
+  double e = fma(-d, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-d, y, 1.0);
+  return fma(y, e, y);
+}
+
 // Double-layer kernel entries (ie_solver/kernel/kernel.cpp:29-91, 123-290).
 // Target (tx, ty, tn) component ta; source (sx, sy, sn, sw, skap) component sb.
 template <class Real>
@@ -114,7 +129,7 @@ __device__ __forceinline__ Real kernel_entry(int pde, Real tx, Real ty, Real tnx
     const Real scale = (Real)(1.0 / (2.0 * CUDART_PI));
     if (tx == sx && ty == sy) return (Real)0.5 + (Real)0.5 * skap * sw * scale;
     Real r0 = tx - sx, r1 = ty - sy;
-    return -sw * scale * (r0 * snx + r1 * sny) / (r0 * r0 + r1 * r1);
+    return -sw * scale * (r0 * snx + r1 * sny) * rcp(r0 * r0 + r1 * r1);
   }
   if (pde == kStokes) {
     const Real scale = (Real)(1.0 / CUDART_PI);
@@ -130,7 +145,8 @@ __device__ __forceinline__ Real kernel_entry(int pde, Real tx, Real ty, Real tnx
     }
     Real r0 = tx - sx, r1 = ty - sy;
     Real d = r0 * r0 + r1 * r1;
-    Real pot = sw * scale * (r0 * snx + r1 * sny) / (d * d);
+    const Real id = rcp(d);
+    Real pot = sw * scale * (r0 * snx + r1 * sny) * (id * id);
     Real ra = ta == 0 ? r0 : r1;
     Real rb = sb == 0 ? r0 : r1;
     return pot * ra * rb + sw * tn_a * sn_b;
@@ -139,7 +155,7 @@ __device__ __forceinline__ Real kernel_entry(int pde, Real tx, Real ty, Real tnx
   const Real scale = (Real)(1.0 / (2.0 * CUDART_PI));
   if (tx == sx && ty == sy) return sw - (Real)0.5 + (Real)0.5 * skap * sw * scale;
   Real r0 = tx - sx, r1 = ty - sy;
-  return sw + sw * scale * (r0 * tnx + r1 * tny) / (r0 * r0 + r1 * r1);
+  return sw + sw * scale * (r0 * tnx + r1 * tny) * rcp(r0 * r0 + r1 * r1);
 }
 
 template <class Real>

@@ -25,19 +25,70 @@
 
 namespace rskel {
 
-constexpr int kChunk = 64;  // rows per fold (two per lane)
+constexpr int kChunk = 64;  // rows per fold
+
+// Thread layout inside a CTA: column c of a tile is owned by a team of TS
+// consecutive threads (TS = 8, 4, 2, 1 for n <= 32, 64, 128, > 128); team
+// thread t handles rows t, t + TS, ...  A Householder step then needs only
+// team-local shuffles for every column's dot product and one CTA barrier
+// (the reflector of step j+1 is formed by the team that just updated
+// column j+1, and the reflector vector is double-buffered).
+struct Layout {
+  int t;       // this thread's index in its team
+  int c0;      // first column owned
+  int cstep;   // column stride between passes
+  int ld;      // row-major leading dimension of tiles (padded)
+};
+
+// Team size for boxes of up to n DOFs.
+__host__ __device__ inline int team_size(int n) { return n <= 64 ? 4 : (n <= 128 ? 2 : 1); }
+
+// Row-major leading dimension: n padded so that ld = 32 / ts (mod 32), which
+// makes a warp's (team, row) accesses hit distinct FP32 banks.
+__host__ __device__ inline int layout_ld(int n, int ts) {
+  const int want = (32 / ts) & 31;
+  int ld = n;
+  while ((ld & 31) != want) ++ld;
+  return ld;
+}
+
+template <int TS>
+__device__ __forceinline__ Layout make_layout(int n) {
+  Layout L;
+  L.t = threadIdx.x % TS;
+  L.c0 = threadIdx.x / TS;
+  L.cstep = blockDim.x / TS;
+  L.ld = layout_ld(n, TS);
+  return L;
+}
+
+// Lanes of this thread's team (teams are aligned groups of ts lanes).
+__device__ __forceinline__ unsigned team_mask(int ts) {
+  const int base = (threadIdx.x & 31) & ~(ts - 1);
+  return ts >= 32 ? 0xffffffffu : (((1u << ts) - 1u) << base);
+}
+
+// Sum over the thread's team; teams may diverge from one another, so every
+// shuffle names only the team's lanes.
+template <int TS, class T>
+__device__ __forceinline__ T team_sum(T v) {
+  const unsigned m = team_mask(TS);
+#pragma unroll
+  for (int o = TS >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o);
+  return v;
+}
 
 template <class Real>
 struct IdShared {
-  Real* R;        // n x n, ld = n
-  Real* C;        // kChunk x n, ld = kChunk
-  Real* v;        // kChunk
+  Real* R;        // n x n, row major, ld = L.ld
+  Real* C;        // kChunk x n, row major, ld = L.ld
+  Real* v;        // 2 x max(kChunk, n): double-buffered reflector
   double* vn1;    // n
   double* vn2;    // n
   int* perm;      // n
-  double* red_v;  // kWarps
-  int* red_i;     // kWarps
-  double* scal;   // [0] tau, [1] scale, [2] thresh, [3] flag
+  double* scal;   // cpqr: [2] thresh (double)
+  Real* rs;       // fold: [0..3] {tau, scale} x 2 buffers; cpqr: [0] tau
+  int* is;        // cpqr: [0] stop flag, [1] pivot
   DofSoA<Real> act;
   DofSoA<Real> row;
   int* kind;      // kChunk
@@ -47,14 +98,15 @@ template <class Real>
 __host__ __device__ size_t id_smem_bytes(int n, bool tile_in_smem) {
   size_t b = 0;
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const int ld = layout_ld(n, team_size(n));
   if (tile_in_smem) {
-    b += al(sizeof(Real) * (size_t)n * n);
-    b += al(sizeof(Real) * (size_t)kChunk * n);
+    b += al(sizeof(Real) * (size_t)n * ld);
+    b += al(sizeof(Real) * (size_t)kChunk * ld);
   }
-  b += al(sizeof(Real) * kChunk);
+  b += al(sizeof(Real) * 2 * (size_t)(n > kChunk ? n : kChunk));
   b += 2 * al(sizeof(double) * n);
   b += al(sizeof(int) * n);
-  b += al(sizeof(double) * kWarps) + al(sizeof(int) * kWarps) + al(sizeof(double) * 4);
+  b += al(sizeof(double) * 8) + al(sizeof(Real) * 8) + al(sizeof(int) * 8);
   b += dofs_bytes<Real>(n) + dofs_bytes<Real>(kChunk);
   b += al(sizeof(int) * kChunk);
   return b;
@@ -64,9 +116,9 @@ size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem) {
   return fp32 ? id_smem_bytes<float>(n, tile_in_smem) : id_smem_bytes<double>(n, tile_in_smem);
 }
 
-// Fills chunk rows [c0, c0 + cnt) of the virtual ID matrix into S.C.
+// Fills chunk rows [c0, c0 + cnt) of the virtual ID matrix into S.C (row major).
 template <class Real>
-__device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S, int c0,
+__device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S, int ld, int c0,
                            int cnt, double ox, double oy) {
   const int n = t.n, q = t.q;
   const int sd = p.sd;
@@ -76,7 +128,7 @@ __device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S
     const double* A = p.dense + t.dense_off;
     for (int e = threadIdx.x; e < kChunk * n; e += blockDim.x) {
       int i = e % kChunk, j = e / kChunk;
-      S.C[i + (size_t)kChunk * j] = i < cnt ? (Real)A[(c0 + i) + (size_t)t.m_dense * j] : (Real)0;
+      S.C[(size_t)i * ld + j] = i < cnt ? (Real)A[(c0 + i) + (size_t)t.m_dense * j] : (Real)0;
     }
     __syncthreads();
     return;
@@ -111,172 +163,247 @@ __device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S
   }
   __syncthreads();
   for (int e = threadIdx.x; e < kChunk * n; e += blockDim.x) {
-    int i = e % kChunk, j = e / kChunk;
+    int i = e / n, j = e % n;
     int kind = S.kind[i];
     Real val = (Real)0;
     if (kind == 0 || kind == 2) val = kernel_dofs<Real>(p.pde, S.row, i, S.act, j);
     else if (kind == 1 || kind == 3) val = kernel_dofs<Real>(p.pde, S.act, j, S.row, i);
-    S.C[i + (size_t)kChunk * j] = val;
+    S.C[(size_t)i * ld + j] = val;
   }
   __syncthreads();
 }
 
-// Folds the chunk into R: Householder QR of [R; C] (R upper triangular).
-template <class Real>
-__device__ void fold_chunk(int n, IdShared<Real>& S) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Folds the chunk into R: Householder QR of [R; C] with R upper triangular.
+// Reflector j has support {row j of R} u {all chunk rows}; its chunk part is
+// column j of C itself (scaled), so nothing but two scalars is published per
+// step.  The team that owns column j+1 accumulates that column's squared
+// norm while applying reflector j, so forming reflector j+1 costs a few
+// scalar operations between barriers.  Each team thread touches kChunk / TS
+// rows (a compile-time count, fully unrolled).
+template <class Real, int TS>
+__device__ void fold_chunk(int n, const Layout& L, int step0, IdShared<Real>& S) {
+  constexpr int kRows = kChunk / TS;
   Real* R = S.R;
   Real* C = S.C;
-  for (int j = 0; j < n; ++j) {
-    if (warp == 0) {
-      Real c0 = C[lane + (size_t)kChunk * j], c1 = C[lane + 32 + (size_t)kChunk * j];
-      double ss = warp_sum((double)c0 * c0 + (double)c1 * c1);
-      double alpha = (double)R[j + (size_t)n * j];
-      double tau = 0.0, scale = 0.0;
-      if (ss > 0.0) {
-        double beta = -copysign(sqrt(alpha * alpha + ss), alpha);
-        tau = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-        if (lane == 0) R[j + (size_t)n * j] = (Real)beta;
-      }
-      S.v[lane] = (Real)(c0 * scale);
-      S.v[lane + 32] = (Real)(c1 * scale);
-      if (lane == 0) S.scal[0] = tau;
+  Real* ssq = S.v;  // squared chunk-column norms, n entries
+  const int t = L.t, ld = L.ld;
+  const Real* Ct = C + (size_t)t * ld;  // this thread's first row
+  const size_t rs = (size_t)TS * ld;    // stride between this thread's rows
+  auto col_sq = [&](int c) {
+    Real ss = 0;
+#pragma unroll
+    for (int q = 0; q < kRows; ++q) {
+      const Real cv = Ct[q * rs + c];
+      ss += cv * cv;
     }
-    __syncthreads();
-    const Real tau = (Real)S.scal[0];
-    if (tau != (Real)0) {
-      const Real v0 = S.v[lane], v1 = S.v[lane + 32];
-      for (int c = j + 1 + warp; c < n; c += kWarps) {
-        Real* cc = C + (size_t)kChunk * c;
-        Real part = v0 * cc[lane] + v1 * cc[lane + 32];
-        part = warp_sum(part);
-        Real wv = R[j + (size_t)n * c] + part;
-        Real tw = tau * wv;
-        cc[lane] -= tw * v0;
-        cc[lane + 32] -= tw * v1;
-        if (lane == 0) R[j + (size_t)n * c] -= tw;
-      }
-    }
-    __syncthreads();
+    return team_sum<TS>(ss);
+  };
+  for (int c = L.c0; c < n; c += L.cstep) {
+    const Real ss = col_sq(c);
+    if (t == 0) ssq[c] = ss;
   }
+  for (int j = 0; j < n; ++j) {
+    const int buf = (step0 + j) & 1;
+    Real* sc = S.rs + 2 * buf;  // {tau, scale}
+    if (L.c0 == (j % L.cstep) && t == 0) {  // owner of column j forms reflector j
+      const Real ss = ssq[j];
+      const Real alpha = R[(size_t)j * ld + j];
+      Real tau = 0, scale = 0;
+      if (ss > (Real)0) {
+        const Real beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+        tau = (beta - alpha) / beta;
+        scale = (Real)1 / (alpha - beta);
+        R[(size_t)j * ld + j] = beta;
+      }
+      sc[0] = tau;
+      sc[1] = scale;
+    }
+    __syncthreads();
+    const Real tau = sc[0];
+    if (tau == (Real)0) {
+      // identity reflector: column j+1 is unchanged, but its norm must be
+      // current for the next step
+      for (int c = L.c0; c < n; c += L.cstep)
+        if (c == j + 1) {
+          const Real ss = col_sq(c);
+          if (t == 0) ssq[c] = ss;
+        }
+      continue;
+    }
+    const Real scale = sc[1];
+    Real cj[kRows];
+#pragma unroll
+    for (int q = 0; q < kRows; ++q) cj[q] = Ct[q * rs + j];
+    for (int c = L.c0; c < n; c += L.cstep) {
+      if (c <= j) continue;
+      Real* Cc = C + (size_t)t * ld + c;
+      Real p4[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < kRows; ++q) p4[q & 3] += cj[q] * Cc[q * rs];
+      Real part = team_sum<TS>((p4[0] + p4[1]) + (p4[2] + p4[3]));
+      const Real tw = tau * (R[(size_t)j * ld + c] + part * scale);
+      const Real tws = tw * scale;
+      if (c == j + 1) {
+        Real ss = 0;
+#pragma unroll
+        for (int q = 0; q < kRows; ++q) {
+          const Real nv = Cc[q * rs] - tws * cj[q];
+          Cc[q * rs] = nv;
+          ss += nv * nv;
+        }
+        ss = team_sum<TS>(ss);
+        if (t == 0) ssq[c] = ss;
+      } else {
+#pragma unroll
+        for (int q = 0; q < kRows; ++q) Cc[q * rs] -= tws * cj[q];
+      }
+      if (t == 0) R[(size_t)j * ld + c] -= tw;
+    }
+  }
+  __syncthreads();
 }
 
-// Column-pivoted Householder QR of the n x n tile R with early stop at the
-// rank (LAPACK dlaqp2 pivoting and norm downdating).  Returns k.
-template <class Real>
-__device__ int cpqr_rank(int n, double tol, IdShared<Real>& S) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Column-pivoted Householder QR of the n x n tile R (row major) with early
+// stop at the rank (LAPACK dlaqp2 pivoting with its norm-downdating
+// safeguard).  The partial norms that choose pivots are kept in the element
+// type; the norm that sets the rank (the pivot column's trailing norm, which
+// is |R_ii|) is accumulated in double.  Returns k.
+template <class Real, int TS>
+__device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) {
   Real* A = S.R;
-  const double eps_data = sizeof(Real) == 4 ? 5.9604644775390625e-08 : 1.1102230246251565e-16;
-  const double tol3z = sqrt(eps_data);
-  for (int c = warp; c < n; c += kWarps) {
-    double s = 0.0;
-    for (int r = lane; r < n; r += 32) { double a = (double)A[r + (size_t)n * c]; s += a * a; }
-    s = warp_sum(s);
-    if (lane == 0) { S.vn1[c] = sqrt(s); S.vn2[c] = sqrt(s); S.perm[c] = c; }
+  constexpr int ts = TS;
+  const int t = L.t, ld = L.ld;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Real tol3z = sizeof(Real) == 4 ? (Real)2.44140625e-4 : (Real)1.0536712127723509e-08;
+  Real* vn1 = reinterpret_cast<Real*>(S.vn1);
+  Real* vn2 = reinterpret_cast<Real*>(S.vn2);
+  for (int c = L.c0; c < n; c += L.cstep) {
+    Real s = 0;
+    for (int r = t; r < n; r += ts) { const Real a = A[(size_t)r * ld + c]; s += a * a; }
+    s = team_sum<TS>(s);
+    if (t == 0) { vn1[c] = sqrt(s); vn2[c] = sqrt(s); S.perm[c] = c; }
   }
   __syncthreads();
   int k = 0;
+  Real* v = S.v;
   for (int i = 0; i < n; ++i) {
-    int pvt = block_argmax(S.vn1, i, n, S.red_v, S.red_i);
+    // pivot: first index of the largest partial norm (idamax)
+    if (warp == 0) {
+      Real best = -1;
+      int bi = n;
+      for (int c = i + lane; c < n; c += 32) {
+        const Real val = vn1[c];
+        if (val > best) { best = val; bi = c; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const Real ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (lane == 0) {
+        S.is[1] = bi;
+        if (bi != i) {
+          int tp = S.perm[bi]; S.perm[bi] = S.perm[i]; S.perm[i] = tp;
+          vn1[bi] = vn1[i];
+          vn2[bi] = vn2[i];
+        }
+      }
+    }
+    __syncthreads();
+    const int pvt = S.is[1];
     if (pvt != i) {
       for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        Real t = A[r + (size_t)n * pvt];
-        A[r + (size_t)n * pvt] = A[r + (size_t)n * i];
-        A[r + (size_t)n * i] = t;
-      }
-      if (threadIdx.x == 0) {
-        int tp = S.perm[pvt]; S.perm[pvt] = S.perm[i]; S.perm[i] = tp;
-        S.vn1[pvt] = S.vn1[i];
-        S.vn2[pvt] = S.vn2[i];
+        Real tmp = A[(size_t)r * ld + pvt];
+        A[(size_t)r * ld + pvt] = A[(size_t)r * ld + i];
+        A[(size_t)r * ld + i] = tmp;
       }
       __syncthreads();
     }
-    if (warp == 0) {
+    if (L.c0 == (i % L.cstep)) {
       double xs = 0.0;
-      for (int r = i + 1 + lane; r < n; r += 32) { double a = (double)A[r + (size_t)n * i]; xs += a * a; }
-      xs = warp_sum(xs);
-      double alpha = (double)A[i + (size_t)n * i];
-      double nrm = sqrt(alpha * alpha + xs);
+      for (int r = i + 1 + t; r < n; r += ts) { const double a = (double)A[(size_t)r * ld + i]; xs += a * a; }
+      xs = team_sum<TS>(xs);
+      const double alpha = (double)A[(size_t)i * ld + i];
+      const double nrm = sqrt(alpha * alpha + xs);  // |R_ii|, sets the rank
       int stop = 0;
       if (i == 0) {
-        if (lane == 0) S.scal[2] = fabs(tol * nrm);
+        if (t == 0) S.scal[2] = fabs(tol * nrm);
       } else if (nrm < S.scal[2]) {
         stop = 1;
       }
-      double tau = 0.0, scale = 0.0;
+      Real tau = 0, scale = 0;
       if (!stop && xs > 0.0) {
-        double beta = -copysign(nrm, alpha);
-        tau = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-        for (int r = i + 1 + lane; r < n; r += 32) A[r + (size_t)n * i] = (Real)((double)A[r + (size_t)n * i] * scale);
-        if (lane == 0) A[i + (size_t)n * i] = (Real)beta;
+        const Real a = (Real)alpha;
+        const Real beta = -copysign((Real)nrm, a);
+        tau = (beta - a) / beta;
+        scale = (Real)1 / (a - beta);
+        if (t == 0) A[(size_t)i * ld + i] = beta;
       }
-      if (lane == 0) { S.scal[0] = tau; S.scal[3] = stop; }
+      for (int r = i + 1 + t; r < n; r += ts) v[r] = A[(size_t)r * ld + i] * scale;
+      if (t == 0) { S.rs[0] = tau; S.is[0] = stop; }
     }
     __syncthreads();
-    if (S.scal[3] != 0.0) { k = i; break; }
-    const Real tau = (Real)S.scal[0];
-    for (int c = i + 1 + warp; c < n; c += kWarps) {
-      Real* cc = A + (size_t)n * c;
-      const Real* vv = A + (size_t)n * i;
-      Real part = (Real)0;
-      for (int r = i + 1 + lane; r < n; r += 32) part += vv[r] * cc[r];
-      part = warp_sum(part);
-      Real wv = cc[i] + part;
-      Real tw = tau * wv;
+    if (S.is[0] != 0) { k = i; break; }
+    const Real tau = S.rs[0];
+    for (int c = L.c0; c < n; c += L.cstep) {
+      if (c <= i) continue;
+      Real aic = A[(size_t)i * ld + c];
       if (tau != (Real)0) {
-        for (int r = i + 1 + lane; r < n; r += 32) cc[r] -= tw * vv[r];
+        Real part = 0;
+        for (int r = i + 1 + t; r < n; r += ts) part += v[r] * A[(size_t)r * ld + c];
+        part = team_sum<TS>(part);
+        const Real tw = tau * (aic + part);
+        for (int r = i + 1 + t; r < n; r += ts) A[(size_t)r * ld + c] -= tw * v[r];
+        aic -= tw;
       }
-      __syncwarp();
-      if (lane == 0 && tau != (Real)0) cc[i] -= tw;
-      __syncwarp();
-      // partial column norm downdate (dlaqp2)
-      double v1 = S.vn1[c];
-      if (v1 != 0.0) {
-        double temp = fabs((double)cc[i]) / v1;
-        temp = 1.0 - temp * temp;
-        temp = temp < 0.0 ? 0.0 : temp;
-        double ratio = v1 / S.vn2[c];
-        double temp2 = temp * ratio * ratio;
-        if (temp2 <= tol3z) {
-          double s = 0.0;
-          for (int r = i + 1 + lane; r < n; r += 32) { double a = (double)cc[r]; s += a * a; }
-          s = warp_sum(s);
-          if (lane == 0) { S.vn1[c] = sqrt(s); S.vn2[c] = sqrt(s); }
-        } else if (lane == 0) {
-          S.vn1[c] = v1 * sqrt(temp);
+      // partial norm downdate: vn1 <- sqrt(vn1^2 - a^2), recomputed when the
+      // remaining fraction (vn1^2 - a^2) / vn2^2 drops below tol3z
+      const Real v1 = vn1[c];
+      if (v1 != (Real)0) {
+        const Real v2 = vn2[c];
+        Real x = v1 * v1 - aic * aic;
+        x = x < (Real)0 ? (Real)0 : x;
+        if (x <= tol3z * v2 * v2) {  // team-uniform decision
+          Real s = 0;
+          for (int r = i + 1 + t; r < n; r += ts) { const Real a = A[(size_t)r * ld + c]; s += a * a; }
+          s = team_sum<TS>(s);
+          if (t == 0) { const Real q = sqrt(s); vn1[c] = q; vn2[c] = q; }
+        } else if (t == 0) {
+          vn1[c] = sqrt(x);
         }
       }
+      __syncwarp(team_mask(ts));
+      if (t == 0) A[(size_t)i * ld + c] = aic;
     }
     __syncthreads();
   }
   return k;
 }
 
-template <class Real>
+template <class Real, int TS>
 __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
   const IdTask t = p.tasks[blockIdx.x];
   const int n = t.n;
+  const Layout L = make_layout<TS>(n);
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
   IdShared<Real> S;
   if (t.scratch_off < 0) {
-    S.R = carve<Real>(sp, n * n);
-    S.C = carve<Real>(sp, kChunk * n);
+    S.R = carve<Real>(sp, n * L.ld);
+    S.C = carve<Real>(sp, kChunk * L.ld);
   } else {
     Real* g = reinterpret_cast<Real*>(p.scratch) + t.scratch_off;
     S.R = g;
-    S.C = g + (size_t)n * n;
+    S.C = g + (size_t)n * L.ld;
   }
-  S.v = carve<Real>(sp, kChunk);
+  S.v = carve<Real>(sp, 2 * (n > kChunk ? n : kChunk));
   S.vn1 = carve<double>(sp, n);
   S.vn2 = carve<double>(sp, n);
   S.perm = carve<int>(sp, n);
-  S.red_v = carve<double>(sp, kWarps);
-  S.red_i = carve<int>(sp, kWarps);
-  S.scal = carve<double>(sp, 4);
+  S.scal = carve<double>(sp, 8);
+  S.rs = carve<Real>(sp, 8);
+  S.is = carve<int>(sp, 8);
   S.act = carve_dofs<Real>(sp, n);
   S.row = carve_dofs<Real>(sp, kChunk);
   S.kind = carve<int>(sp, kChunk);
@@ -289,46 +416,66 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
   if (t.dense_off < 0)
     for (int j = threadIdx.x; j < n; j += blockDim.x)
       load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], ox, oy, S.act, j);
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) S.R[e] = (Real)0;
+  for (int e = threadIdx.x; e < n * L.ld; e += blockDim.x) S.R[e] = (Real)0;
   __syncthreads();
 
   const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
   const int m = t.dense_off >= 0 ? t.m_dense : 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+  int step0 = 0;
   for (int c0 = 0; c0 < m; c0 += kChunk) {
     int cnt = m - c0 < kChunk ? m - c0 : kChunk;
-    fill_chunk<Real>(p, t, S, c0, cnt, ox, oy);
-    fold_chunk<Real>(n, S);
+    fill_chunk<Real>(p, t, S, L.ld, c0, cnt, ox, oy);
+    fold_chunk<Real, TS>(n, L, step0, S);
+    step0 += n;
   }
-  int k = m > 0 ? cpqr_rank<Real>(n, p.tol, S) : 0;
+  int k = m > 0 ? cpqr_rank<Real, TS>(n, p.tol, L, S) : 0;
   if (threadIdx.x == 0) p.ranks[t.slot] = k;
   for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];
   if (k > 0) {
-    // Z = R11^{-1} R12: one warp per column of R12, lanes over rows.
+    // Z = R11^{-1} R12 by back substitution, one team per column of R12.
     const int r = n - k;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int ts = TS;
+    const int tt = L.t, ld = L.ld;
     Real* T = reinterpret_cast<Real*>(p.fac) + t.fac_off + fac_T(k, r);
-    for (int c = warp; c < r; c += kWarps) {
-      Real* z = S.R + (size_t)n * (k + c);  // solve in place in R12's column
+    for (int c = L.c0; c < r; c += L.cstep) {
+      const int col = k + c;
       for (int row = k - 1; row >= 0; --row) {
-        Real zr = z[row] / S.R[row + (size_t)n * row];
-        __syncwarp();
-        for (int q2 = lane; q2 < row; q2 += 32) z[q2] -= zr * S.R[q2 + (size_t)n * row];
-        if (lane == 0) z[row] = zr;
-        __syncwarp();
+        // owner thread of `row` finalises z[row]; the team then updates rows above
+        Real zr = 0;
+        if ((row % ts) == tt) {
+          zr = S.R[(size_t)row * ld + col] * ((Real)1 / S.R[(size_t)row * ld + row]);
+          S.R[(size_t)row * ld + col] = zr;
+        }
+        // broadcast within the team (the owner is lane (row % ts) of the team)
+        const int base = (threadIdx.x & 31) - tt;
+        zr = __shfl_sync(team_mask(ts), zr, base + (row % ts));
+        for (int q2 = tt; q2 < row; q2 += ts) S.R[(size_t)q2 * ld + col] -= zr * S.R[(size_t)q2 * ld + row];
+        __syncwarp(team_mask(ts));
       }
-      for (int row = lane; row < k; row += 32) T[row + (size_t)k * c] = z[row];
+      for (int row = tt; row < k; row += ts) T[row + (size_t)k * c] = S.R[(size_t)row * ld + col];
     }
   }
 }
 
-void launch_id(const IdParams& p, int num_tasks, size_t smem, bool fp32, cudaStream_t st) {
+template <class Real, int TS>
+static void launch_id_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
+  cudaFuncSetAttribute(id_kernel<Real, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  id_kernel<Real, TS><<<num_tasks, kThreads, smem, st>>>(p);
+}
+
+// All tasks of one launch use the team size of its largest box.
+void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
+               cudaStream_t st) {
   if (num_tasks <= 0) return;
+  const int ts = team_size(nmax);
   if (fp32) {
-    cudaFuncSetAttribute(id_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    id_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
+    if (ts == 4) launch_id_t<float, 4>(p, num_tasks, smem, st);
+    else if (ts == 2) launch_id_t<float, 2>(p, num_tasks, smem, st);
+    else launch_id_t<float, 1>(p, num_tasks, smem, st);
   } else {
-    cudaFuncSetAttribute(id_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    id_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
+    if (ts == 4) launch_id_t<double, 4>(p, num_tasks, smem, st);
+    else if (ts == 2) launch_id_t<double, 2>(p, num_tasks, smem, st);
+    else launch_id_t<double, 1>(p, num_tasks, smem, st);
   }
 }
 

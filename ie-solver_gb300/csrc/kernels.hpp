@@ -62,7 +62,8 @@ struct SweepParams {
 size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);
 size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
 
-void launch_id(const IdParams& p, int num_tasks, size_t smem, bool fp32, cudaStream_t st);
+void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
+               cudaStream_t st);
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
                      cudaStream_t st);
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st);

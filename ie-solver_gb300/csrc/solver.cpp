@@ -18,6 +18,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -108,6 +109,7 @@ struct rs_solver {
 
   rs_stats stats;
   int launches = 0;
+  bool trace = false;  // RSKEL_TRACE=1: per-level timing on stderr
 };
 
 // ---------------------------------------------------------------------------
@@ -288,17 +290,20 @@ Factor<double>& factor_of<double>(rs_solver* s) { return s->F64; }
 template <>
 Factor<float>& factor_of<float>(rs_solver* s) { return s->F32; }
 
-// Splits tasks into launches of similar size (so the shared-memory request of
-// a launch fits its boxes) and launches them.
-template <class Task, class Launch>
-void launch_binned(const std::vector<Task>& tasks, const Task* dev_tasks, Launch&& fn) {
-  // tasks are pre-sorted by n; group consecutive tasks with equal ceil(n/32)
+// Splits a level's tasks (sorted by n) into at most three launches: boxes of
+// up to 64 DOFs, larger boxes whose tiles fit in shared memory, and boxes
+// that need global-memory tiles.  Few launches keep every box of a level in
+// flight at once; the shared-memory request of each launch is its largest box.
+template <class Task, class Fits, class Launch>
+void launch_binned(const std::vector<Task>& tasks, const Task* dev_tasks, Fits&& fits,
+                   Launch&& fn) {
+  auto cls = [&](int n) { return n <= 64 ? 0 : (fits(n) ? 1 : 2); };
   size_t i = 0;
   while (i < tasks.size()) {
-    int cls = (tasks[i].n + 31) / 32;
+    const int c = cls(tasks[i].n);
     size_t j = i;
     int nmax = 0;
-    while (j < tasks.size() && (tasks[j].n + 31) / 32 == cls) {
+    while (j < tasks.size() && cls(tasks[j].n) == c) {
       nmax = std::max(nmax, tasks[j].n);
       ++j;
     }
@@ -437,7 +442,7 @@ rs_status factor_impl(rs_solver* s) {
     for (IdTask& t : idt_s)
       if (id_kernel_smem(t.n, f32, true) > kSmemMax) {
         t.scratch_off = (int64_t)scratch_need;
-        scratch_need += (size_t)t.n * t.n + 64 * (size_t)t.n + 64;
+        scratch_need += (size_t)(t.n + 32) * (t.n + 64) + 64;
       }
     for (DecoupleTask& t : dct_s)
       if (decouple_kernel_smem(t.n, f32, true) > kSmemMax) {
@@ -482,11 +487,13 @@ rs_status factor_impl(rs_solver* s) {
     ip.scratch = F.scratch.p;
     ip.dense = nullptr;
     CU(cudaEventRecord(s->ev_a, s->stream));
-    launch_binned(idt_s, s->id_tasks.p, [&](const IdTask* dt, int cnt, int nmax) {
+    auto id_fits = [&](int n) { return id_kernel_smem(n, f32, true) <= kSmemMax; };
+    auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
+    launch_binned(idt_s, s->id_tasks.p, id_fits, [&](const IdTask* dt, int cnt, int nmax) {
       IdParams q = ip;
       q.tasks = dt;
       bool in_smem = id_kernel_smem(nmax, f32, true) <= kSmemMax;
-      launch_id(q, cnt, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
+      launch_id(q, cnt, nmax, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
       ++s->launches;
     });
     CU(cudaGetLastError());
@@ -506,7 +513,7 @@ rs_status factor_impl(rs_solver* s) {
     dp.epool = F.epool.p;
     dp.scratch = F.scratch.p;
     dp.status = s->status.p;
-    launch_binned(dct_s, s->dc_tasks.p, [&](const DecoupleTask* dt, int cnt, int nmax) {
+    launch_binned(dct_s, s->dc_tasks.p, dc_fits, [&](const DecoupleTask* dt, int cnt, int nmax) {
       DecoupleParams q = dp;
       q.tasks = dt;
       bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
@@ -530,6 +537,20 @@ rs_status factor_impl(rs_solver* s) {
     cudaEventElapsedTime(&ms_dc, s->ev_b, s->ev_f1);
     s->stats.id_ms += ms_id;
     s->stats.decouple_ms += ms_dc;
+    if (s->trace) {
+      int mmax = 0, nmax = 0;
+      double msum = 0;
+      for (size_t q = 0; q < idt.size(); ++q) {
+        mmax = std::max(mmax, m_of_slot[q]);
+        nmax = std::max(nmax, idt[q].n);
+        msum += m_of_slot[q];
+      }
+      std::fprintf(stderr,
+                   "[rskel] level %2d: %5zu ID boxes (m max %5d avg %6.0f, n max %4d), %5zu "
+                   "eliminations; ID %.3f ms, Schur %.3f ms\n",
+                   lv, idt.size(), mmax, idt.empty() ? 0.0 : msum / idt.size(), nmax, dct.size(),
+                   ms_id, ms_dc);
+    }
     for (size_t c = 0; c < cand_ids.size(); ++c) {
       const int id = cand_ids[c];
       NodeState& S = s->st[id];
@@ -991,6 +1012,8 @@ rs_status rs_create(const rs_config* cfg, rs_solver** out) {
   if (cfg->precision != RS_FP64 && cfg->precision != RS_FP32_REFINE) return RS_ERR_ARG;
   rs_solver* s = new rs_solver();
   s->cfg = *cfg;
+  const char* tr = std::getenv("RSKEL_TRACE");
+  s->trace = tr && tr[0] == '1';
   s->sd = want_sd;
   s->fp32 = cfg->precision == RS_FP32_REFINE;
   if (s->fp32 && !(s->cfg.fp32_id_tol > 0)) s->cfg.fp32_id_tol = 1e-6;
@@ -1220,7 +1243,7 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
   for (IdTask& t : sorted)
     if (id_kernel_smem(t.n, false, true) > kSmemMax) {
       t.scratch_off = (int64_t)scratch;
-      scratch += (size_t)t.n * t.n + 64 * (size_t)t.n + 64;
+      scratch += (size_t)(t.n + 32) * (t.n + 64) + 64;
     }
   DevBuf<double> dA, dZ, dS;
   DevBuf<int> dP, dR;
@@ -1243,11 +1266,12 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
   ip.dense = dA.p;
   ip.sd = 1;
   ip.npp = 1;
-  launch_binned(sorted, dT.p, [&](const IdTask* dt, int cnt, int nmax) {
+  auto id_fits = [&](int nn) { return id_kernel_smem(nn, false, true) <= kSmemMax; };
+  launch_binned(sorted, dT.p, id_fits, [&](const IdTask* dt, int cnt, int nmax) {
     IdParams q = ip;
     q.tasks = dt;
     bool in_smem = id_kernel_smem(nmax, false, true) <= kSmemMax;
-    launch_id(q, cnt, id_kernel_smem(nmax, false, in_smem), false, s->stream);
+    launch_id(q, cnt, nmax, id_kernel_smem(nmax, false, in_smem), false, s->stream);
   });
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(ranks, dR.p, count * 4, cudaMemcpyDeviceToHost, s->stream));

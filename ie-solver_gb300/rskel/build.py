@@ -80,7 +80,7 @@ def build(verbose=False, force=False):
             if verbose and warn:
                 print(warn)
     if force or jobs or _stale(LIB, objs):
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-Xlinker", "--no-undefined"]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)
