@@ -103,7 +103,7 @@ __host__ __device__ size_t id_smem_bytes(int n, bool tile_in_smem) {
     b += al(sizeof(Real) * (size_t)n * ld);
     b += al(sizeof(Real) * (size_t)kChunk * ld);
   }
-  b += al(sizeof(Real) * 2 * (size_t)(n > kChunk ? n : kChunk));
+  b += al(sizeof(Real) * (3 * (size_t)(n > kChunk ? n : kChunk) + 3 * 32 * 32));
   b += 2 * al(sizeof(double) * n);
   b += al(sizeof(int) * n);
   b += al(sizeof(double) * 8) + al(sizeof(Real) * 8) + al(sizeof(int) * 8);
@@ -263,13 +263,13 @@ __device__ void fold_chunk(int n, const Layout& L, int step0, IdShared<Real>& S)
   __syncthreads();
 }
 
-// Column-pivoted Householder QR of the n x n tile R (row major) with early
+// Column-pivoted Householder QR of the mr x n tile R (row major) with early
 // stop at the rank (LAPACK dlaqp2 pivoting with its norm-downdating
 // safeguard).  The partial norms that choose pivots are kept in the element
 // type; the norm that sets the rank (the pivot column's trailing norm, which
 // is |R_ii|) is accumulated in double.  Returns k.
 template <class Real, int TS>
-__device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) {
+__device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Real>& S) {
   Real* A = S.R;
   constexpr int ts = TS;
   const int t = L.t, ld = L.ld;
@@ -279,14 +279,15 @@ __device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) 
   Real* vn2 = reinterpret_cast<Real*>(S.vn2);
   for (int c = L.c0; c < n; c += L.cstep) {
     Real s = 0;
-    for (int r = t; r < n; r += ts) { const Real a = A[(size_t)r * ld + c]; s += a * a; }
+    for (int r = t; r < mr; r += ts) { const Real a = A[(size_t)r * ld + c]; s += a * a; }
     s = team_sum<TS>(s);
     if (t == 0) { vn1[c] = sqrt(s); vn2[c] = sqrt(s); S.perm[c] = c; }
   }
   __syncthreads();
   int k = 0;
   Real* v = S.v;
-  for (int i = 0; i < n; ++i) {
+  const int kmax = n < mr ? n : mr;
+  for (int i = 0; i < kmax; ++i) {
     // pivot: first index of the largest partial norm (idamax)
     if (warp == 0) {
       Real best = -1;
@@ -313,7 +314,7 @@ __device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) 
     __syncthreads();
     const int pvt = S.is[1];
     if (pvt != i) {
-      for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      for (int r = threadIdx.x; r < mr; r += blockDim.x) {
         Real tmp = A[(size_t)r * ld + pvt];
         A[(size_t)r * ld + pvt] = A[(size_t)r * ld + i];
         A[(size_t)r * ld + i] = tmp;
@@ -322,7 +323,7 @@ __device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) 
     }
     if (L.c0 == (i % L.cstep)) {
       double xs = 0.0;
-      for (int r = i + 1 + t; r < n; r += ts) { const double a = (double)A[(size_t)r * ld + i]; xs += a * a; }
+      for (int r = i + 1 + t; r < mr; r += ts) { const double a = (double)A[(size_t)r * ld + i]; xs += a * a; }
       xs = team_sum<TS>(xs);
       const double alpha = (double)A[(size_t)i * ld + i];
       const double nrm = sqrt(alpha * alpha + xs);  // |R_ii|, sets the rank
@@ -340,7 +341,7 @@ __device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) 
         scale = (Real)1 / (a - beta);
         if (t == 0) A[(size_t)i * ld + i] = beta;
       }
-      for (int r = i + 1 + t; r < n; r += ts) v[r] = A[(size_t)r * ld + i] * scale;
+      for (int r = i + 1 + t; r < mr; r += ts) v[r] = A[(size_t)r * ld + i] * scale;
       if (t == 0) { S.rs[0] = tau; S.is[0] = stop; }
     }
     __syncthreads();
@@ -351,10 +352,10 @@ __device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) 
       Real aic = A[(size_t)i * ld + c];
       if (tau != (Real)0) {
         Real part = 0;
-        for (int r = i + 1 + t; r < n; r += ts) part += v[r] * A[(size_t)r * ld + c];
+        for (int r = i + 1 + t; r < mr; r += ts) part += v[r] * A[(size_t)r * ld + c];
         part = team_sum<TS>(part);
         const Real tw = tau * (aic + part);
-        for (int r = i + 1 + t; r < n; r += ts) A[(size_t)r * ld + c] -= tw * v[r];
+        for (int r = i + 1 + t; r < mr; r += ts) A[(size_t)r * ld + c] -= tw * v[r];
         aic -= tw;
       }
       // partial norm downdate: vn1 <- sqrt(vn1^2 - a^2), recomputed when the
@@ -366,7 +367,7 @@ __device__ int cpqr_rank(int n, double tol, const Layout& L, IdShared<Real>& S) 
         x = x < (Real)0 ? (Real)0 : x;
         if (x <= tol3z * v2 * v2) {  // team-uniform decision
           Real s = 0;
-          for (int r = i + 1 + t; r < n; r += ts) { const Real a = A[(size_t)r * ld + c]; s += a * a; }
+          for (int r = i + 1 + t; r < mr; r += ts) { const Real a = A[(size_t)r * ld + c]; s += a * a; }
           s = team_sum<TS>(s);
           if (t == 0) { const Real q = sqrt(s); vn1[c] = q; vn2[c] = q; }
         } else if (t == 0) {
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
     S.R = g;
     S.C = g + (size_t)n * L.ld;
   }
-  S.v = carve<Real>(sp, 2 * (n > kChunk ? n : kChunk));
+  S.v = carve<Real>(sp, 3 * (n > kChunk ? n : kChunk) + 3 * 32 * 32);
   S.vn1 = carve<double>(sp, n);
   S.vn2 = carve<double>(sp, n);
   S.perm = carve<int>(sp, n);
@@ -422,13 +423,20 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
   const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
   const int m = t.dense_off >= 0 ? t.m_dense : 2 * t.q + (t.use_proxy ? 2 * prow : 0);
   int step0 = 0;
+  long long clk_fill = 0, clk_fold = 0, clk0 = clock64();
   for (int c0 = 0; c0 < m; c0 += kChunk) {
     int cnt = m - c0 < kChunk ? m - c0 : kChunk;
     fill_chunk<Real>(p, t, S, L.ld, c0, cnt, ox, oy);
+    const long long c1 = clock64();
     fold_chunk<Real, TS>(n, L, step0, S);
+    const long long c2 = clock64();
+    clk_fill += c1 - clk0;
+    clk_fold += c2 - c1;
+    clk0 = c2;
     step0 += n;
   }
-  int k = m > 0 ? cpqr_rank<Real, TS>(n, p.tol, L, S) : 0;
+  int k = m > 0 ? cpqr_rank<Real, TS>(n, n, p.tol, L, S) : 0;
+  const long long clk_cpqr = clock64() - clk0;
   if (threadIdx.x == 0) p.ranks[t.slot] = k;
   for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];
   if (k > 0) {
@@ -455,6 +463,200 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
       for (int row = tt; row < k; row += ts) T[row + (size_t)k * c] = S.R[(size_t)row * ld + col];
     }
   }
+  if (p.phase_clk != nullptr && threadIdx.x == 0) {
+    long long* o = p.phase_clk + 4 * (size_t)t.slot;
+    o[0] = clk_fill;
+    o[1] = clk_fold;
+    o[2] = clk_cpqr;
+    o[3] = clock64() - clk0 - clk_cpqr;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 randomized ID (the mixed-precision factorization's compression).
+//
+// The m x n ID matrix is sketched from the left, Y = Omega A with a dense
+// +-1 matrix Omega of ell = n + kOversample rows (signs hashed from the
+// sketch row and the global matrix row), accumulated chunk by chunk in
+// register tiles: no serial chain, unlike the Householder fold.  Column-
+// pivoted QR of the small ell x n sketch then picks the skeleton, the rank
+// (first |R_ii| < tol |R_00|) and Z = R11^{-1} R12 -- the randomized
+// interpolative decomposition (Martinsson, Rokhlin & Tygert 2011; Liberty et
+// al. 2007).  Omega Q is a well-conditioned ell x n matrix for the n-column
+// orthonormal factor Q of A, so the sketch's column norms track A's within a
+// small factor: ranks may differ by one or two from a deterministic CPQR at
+// the same tolerance and the interpolation error stays of order tol.  This
+// path is only used by the FP32 factorization, whose accuracy is recovered
+// by FP64 refinement; the FP64 path keeps the exact pivoted QR.
+// ---------------------------------------------------------------------------
+constexpr int kOversample = 16;
+// 4x4 accumulator tiles per thread: 2 cover n <= 64 (team size 4), 5 cover n <= 128.
+template <int TS>
+constexpr int max_tiles() { return TS == 4 ? 2 : 5; }
+
+__device__ __forceinline__ float sketch_sign(int r, int i) {
+  unsigned x = (unsigned)r * 0x9E3779B1u ^ (unsigned)i * 0x85EBCA77u ^ 0x27D4EB2Fu;
+  x ^= x >> 15;
+  x *= 0x2C1B3C6Du;
+  x ^= x >> 12;
+  x *= 0x297A2D39u;
+  x ^= x >> 15;
+  return (x & 0x80000000u) ? -1.0f : 1.0f;
+}
+
+__host__ __device__ inline int sketch_rows(int n) { return n + kOversample; }
+
+size_t id_sketch_smem(int n) {
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const int ld = layout_ld(n, team_size(n));
+  const int ell = sketch_rows(n);
+  const int lp = (ell + 3) & ~3;
+  size_t b = 0;
+  b += al(sizeof(float) * (size_t)ell * ld);      // Y
+  b += al(sizeof(float) * (size_t)kChunk * ld);   // C
+  b += al(sizeof(float) * (size_t)kChunk * lp);   // signs
+  b += al(sizeof(float) * (3 * (size_t)(ell > kChunk ? ell : kChunk) + 3 * 32 * 32));
+  b += 2 * al(sizeof(double) * n);
+  b += al(sizeof(int) * n);
+  b += al(sizeof(double) * 8) + al(sizeof(float) * 8) + al(sizeof(int) * 8);
+  b += dofs_bytes<float>(n) + dofs_bytes<float>(kChunk);
+  b += al(sizeof(int) * kChunk);
+  return b;
+}
+
+template <int TS>
+__global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
+  using Real = float;
+  const IdTask t = p.tasks[blockIdx.x];
+  const int n = t.n;
+  const Layout L = make_layout<TS>(n);
+  const int ld = L.ld;
+  const int ell = sketch_rows(n);
+  const int lp = (ell + 3) & ~3;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* sp = smem;
+  IdShared<Real> S;
+  S.R = carve<Real>(sp, ell * ld);  // holds the sketch Y (or A itself when m <= ell)
+  S.C = carve<Real>(sp, kChunk * ld);
+  Real* sg = carve<Real>(sp, kChunk * lp);
+  S.v = carve<Real>(sp, 3 * (ell > kChunk ? ell : kChunk) + 3 * 32 * 32);
+  S.vn1 = carve<double>(sp, n);
+  S.vn2 = carve<double>(sp, n);
+  S.perm = carve<int>(sp, n);
+  S.scal = carve<double>(sp, 8);
+  S.rs = carve<Real>(sp, 8);
+  S.is = carve<int>(sp, 8);
+  S.act = carve_dofs<Real>(sp, n);
+  S.row = carve_dofs<Real>(sp, kChunk);
+  S.kind = carve<int>(sp, kChunk);
+
+  const double ox = t.cx, oy = t.cy;
+  for (int j = threadIdx.x; j < n; j += blockDim.x)
+    load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], ox, oy, S.act, j);
+  __syncthreads();
+  const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
+  const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+  long long clk0 = clock64(), clk_fill = 0, clk_fold = 0;
+  int mr;
+  if (m <= ell) {
+    // small matrix: factor A itself
+    mr = m;
+    for (int c0 = 0; c0 < m; c0 += kChunk) {
+      const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
+      fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
+      for (int e = threadIdx.x; e < cnt * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        S.R[(size_t)(c0 + i) * ld + j] = S.C[(size_t)i * ld + j];
+      }
+      __syncthreads();
+    }
+    clk_fill = clock64() - clk0;
+  } else {
+    mr = ell;
+    const int nrb = lp / 4, ncb = (n + 3) / 4, ntiles = nrb * ncb;
+    constexpr int kMaxTiles = max_tiles<TS>();
+    float acc[kMaxTiles][16];
+#pragma unroll
+    for (int q = 0; q < kMaxTiles; ++q)
+#pragma unroll
+      for (int e = 0; e < 16; ++e) acc[q][e] = 0.f;
+    for (int c0 = 0; c0 < m; c0 += kChunk) {
+      const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
+      fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
+      for (int e = threadIdx.x; e < kChunk * lp; e += blockDim.x) {
+        const int ii = e / lp, r = e % lp;
+        sg[e] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
+      }
+      __syncthreads();
+      const long long c1 = clock64();
+#pragma unroll
+      for (int q = 0; q < kMaxTiles; ++q) {
+        const int tile = threadIdx.x + q * kThreads;
+        if (tile >= ntiles) break;
+        const int r0 = 4 * (tile / ncb), cc0 = 4 * (tile % ncb);
+        float* a = acc[q];
+#pragma unroll 4
+        for (int ii = 0; ii < kChunk; ++ii) {
+          const float4 cv = *reinterpret_cast<const float4*>(S.C + (size_t)ii * ld + cc0);
+          const float4 sv = *reinterpret_cast<const float4*>(sg + (size_t)ii * lp + r0);
+          a[0] += sv.x * cv.x;  a[1] += sv.x * cv.y;  a[2] += sv.x * cv.z;  a[3] += sv.x * cv.w;
+          a[4] += sv.y * cv.x;  a[5] += sv.y * cv.y;  a[6] += sv.y * cv.z;  a[7] += sv.y * cv.w;
+          a[8] += sv.z * cv.x;  a[9] += sv.z * cv.y;  a[10] += sv.z * cv.z; a[11] += sv.z * cv.w;
+          a[12] += sv.w * cv.x; a[13] += sv.w * cv.y; a[14] += sv.w * cv.z; a[15] += sv.w * cv.w;
+        }
+      }
+      __syncthreads();
+      const long long c2 = clock64();
+      clk_fill += c1 - clk0;
+      clk_fold += c2 - c1;
+      clk0 = c2;
+    }
+#pragma unroll
+    for (int q = 0; q < kMaxTiles; ++q) {
+      const int tile = threadIdx.x + q * kThreads;
+      if (tile >= ntiles) break;
+      const int r0 = 4 * (tile / ncb), cc0 = 4 * (tile % ncb);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int r = r0 + e / 4, c = cc0 + e % 4;
+        if (r < ell && c < n) S.R[(size_t)r * ld + c] = acc[q][e];
+      }
+    }
+    __syncthreads();
+  }
+  clk0 = clock64();
+  const int k = mr > 0 ? cpqr_rank<Real, TS>(n, mr, p.tol, L, S) : 0;
+  const long long clk_cpqr = clock64() - clk0;
+  if (threadIdx.x == 0) p.ranks[t.slot] = k;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];
+  if (k > 0) {
+    const int r = n - k;
+    constexpr int ts = TS;
+    const int tt = L.t;
+    Real* T = reinterpret_cast<Real*>(p.fac) + t.fac_off + fac_T(k, r);
+    for (int c = L.c0; c < r; c += L.cstep) {
+      const int col = k + c;
+      for (int row = k - 1; row >= 0; --row) {
+        Real zr = 0;
+        if ((row % ts) == tt) {
+          zr = S.R[(size_t)row * ld + col] * ((Real)1 / S.R[(size_t)row * ld + row]);
+          S.R[(size_t)row * ld + col] = zr;
+        }
+        const int base = (threadIdx.x & 31) - tt;
+        zr = __shfl_sync(team_mask(ts), zr, base + (row % ts));
+        for (int q2 = tt; q2 < row; q2 += ts) S.R[(size_t)q2 * ld + col] -= zr * S.R[(size_t)q2 * ld + row];
+        __syncwarp(team_mask(ts));
+      }
+      for (int row = tt; row < k; row += ts) T[row + (size_t)k * c] = S.R[(size_t)row * ld + col];
+    }
+  }
+  if (p.phase_clk != nullptr && threadIdx.x == 0) {
+    long long* o = p.phase_clk + 4 * (size_t)t.slot;
+    o[0] = clk_fill;
+    o[1] = clk_fold;
+    o[2] = clk_cpqr;
+    o[3] = clock64() - clk0 - clk_cpqr;
+  }
 }
 
 template <class Real, int TS>
@@ -463,11 +665,27 @@ static void launch_id_t(const IdParams& p, int num_tasks, size_t smem, cudaStrea
   id_kernel<Real, TS><<<num_tasks, kThreads, smem, st>>>(p);
 }
 
+template <int TS>
+static void launch_sketch_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
+  cudaFuncSetAttribute(id_sketch_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  id_sketch_kernel<TS><<<num_tasks, kThreads, smem, st>>>(p);
+}
+
+bool id_sketch_ok(int nmax) {
+  return nmax <= 128 && id_sketch_smem(nmax) <= 227 * 1024;
+}
+
 // All tasks of one launch use the team size of its largest box.
 void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
                cudaStream_t st) {
   if (num_tasks <= 0) return;
   const int ts = team_size(nmax);
+  if (fp32 && p.dense == nullptr && id_sketch_ok(nmax)) {
+    const size_t sm = id_sketch_smem(nmax);
+    if (ts == 4) launch_sketch_t<4>(p, num_tasks, sm, st);
+    else launch_sketch_t<2>(p, num_tasks, sm, st);
+    return;
+  }
   if (fp32) {
     if (ts == 4) launch_id_t<float, 4>(p, num_tasks, smem, st);
     else if (ts == 2) launch_id_t<float, 2>(p, num_tasks, smem, st);

@@ -23,6 +23,7 @@ struct IdParams {
   void* fac;       // T output (Real)
   void* scratch;   // global tiles for large boxes (Real)
   const double* dense;  // matrices for rs_id_batched (column major)
+  long long* phase_clk; // optional: per-task cycle counts {fill, fold, cpqr, z} (trace mode)
 };
 
 struct DecoupleParams {

@@ -110,6 +110,7 @@ struct rs_solver {
   rs_stats stats;
   int launches = 0;
   bool trace = false;  // RSKEL_TRACE=1: per-level timing on stderr
+  DevBuf<long long> clk;
 };
 
 // ---------------------------------------------------------------------------
@@ -486,6 +487,12 @@ rs_status factor_impl(rs_solver* s) {
     ip.fac = F.fac.p;
     ip.scratch = F.scratch.p;
     ip.dense = nullptr;
+    ip.phase_clk = nullptr;
+    if (s->trace) {
+      CU(s->clk.ensure(4 * std::max<size_t>(idt.size(), 1)));
+      CU(cudaMemsetAsync(s->clk.p, 0, 4 * idt.size() * sizeof(long long), s->stream));
+      ip.phase_clk = s->clk.p;
+    }
     CU(cudaEventRecord(s->ev_a, s->stream));
     auto id_fits = [&](int n) { return id_kernel_smem(n, f32, true) <= kSmemMax; };
     auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
@@ -538,6 +545,17 @@ rs_status factor_impl(rs_solver* s) {
     s->stats.id_ms += ms_id;
     s->stats.decouple_ms += ms_dc;
     if (s->trace) {
+      std::vector<long long> clk(4 * idt.size());
+      CU(cudaMemcpy(clk.data(), s->clk.p, clk.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+      double ph[4] = {0, 0, 0, 0}, mx[4] = {0, 0, 0, 0};
+      for (size_t q = 0; q < idt.size(); ++q)
+        for (int z = 0; z < 4; ++z) {
+          ph[z] += (double)clk[4 * q + z];
+          mx[z] = std::max(mx[z], (double)clk[4 * q + z]);
+        }
+      const double cnt = idt.empty() ? 1.0 : (double)idt.size();
+      std::fprintf(stderr, "[rskel]   ID cycles per box avg/max: fill %.0f/%.0f fold %.0f/%.0f cpqr %.0f/%.0f z %.0f/%.0f\n",
+                   ph[0] / cnt, mx[0], ph[1] / cnt, mx[1], ph[2] / cnt, mx[2], ph[3] / cnt, mx[3]);
       int mmax = 0, nmax = 0;
       double msum = 0;
       for (size_t q = 0; q < idt.size(); ++q) {
@@ -1264,6 +1282,7 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
   ip.fac = dZ.p;
   ip.scratch = dS.p;
   ip.dense = dA.p;
+  ip.phase_clk = nullptr;
   ip.sd = 1;
   ip.npp = 1;
   auto id_fits = [&](int nn) { return id_kernel_smem(nn, false, true) <= kSmemMax; };
