@@ -9,6 +9,19 @@
 namespace rskel {
 
 constexpr int kThreads = 256;              // threads per box (8 warps)
+constexpr int kSmemOptIn = 227 * 1024;     // opt-in dynamic shared memory per CTA
+
+// Raises a kernel's dynamic shared-memory limit to the opt-in maximum once
+// per process (a driver call per launch would sit on every level's path).
+// (One flag per kernel: the kernel is a template argument.)
+template <auto Kernel>
+inline void set_smem_once() {
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn);
+    done = true;
+  }
+}
 constexpr int kWarps = kThreads / 32;
 
 template <class T>

@@ -256,12 +256,10 @@ void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool f
                      cudaStream_t st) {
   if (num_tasks <= 0) return;
   if (fp32) {
-    cudaFuncSetAttribute(decouple_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+    set_smem_once<decouple_kernel<float>>();
     decouple_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
   } else {
-    cudaFuncSetAttribute(decouple_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+    set_smem_once<decouple_kernel<double>>();
     decouple_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
   }
 }

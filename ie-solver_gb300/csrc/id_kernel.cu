@@ -661,13 +661,13 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
 
 template <class Real, int TS>
 static void launch_id_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
-  cudaFuncSetAttribute(id_kernel<Real, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_once<id_kernel<Real, TS>>();
   id_kernel<Real, TS><<<num_tasks, kThreads, smem, st>>>(p);
 }
 
 template <int TS>
 static void launch_sketch_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
-  cudaFuncSetAttribute(id_sketch_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_once<id_sketch_kernel<TS>>();
   id_sketch_kernel<TS><<<num_tasks, kThreads, smem, st>>>(p);
 }
 

@@ -129,10 +129,10 @@ void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cuda
   size_t es = fp32 ? sizeof(float) : sizeof(double);
   size_t smem = 2 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) + sizeof(int) * nmax + 64;
   if (fp32) {
-    cudaFuncSetAttribute(sweep_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set_smem_once<sweep_kernel<float>>();
     sweep_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
   } else {
-    cudaFuncSetAttribute(sweep_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set_smem_once<sweep_kernel<double>>();
     sweep_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
   }
 }

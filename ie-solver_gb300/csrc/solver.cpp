@@ -39,7 +39,8 @@ constexpr size_t kSmemMax = 227 * 1024;
 struct NodeState {
   int compressed = 0;
   int k = 0, r = 0;
-  std::vector<int> active, skel, red, near_, perm;
+  std::vector<int> active, skel, red, near_, perm, rows;
+  int use_proxy = 0;
   int64_t fac_off = -1, piv_off = -1, e_off = -1;
   int e_ld = 0;  // leading dimension of this box's block E (0: none, use the kernel)
   int slot = -1;
@@ -72,6 +73,10 @@ struct rs_solver {
 
   bool dev_ready = false;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // read-back of ranks while eliminations run
+  cudaEvent_t ev_c = nullptr;
+  std::vector<cudaEvent_t> lv_ev;  // per level: ID start, ID end, Schur end
+  std::vector<int> timed_levels;
   cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr, ev_a = nullptr, ev_b = nullptr;
   cudaEvent_t ev_f0 = nullptr, ev_f1 = nullptr;
   DevBuf<double> gx, gy, gnx, gny, gw, gk, pxy_c, pxy_s;
@@ -144,6 +149,8 @@ rs_status ensure_device(rs_solver* s) {
   if (s->cfg.device < 0 || s->cfg.device >= count) return fail(s, RS_ERR_ARG, "bad device ordinal");
   CU(cudaSetDevice(s->cfg.device));
   CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  CU(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
+  CU(cudaEventCreateWithFlags(&s->ev_c, cudaEventDisableTiming));
   CU(cudaEventCreate(&s->ev_t0));
   CU(cudaEventCreate(&s->ev_t1));
   CU(cudaEventCreate(&s->ev_a));
@@ -254,10 +261,14 @@ void id_rows(rs_solver* s, int id, std::vector<int>* rows, int* use_proxy) {
   const double cx = nd.corners[0] + nd.side / 2.0;
   const double cy = nd.corners[1] + nd.side / 2.0;
   const double lim = s->cfg.radius_ratio * nd.side;
+  // The reference's test is sqrt(dx^2 + dy^2) < lim; squared distances well
+  // away from lim^2 decide it without the square root.
+  const double lim2 = lim * lim, lo = lim2 * (1.0 - 1e-12), hi = lim2 * (1.0 + 1e-12);
   for (int mi : s->st[id].near_) {
     const int pv = (mi / s->sd) * 2;
     const double dx = cx - s->pts[pv], dy = cy - s->pts[pv + 1];
-    if (std::sqrt(dx * dx + dy * dy) < lim) rows->push_back(mi);
+    const double d2 = dx * dx + dy * dy;
+    if (d2 < lo || (d2 <= hi && std::sqrt(d2) < lim)) rows->push_back(mi);
   }
   *use_proxy = 1;
 }
@@ -344,11 +355,29 @@ rs_status factor_impl(rs_solver* s) {
   std::vector<int> m_of_slot;
   // Contents below these marks are live and survive buffer growth.
   size_t fac_prev = 0, e_prev = 0, piv_prev = 0;
+  double t_plan = 0, t_wait = 0, t_post = 0;
+  while ((int)s->lv_ev.size() < 3 * L) {
+    cudaEvent_t e;
+    CU(cudaEventCreate(&e));
+    s->lv_ev.push_back(e);
+  }
+  s->timed_levels.clear();
   for (int lv = L - 1; lv >= 1; --lv) {
+    const double h0 = now_ms();
     const std::vector<int>& lvl = s->tree.levels[lv];
-    for (int id : lvl)
-      if (!s->st[id].compressed) compute_active(s, id);
-    for (int id : lvl) compute_near(s, id);
+    const int nl = (int)lvl.size();
+    // Per-box list construction is independent across the boxes of a level.
+#pragma omp parallel for schedule(dynamic, 32) if (nl > 256)
+    for (int q = 0; q < nl; ++q)
+      if (!s->st[lvl[q]].compressed) compute_active(s, lvl[q]);
+#pragma omp parallel for schedule(dynamic, 32) if (nl > 256)
+    for (int q = 0; q < nl; ++q) {
+      const int id = lvl[q];
+      compute_near(s, id);
+      NodeState& S = s->st[id];
+      if (!S.compressed && (int)S.active.size() >= s->cfg.min_dofs_to_compress)
+        id_rows(s, id, &S.rows, &S.use_proxy);
+    }
     idt.clear();
     dct.clear();
     blk.clear();
@@ -372,8 +401,8 @@ rs_status factor_impl(rs_solver* s) {
       S.fac_off = -1;
       S.slot = -1;
       if (cand) {
-        int use_proxy = 0;
-        id_rows(s, id, &rows, &use_proxy);
+        const std::vector<int>& rows = S.rows;
+        const int use_proxy = S.use_proxy;
         const int rows_off = (int)s->pool.size();
         s->pool.insert(s->pool.end(), rows.begin(), rows.end());
         IdTask t{};
@@ -493,7 +522,8 @@ rs_status factor_impl(rs_solver* s) {
       CU(cudaMemsetAsync(s->clk.p, 0, 4 * idt.size() * sizeof(long long), s->stream));
       ip.phase_clk = s->clk.p;
     }
-    CU(cudaEventRecord(s->ev_a, s->stream));
+    CU(cudaEventRecord(s->lv_ev[3 * lv], s->stream));
+    s->timed_levels.push_back(lv);
     auto id_fits = [&](int n) { return id_kernel_smem(n, f32, true) <= kSmemMax; };
     auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
     launch_binned(idt_s, s->id_tasks.p, id_fits, [&](const IdTask* dt, int cnt, int nmax) {
@@ -504,7 +534,18 @@ rs_status factor_impl(rs_solver* s) {
       ++s->launches;
     });
     CU(cudaGetLastError());
-    CU(cudaEventRecord(s->ev_b, s->stream));
+    CU(cudaEventRecord(s->lv_ev[3 * lv + 1], s->stream));
+    // ranks and pivots come back on the side stream while the eliminations run
+    const size_t seg1 = s->pool.size();
+    CU(s->h_ranks.ensure(std::max<size_t>(idt.size(), 1)));
+    CU(s->h_perm.ensure(seg1 - seg0 + 1));
+    CU(cudaStreamWaitEvent(s->stream2, s->lv_ev[3 * lv + 1], 0));
+    if (!idt.empty())
+      CU(cudaMemcpyAsync(s->h_ranks.p, s->ranks.p, idt.size() * sizeof(int),
+                         cudaMemcpyDeviceToHost, s->stream2));
+    CU(cudaMemcpyAsync(s->h_perm.p, s->perm.p + seg0, (seg1 - seg0) * sizeof(int),
+                       cudaMemcpyDeviceToHost, s->stream2));
+    CU(cudaEventRecord(s->ev_c, s->stream2));
     // decouple launches
     DecoupleParams dp{};
     dp.geo = geo_of(s);
@@ -528,23 +569,17 @@ rs_status factor_impl(rs_solver* s) {
       ++s->launches;
     });
     CU(cudaGetLastError());
-    CU(cudaEventRecord(s->ev_f1, s->stream));
-    // read back ranks and pivots
-    const size_t seg1 = s->pool.size();
-    CU(s->h_ranks.ensure(std::max<size_t>(idt.size(), 1)));
-    CU(s->h_perm.ensure(seg1 - seg0 + 1));
-    if (!idt.empty())
-      CU(cudaMemcpyAsync(s->h_ranks.p, s->ranks.p, idt.size() * sizeof(int),
-                         cudaMemcpyDeviceToHost, s->stream));
-    CU(cudaMemcpyAsync(s->h_perm.p, s->perm.p + seg0, (seg1 - seg0) * sizeof(int),
-                       cudaMemcpyDeviceToHost, s->stream));
-    CU(cudaStreamSynchronize(s->stream));
-    float ms_id = 0, ms_dc = 0;
-    cudaEventElapsedTime(&ms_id, s->ev_a, s->ev_b);
-    cudaEventElapsedTime(&ms_dc, s->ev_b, s->ev_f1);
-    s->stats.id_ms += ms_id;
-    s->stats.decouple_ms += ms_dc;
+    CU(cudaEventRecord(s->lv_ev[3 * lv + 2], s->stream));
+    const double h1 = now_ms();
+    CU(cudaEventSynchronize(s->ev_c));
+    const double h2 = now_ms();
+    t_plan += h1 - h0;
+    t_wait += h2 - h1;
     if (s->trace) {
+      CU(cudaStreamSynchronize(s->stream));
+      float ms_id = 0, ms_dc = 0;
+      cudaEventElapsedTime(&ms_id, s->lv_ev[3 * lv], s->lv_ev[3 * lv + 1]);
+      cudaEventElapsedTime(&ms_dc, s->lv_ev[3 * lv + 1], s->lv_ev[3 * lv + 2]);
       std::vector<long long> clk(4 * idt.size());
       CU(cudaMemcpy(clk.data(), s->clk.p, clk.size() * sizeof(long long), cudaMemcpyDeviceToHost));
       double ph[4] = {0, 0, 0, 0}, mx[4] = {0, 0, 0, 0};
@@ -596,7 +631,12 @@ rs_status factor_impl(rs_solver* s) {
       NodeState& S = s->st[id];
       if (S.slot < 0) S.e_ld = (int)S.active.size();
     }
+    t_post += now_ms() - h2;
   }
+  if (s->trace)
+    std::fprintf(stderr, "[rskel] host: plan+launch %.3f ms, wait %.3f ms, post %.3f ms\n", t_plan,
+                 t_wait, t_post);
+  const double h3 = now_ms();
   // remove_inactive_dofs_at_all_boxes (quadtree.cpp:989-995): only the root
   // (and level-0 bookkeeping) changes for a fresh factorization.
   {
@@ -707,6 +747,7 @@ rs_status factor_impl(rs_solver* s) {
     ++s->launches;
   }
   CU(cudaGetLastError());
+  if (s->trace) std::fprintf(stderr, "[rskel] host: root + solve plan %.3f ms\n", now_ms() - h3);
   return RS_OK;
 }
 
@@ -1051,6 +1092,9 @@ rs_status rs_destroy(rs_solver* s) {
     cudaEventDestroy(s->ev_b);
     cudaEventDestroy(s->ev_f0);
     cudaEventDestroy(s->ev_f1);
+    cudaEventDestroy(s->ev_c);
+    for (cudaEvent_t e : s->lv_ev) cudaEventDestroy(e);
+    if (s->stream2) cudaStreamDestroy(s->stream2);
   }
   cudaStream_t st = s->stream;
   delete s;  // device buffers free themselves
@@ -1134,6 +1178,15 @@ rs_status rs_factor(rs_solver* s) {
   cudaEventElapsedTime(&ms, s->ev_f0, s->ev_f1);
   s->stats.dev_factor_ms = ms;
   s->stats.t_factor_ms = now_ms() - t0;
+  s->stats.id_ms = 0;
+  s->stats.decouple_ms = 0;
+  for (int lv : s->timed_levels) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, s->lv_ev[3 * lv], s->lv_ev[3 * lv + 1]);
+    cudaEventElapsedTime(&b, s->lv_ev[3 * lv + 1], s->lv_ev[3 * lv + 2]);
+    s->stats.id_ms += a;
+    s->stats.decouple_ms += b;
+  }
   int nc = 0;
   for (const NodeState& S : s->st) nc += S.compressed;
   s->stats.num_compressed = nc;

@@ -43,7 +43,7 @@ def _compile(src, obj, verbose):
                "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
                "-I", CSRC, "-c", path, "-o", obj]
     else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall",
                "-Wno-unused-function", "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include"),
                "-c", path, "-o", obj]
     if verbose:
@@ -80,7 +80,7 @@ def build(verbose=False, force=False):
             if verbose and warn:
                 print(warn)
     if force or jobs or _stale(LIB, objs):
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-Xlinker", "--no-undefined"]
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lgomp", "-Xlinker", "--no-undefined"]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)
