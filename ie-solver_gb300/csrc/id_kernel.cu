@@ -112,6 +112,11 @@ __host__ __device__ size_t id_smem_bytes(int n, bool tile_in_smem) {
   return b;
 }
 
+size_t id_direct_tile(int m, int n) {
+  const size_t mp = (size_t)((m + kChunk - 1) / kChunk) * kChunk;
+  return mp * (size_t)(n + 32) + mp + 64;  // tile + reflector
+}
+
 size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem) {
   return fp32 ? id_smem_bytes<float>(n, tile_in_smem) : id_smem_bytes<double>(n, tile_in_smem);
 }
@@ -390,7 +395,10 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
   IdShared<Real> S;
-  if (t.scratch_off < 0) {
+  if (p.direct) {
+    S.R = nullptr;
+    S.C = nullptr;
+  } else if (t.scratch_off < 0) {
     S.R = carve<Real>(sp, n * L.ld);
     S.C = carve<Real>(sp, kChunk * L.ld);
   } else {
@@ -417,25 +425,46 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
   if (t.dense_off < 0)
     for (int j = threadIdx.x; j < n; j += blockDim.x)
       load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], ox, oy, S.act, j);
-  for (int e = threadIdx.x; e < n * L.ld; e += blockDim.x) S.R[e] = (Real)0;
+  if (!p.direct)
+    for (int e = threadIdx.x; e < n * L.ld; e += blockDim.x) S.R[e] = (Real)0;
   __syncthreads();
 
   const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
   const int m = t.dense_off >= 0 ? t.m_dense : 2 * t.q + (t.use_proxy ? 2 * prow : 0);
   int step0 = 0;
   long long clk_fill = 0, clk_fold = 0, clk0 = clock64();
-  for (int c0 = 0; c0 < m; c0 += kChunk) {
-    int cnt = m - c0 < kChunk ? m - c0 : kChunk;
-    fill_chunk<Real>(p, t, S, L.ld, c0, cnt, ox, oy);
-    const long long c1 = clock64();
-    fold_chunk<Real, TS>(n, L, step0, S);
-    const long long c2 = clock64();
-    clk_fill += c1 - clk0;
-    clk_fold += c2 - c1;
-    clk0 = c2;
-    step0 += n;
+  int k = 0;
+  if (p.direct) {
+    // Column-pivoted QR directly on the whole m x n ID matrix (held in the
+    // task's global tile), stopping at the rank: dgeqp3 as the reference
+    // calls it (ie_mat.cpp:556), minus the steps after the rank is known.
+    Real* A = reinterpret_cast<Real*>(p.scratch) + t.scratch_off;
+    Real* chunk_save = S.C;
+    for (int c0 = 0; c0 < m; c0 += kChunk) {
+      const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
+      S.C = A + (size_t)c0 * L.ld;
+      fill_chunk<Real>(p, t, S, L.ld, c0, cnt, ox, oy);
+    }
+    S.C = chunk_save;
+    S.R = A;
+    S.v = A + (size_t)((m + kChunk - 1) / kChunk) * kChunk * L.ld;  // reflector (m entries)
+    clk_fill = clock64() - clk0;
+    clk0 = clock64();
+    k = m > 0 ? cpqr_rank<Real, TS>(n, m, p.tol, L, S) : 0;
+  } else {
+    for (int c0 = 0; c0 < m; c0 += kChunk) {
+      int cnt = m - c0 < kChunk ? m - c0 : kChunk;
+      fill_chunk<Real>(p, t, S, L.ld, c0, cnt, ox, oy);
+      const long long c1 = clock64();
+      fold_chunk<Real, TS>(n, L, step0, S);
+      const long long c2 = clock64();
+      clk_fill += c1 - clk0;
+      clk_fold += c2 - c1;
+      clk0 = c2;
+      step0 += n;
+    }
+    k = m > 0 ? cpqr_rank<Real, TS>(n, n, p.tol, L, S) : 0;
   }
-  int k = m > 0 ? cpqr_rank<Real, TS>(n, n, p.tol, L, S) : 0;
   const long long clk_cpqr = clock64() - clk0;
   if (threadIdx.x == 0) p.ranks[t.slot] = k;
   for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];

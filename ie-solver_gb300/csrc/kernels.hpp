@@ -24,6 +24,7 @@ struct IdParams {
   void* scratch;   // global tiles for large boxes (Real)
   const double* dense;  // matrices for rs_id_batched (column major)
   long long* phase_clk; // optional: per-task cycle counts {fill, fold, cpqr, z} (trace mode)
+  int direct;           // 1: pivoted QR on the whole matrix in the task's global tile
 };
 
 struct DecoupleParams {
@@ -61,6 +62,8 @@ struct SweepParams {
 };
 
 size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);
+// Doubles of global tile a direct-QR task with m rows and n columns needs.
+size_t id_direct_tile(int m, int n);
 size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
 
 void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,

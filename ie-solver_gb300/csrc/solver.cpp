@@ -469,11 +469,16 @@ rs_status factor_impl(rs_solver* s) {
     for (size_t i = 0; i < od.size(); ++i) dct_s[i] = dct[od[i]];
     // global-memory tiles for boxes whose tiles do not fit in shared memory
     size_t scratch_need = 0;
-    for (IdTask& t : idt_s)
-      if (id_kernel_smem(t.n, f32, true) > kSmemMax) {
+    for (IdTask& t : idt_s) {
+      if (!f32) {  // FP64: direct pivoted QR on the whole ID matrix
+        const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+        t.scratch_off = (int64_t)scratch_need;
+        scratch_need += id_direct_tile(m, t.n);
+      } else if (id_kernel_smem(t.n, f32, true) > kSmemMax) {
         t.scratch_off = (int64_t)scratch_need;
         scratch_need += (size_t)(t.n + 32) * (t.n + 64) + 64;
       }
+    }
     for (DecoupleTask& t : dct_s)
       if (decouple_kernel_smem(t.n, f32, true) > kSmemMax) {
         t.scratch_off = (int64_t)scratch_need;
@@ -516,6 +521,7 @@ rs_status factor_impl(rs_solver* s) {
     ip.fac = F.fac.p;
     ip.scratch = F.scratch.p;
     ip.dense = nullptr;
+    ip.direct = f32 ? 0 : 1;
     ip.phase_clk = nullptr;
     if (s->trace) {
       CU(s->clk.ensure(4 * std::max<size_t>(idt.size(), 1)));
@@ -529,7 +535,7 @@ rs_status factor_impl(rs_solver* s) {
     launch_binned(idt_s, s->id_tasks.p, id_fits, [&](const IdTask* dt, int cnt, int nmax) {
       IdParams q = ip;
       q.tasks = dt;
-      bool in_smem = id_kernel_smem(nmax, f32, true) <= kSmemMax;
+      bool in_smem = !ip.direct && id_kernel_smem(nmax, f32, true) <= kSmemMax;
       launch_id(q, cnt, nmax, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
       ++s->launches;
     });
@@ -1335,6 +1341,7 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
   ip.fac = dZ.p;
   ip.scratch = dS.p;
   ip.dense = dA.p;
+  ip.direct = 0;
   ip.phase_clk = nullptr;
   ip.sd = 1;
   ip.npp = 1;
