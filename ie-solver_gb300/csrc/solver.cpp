@@ -26,6 +26,7 @@
 #include "../../include/rskel.h"
 #include "border.hpp"
 #include "devbuf.hpp"
+#include "fmm.hpp"
 #include "kernels.hpp"
 #include "plan.hpp"
 #include "tree.hpp"
@@ -111,6 +112,8 @@ struct rs_solver {
   // solve buffers
   DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev;
   HostBuf<double> h_io;
+
+  FmmPlan fmm;
 
   rs_stats stats;
   int launches = 0;
@@ -959,7 +962,12 @@ namespace {
 rs_status residual(rs_solver* s, const double* f, const double* mu, const double* alpha,
                    int nrhs, double* r, double* rg) {
   const int D = s->D;
-  launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, mu, nrhs, r, s->stream);
+  if (s->fmm.built) {
+    CU(fmm_laplace_apply(s->fmm, geo_of(s), mu, nrhs, r, s->stream));
+    s->launches += 5 + 2 * s->fmm.nlevels;
+  } else {
+    launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, mu, nrhs, r, s->stream);
+  }
   launch_axpby(r, f, 1.0, -1.0, (size_t)D * nrhs, s->stream);
   s->launches += 2;
   if (s->nb > 0) {
@@ -1062,6 +1070,7 @@ void rs_config_default(rs_config* c) {
   c->refine_max_iters = 10;
   c->fp32_id_tol = 1e-6;
   c->device = 0;
+  c->fmm_order = 0;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -1133,6 +1142,7 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
   s->tree_built = false;
   s->factored = false;
   s->geo_on_dev = false;
+  s->fmm.built = false;
   return RS_OK;
 }
 
@@ -1142,6 +1152,7 @@ rs_status rs_build_tree(rs_solver* s) {
   double t0 = now_ms();
   if (!s->tree.build(s->pts.data(), s->n, s->sd, s->cfg.max_leaf_dofs))
     return fail(s, RS_ERR_ARG, "tree build failed");
+  s->fmm.built = false;
   s->tree_built = true;
   s->factored = false;
   s->st.assign(s->tree.nodes.size(), NodeState());
@@ -1162,6 +1173,11 @@ rs_status rs_factor(rs_solver* s) {
   CU(cudaSetDevice(s->cfg.device));
   rc = upload_geometry(s);
   if (rc != RS_OK) return rc;
+  if (s->fp32 && s->cfg.pde == kLaplace && !s->fmm.built) {
+    const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : 40;
+    if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, s->stream))
+      return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
+  }
   double t0 = now_ms();
   CU(cudaEventRecord(s->ev_f0, s->stream));
   s->factored = false;
@@ -1279,6 +1295,34 @@ rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y) {
   CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
   launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, dx.p, nrhs, dy.p, s->stream);
   CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y) {
+  if (!s || !x || !y || nrhs < 1) return fail(s, RS_ERR_ARG, "bad matvec arguments");
+  if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
+  if (s->cfg.pde != kLaplace) return rs_matvec(s, x, nrhs, y);
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  rc = upload_geometry(s);
+  if (rc != RS_OK) return rc;
+  if (!s->tree_built) {
+    rc = rs_build_tree(s);
+    if (rc != RS_OK) return rc;
+  }
+  if (!s->fmm.built) {
+    const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : 40;
+    if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, s->stream))
+      return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
+  }
+  const size_t nd = (size_t)s->D * nrhs;
+  DevBuf<double> dx, dy;
+  CU(dx.ensure(nd));
+  CU(dy.ensure(nd));
+  CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
+  CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, s->stream));
   CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   return RS_OK;

@@ -22,8 +22,9 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["id_kernel.cu", "decouple_kernel.cu", "solve_kernels.cu", "border_kernels.cu"]
-CPP_SOURCES = ["tree.cpp", "solver.cpp"]
+CU_SOURCES = ["id_kernel.cu", "decouple_kernel.cu", "solve_kernels.cu", "border_kernels.cu",
+              "fmm.cu"]
+CPP_SOURCES = ["tree.cpp", "solver.cpp", "fmm_plan.cpp"]
 
 
 def _nvcc():

@@ -25,6 +25,7 @@ STATUS = {0: "RS_OK", 1: "RS_ERR_ARG", 2: "RS_ERR_STATE", 3: "RS_ERR_CUDA",
 # Every function the C ABI exports (include/rskel.h).
 EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
+           "rs_matvec_fast",
            "rs_id_batched", "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
            "rs_allskel", "rs_timer_start", "rs_timer_stop", "rs_synchronize", "rs_last_error"]
 
@@ -36,7 +37,8 @@ class RsConfig(ctypes.Structure):
                 ("radius_ratio", ctypes.c_double), ("min_dofs_to_compress", ctypes.c_int),
                 ("is_strong_admissibility", ctypes.c_int), ("precision", ctypes.c_int),
                 ("refine_tol", ctypes.c_double), ("refine_max_iters", ctypes.c_int),
-                ("fp32_id_tol", ctypes.c_double), ("device", ctypes.c_int)]
+                ("fp32_id_tol", ctypes.c_double), ("device", ctypes.c_int),
+                ("fmm_order", ctypes.c_int)]
 
 
 class RsStats(ctypes.Structure):
@@ -80,6 +82,7 @@ def lib():
         L.rs_solve_device.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp]
         L.rs_kernel_block.argtypes = [_vp, _ip, ctypes.c_int, _ip, ctypes.c_int, _dp]
         L.rs_matvec.argtypes = [_vp, _dp, ctypes.c_int, _dp]
+        L.rs_matvec_fast.argtypes = [_vp, _dp, ctypes.c_int, _dp]
         L.rs_id_batched.argtypes = [_vp, ctypes.c_int, _dp, _lp, _ip, _ip, ctypes.c_double, _ip,
                                     _ip, _lp, _dp, _lp]
         L.rs_get_stats.argtypes = [_vp, ctypes.POINTER(RsStats)]
@@ -134,13 +137,14 @@ class Solver:
     """One boundary problem: geometry -> quadtree -> factor -> solves."""
 
     def __init__(self, geo, pde, tol, leaf=64, npp=64, precision=RS_FP64, refine_tol=1e-12,
-                 refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16):
+                 refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16, fmm_order=0):
         self.sd = 2 if pde == RS_STOKES else 1
         self.cfg = default_config(pde=pde, solution_dimension=self.sd, id_tol=tol,
                                   max_leaf_dofs=leaf, num_proxy_points=npp,
                                   precision=precision, refine_tol=refine_tol,
                                   refine_max_iters=refine_max_iters, fp32_id_tol=fp32_id_tol,
-                                  device=device, min_dofs_to_compress=min_dofs)
+                                  device=device, min_dofs_to_compress=min_dofs,
+                                  fmm_order=fmm_order)
         h = _vp()
         self._check(lib().rs_create(ctypes.byref(self.cfg), ctypes.byref(h)), None)
         self.h = h
@@ -203,13 +207,14 @@ class Solver:
         self._check(lib().rs_kernel_block(self.h, _i(I), I.size, _i(J), J.size, _d(out)))
         return out
 
-    def matvec(self, x):
+    def matvec(self, x, fast=False):
         x = np.asfortranarray(x, dtype=np.float64)
         sq = x.ndim == 1
         if sq:
             x = x[:, None]
         y = np.zeros_like(x, order="F")
-        self._check(lib().rs_matvec(self.h, _d(x), x.shape[1], _d(y)))
+        fn = lib().rs_matvec_fast if fast else lib().rs_matvec
+        self._check(fn(self.h, _d(x), x.shape[1], _d(y)))
         return y[:, 0] if sq else y
 
     def stats(self):

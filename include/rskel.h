@@ -59,6 +59,8 @@ typedef struct {
   double fp32_id_tol;        /* RS_FP32_REFINE: ID tolerance of the FP32 factor
                                 (at least id_tol; FP32 cannot resolve below ~1e-6) */
   int device;                /* CUDA device ordinal */
+  int fmm_order;             /* RS_FP32_REFINE: multipole order of the FP64
+                                residual (0 = automatic) */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
@@ -109,6 +111,12 @@ rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int 
 /* y = K x over all DOFs (dense, FP64 accurate, on the GPU), the operator whose
  * inverse the factorization represents.  x, y: (num_points*sd) x nrhs. */
 rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
+
+/* y = K x through the FP64 fast multipole method used for the refinement
+ * residual (Laplace); falls back to rs_matvec for other kernels.  No
+ * reference counterpart: the reference applies K only densely in its tests
+ * (ie_solver_test.cpp:87-95). */
+rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y);
 
 /* ie_Mat::id (ie_mat.cpp:548-588) for a batch of matrices on the GPU.
  * mats: concatenated column-major m_i x n_i blocks (offsets a_off, in

@@ -1,0 +1,61 @@
+"""GPU: the FP64 fast multipole Laplace double-layer product used for the
+refinement residual, against the dense FP64 product (rs_matvec).
+
+Tolerance: max |y_fmm - y_dense| <= 1e-10 max |y_dense| per column at the
+default order (40), with separation ratio sqrt(2)/(4 - sqrt(2)) ~ 0.55 giving
+a worst-case truncation 0.55^40 ~ 4e-11; lower orders must be no more
+accurate than higher ones.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_geometry, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(y, z):
+    return float((np.abs(y - z).max(axis=0) / np.abs(z).max(axis=0)).max())
+
+
+@pytest.mark.parametrize("name", ["laplace_circle_512", "laplace_annulus_512",
+                                  "laplace_star_8192_2rhs", "laplace_unit_circle_4096"])
+def test_fmm_matches_dense_golden(name, solver_lib):
+    d = load_golden(name)
+    geo = golden_geometry(d)
+    pde, sd, leaf, npp = (int(x) for x in d["meta"][:4])
+    s = solver_lib.Solver(geo, pde, float(d["tol"][0]), leaf=leaf, npp=npp)
+    x = np.random.default_rng(3).standard_normal((s.D, 3))
+    assert _rel(s.matvec(x, fast=True), s.matvec(x)) <= 1e-10
+
+
+def test_fmm_large_star_many_rhs(solver_lib):
+    from rskel import geometry as G
+    geo = G.star(65536)
+    s = solver_lib.Solver(geo, solver_lib.RS_LAPLACE, 1e-8)
+    x = np.random.default_rng(4).standard_normal((s.D, 10))  # two passes of at most 8
+    y = s.matvec(x, fast=True)
+    z = s.matvec(x)
+    assert _rel(y, z) <= 1e-10
+    # column independence: the second pass equals a one-column product
+    y9 = s.matvec(x[:, 9], fast=True)
+    assert np.abs(y9 - y[:, 9]).max() <= 1e-13 * np.abs(y[:, 9]).max()
+
+
+def test_fmm_order_monotone(solver_lib):
+    d = load_golden("laplace_star_8192_2rhs")
+    geo = golden_geometry(d)
+    x = np.random.default_rng(5).standard_normal((geo.n, 2))
+    errs = []
+    for p in (10, 20, 40):
+        s = solver_lib.Solver(geo, solver_lib.RS_LAPLACE, 1e-8, fmm_order=p)
+        errs.append(_rel(s.matvec(x, fast=True), s.matvec(x)))
+    assert errs[0] >= errs[1] >= errs[2] and errs[0] <= 1e-2, errs
+
+
+def test_fmm_other_kernels_fall_back_to_dense(solver_lib):
+    d = load_golden("stokes_circle_512")
+    geo = golden_geometry(d)
+    s = solver_lib.Solver(geo, solver_lib.RS_STOKES, 1e-8)
+    x = np.random.default_rng(6).standard_normal((s.D, 2))
+    assert np.array_equal(s.matvec(x, fast=True), s.matvec(x))
