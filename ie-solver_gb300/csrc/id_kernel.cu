@@ -726,4 +726,18 @@ void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp3
   }
 }
 
+// Sets the dynamic shared-memory limit of the three FP64 ID kernel variants
+// on the current device (the set-up step of rs_id_noalloc).
+cudaError_t id_noalloc_prepare() {
+  cudaError_t e = cudaFuncSetAttribute(id_kernel<double, 4>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(id_kernel<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kSmemOptIn);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(id_kernel<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kSmemOptIn);
+  return e;
+}
+
 }  // namespace rskel

@@ -66,6 +66,8 @@ size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);
 size_t id_direct_tile(int m, int n);
 size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
 
+// Shared-memory attribute set-up of the FP64 ID kernels on the current device.
+cudaError_t id_noalloc_prepare();
 void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
                cudaStream_t st);
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,

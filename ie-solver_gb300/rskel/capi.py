@@ -26,7 +26,7 @@ STATUS = {0: "RS_OK", 1: "RS_ERR_ARG", 2: "RS_ERR_STATE", 3: "RS_ERR_CUDA",
 EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
            "rs_matvec_fast",
-           "rs_id_batched", "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
+           "rs_id_batched", "rs_id_noalloc", "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
            "rs_allskel", "rs_timer_start", "rs_timer_stop", "rs_synchronize", "rs_last_error"]
 
 
@@ -85,6 +85,8 @@ def lib():
         L.rs_matvec_fast.argtypes = [_vp, _dp, ctypes.c_int, _dp]
         L.rs_id_batched.argtypes = [_vp, ctypes.c_int, _dp, _lp, _ip, _ip, ctypes.c_double, _ip,
                                     _ip, _lp, _dp, _lp]
+        L.rs_id_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double, _vp, _vp, _vp,
+                                    _vp]
         L.rs_get_stats.argtypes = [_vp, ctypes.POINTER(RsStats)]
         L.rs_node_info.argtypes = [_vp, ctypes.c_int, _ip, _dp, _dp]
         L.rs_node_list.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip]

@@ -127,6 +127,26 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
                         const int* m, const int* n, double tol, int* ranks, int* perm,
                         const int64_t* p_off, double* Z, const int64_t* z_off);
 
+/* One FP64 ID of a device-resident column-major m x n matrix A (lda = m) on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) of the current
+ * device, with no device allocation.  No counterpart in the reference: it is
+ * rs_id_batched's kernel with its global scratch tile taken from a fixed
+ * 4 MiB file-scope device array instead of cudaMalloc.
+ * Outputs (device pointers): *rank = k (0 = no compression), perm = n
+ * 0-based column indices, Z = k x (n - k) column major (reserve n*n/4 + 1
+ * doubles).  Asynchronous: results are ready when `stream` is.
+ * Limits: the padded tile, ceil(m/64)*64 * (n + 32) + ceil(m/64)*64 + 64
+ * doubles, must fit in 524288 doubles (for example m = 2048 with n <= 222,
+ * or m = 1024 with n <= 478), and the kernel's shared memory must fit in
+ * 227 KB; larger sizes return RS_ERR_CAPACITY without touching the device.
+ * The first call on a device sets up the device (symbol addresses and the
+ * kernel's shared-memory attribute): make it before any stream capture.
+ * All calls on a device share the scratch array: calls that overlap in time
+ * race and must be serialised by the caller.  Nothing needs to start at
+ * zero. */
+rs_status rs_id_noalloc(int m, int n, const double* A, double tol, int* rank, int* perm,
+                        double* Z, void* stream);
+
 /* --- introspection (tree and factorization), for tests and tooling --- */
 typedef struct {
   int num_levels, num_nodes, num_compressed, num_skel_root;
