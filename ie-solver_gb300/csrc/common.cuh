@@ -18,7 +18,12 @@ template <auto Kernel>
 inline void set_smem_once() {
   static bool done = false;
   if (!done) {
-    cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn);
+    // The limit covers static plus dynamic shared memory.
+    cudaFuncAttributes a{};
+    size_t stat = 0;
+    if (cudaFuncGetAttributes(&a, Kernel) == cudaSuccess) stat = a.sharedSizeBytes;
+    cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kSmemOptIn - stat));
     done = true;
   }
 }

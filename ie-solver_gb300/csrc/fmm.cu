@@ -1,5 +1,6 @@
-// FP64 fast multipole kernels for the Laplace double-layer residual; see
-// fmm.hpp for the formulation.  Complex numbers are (re, im) double pairs.
+// Fast multipole kernels for the Laplace double-layer product; see fmm.hpp
+// for the formulation.  Templated on the arithmetic type R (double or
+// float); complex numbers are (re, im) pairs of R.
 //
 // Scaled expansions for a box with centre z_B and side s_B:
 //   multipole  phi(z) = sum_k  M_k s^k / (z - z_B)^(k+1)
@@ -7,6 +8,7 @@
 // Translations (d = z_B - z_C for M2L, e = z_child - z_parent):
 //   P2M  M_k = sum_j c_j ((z_j - z_B) / s_B)^k
 //   M2M  M_l(P) = sum_{k<=l} M_k(C) C(l,k) (s_C/s_P)^k ((z_C - z_P)/s_P)^(l-k)
+//        (s_C/s_P = 1/2 in a quadtree)
 //   M2L  L_l(B) = (-1)^l (s_B/d)^l / d * sum_k C(k+l,l) M_k(C) (s_C/d)^k
 //   L2L  L_m(C) = sum_{l>=m} L_l(P) C(l,m) (s_C/s_P)^m (e/s_P)^(l-m)
 //   P2L  L_l(B) -= c_j / w (s_B / w)^l,       w = z_j - z_B
@@ -24,64 +26,119 @@ namespace {
 
 constexpr int kFmmThreads = 128;
 constexpr int kMaxRhs = 8;  // right-hand sides per pass (larger batches loop)
+constexpr int kStage = 64;  // points staged in shared memory at a time
+constexpr int kEvalThreads = 128;
 
+template <class R>
 struct Cx {
-  double re, im;
+  R re, im;
 };
-__device__ __forceinline__ Cx cmul(Cx a, Cx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
-__device__ __forceinline__ Cx cadd(Cx a, Cx b) { return {a.re + b.re, a.im + b.im}; }
-__device__ __forceinline__ Cx cinv(Cx a) {
-  const double d = rcp(a.re * a.re + a.im * a.im);
+template <class R>
+__device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <class R>
+__device__ __forceinline__ Cx<R> cadd(Cx<R> a, Cx<R> b) {
+  return {a.re + b.re, a.im + b.im};
+}
+template <class R>
+__device__ __forceinline__ Cx<R> cinv(Cx<R> a) {
+  const R d = rcp(a.re * a.re + a.im * a.im);
   return {a.re * d, -a.im * d};
 }
-__device__ __forceinline__ Cx cscale(Cx a, double s) { return {a.re * s, a.im * s}; }
+template <class R>
+__device__ __forceinline__ Cx<R> cscale(Cx<R> a, R s) {
+  return {a.re * s, a.im * s};
+}
+// Positions: FP64 coordinates, or FP32 (hi, lo) pairs whose difference is
+// formed hi - hi (exact for nearby points) plus lo - lo.
+template <class R>
+struct Pos;
+template <>
+struct Pos<double> {
+  double x, y;
+};
+template <>
+struct Pos<float> {
+  float hx, lx, hy, ly;
+};
+__device__ __forceinline__ Cx<double> sub(Pos<double> a, Pos<double> b) {
+  return {a.x - b.x, a.y - b.y};
+}
+__device__ __forceinline__ Cx<float> sub(Pos<float> a, Pos<float> b) {
+  return {(a.hx - b.hx) + (a.lx - b.lx), (a.hy - b.hy) + (a.ly - b.ly)};
+}
 
+template <class R>
 struct FmmArgs {
-  const double *cx, *cy, *side, *zx, *zy, *binom;
-  const int *pstart, *pcount, *parent, *slot_pt;
+  const double *cx, *cy, *zx, *zy;
+  const float *cxh, *cxl, *cyh, *cyl, *zxh, *zxl, *zyh, *zyl;
+  const R* side;
+  const R* binom;
+  const int *pstart, *pcount, *parent, *slot_pt, *children;
   const int *v_off, *v_idx, *w_off, *w_idx, *x_off, *x_idx, *u_off, *u_idx;
   const int* boxes;
   int p, npts, nrhs;
-  const double* charge;  // complex, 2 * (slot + npts * q)
-  double* mpole;         // complex, 2 * (k + p * (q + nrhs * box))
-  double* local;
+  const R* charge;  // complex, 2 * (slot + npts * q)
+  R* mpole;         // complex, 2 * (k + p * (q + nrhs * box))
+  R* local;
 };
 
-__device__ __forceinline__ Cx ld_c(const double* a, size_t i) { return {a[2 * i], a[2 * i + 1]}; }
-__device__ __forceinline__ void st_c(double* a, size_t i, Cx v) {
+__device__ __forceinline__ Pos<double> box_pos(const FmmArgs<double>& a, int b) {
+  return {a.cx[b], a.cy[b]};
+}
+__device__ __forceinline__ Pos<float> box_pos(const FmmArgs<float>& a, int b) {
+  return {a.cxh[b], a.cxl[b], a.cyh[b], a.cyl[b]};
+}
+__device__ __forceinline__ Pos<double> pt_pos(const FmmArgs<double>& a, int s) {
+  return {a.zx[s], a.zy[s]};
+}
+__device__ __forceinline__ Pos<float> pt_pos(const FmmArgs<float>& a, int s) {
+  return {a.zxh[s], a.zxl[s], a.zyh[s], a.zyl[s]};
+}
+
+template <class R>
+__device__ __forceinline__ Cx<R> ld_c(const R* a, size_t i) {
+  return {a[2 * i], a[2 * i + 1]};
+}
+template <class R>
+__device__ __forceinline__ void st_c(R* a, size_t i, Cx<R> v) {
   a[2 * i] = v.re;
   a[2 * i + 1] = v.im;
 }
 
 // Complex charges c_j = -(w_j / 2pi) (n_x + i n_y) mu_j in slot order.
+template <class R>
 __global__ void charges_kernel(Geo<double> g, const int* slot_pt, int npts, const double* mu,
-                               int nrhs, double* charge) {
+                               int nrhs, R* charge) {
   const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= (size_t)npts * nrhs) return;
   const int s = (int)(e % npts), q = (int)(e / npts);
   const int pt = slot_pt[s];
   const double a = -g.w[pt] * (1.0 / (2.0 * CUDART_PI)) * mu[pt + (size_t)npts * q];
-  charge[2 * e] = a * g.nx[pt];
-  charge[2 * e + 1] = a * g.ny[pt];
+  charge[2 * e] = (R)(a * g.nx[pt]);
+  charge[2 * e + 1] = (R)(a * g.ny[pt]);
 }
 
-// P2M for every leaf (points staged 64 at a time).
-__global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs a) {
+// P2M for every non-empty leaf (points staged kStage at a time).
+template <class R>
+__global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b = a.boxes[blockIdx.x];
   const int s0 = a.pstart[b], cnt = a.pcount[b], p = a.p;
-  Cx* pw = reinterpret_cast<Cx*>(smem);  // 64 x p
-  const double cx = a.cx[b], cy = a.cy[b], is = rcp(a.side[b]);
+  Cx<R>* pw = reinterpret_cast<Cx<R>*>(smem);  // kStage x p
+  const Pos<R> c = box_pos(a, b);
+  const R is = rcp(a.side[b]);
   constexpr int kPer = 4;  // (k, q) pairs per thread (p * nrhs <= 512)
-  Cx acc[kPer];
+  Cx<R> acc[kPer];
 #pragma unroll
-  for (int t = 0; t < kPer; ++t) acc[t] = {0.0, 0.0};
-  for (int j0 = 0; j0 < cnt; j0 += 64) {
-    const int jc = cnt - j0 < 64 ? cnt - j0 : 64;
+  for (int t = 0; t < kPer; ++t) acc[t] = {(R)0, (R)0};
+  for (int j0 = 0; j0 < cnt; j0 += kStage) {
+    const int jc = cnt - j0 < kStage ? cnt - j0 : kStage;
     __syncthreads();
     for (int j = threadIdx.x; j < jc; j += blockDim.x) {
-      const Cx rho = {(a.zx[s0 + j0 + j] - cx) * is, (a.zy[s0 + j0 + j] - cy) * is};
-      Cx v = {1.0, 0.0};
+      const Cx<R> rho = cscale(sub(pt_pos(a, s0 + j0 + j), c), is);
+      Cx<R> v = {(R)1, (R)0};
       for (int k = 0; k < p; ++k) {
         pw[j * p + k] = v;
         v = cmul(v, rho);
@@ -106,79 +163,98 @@ __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs a) {
   }
 }
 
-// M2M: each non-leaf box of a level pulls its four children's expansions.
-__global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs a, const int* children) {
+// M2M: each non-empty, non-leaf box of a level pulls its children's
+// expansions.  With d = (z_C - z_P)/s_P and g = 1/(2d) the shift is
+//   M_l(P) = sum_C d^l sum_{k<=l} C(l,k) (M_k(C) g^k),
+// a real Pascal-matrix product between two diagonal complex scalings.
+template <class R>
+__global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int P = a.boxes[blockIdx.x];
-  if (a.pcount[P] > 0 || children[4 * P] < 0) return;  // leaf: filled by P2M
-  const int p = a.p;
-  Cx* dp = reinterpret_cast<Cx*>(smem);  // 4 x p powers of (z_C - z_P) / s_P
-  const double isp = rcp(a.side[P]);
-  if (threadIdx.x < 4) {
-    const int C = children[4 * P + threadIdx.x];
-    const Cx d = {(a.cx[C] - a.cx[P]) * isp, (a.cy[C] - a.cy[P]) * isp};
-    Cx v = {1.0, 0.0};
-    for (int m = 0; m < p; ++m) {
-      dp[threadIdx.x * p + m] = v;
-      v = cmul(v, d);
+  if (a.pcount[P] > 0) return;  // leaf: filled by P2M
+  const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
+  Cx<R>* dl = reinterpret_cast<Cx<R>*>(smem);  // 4 x p: d_c^l
+  Cx<R>* gk = dl + 4 * p;                      // 4 x p: g_c^k
+  Cx<R>* av = gk + 4 * p;                      // 4 x nrhs x p: M_k(c) g_c^k
+  const R isp = rcp(a.side[P]);
+  if (threadIdx.x < 8) {
+    const int c = threadIdx.x & 3;
+    const int C = a.children[4 * P + c];
+    if (C >= 0) {
+      const Cx<R> d = cscale(sub(box_pos(a, C), box_pos(a, P)), isp);
+      const Cx<R> base = threadIdx.x < 4 ? d : cinv(cscale(d, (R)2));
+      Cx<R>* out = (threadIdx.x < 4 ? dl : gk) + c * p;
+      Cx<R> v = {(R)1, (R)0};
+      for (int m = 0; m < p; ++m) {
+        out[m] = v;
+        v = cmul(v, base);
+      }
     }
   }
   __syncthreads();
-  const int P2 = 2 * p;
-  for (int e = threadIdx.x; e < p * a.nrhs; e += blockDim.x) {
+  for (int e = threadIdx.x; e < 4 * p * nrhs; e += blockDim.x) {
+    const int k = e % p, q = (e / p) % nrhs, c = e / (p * nrhs);
+    const int C = a.children[4 * P + c];
+    av[e] = C >= 0 ? cmul(ld_c(a.mpole, k + (size_t)p * (q + nrhs * (size_t)C)), gk[c * p + k])
+                   : Cx<R>{(R)0, (R)0};
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < p * nrhs; e += blockDim.x) {
     const int l = e % p, q = e / p;
-    Cx acc = {0.0, 0.0};
+    Cx<R> acc = {(R)0, (R)0};
     for (int c = 0; c < 4; ++c) {
-      const int C = children[4 * P + c];
-      const double* M = a.mpole + 2 * (size_t)p * (q + a.nrhs * (size_t)C);
-      double half = 1.0;
+      if (a.children[4 * P + c] < 0) continue;
+      const Cx<R>* ac = av + (size_t)p * (q + nrhs * c);
+      Cx<R> t = {(R)0, (R)0};
       for (int k = 0; k <= l; ++k) {
-        const double f = a.binom[l * P2 + k] * half;
-        acc = cadd(acc, cscale(cmul(ld_c(M, k), dp[c * p + l - k]), f));
-        half *= 0.5;
+        const R bk = a.binom[l * P2 + k];
+        t.re += bk * ac[k].re;
+        t.im += bk * ac[k].im;
       }
+      acc = cadd(acc, cmul(dl[c * p + l], t));
     }
-    st_c(a.mpole, l + (size_t)p * (q + a.nrhs * (size_t)P), acc);
+    st_c(a.mpole, l + (size_t)p * (q + nrhs * (size_t)P), acc);
   }
 }
 
 // M2L from the V list and P2L from the X list; writes the box's local expansion.
-__global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs a) {
+template <class R>
+__global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = a.boxes[blockIdx.x];
   const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
-  Cx* av = reinterpret_cast<Cx*>(smem);      // p x nrhs scaled source coefficients
-  Cx* vp = av + (size_t)p * nrhs;            // p: (-1)^l (s_B/d)^l / d
-  Cx* pw = vp + p;                           // 64 x p powers for P2L
-  const double zbx = a.cx[B], zby = a.cy[B], sB = a.side[B];
+  Cx<R>* av = reinterpret_cast<Cx<R>*>(smem);  // p x nrhs scaled source coefficients
+  Cx<R>* vp = av + (size_t)p * nrhs;           // p: (-1)^l (s_B/d)^l / d
+  Cx<R>* pw = vp + p;                          // kStage x p powers for P2L
+  const Pos<R> zb = box_pos(a, B);
+  const R sB = a.side[B];
   constexpr int kPer = 4;  // (l, q) pairs per thread (p * nrhs <= 512)
-  Cx acc[kPer];
+  Cx<R> acc[kPer];
 #pragma unroll
-  for (int t = 0; t < kPer; ++t) acc[t] = {0.0, 0.0};
+  for (int t = 0; t < kPer; ++t) acc[t] = {(R)0, (R)0};
   for (int vi = a.v_off[B]; vi < a.v_off[B + 1]; ++vi) {
     const int C = a.v_idx[vi];
-    const Cx d = {zbx - a.cx[C], zby - a.cy[C]};
-    const Cx id = cinv(d);
     if (threadIdx.x < 2) {
+      const Cx<R> id = cinv(sub(zb, box_pos(a, C)));
       // thread 0: u^k (u = s_C / d) into pw; thread 1: vp
       if (threadIdx.x == 0) {
-        const Cx u = cscale(id, a.side[C]);
-        Cx v = {1.0, 0.0};
+        const Cx<R> u = cscale(id, a.side[C]);
+        Cx<R> v = {(R)1, (R)0};
         for (int k = 0; k < p; ++k) {
           pw[k] = v;
           v = cmul(v, u);
         }
       } else {
-        const Cx w = cscale(id, sB);
-        Cx v = id;
+        const Cx<R> w = cscale(id, sB);
+        Cx<R> v = id;
         for (int l = 0; l < p; ++l) {
-          vp[l] = (l & 1) ? Cx{-v.re, -v.im} : v;
+          vp[l] = (l & 1) ? Cx<R>{-v.re, -v.im} : v;
           v = cmul(v, w);
         }
       }
     }
     __syncthreads();
-    const double* M = a.mpole + 2 * (size_t)p * nrhs * C;
+    const R* M = a.mpole + 2 * (size_t)p * nrhs * C;
     for (int e = threadIdx.x; e < p * nrhs; e += blockDim.x) {
       const int k = e % p, q = e / p;
       av[k + p * q] = cmul(ld_c(M, k + (size_t)p * q), pw[k]);
@@ -189,10 +265,10 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs a) {
       const int e = threadIdx.x + t * blockDim.x;
       if (e >= p * nrhs) break;
       const int l = e % p, q = e / p;
-      Cx s = {0.0, 0.0};
-      const double* brow = a.binom + (size_t)l;  // C(k + l, l) = binom[(k + l) * P2 + l]
+      Cx<R> s = {(R)0, (R)0};
+      const R* brow = a.binom + (size_t)l;  // C(k + l, l) = binom[(k + l) * P2 + l]
       for (int k = 0; k < p; ++k) {
-        const double bk = brow[(size_t)(k + l) * P2];
+        const R bk = brow[(size_t)(k + l) * P2];
         s.re += bk * av[k + p * q].re;
         s.im += bk * av[k + p * q].im;
       }
@@ -203,13 +279,12 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs a) {
   for (int xi = a.x_off[B]; xi < a.x_off[B + 1]; ++xi) {
     const int S = a.x_idx[xi];
     const int s0 = a.pstart[S], cnt = a.pcount[S];
-    for (int j0 = 0; j0 < cnt; j0 += 64) {
-      const int jc = cnt - j0 < 64 ? cnt - j0 : 64;
+    for (int j0 = 0; j0 < cnt; j0 += kStage) {
+      const int jc = cnt - j0 < kStage ? cnt - j0 : kStage;
       for (int j = threadIdx.x; j < jc; j += blockDim.x) {
-        const Cx w = {a.zx[s0 + j0 + j] - zbx, a.zy[s0 + j0 + j] - zby};
-        const Cx iw = cinv(w);
-        const Cx r = cscale(iw, sB);
-        Cx v = iw;  // 1/w * r^l
+        const Cx<R> iw = cinv(sub(pt_pos(a, s0 + j0 + j), zb));
+        const Cx<R> r = cscale(iw, sB);
+        Cx<R> v = iw;  // 1/w * r^l
         for (int l = 0; l < p; ++l) {
           pw[j * p + l] = v;
           v = cmul(v, r);
@@ -222,8 +297,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs a) {
         if (e >= p * nrhs) break;
         const int l = e % p, q = e / p;
         for (int j = 0; j < jc; ++j) {
-          const Cx c = ld_c(a.charge, s0 + j0 + j + (size_t)a.npts * q);
-          const Cx v = cmul(c, pw[j * p + l]);
+          const Cx<R> v = cmul(ld_c(a.charge, s0 + j0 + j + (size_t)a.npts * q), pw[j * p + l]);
           acc[t].re -= v.re;
           acc[t].im -= v.im;
         }
@@ -240,190 +314,271 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs a) {
   }
 }
 
-// L2L: each box of a level adds its parent's shifted local expansion.
-__global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs a) {
+// L2L: each non-empty box of a level adds its parent's shifted local
+// expansion.  With e = (z_C - z_P)/s_P the shift is
+//   L_m(C) += (2e)^-m sum_{l>=m} C(l,m) (L_l(P) e^l).
+template <class R>
+__global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int C = a.boxes[blockIdx.x];
   const int P = a.parent[C];
   if (P < 0) return;
-  const int p = a.p, P2 = 2 * p;
-  Cx* ep = reinterpret_cast<Cx*>(smem);
-  if (threadIdx.x == 0) {
-    const double isp = rcp(a.side[P]);
-    const Cx e = {(a.cx[C] - a.cx[P]) * isp, (a.cy[C] - a.cy[P]) * isp};
-    Cx v = {1.0, 0.0};
+  const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
+  Cx<R>* el = reinterpret_cast<Cx<R>*>(smem);  // p: e^l
+  Cx<R>* hm = el + p;                          // p: (2e)^-m
+  Cx<R>* bv = hm + p;                          // nrhs x p: L_l(P) e^l
+  if (threadIdx.x < 2) {
+    const Cx<R> e = cscale(sub(box_pos(a, C), box_pos(a, P)), rcp(a.side[P]));
+    const Cx<R> base = threadIdx.x == 0 ? e : cinv(cscale(e, (R)2));
+    Cx<R>* out = threadIdx.x == 0 ? el : hm;
+    Cx<R> v = {(R)1, (R)0};
     for (int m = 0; m < p; ++m) {
-      ep[m] = v;
-      v = cmul(v, e);
+      out[m] = v;
+      v = cmul(v, base);
     }
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < p * a.nrhs; e += blockDim.x) {
+  for (int e = threadIdx.x; e < p * nrhs; e += blockDim.x) {
+    const int l = e % p, q = e / p;
+    bv[e] = cmul(ld_c(a.local, l + (size_t)p * (q + nrhs * (size_t)P)), el[l]);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < p * nrhs; e += blockDim.x) {
     const int m = e % p, q = e / p;
-    const double* Lp = a.local + 2 * (size_t)p * (q + a.nrhs * (size_t)P);
-    Cx acc = {0.0, 0.0};
-    for (int l = m; l < p; ++l) acc = cadd(acc, cscale(cmul(ld_c(Lp, l), ep[l - m]), a.binom[l * P2 + m]));
-    acc = cscale(acc, ldexp(1.0, -m));
-    const size_t o = m + (size_t)p * (q + a.nrhs * (size_t)C);
-    st_c(a.local, o, cadd(ld_c(a.local, o), acc));
+    const Cx<R>* bq = bv + (size_t)p * q;
+    Cx<R> t = {(R)0, (R)0};
+    for (int l = m; l < p; ++l) {
+      const R bl = a.binom[l * P2 + m];
+      t.re += bl * bq[l].re;
+      t.im += bl * bq[l].im;
+    }
+    const size_t o = m + (size_t)p * (q + nrhs * (size_t)C);
+    st_c(a.local, o, cadd(ld_c(a.local, o), cmul(hm[m], t)));
   }
 }
 
-// Evaluation at a leaf's points: L2P + M2P (W list) + P2P (U list).
-__global__ void __launch_bounds__(kFmmThreads) eval_kernel(FmmArgs a, Geo<double> g,
-                                                           const double* mu, double* y) {
+// Evaluation at a leaf's points: L2P + M2P (W list) + P2P (U list), then
+// y = ya * y + yb * (diag mu + phi).  A leaf holds ~30 points on average, so
+// each target is shared by nsplit = blockDim / cnt threads: they split the
+// right-hand sides of L2P / M2P and the sources of P2P (the t-th thread of a
+// target takes every nsplit-th one, starting at t), and their partial
+// sums are added in a fixed order.
+template <class R>
+__global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo<double> g,
+                                                               const double* mu, double* y,
+                                                               double ya, double yb) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = a.boxes[blockIdx.x];
   const int s0 = a.pstart[B], cnt = a.pcount[B];
   const int p = a.p, nrhs = a.nrhs;
-  double* sx = reinterpret_cast<double*>(smem);  // staged sources: 64 x (2 + 2 nrhs)
-  double* sy = sx + 64;
-  double* sc = sy + 64;                          // 64 x nrhs complex
-  const double zbx = a.cx[B], zby = a.cy[B], isB = rcp(a.side[B]);
-  for (int j0 = 0; j0 < cnt; j0 += blockDim.x) {
-    const int j = j0 + threadIdx.x;
-    const bool act = j < cnt;
-    double phi[kMaxRhs];
+  Pos<R>* sp = reinterpret_cast<Pos<R>*>(smem);                 // staged source positions
+  R* sc = reinterpret_cast<R*>(sp + kStage);                    // kStage x kMaxRhs complex
+  double* red = reinterpret_cast<double*>(sc + 2 * kStage * kMaxRhs);  // blockDim x kMaxRhs
+  const Pos<R> zb = box_pos(a, B);
+  const R isB = rcp(a.side[B]);
+  const int nsplit = (cnt > 0 && 2 * cnt <= (int)blockDim.x) ? (int)blockDim.x / cnt : 1;
+  const int span = nsplit > 1 ? cnt : (int)blockDim.x;  // targets per pass
+  const int part = threadIdx.x / span, tj = threadIdx.x % span;
+  for (int j0 = 0; j0 < cnt; j0 += span) {
+    const int j = j0 + tj;
+    const bool act = j < cnt && part < nsplit;
+    R phi[kMaxRhs];
 #pragma unroll
-    for (int q = 0; q < kMaxRhs; ++q) phi[q] = 0.0;
-    double tx = 0, ty = 0;
+    for (int q = 0; q < kMaxRhs; ++q) phi[q] = (R)0;
+    Pos<R> tp{};
     if (act) {
-      tx = a.zx[s0 + j];
-      ty = a.zy[s0 + j];
-      // L2P (Horner on the real part at the end)
-      const Cx rho = {(tx - zbx) * isB, (ty - zby) * isB};
-      for (int q = 0; q < nrhs; ++q) {
-        const double* L = a.local + 2 * (size_t)p * (q + nrhs * (size_t)B);
-        Cx h = ld_c(L, p - 1);
-        for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
-        phi[q] += h.re;
+      tp = pt_pos(a, s0 + j);
+      // L2P
+      const Cx<R> rho = cscale(sub(tp, zb), isB);
+#pragma unroll
+      for (int q = 0; q < kMaxRhs; ++q) {
+        if (q < nrhs && q % nsplit == part) {
+          const R* L = a.local + 2 * (size_t)p * (q + nrhs * (size_t)B);
+          Cx<R> h = ld_c(L, p - 1);
+          for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
+          phi[q] += h.re;
+        }
       }
       // M2P from the W list
       for (int wi = a.w_off[B]; wi < a.w_off[B + 1]; ++wi) {
         const int C = a.w_idx[wi];
-        const Cx w = {tx - a.cx[C], ty - a.cy[C]};
-        const Cx iw = cinv(w);
-        const Cx t = cscale(iw, a.side[C]);
-        for (int q = 0; q < nrhs; ++q) {
-          const double* M = a.mpole + 2 * (size_t)p * (q + nrhs * (size_t)C);
-          Cx h = ld_c(M, p - 1);
-          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, t), ld_c(M, k));
-          phi[q] += cmul(h, iw).re;
-        }
-      }
-    }
-    // P2P from the U list (sources staged 64 at a time)
-    for (int ui = a.u_off[B]; ui < a.u_off[B + 1]; ++ui) {
-      const int D = a.u_idx[ui];
-      const int d0 = a.pstart[D], dcnt = a.pcount[D];
-      for (int i0 = 0; i0 < dcnt; i0 += 64) {
-        const int ic = dcnt - i0 < 64 ? dcnt - i0 : 64;
-        __syncthreads();
-        for (int e = threadIdx.x; e < ic; e += blockDim.x) {
-          sx[e] = a.zx[d0 + i0 + e];
-          sy[e] = a.zy[d0 + i0 + e];
-        }
-        for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
-          const int i = e % ic, q = e / ic;
-          const size_t src = d0 + i0 + i + (size_t)a.npts * q;
-          sc[2 * (i + 64 * q)] = a.charge[2 * src];
-          sc[2 * (i + 64 * q) + 1] = a.charge[2 * src + 1];
-        }
-        __syncthreads();
-        if (act) {
-          for (int i = 0; i < ic; ++i) {
-            if (d0 + i0 + i == s0 + j) continue;  // self
-            const Cx iv = cinv(Cx{tx - sx[i], ty - sy[i]});
+        const Cx<R> iw = cinv(sub(tp, box_pos(a, C)));
+        const Cx<R> t = cscale(iw, a.side[C]);
 #pragma unroll
-            for (int q = 0; q < kMaxRhs; ++q)
-              if (q < nrhs) phi[q] += sc[2 * (i + 64 * q)] * iv.re - sc[2 * (i + 64 * q) + 1] * iv.im;
+        for (int q = 0; q < kMaxRhs; ++q) {
+          if (q < nrhs && q % nsplit == part) {
+            const R* M = a.mpole + 2 * (size_t)p * (q + nrhs * (size_t)C);
+            Cx<R> h = ld_c(M, p - 1);
+            for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, t), ld_c(M, k));
+            phi[q] += cmul(h, iw).re;
           }
         }
       }
     }
-    if (act) {
+    // P2P from the U list (sources staged kStage at a time)
+    for (int ui = a.u_off[B]; ui < a.u_off[B + 1]; ++ui) {
+      const int D = a.u_idx[ui];
+      const int d0 = a.pstart[D], dcnt = a.pcount[D];
+      for (int i0 = 0; i0 < dcnt; i0 += kStage) {
+        const int ic = dcnt - i0 < kStage ? dcnt - i0 : kStage;
+        __syncthreads();
+        for (int e = threadIdx.x; e < ic; e += blockDim.x) sp[e] = pt_pos(a, d0 + i0 + e);
+        for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
+          const int i = e % ic, q = e / ic;
+          const size_t src = d0 + i0 + i + (size_t)a.npts * q;
+          sc[2 * (i + kStage * q)] = a.charge[2 * src];
+          sc[2 * (i + kStage * q) + 1] = a.charge[2 * src + 1];
+        }
+        __syncthreads();
+        if (act) {
+          for (int i = part; i < ic; i += nsplit) {
+            if (d0 + i0 + i == s0 + j) continue;  // self
+            const Cx<R> iv = cinv(sub(tp, sp[i]));
+#pragma unroll
+            for (int q = 0; q < kMaxRhs; ++q)
+              if (q < nrhs)
+                phi[q] += sc[2 * (i + kStage * q)] * iv.re - sc[2 * (i + kStage * q) + 1] * iv.im;
+          }
+        }
+      }
+    }
+    double tot[kMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) tot[q] = (double)phi[q];
+    if (nsplit > 1) {
+      __syncthreads();
+      if (act)
+#pragma unroll
+        for (int q = 0; q < kMaxRhs; ++q) red[threadIdx.x * kMaxRhs + q] = tot[q];
+      __syncthreads();
+      if (act && part == 0)
+        for (int t = 1; t < nsplit; ++t)
+#pragma unroll
+          for (int q = 0; q < kMaxRhs; ++q) tot[q] += red[(t * span + tj) * kMaxRhs + q];
+    }
+    if (act && part == 0) {
       const int pt = a.slot_pt[s0 + j];
       const double diag = 0.5 + 0.5 * g.kap[pt] * g.w[pt] * (1.0 / (2.0 * CUDART_PI));
-      for (int q = 0; q < nrhs; ++q)
-        y[pt + (size_t)a.npts * q] = diag * mu[pt + (size_t)a.npts * q] + phi[q];
+#pragma unroll
+      for (int q = 0; q < kMaxRhs; ++q) {
+        if (q < nrhs) {
+          const size_t o = pt + (size_t)a.npts * q;
+          const double v = yb * (diag * mu[o] + tot[q]);
+          y[o] = ya == 0.0 ? v : ya * y[o] + v;
+        }
+      }
     }
   }
+}
+
+template <class R>
+cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs, double* y,
+                    double ya, double yb, cudaStream_t st) {
+  constexpr bool f32 = sizeof(R) == 4;
+  const int p = f32 ? f.p32 : f.p;
+  const int npts = f.npts, nb = f.nbox;
+  if (p < 2 || p * kMaxRhs > 4 * kFmmThreads) return cudaErrorInvalidValue;
+  set_smem_once<p2m_kernel<R>>();
+  set_smem_once<m2m_kernel<R>>();
+  set_smem_once<m2l_kernel<R>>();
+  set_smem_once<l2l_kernel<R>>();
+  const int pmax = f.p > f.p32 ? f.p : f.p32;
+  cudaError_t e;
+  if ((e = f.charge.ensure(2 * (size_t)npts * kMaxRhs)) != cudaSuccess) return e;
+  if ((e = f.mpole.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
+  if ((e = f.local.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
+  FmmArgs<R> a{};
+  a.cx = f.cx.p;
+  a.cy = f.cy.p;
+  a.zx = f.zx.p;
+  a.zy = f.zy.p;
+  a.cxh = f.cxh.p;
+  a.cxl = f.cxl.p;
+  a.cyh = f.cyh.p;
+  a.cyl = f.cyl.p;
+  a.zxh = f.zxh.p;
+  a.zxl = f.zxl.p;
+  a.zyh = f.zyh.p;
+  a.zyl = f.zyl.p;
+  if constexpr (f32) {
+    a.side = f.side32.p;
+    a.binom = f.binom32.p;
+  } else {
+    a.side = f.side.p;
+    a.binom = f.binom.p;
+  }
+  a.pstart = f.pstart.p;
+  a.pcount = f.pcount.p;
+  a.parent = f.parent.p;
+  a.slot_pt = f.slot_pt.p;
+  a.children = f.children.p;
+  a.v_off = f.v_off.p;
+  a.v_idx = f.v_idx.p;
+  a.w_off = f.w_off.p;
+  a.w_idx = f.w_idx.p;
+  a.x_off = f.x_off.p;
+  a.x_idx = f.x_idx.p;
+  a.u_off = f.u_off.p;
+  a.u_idx = f.u_idx.p;
+  a.p = p;
+  a.npts = npts;
+  R* charge = reinterpret_cast<R*>(f.charge.p);
+  a.charge = charge;
+  a.mpole = reinterpret_cast<R*>(f.mpole.p);
+  a.local = reinterpret_cast<R*>(f.local.p);
+  const unsigned nleaves = (unsigned)f.leaves_h.size();
+  for (int q0 = 0; q0 < nrhs; q0 += kMaxRhs) {
+    const int nq = nrhs - q0 < kMaxRhs ? nrhs - q0 : kMaxRhs;
+    a.nrhs = nq;
+    const double* muq = mu + (size_t)npts * q0;
+    double* yq = y + (size_t)npts * q0;
+    const size_t tot = (size_t)npts * nq;
+    charges_kernel<R><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(geo, f.slot_pt.p, npts, muq,
+                                                                     nq, charge);
+    // upward pass
+    a.boxes = f.leaves.p;
+    if (nleaves)
+      p2m_kernel<R><<<nleaves, kFmmThreads, sizeof(Cx<R>) * kStage * (size_t)p, st>>>(a);
+    // levels 0 and 1 have no V, W or X partners: their multipoles are unused
+    for (int lv = f.nlevels - 2; lv >= 2; --lv) {
+      const int cnt = f.level_off[lv + 1] - f.level_off[lv];
+      if (!cnt) continue;
+      a.boxes = f.lvl_boxes.p + f.level_off[lv];
+      m2m_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (8 * (size_t)p + 4 * (size_t)p * nq), st>>>(a);
+    }
+    // interactions and downward pass
+    if ((e = cudaMemsetAsync(f.local.p, 0, 2 * sizeof(R) * (size_t)p * nq * nb, st)) != cudaSuccess)
+      return e;
+    if (!f.m2l_boxes_h.empty()) {
+      a.boxes = f.m2l_boxes.p;
+      m2l_kernel<R><<<(unsigned)f.m2l_boxes_h.size(), kFmmThreads,
+                      sizeof(Cx<R>) * ((size_t)p * nq + p + kStage * (size_t)p), st>>>(a);
+    }
+    // locals of levels <= 2 come only from M2L (level 0/1 locals are zero)
+    for (int lv = 3; lv < f.nlevels; ++lv) {
+      const int cnt = f.level_off[lv + 1] - f.level_off[lv];
+      if (!cnt) continue;
+      a.boxes = f.lvl_boxes.p + f.level_off[lv];
+      l2l_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (2 * (size_t)p + (size_t)p * nq), st>>>(a);
+    }
+    a.boxes = f.leaves.p;
+    if (nleaves)
+      eval_kernel<R><<<nleaves, kEvalThreads,
+                       sizeof(Pos<R>) * kStage + sizeof(Cx<R>) * kStage * kMaxRhs +
+                           sizeof(double) * kEvalThreads * kMaxRhs, st>>>(
+          a, geo, muq, yq, ya, yb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
 
 cudaError_t fmm_laplace_apply(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs,
-                              double* y, cudaStream_t st) {
+                              double* y, double ya, double yb, bool fp32, cudaStream_t st) {
   if (!f.built) return cudaErrorInvalidValue;
-  const int p = f.p, npts = f.npts, nb = f.nbox;
-  if (p < 2 || p * kMaxRhs > 4 * kFmmThreads) return cudaErrorInvalidValue;
-  set_smem_once<p2m_kernel>();
-  set_smem_once<m2l_kernel>();
-  for (int q0 = 0; q0 < nrhs; q0 += kMaxRhs) {
-    const int nq = nrhs - q0 < kMaxRhs ? nrhs - q0 : kMaxRhs;
-    cudaError_t e;
-    if ((e = f.charge.ensure(2 * (size_t)npts * kMaxRhs)) != cudaSuccess) return e;
-    if ((e = f.mpole.ensure(2 * (size_t)p * kMaxRhs * nb)) != cudaSuccess) return e;
-    if ((e = f.local.ensure(2 * (size_t)p * kMaxRhs * nb)) != cudaSuccess) return e;
-    FmmArgs a{};
-    a.cx = f.cx.p;
-    a.cy = f.cy.p;
-    a.side = f.side.p;
-    a.zx = f.zx.p;
-    a.zy = f.zy.p;
-    a.binom = f.binom.p;
-    a.pstart = f.pstart.p;
-    a.pcount = f.pcount.p;
-    a.parent = f.parent.p;
-    a.slot_pt = f.slot_pt.p;
-    a.v_off = f.v_off.p;
-    a.v_idx = f.v_idx.p;
-    a.w_off = f.w_off.p;
-    a.w_idx = f.w_idx.p;
-    a.x_off = f.x_off.p;
-    a.x_idx = f.x_idx.p;
-    a.u_off = f.u_off.p;
-    a.u_idx = f.u_idx.p;
-    a.p = p;
-    a.npts = npts;
-    a.nrhs = nq;
-    a.charge = f.charge.p;
-    a.mpole = f.mpole.p;
-    a.local = f.local.p;
-    const double* muq = mu + (size_t)npts * q0;
-    double* yq = y + (size_t)npts * q0;
-    const size_t tot = (size_t)npts * nq;
-    charges_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq,
-                                                                  f.charge.p);
-    // upward pass
-    a.boxes = f.leaves.p;
-    p2m_kernel<<<(unsigned)f.leaves_h.size(), kFmmThreads, sizeof(Cx) * 64 * (size_t)p, st>>>(a);
-    for (int lv = f.nlevels - 2; lv >= 0; --lv) {
-      const int cnt = f.level_off[lv + 1] - f.level_off[lv];
-      if (!cnt) continue;
-      a.boxes = f.lvl_boxes.p + f.level_off[lv];
-      m2m_kernel<<<cnt, kFmmThreads, sizeof(Cx) * 4 * p, st>>>(a, f.children.p);
-    }
-    // interactions and downward pass
-    if ((e = cudaMemsetAsync(f.local.p, 0, 2 * sizeof(double) * (size_t)p * nq * nb, st)) != cudaSuccess)
-      return e;
-    if (!f.m2l_boxes_h.empty()) {
-      a.boxes = f.m2l_boxes.p;
-      m2l_kernel<<<(unsigned)f.m2l_boxes_h.size(), kFmmThreads,
-                   sizeof(Cx) * ((size_t)p * nq + p + 64 * (size_t)p), st>>>(a);
-    }
-    for (int lv = 1; lv < f.nlevels; ++lv) {
-      const int cnt = f.level_off[lv + 1] - f.level_off[lv];
-      if (!cnt) continue;
-      a.boxes = f.lvl_boxes.p + f.level_off[lv];
-      l2l_kernel<<<cnt, kFmmThreads, sizeof(Cx) * p, st>>>(a);
-    }
-    a.boxes = f.leaves.p;
-    eval_kernel<<<(unsigned)f.leaves_h.size(), kFmmThreads,
-                  sizeof(double) * (128 + 2 * 64 * kMaxRhs), st>>>(a, geo, muq, yq);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return fp32 ? apply_t<float>(f, geo, mu, nrhs, y, ya, yb, st)
+              : apply_t<double>(f, geo, mu, nrhs, y, ya, yb, st);
 }
 
 }  // namespace rskel

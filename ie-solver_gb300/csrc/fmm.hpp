@@ -1,5 +1,5 @@
-// Fast multipole evaluation of the Laplace double-layer operator in FP64,
-// used for the residual of the FP32 factorization's iterative refinement.
+// Fast multipole evaluation of the Laplace double-layer operator, used for
+// the residual of the FP32 factorization's iterative refinement.
 //
 // In complex notation (z = x + iy, nu = n_x + i n_y) the double-layer kernel
 // of ie_solver/kernel/kernel.cpp:123-165 is
@@ -10,7 +10,14 @@
 // adaptive U/V/W/X lists of Carrier, Greengard & Rokhlin (1988) built on the
 // solver's own quadtree.  Expansions are scaled by box size (multipole
 // coefficients by s^-k, local coefficients by s^l) so that no power
-// overflows for small boxes.
+// overflows for small boxes.  Boxes holding no points are left out of every
+// list: their expansions are zero and they have no targets.
+//
+// Two arithmetic variants share one plan: FP64 (order p) for the first,
+// full residual, and FP32 (order p32) for products with refinement
+// corrections, whose size is already ~1e-6 of the solution's.  The FP32
+// variant keeps every coordinate as an unevaluated float pair (hi + lo), so
+// differences of nearby points are exact to FP32 rounding.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,45 +31,48 @@
 namespace rskel {
 
 struct FmmPlan {
-  int p = 0;          // expansion order
+  int p = 0;          // expansion order, FP64 variant
+  int p32 = 0;        // expansion order, FP32 variant
   int nbox = 0;
   int npts = 0;
   int nlevels = 0;
   bool built = false;
   // per box (tree node id order)
   DevBuf<double> cx, cy, side;
+  DevBuf<float> cxh, cxl, cyh, cyl, side32;
   DevBuf<int> pstart, pcount;  // leaf point ranges in slot order (count 0: not a leaf)
   DevBuf<int> parent;
-  DevBuf<int> children;        // 4 per box, -1 for leaves
-  int max_leaf_pts = 0;
+  DevBuf<int> children;        // 4 per box, -1 for leaves or empty children
   // slot order of points (leaf by leaf)
   DevBuf<int> slot_pt;         // slot -> point
   DevBuf<double> zx, zy;       // slot coordinates
+  DevBuf<float> zxh, zxl, zyh, zyl;
   // interaction lists (CSR over boxes)
   DevBuf<int> v_off, v_idx, w_off, w_idx, x_off, x_idx, u_off, u_idx;
-  // boxes grouped by level for the tree passes (deepest first in host order)
-  std::vector<std::vector<int>> level_boxes;
+  // non-empty boxes grouped by level (tree passes)
   std::vector<int> level_off;
   DevBuf<int> lvl_boxes;       // concatenated level lists
-  std::vector<int> leaves_h;
+  std::vector<int> leaves_h;   // non-empty leaves
   DevBuf<int> leaves;
   std::vector<int> m2l_boxes_h;
   DevBuf<int> m2l_boxes;       // boxes with non-empty V or X lists
   DevBuf<double> binom;        // (2p) x (2p), binom[a * 2p + b] = C(a, b)
-  // work buffers
-  DevBuf<double> charge;       // complex charges, slot-major: 2 * (slot + npts * rhs)
-  DevBuf<double> mpole, local; // complex: 2 * (k + p * (rhs + nrhs * box))
-  int cap_rhs = 0;
+  DevBuf<float> binom32;       // (2 p32) x (2 p32)
+  size_t v_pairs = 0, u_pairs = 0, w_pairs = 0, x_pairs = 0;
+  // work buffers (complex Real pairs; sized for FP64)
+  DevBuf<double> charge;       // 2 * (slot + npts * rhs)
+  DevBuf<double> mpole, local; // 2 * (k + p * (rhs + nrhs * box))
 };
 
 // Builds the lists on the host from the tree (points interleaved, sd = 1).
-// Expansion orders 2..64 are supported.
-bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p,
+// Orders 2..64 are supported for both variants.
+bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p, int p32,
                cudaStream_t st);
 
-// y[:, q] = K mu[:, q] for the Laplace double layer (device pointers, column
-// major npts x nrhs); geo holds the per-point boundary data.
+// y[:, q] = ya * y[:, q] + yb * (K mu)[:, q] for the Laplace double layer
+// (device pointers, column major npts x nrhs; y is not read when ya == 0).
+// fp32 selects the FP32 variant.  geo holds the per-point boundary data.
 cudaError_t fmm_laplace_apply(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs,
-                              double* y, cudaStream_t st);
+                              double* y, double ya, double yb, bool fp32, cudaStream_t st);
 
 }  // namespace rskel

@@ -9,6 +9,7 @@
 //   touches B is descended into (or, if a leaf, joins U(B), and B joins its
 //   U list); a child that does not touch B joins W(B) and B joins its X list.
 //   Leaf colleagues (and B itself) join U(B).
+// Boxes with no points are skipped throughout.
 // The quadtree's own neighbour lists follow the reference's construction,
 // including its `y < top && y < bottom` condition (quadtree.cpp:209), so the
 // FMM recomputes adjacency from the box geometry instead.
@@ -50,27 +51,40 @@ void csr(const std::vector<std::vector<int>>& lists, std::vector<int>* off, std:
 
 }  // namespace
 
-bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p,
+bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p, int p32,
                cudaStream_t st) {
   (void)st;
-  if (p < 2 || p > 64 || npts <= 0) return false;
+  if (p < 2 || p > 64 || p32 < 2 || p32 > 64 || npts <= 0) return false;
   const int nb = (int)tree.nodes.size();
   f.p = p;
+  f.p32 = p32;
   f.nbox = nb;
   f.npts = npts;
   std::vector<Box> box(nb);
   for (int i = 0; i < nb; ++i)
     box[i] = Box{tree.nodes[i].corners[0], tree.nodes[i].corners[1], tree.nodes[i].side};
+  // points per subtree; empty boxes take part in nothing
+  std::vector<int> cnt(nb, 0);
+  for (int lv = (int)tree.levels.size() - 1; lv >= 0; --lv)
+    for (int b : tree.levels[lv]) {
+      const TreeNode& nd = tree.nodes[b];
+      if (nd.is_leaf) cnt[b] = (int)nd.original.size() / tree.sd;
+      else
+        for (int q = 0; q < 4; ++q) cnt[b] += cnt[nd.children[q]];
+    }
+  auto live = [&](int b) { return cnt[b] > 0; };
   const double eps = 1e-9 * tree.nodes[tree.root].side;
   std::vector<std::vector<int>> coll(nb), V(nb), W(nb), X(nb), U(nb);
-  coll[tree.root].push_back(tree.root);
+  if (live(tree.root)) coll[tree.root].push_back(tree.root);
   for (size_t lv = 1; lv < tree.levels.size(); ++lv) {
     for (int b : tree.levels[lv]) {
+      if (!live(b)) continue;
       const int par = tree.nodes[b].parent;
       for (int c : coll[par]) {
         if (tree.nodes[c].is_leaf) continue;
         for (int q = 0; q < 4; ++q) {
           const int d = tree.nodes[c].children[q];
+          if (!live(d)) continue;
           if (touch(box[d], box[b], eps)) coll[b].push_back(d);
           else V[b].push_back(d);
         }
@@ -80,7 +94,7 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
   // U, W, X for leaves
   std::vector<int> stack;
   for (int b = 0; b < nb; ++b) {
-    if (!tree.nodes[b].is_leaf) continue;
+    if (!tree.nodes[b].is_leaf || !live(b)) continue;
     for (int c : coll[b]) {
       if (tree.nodes[c].is_leaf) {
         U[b].push_back(c);
@@ -92,6 +106,7 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
         stack.pop_back();
         for (int q = 0; q < 4; ++q) {
           const int d = tree.nodes[node].children[q];
+          if (!live(d)) continue;
           if (touch(box[d], box[b], eps)) {
             if (tree.nodes[d].is_leaf) {
               U[b].push_back(d);
@@ -117,34 +132,44 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
     for (size_t q = 0; q < tree.nodes[id].original.size(); q += tree.sd)
       slot_pt.push_back(tree.nodes[id].original[q] / tree.sd);
     pcount[id] = (int)slot_pt.size() - pstart[id];
-    f.leaves_h.push_back(id);
+    if (pcount[id] > 0) f.leaves_h.push_back(id);
   }
   if ((int)slot_pt.size() != npts) return false;
+  auto split = [](double v, float* hi, float* lo) {
+    *hi = (float)v;
+    *lo = (float)(v - (double)*hi);
+  };
   std::vector<double> zx(npts), zy(npts), cx(nb), cy(nb), side(nb);
+  std::vector<float> zxh(npts), zxl(npts), zyh(npts), zyl(npts);
+  std::vector<float> cxh(nb), cxl(nb), cyh(nb), cyl(nb), side32(nb);
   for (int s = 0; s < npts; ++s) {
     zx[s] = points[2 * slot_pt[s]];
     zy[s] = points[2 * slot_pt[s] + 1];
+    split(zx[s], &zxh[s], &zxl[s]);
+    split(zy[s], &zyh[s], &zyl[s]);
   }
   std::vector<int> parent(nb), children(4 * (size_t)nb, -1);
-  f.max_leaf_pts = 0;
-  for (int i = 0; i < nb; ++i) f.max_leaf_pts = std::max(f.max_leaf_pts, pcount[i]);
   for (int i = 0; i < nb; ++i) {
     if (!tree.nodes[i].is_leaf)
-      for (int q = 0; q < 4; ++q) children[4 * (size_t)i + q] = tree.nodes[i].children[q];
+      for (int q = 0; q < 4; ++q) {
+        const int c = tree.nodes[i].children[q];
+        children[4 * (size_t)i + q] = live(c) ? c : -1;
+      }
     cx[i] = box[i].x0 + box[i].s / 2.0;
     cy[i] = box[i].y0 + box[i].s / 2.0;
     side[i] = box[i].s;
+    split(cx[i], &cxh[i], &cxl[i]);
+    split(cy[i], &cyh[i], &cyl[i]);
+    side32[i] = (float)side[i];
     parent[i] = tree.nodes[i].parent;
   }
-  // levels (for the upward pass only non-leaf boxes; downward all non-root)
+  // non-empty boxes by level
   f.nlevels = (int)tree.levels.size();
-  f.level_boxes.assign(f.nlevels, {});
-  for (int lv = 0; lv < f.nlevels; ++lv)
-    for (int b : tree.levels[lv]) f.level_boxes[lv].push_back(b);
   std::vector<int> lvl_flat;
   f.level_off.assign(f.nlevels + 1, 0);
   for (int lv = 0; lv < f.nlevels; ++lv) {
-    lvl_flat.insert(lvl_flat.end(), f.level_boxes[lv].begin(), f.level_boxes[lv].end());
+    for (int b : tree.levels[lv])
+      if (live(b)) lvl_flat.push_back(b);
     f.level_off[lv + 1] = (int)lvl_flat.size();
   }
   f.m2l_boxes_h.clear();
@@ -155,26 +180,41 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
   csr(W, &wo, &wi);
   csr(X, &xo, &xi);
   csr(U, &uo, &ui);
-  // binomial table (2p x 2p)
-  const int P2 = 2 * p;
-  std::vector<double> binom((size_t)P2 * P2, 0.0);
-  for (int a = 0; a < P2; ++a) {
-    binom[(size_t)a * P2] = 1.0;
-    for (int b = 1; b <= a; ++b)
-      binom[(size_t)a * P2 + b] = binom[(size_t)(a - 1) * P2 + b - 1] +
-                                  (b < a ? binom[(size_t)(a - 1) * P2 + b] : 0.0);
-  }
+  f.v_pairs = vi.size();
+  f.w_pairs = wi.size();
+  f.x_pairs = xi.size();
+  f.u_pairs = ui.size();
+  // binomial tables (2p x 2p)
+  auto pascal = [](int P2, std::vector<double>* t) {
+    t->assign((size_t)P2 * P2, 0.0);
+    for (int a = 0; a < P2; ++a) {
+      (*t)[(size_t)a * P2] = 1.0;
+      for (int b = 1; b <= a; ++b)
+        (*t)[(size_t)a * P2 + b] =
+            (*t)[(size_t)(a - 1) * P2 + b - 1] + (b < a ? (*t)[(size_t)(a - 1) * P2 + b] : 0.0);
+    }
+  };
+  std::vector<double> binom, b32d;
+  pascal(2 * p, &binom);
+  pascal(2 * p32, &b32d);
+  std::vector<float> binom32(b32d.begin(), b32d.end());
   bool ok = upload(f.cx, cx) == cudaSuccess && upload(f.cy, cy) == cudaSuccess &&
-            upload(f.side, side) == cudaSuccess && upload(f.pstart, pstart) == cudaSuccess &&
-            upload(f.pcount, pcount) == cudaSuccess && upload(f.parent, parent) == cudaSuccess && upload(f.children, children) == cudaSuccess &&
+            upload(f.side, side) == cudaSuccess && upload(f.cxh, cxh) == cudaSuccess &&
+            upload(f.cxl, cxl) == cudaSuccess && upload(f.cyh, cyh) == cudaSuccess &&
+            upload(f.cyl, cyl) == cudaSuccess && upload(f.side32, side32) == cudaSuccess &&
+            upload(f.pstart, pstart) == cudaSuccess && upload(f.pcount, pcount) == cudaSuccess &&
+            upload(f.parent, parent) == cudaSuccess && upload(f.children, children) == cudaSuccess &&
             upload(f.slot_pt, slot_pt) == cudaSuccess && upload(f.zx, zx) == cudaSuccess &&
-            upload(f.zy, zy) == cudaSuccess && upload(f.v_off, vo) == cudaSuccess &&
+            upload(f.zy, zy) == cudaSuccess && upload(f.zxh, zxh) == cudaSuccess &&
+            upload(f.zxl, zxl) == cudaSuccess && upload(f.zyh, zyh) == cudaSuccess &&
+            upload(f.zyl, zyl) == cudaSuccess && upload(f.v_off, vo) == cudaSuccess &&
             upload(f.v_idx, vi) == cudaSuccess && upload(f.w_off, wo) == cudaSuccess &&
             upload(f.w_idx, wi) == cudaSuccess && upload(f.x_off, xo) == cudaSuccess &&
             upload(f.x_idx, xi) == cudaSuccess && upload(f.u_off, uo) == cudaSuccess &&
             upload(f.u_idx, ui) == cudaSuccess && upload(f.lvl_boxes, lvl_flat) == cudaSuccess &&
             upload(f.leaves, f.leaves_h) == cudaSuccess &&
-            upload(f.m2l_boxes, f.m2l_boxes_h) == cudaSuccess && upload(f.binom, binom) == cudaSuccess;
+            upload(f.m2l_boxes, f.m2l_boxes_h) == cudaSuccess &&
+            upload(f.binom, binom) == cudaSuccess && upload(f.binom32, binom32) == cudaSuccess;
   f.built = ok;
   return ok;
 }

@@ -59,6 +59,7 @@ struct SweepParams {
   void* x;          // Real, D x nrhs, column major
   int ld, nrhs;
   int mode;
+  int stage_x;      // set by launch_sweep: X_rr's LU factors staged in shared memory
 };
 
 size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);
@@ -84,6 +85,7 @@ void launch_dense_solve_gather(const void* lu, bool fp32, int n, const int* piv,
 // Precision conversions and residual update for refinement.
 void launch_d2f(const double* in, float* out, size_t n, cudaStream_t st);
 void launch_add_f2d(double* acc, const float* inc, size_t n, cudaStream_t st);
+void launch_f2d(const float* in, double* out, size_t n, cudaStream_t st);
 
 // Dense double-layer block K(I, J) (FP64), column major.
 void launch_kernel_block(const Geo<double>& g, int pde, int sd, const int* I, int nI,

@@ -55,6 +55,13 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(SweepParams p) {
   const Real* L = fac + fac_L(k, r);
   const Real* U = fac + fac_U(k, r);
   const Real* X = fac + fac_X(k, r);
+  // The triangular solves with X_rr are chains of dependent steps: one bulk
+  // copy to shared memory replaces a global round trip per step.
+  if (p.stage_x && (p.mode == kUpSolve || p.mode == kDiagOnly)) {
+    Real* xsh = carve<Real>(sp, r * r);
+    for (int e = threadIdx.x; e < r * r; e += blockDim.x) xsh[e] = X[e];
+    X = xsh;
+  }
   Real* x = reinterpret_cast<Real*>(p.x);
   const int* sk = p.dofs + t.skel_off;
   const int* rd = p.dofs + t.red_off;
@@ -127,26 +134,39 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(SweepParams p) {
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st) {
   if (num_tasks <= 0) return;
   size_t es = fp32 ? sizeof(float) : sizeof(double);
-  size_t smem = 2 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) + sizeof(int) * nmax + 64;
+  size_t smem = 2 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
+                ((sizeof(int) * nmax + 15) & ~size_t(15)) + 64;
+  SweepParams q = p;
+  const size_t xb = ((size_t)nmax * nmax * es + 15) & ~size_t(15);
+  q.stage_x = (p.mode == kUpSolve || p.mode == kDiagOnly) && smem + xb <= (size_t)kSmemOptIn;
+  if (q.stage_x) smem += xb;
   if (fp32) {
     set_smem_once<sweep_kernel<float>>();
-    sweep_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
+    sweep_kernel<float><<<num_tasks, kThreads, smem, st>>>(q);
   } else {
     set_smem_once<sweep_kernel<double>>();
-    sweep_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
+    sweep_kernel<double><<<num_tasks, kThreads, smem, st>>>(q);
   }
 }
 
 // ---------------------------------------------------------------------------
 // Dense LU (dgetrf with partial pivoting), one CTA, matrix in global memory.
 // ---------------------------------------------------------------------------
+// LU with partial pivoting of one n x n block by one CTA (dgetrf as the
+// reference calls it for the root, ie_mat.cpp:449-470).  With staged != 0
+// the block is held in shared memory for the whole factorization.
 template <class Real>
-__global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* A, int n, int* piv,
-                                                            int* status) {
+__global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* Ag, int n, int* piv,
+                                                            int* status, int staged) {
+  extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_piv;
   __shared__ int s_bad;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  Real* A = staged ? reinterpret_cast<Real*>(smem) : Ag;
+  if (staged)
+    for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) A[e] = Ag[e];
   if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
   for (int j = 0; j < n; ++j) {
     if (warp == 0) {
       double best = -1.0;
@@ -183,35 +203,61 @@ __global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* A, int n, int*
       for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)n * j] *= inv;
     }
     __syncthreads();
-    const int rem = n - j - 1;
     for (int c = j + 1 + warp; c < n; c += kWarps) {
       const Real ajc = A[j + (size_t)n * c];
       for (int i = j + 1 + lane; i < n; i += 32) A[i + (size_t)n * c] -= A[i + (size_t)n * j] * ajc;
     }
-    (void)rem;
     __syncthreads();
   }
+  if (staged)
+    for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) Ag[e] = A[e];
   if (threadIdx.x == 0 && s_bad) atomicExch(status, 1);
 }
 
+template <class Real>
+static void launch_dense_lu_t(Real* a, int n, int* piv, int* status, cudaStream_t st) {
+  if (n <= 0) return;
+  const size_t bytes = sizeof(Real) * (size_t)n * n;
+  const int staged = bytes + 1024 <= (size_t)kSmemOptIn;  // room for the static variables
+  set_smem_once<dense_lu_kernel<Real>>();
+  dense_lu_kernel<Real><<<1, kThreads, staged ? bytes : 0, st>>>(a, n, piv, status, staged);
+}
 void launch_dense_lu(double* a, int n, int* piv, int* status, cudaStream_t st) {
-  if (n > 0) dense_lu_kernel<double><<<1, kThreads, 0, st>>>(a, n, piv, status);
+  launch_dense_lu_t<double>(a, n, piv, status, st);
 }
 void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st) {
-  if (n > 0) dense_lu_kernel<float><<<1, kThreads, 0, st>>>(a, n, piv, status);
+  launch_dense_lu_t<float>(a, n, piv, status, st);
 }
 
-// x[idx, c] = LU^{-1} x[idx, c]: one CTA; the gathered block lives in global
-// scratch-free form by solving column by column directly on x (one warp per
-// column; rows are reached through idx).
+// x[idx, c] = LU^{-1} x[idx, c] for the root block (dgetrs), up to kWarps
+// columns per CTA, one warp per column.  staged: 0 = work on x and LU in
+// global memory; 1 = gathered columns in shared memory (n x cols); 2 = the
+// LU factors in shared memory too.
 template <class Real>
-__global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LU, int n,
+__global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LUg, int n,
                                                                const int* piv, const int* idx,
-                                                               Real* x, int ld, int nrhs) {
+                                                               Real* x, int ld, int nrhs,
+                                                               int staged) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Real* sx = reinterpret_cast<Real*>(smem);
+  Real* sl = sx + (size_t)n * nrhs;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Real* LU = LUg;
+  if (staged) {
+    for (int e = threadIdx.x; e < n * nrhs; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      sx[e] = x[(idx ? idx[i] : i) + (size_t)ld * c];
+    }
+    if (staged == 2) {
+      for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) sl[e] = LUg[e];
+      LU = sl;
+    }
+    __syncthreads();
+  }
   for (int c = warp; c < nrhs; c += kWarps) {
-    Real* v = x + (size_t)ld * c;
-    auto at = [&](int i) -> Real& { return v[idx ? idx[i] : i]; };
+    Real* v = staged ? sx + (size_t)n * c : x + (size_t)ld * c;
+    const int* ix = staged ? nullptr : idx;
+    auto at = [&](int i) -> Real& { return v[ix ? ix[i] : i]; };
     if (lane == 0)
       for (int j = 0; j < n; ++j)
         if (piv[j] != j) { Real t = at(j); at(j) = at(piv[j]); at(piv[j]) = t; }
@@ -230,22 +276,36 @@ __global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LU, i
       __syncwarp();
     }
   }
+  if (staged) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * nrhs; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      x[(idx ? idx[i] : i) + (size_t)ld * c] = sx[e];
+    }
+  }
+}
+
+template <class Real>
+static void launch_dense_solve_t(const Real* lu, int n, const int* piv, const int* idx, Real* x,
+                                 int ld, int nrhs, cudaStream_t st) {
+  set_smem_once<dense_solve_kernel<Real>>();
+  for (int c0 = 0; c0 < nrhs; c0 += kWarps) {
+    const int cols = nrhs - c0 < kWarps ? nrhs - c0 : kWarps;
+    const size_t xb = sizeof(Real) * (size_t)n * cols, lb = sizeof(Real) * (size_t)n * n;
+    const int staged = xb + lb <= (size_t)kSmemOptIn ? 2 : xb <= (size_t)kSmemOptIn ? 1 : 0;
+    const size_t smem = staged == 2 ? xb + lb : staged == 1 ? xb : 0;
+    dense_solve_kernel<Real><<<1, kThreads, smem, st>>>(lu, n, piv, idx, x + (size_t)ld * c0, ld,
+                                                        cols, staged);
+  }
 }
 
 void launch_dense_solve_gather(const void* lu, bool fp32, int n, const int* piv,
                                const int* idx, void* x, int ld, int nrhs, cudaStream_t st) {
   if (n <= 0 || nrhs <= 0) return;
-  int blocks = (nrhs + kWarps - 1) / kWarps;
-  // Each CTA handles kWarps columns.
-  for (int b = 0; b < blocks; ++b) {
-    int cols = nrhs - b * kWarps < kWarps ? nrhs - b * kWarps : kWarps;
-    if (fp32)
-      dense_solve_kernel<float><<<1, kThreads, 0, st>>>(
-          (const float*)lu, n, piv, idx, (float*)x + (size_t)ld * b * kWarps, ld, cols);
-    else
-      dense_solve_kernel<double><<<1, kThreads, 0, st>>>(
-          (const double*)lu, n, piv, idx, (double*)x + (size_t)ld * b * kWarps, ld, cols);
-  }
+  if (fp32)
+    launch_dense_solve_t<float>((const float*)lu, n, piv, idx, (float*)x, ld, nrhs, st);
+  else
+    launch_dense_solve_t<double>((const double*)lu, n, piv, idx, (double*)x, ld, nrhs, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -366,6 +426,13 @@ void launch_d2f(const double* in, float* out, size_t n, cudaStream_t st) {
 void launch_add_f2d(double* acc, const float* inc, size_t n, cudaStream_t st) {
   if (n) add_f2d_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(acc, inc, n);
 }
+__global__ void f2d_kernel(const float* in, double* out, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i];
+}
+void launch_f2d(const float* in, double* out, size_t n, cudaStream_t st) {
+  if (n) f2d_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+}
 void launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st) {
   if (n) axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, x, a, b, n);
 }
@@ -375,11 +442,15 @@ void launch_axpby(double* y, const double* x, double a, double b, size_t n, cuda
 namespace rskel {
 
 // out[c] = || x[:, c] ||_2
-__global__ void col_norms_kernel(const double* x, int rows, double* out) {
-  const int c = blockIdx.x;
+// Two passes with a fixed summation order (the convergence test must not
+// depend on scheduling): kNormBlocks partial sums per column, then one
+// warp per column adds them.
+constexpr int kNormBlocks = 64;
+__global__ void col_norms_partial_kernel(const double* x, int rows, double* part) {
+  const int c = blockIdx.y, b = blockIdx.x;
   double s = 0.0;
-  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
-    double v = x[i + (size_t)rows * c];
+  for (int i = b * blockDim.x + threadIdx.x; i < rows; i += kNormBlocks * blockDim.x) {
+    const double v = x[i + (size_t)rows * c];
     s += v * v;
   }
   s = warp_sum(s);
@@ -389,12 +460,26 @@ __global__ void col_norms_kernel(const double* x, int rows, double* out) {
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    out[c] = sqrt(t);
+    part[b + kNormBlocks * (size_t)c] = t;
   }
 }
 
+__global__ void col_norms_final_kernel(const double* part, int cols, double* out) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= cols) return;
+  double s = 0.0;
+  for (int b = lane; b < kNormBlocks; b += 32) s += part[b + kNormBlocks * (size_t)c];
+  s = warp_sum(s);
+  if (lane == 0) out[c] = sqrt(s);
+}
+
+// out[c] = ||x[:, c]||_2; out must hold cols + kNormBlocks * cols doubles
+// (the tail holds the partial sums).
 void launch_col_norms(const double* x, int rows, int cols, double* out, cudaStream_t st) {
-  if (cols > 0) col_norms_kernel<<<cols, 256, 0, st>>>(x, rows, out);
+  if (cols <= 0) return;
+  double* part = out + cols;
+  col_norms_partial_kernel<<<dim3(kNormBlocks, cols), 256, 0, st>>>(x, rows, part);
+  col_norms_final_kernel<<<(cols + 7) / 8, 256, 0, st>>>(part, cols, out);
 }
 
 // r[l] -= sum_j U[l, j] a[j]

@@ -110,10 +110,11 @@ struct rs_solver {
   DevBuf<int> S_piv;
 
   // solve buffers
-  DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev;
+  DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev, x64, xa64, g64;
   HostBuf<double> h_io;
 
   FmmPlan fmm;
+  double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
   rs_stats stats;
   int launches = 0;
@@ -642,6 +643,9 @@ rs_status factor_impl(rs_solver* s) {
     }
     t_post += now_ms() - h2;
   }
+  s->host_plan_ms = t_plan;
+  s->host_wait_ms = t_wait;
+  s->host_post_ms = t_post;
   if (s->trace)
     std::fprintf(stderr, "[rskel] host: plan+launch %.3f ms, wait %.3f ms, post %.3f ms\n", t_plan,
                  t_wait, t_post);
@@ -959,11 +963,24 @@ namespace {
 
 // r = f - K mu - U alpha;  rg = alpha - Psi mu  (bordered operator of
 // ie_solver_test.cpp:43-83, [K U; Psi -I]).
+// Multipole plan for the refinement residual (Laplace): FP64 order from the
+// configuration (default 32: ~1e-13 relative to the dense FP64 product on the
+// 65536-point star), FP32 order 16 for correction products.
+constexpr int kFmmOrderDefault = 32;
+constexpr int kFmmOrder32 = 16;
+rs_status build_fmm(rs_solver* s) {
+  const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : kFmmOrderDefault;
+  if (p > 64) return fail(s, RS_ERR_ARG, "fmm_order above 64");
+  if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, kFmmOrder32, s->stream))
+    return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
+  return RS_OK;
+}
+
 rs_status residual(rs_solver* s, const double* f, const double* mu, const double* alpha,
                    int nrhs, double* r, double* rg) {
   const int D = s->D;
   if (s->fmm.built) {
-    CU(fmm_laplace_apply(s->fmm, geo_of(s), mu, nrhs, r, s->stream));
+    CU(fmm_laplace_apply(s->fmm, geo_of(s), mu, nrhs, r, 0.0, 1.0, false, s->stream));
     s->launches += 5 + 2 * s->fmm.nlevels;
   } else {
     launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, mu, nrhs, r, s->stream);
@@ -978,6 +995,30 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
                            rg + (size_t)nb * c, nb, s->stream);
       launch_axpby(rg + (size_t)nb * c, alpha + (size_t)nb * c, 1.0, -1.0, nb, s->stream);
       s->launches += 3;
+    }
+  }
+  CU(cudaGetLastError());
+  return RS_OK;
+}
+
+// Residual recurrence for a refinement correction (x, xa) of (mu, alpha):
+// r -= K x + U xa and rg -= Psi x - xa, with K x from the FP32 multipole
+// variant (the correction is ~1e-6 of the solution, so FP32 accuracy of the
+// product leaves the residual exact to ~1e-13 of the data).
+rs_status residual_update(rs_solver* s, const double* x, const double* xa, int nrhs, double* r,
+                          double* rg, double* g) {
+  const int D = s->D;
+  CU(fmm_laplace_apply(s->fmm, geo_of(s), x, nrhs, r, 1.0, -1.0, true, s->stream));
+  s->launches += 5 + 2 * s->fmm.nlevels;
+  if (s->nb > 0) {
+    const int nb = s->nb;
+    for (int c = 0; c < nrhs; ++c) {
+      launch_gemv_sub(r + (size_t)D * c, s->U0.p, xa + (size_t)nb * c, D, nb, s->stream);
+      masked_cross<double>(s->PsiT0.p, D, nb, x + (size_t)D * c, D, 1, s->ones_mask.p, D,
+                           g + (size_t)nb * c, nb, s->stream);
+      launch_axpby(rg + (size_t)nb * c, g + (size_t)nb * c, -1.0, 1.0, nb, s->stream);
+      launch_axpby(rg + (size_t)nb * c, xa + (size_t)nb * c, 1.0, 1.0, nb, s->stream);
+      s->launches += 4;
     }
   }
   CU(cudaGetLastError());
@@ -1004,7 +1045,7 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   CU(F.tmp.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
   CU(s->r64.ensure(nd));
   CU(s->acc64.ensure(std::max<size_t>(2 * (size_t)nb * nrhs, 1)));
-  CU(s->nrm_dev.ensure(2 * (size_t)nrhs + 2));
+  CU(s->nrm_dev.ensure(65 * (size_t)nrhs + 2));  // norms + partial sums
   CU(s->h_io.ensure(4 * (size_t)nrhs + 4));
   double* rg = s->acc64.p;
   double* a64 = alpha;
@@ -1018,14 +1059,31 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   int it = 0;
   double worst = 0;
   const int max_it = std::max(1, s->cfg.refine_max_iters);
+  const bool recur = s->fmm.built;
+  if (recur) {
+    CU(s->x64.ensure(nd));
+    CU(s->xa64.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
+    CU(s->g64.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
+  }
   for (it = 0; it < max_it; ++it) {
     launch_d2f(s->r64.p, F.x.p, nd, s->stream);
     rs_status rc = apply_inverse<float>(s, F.x.p, nrhs, F.tmp.p, it == 0 || !nb ? nullptr : rg);
     if (rc != RS_OK) return rc;
-    launch_add_f2d(mu, F.x.p, nd, s->stream);
-    if (nb) launch_add_f2d(a64, F.tmp.p, (size_t)nb * nrhs, s->stream);
-    s->launches += 3;
-    rc = residual(s, f, mu, a64, nrhs, s->r64.p, rg);
+    if (recur && it > 0) {
+      launch_f2d(F.x.p, s->x64.p, nd, s->stream);
+      launch_axpby(mu, s->x64.p, 1.0, 1.0, nd, s->stream);
+      if (nb) {
+        launch_f2d(F.tmp.p, s->xa64.p, (size_t)nb * nrhs, s->stream);
+        launch_axpby(a64, s->xa64.p, 1.0, 1.0, (size_t)nb * nrhs, s->stream);
+      }
+      s->launches += 4;
+      rc = residual_update(s, s->x64.p, s->xa64.p, nrhs, s->r64.p, rg, s->g64.p);
+    } else {
+      launch_add_f2d(mu, F.x.p, nd, s->stream);
+      if (nb) launch_add_f2d(a64, F.tmp.p, (size_t)nb * nrhs, s->stream);
+      s->launches += 3;
+      rc = residual(s, f, mu, a64, nrhs, s->r64.p, rg);
+    }
     if (rc != RS_OK) return rc;
     launch_col_norms(s->r64.p, D, nrhs, s->nrm_dev.p, s->stream);
     CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
@@ -1174,9 +1232,8 @@ rs_status rs_factor(rs_solver* s) {
   rc = upload_geometry(s);
   if (rc != RS_OK) return rc;
   if (s->fp32 && s->cfg.pde == kLaplace && !s->fmm.built) {
-    const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : 40;
-    if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, s->stream))
-      return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
+    rc = build_fmm(s);
+    if (rc != RS_OK) return rc;
   }
   double t0 = now_ms();
   CU(cudaEventRecord(s->ev_f0, s->stream));
@@ -1300,8 +1357,9 @@ rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y) {
   return RS_OK;
 }
 
-rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y) {
-  if (!s || !x || !y || nrhs < 1) return fail(s, RS_ERR_ARG, "bad matvec arguments");
+rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int fp32) {
+  if (!s || !x || !y || nrhs < 1 || fp32 < 0 || fp32 > 1)
+    return fail(s, RS_ERR_ARG, "bad matvec arguments");
   if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
   if (s->cfg.pde != kLaplace) return rs_matvec(s, x, nrhs, y);
   rs_status rc = ensure_device(s);
@@ -1313,16 +1371,15 @@ rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y) {
     if (rc != RS_OK) return rc;
   }
   if (!s->fmm.built) {
-    const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : 40;
-    if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, s->stream))
-      return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
+    rc = build_fmm(s);
+    if (rc != RS_OK) return rc;
   }
   const size_t nd = (size_t)s->D * nrhs;
   DevBuf<double> dx, dy;
   CU(dx.ensure(nd));
   CU(dy.ensure(nd));
   CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
-  CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, s->stream));
+  CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, fp32 == 1, s->stream));
   CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   return RS_OK;
@@ -1408,6 +1465,9 @@ rs_status rs_get_stats(const rs_solver* s, rs_stats* out) {
   if (!s || !out) return RS_ERR_ARG;
   *out = s->stats;
   out->kernel_launches = s->launches;
+  out->host_plan_ms = s->host_plan_ms;
+  out->host_wait_ms = s->host_wait_ms;
+  out->host_post_ms = s->host_post_ms;
   return RS_OK;
 }
 

@@ -52,7 +52,8 @@ class RsStats(ctypes.Structure):
                 ("decouple_flops", ctypes.c_double), ("solve_bytes", ctypes.c_double),
                 ("id_ms", ctypes.c_double), ("decouple_ms", ctypes.c_double),
                 ("refine_iters", ctypes.c_int), ("refine_residual", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int)]
+                ("kernel_launches", ctypes.c_int), ("host_plan_ms", ctypes.c_double),
+                ("host_wait_ms", ctypes.c_double), ("host_post_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -82,7 +83,7 @@ def lib():
         L.rs_solve_device.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp]
         L.rs_kernel_block.argtypes = [_vp, _ip, ctypes.c_int, _ip, ctypes.c_int, _dp]
         L.rs_matvec.argtypes = [_vp, _dp, ctypes.c_int, _dp]
-        L.rs_matvec_fast.argtypes = [_vp, _dp, ctypes.c_int, _dp]
+        L.rs_matvec_fast.argtypes = [_vp, _dp, ctypes.c_int, _dp, ctypes.c_int]
         L.rs_id_batched.argtypes = [_vp, ctypes.c_int, _dp, _lp, _ip, _ip, ctypes.c_double, _ip,
                                     _ip, _lp, _dp, _lp]
         L.rs_id_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double, _vp, _vp, _vp,
@@ -209,14 +210,16 @@ class Solver:
         self._check(lib().rs_kernel_block(self.h, _i(I), I.size, _i(J), J.size, _d(out)))
         return out
 
-    def matvec(self, x, fast=False):
+    def matvec(self, x, fast=False, fp32=False):
         x = np.asfortranarray(x, dtype=np.float64)
         sq = x.ndim == 1
         if sq:
             x = x[:, None]
         y = np.zeros_like(x, order="F")
-        fn = lib().rs_matvec_fast if fast else lib().rs_matvec
-        self._check(fn(self.h, _d(x), x.shape[1], _d(y)))
+        if fast:
+            self._check(lib().rs_matvec_fast(self.h, _d(x), x.shape[1], _d(y), int(fp32)))
+        else:
+            self._check(lib().rs_matvec(self.h, _d(x), x.shape[1], _d(y)))
         return y[:, 0] if sq else y
 
     def stats(self):

@@ -59,8 +59,8 @@ typedef struct {
   double fp32_id_tol;        /* RS_FP32_REFINE: ID tolerance of the FP32 factor
                                 (at least id_tol; FP32 cannot resolve below ~1e-6) */
   int device;                /* CUDA device ordinal */
-  int fmm_order;             /* RS_FP32_REFINE: multipole order of the FP64
-                                residual (0 = automatic) */
+  int fmm_order;             /* RS_FP32_REFINE, Laplace: multipole order of the
+                                FP64 residual, 2..64 (0 = automatic: 32) */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
@@ -112,11 +112,13 @@ rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int 
  * inverse the factorization represents.  x, y: (num_points*sd) x nrhs. */
 rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
 
-/* y = K x through the FP64 fast multipole method used for the refinement
- * residual (Laplace); falls back to rs_matvec for other kernels.  No
+/* y = K x through the fast multipole method used by the refinement (Laplace);
+ * falls back to rs_matvec for other kernels.  fp32 = 0: the FP64 variant of
+ * the full residual (order rs_config.fmm_order); fp32 = 1: the FP32 variant
+ * used for products with refinement corrections (~1e-7 relative).  No
  * reference counterpart: the reference applies K only densely in its tests
  * (ie_solver_test.cpp:87-95). */
-rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y);
+rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int fp32);
 
 /* ie_Mat::id (ie_mat.cpp:548-588) for a batch of matrices on the GPU.
  * mats: concatenated column-major m_i x n_i blocks (offsets a_off, in
@@ -158,6 +160,9 @@ typedef struct {
   int refine_iters;                            /* iterations of last solve */
   double refine_residual;                      /* final relative residual */
   int kernel_launches;                         /* kernels launched by last factor+solve */
+  double host_plan_ms, host_wait_ms, host_post_ms; /* last factor: host list building and
+                                                      launches, waiting for ranks, and
+                                                      bookkeeping after them */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 

@@ -182,3 +182,9 @@ def test_fp32_refined_matches_fp64_oracle(name, solver_lib, oracle_lib):
     rel = np.linalg.norm(mu - mo) / np.linalg.norm(mo)
     assert rel <= max(1e-8, 10 * tol), (rel, st["refine_iters"], st["refine_residual"])
     assert st["refine_residual"] <= 1e-12
+    if geo.num_holes == 0:
+        # the true residual against the dense FP64 operator (the refinement's
+        # own residual is a recurrence for Laplace)
+        f = np.asarray(d["rhs"]).reshape(np.shape(mu), order="F")
+        r = f - s.matvec(mu)
+        assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm(f)
