@@ -1056,6 +1056,8 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   std::vector<double> fn(s->h_io.p, s->h_io.p + nrhs);
+  s->stats.residual64_ms = 0;
+  s->stats.residual32_ms = 0;
   int it = 0;
   double worst = 0;
   const int max_it = std::max(1, s->cfg.refine_max_iters);
@@ -1069,7 +1071,9 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
     launch_d2f(s->r64.p, F.x.p, nd, s->stream);
     rs_status rc = apply_inverse<float>(s, F.x.p, nrhs, F.tmp.p, it == 0 || !nb ? nullptr : rg);
     if (rc != RS_OK) return rc;
-    if (recur && it > 0) {
+    CU(cudaEventRecord(s->ev_a, s->stream));
+    const bool upd = recur && it > 0;
+    if (upd) {
       launch_f2d(F.x.p, s->x64.p, nd, s->stream);
       launch_axpby(mu, s->x64.p, 1.0, 1.0, nd, s->stream);
       if (nb) {
@@ -1085,9 +1089,13 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
       rc = residual(s, f, mu, a64, nrhs, s->r64.p, rg);
     }
     if (rc != RS_OK) return rc;
+    CU(cudaEventRecord(s->ev_b, s->stream));
     launch_col_norms(s->r64.p, D, nrhs, s->nrm_dev.p, s->stream);
     CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
     CU(cudaStreamSynchronize(s->stream));
+    float ms_res = 0;
+    CU(cudaEventElapsedTime(&ms_res, s->ev_a, s->ev_b));
+    (upd ? s->stats.residual32_ms : s->stats.residual64_ms) += ms_res;
     worst = 0;
     for (int c = 0; c < nrhs; ++c) {
       double rel = fn[c] > 0 ? s->h_io.p[c] / fn[c] : s->h_io.p[c];
@@ -1468,6 +1476,8 @@ rs_status rs_get_stats(const rs_solver* s, rs_stats* out) {
   out->host_plan_ms = s->host_plan_ms;
   out->host_wait_ms = s->host_wait_ms;
   out->host_post_ms = s->host_post_ms;
+  out->residual64_ms = s->stats.residual64_ms;
+  out->residual32_ms = s->stats.residual32_ms;
   return RS_OK;
 }
 

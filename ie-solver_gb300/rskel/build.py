@@ -3,6 +3,8 @@
 Compiles every translation unit in ``csrc/`` in parallel and links
 ``lib/librskel.so`` in-tree.  Host C++ is compiled with floating-point
 contraction disabled so the quadtree is identical on x86-64 and aarch64.
+Also links ``lib/libfmapeak.so`` (``csrc/fma_peak.cu``), the CUDA-core FMA
+peak measurement the benchmark uses as its roofline denominator.
 """
 from __future__ import annotations
 
@@ -16,6 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "librskel.so")
+PEAK_LIB = os.path.join(LIB_DIR, "libfmapeak.so")
 ROOT = os.path.dirname(PKG)
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -80,6 +83,13 @@ def build(verbose=False, force=False):
             warn = f.result()
             if verbose and warn:
                 print(warn)
+    peak_src = os.path.join(CSRC, "fma_peak.cu")
+    if force or _stale(PEAK_LIB, [peak_src]):
+        cmd = [_nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", peak_src,
+               "-o", PEAK_LIB, "-lcudart"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"fma_peak build failed\n{res.stdout}\n{res.stderr}")
     if force or jobs or _stale(LIB, objs):
         cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lgomp", "-Xlinker", "--no-undefined"]
         if verbose:

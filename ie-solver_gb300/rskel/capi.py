@@ -53,7 +53,8 @@ class RsStats(ctypes.Structure):
                 ("id_ms", ctypes.c_double), ("decouple_ms", ctypes.c_double),
                 ("refine_iters", ctypes.c_int), ("refine_residual", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int), ("host_plan_ms", ctypes.c_double),
-                ("host_wait_ms", ctypes.c_double), ("host_post_ms", ctypes.c_double)]
+                ("host_wait_ms", ctypes.c_double), ("host_post_ms", ctypes.c_double),
+                ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -151,11 +152,16 @@ class Solver:
         h = _vp()
         self._check(lib().rs_create(ctypes.byref(self.cfg), ctypes.byref(h)), None)
         self.h = h
+        self.pde = pde
+        self.set_geometry(geo)
+
+    def set_geometry(self, geo):
+        """rs_set_geometry: a new boundary for this handle (tree and factors reset)."""
         self.n = geo.n
         self.D = geo.n * self.sd
         self.nh = geo.num_holes
-        self.nb = 0 if geo.num_holes == 0 or pde == RS_LAPLACE_NEUMANN else (
-            3 * geo.num_holes if pde == RS_STOKES else geo.num_holes)
+        self.nb = 0 if geo.num_holes == 0 or self.pde == RS_LAPLACE_NEUMANN else (
+            3 * geo.num_holes if self.pde == RS_STOKES else geo.num_holes)
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in
                 (geo.points, geo.normals, geo.weights, geo.curvatures)]
         hc = np.ascontiguousarray(geo.hole_centers if geo.num_holes else np.zeros(2))

@@ -163,6 +163,9 @@ typedef struct {
   double host_plan_ms, host_wait_ms, host_post_ms; /* last factor: host list building and
                                                       launches, waiting for ranks, and
                                                       bookkeeping after them */
+  double residual64_ms, residual32_ms;         /* last RS_FP32_REFINE solve: CUDA-event time of
+                                                  the FP64 residual products and of the FP32
+                                                  correction products */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 
