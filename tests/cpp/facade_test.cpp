@@ -1,0 +1,202 @@
+// Drives the C++ facade (include/ie_solver_gb300.hpp) the way the
+// reference's own test drives its solver (ie_solver_test.cpp:29-96,
+// check_solve_err): build the tree, skeletonize, linear_solve, and check the
+// backward error against the dense operator assembled through Kernel and,
+// with holes, initialize_U_mat / initialize_Psi_mat: max |K mu - f| <= 50 tol.
+//
+//   facade_test            all cases (needs a GPU)
+//   facade_test --host     host-only checks: tree construction and mirroring,
+//                          ie_Mat arithmetic, and the error a factorization
+//                          reports without a GPU.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ie_solver_gb300.hpp"
+
+using namespace ie_solver;
+
+static int g_fail = 0;
+#define EXPECT(cond)                                                   \
+  do {                                                                 \
+    if (!(cond)) {                                                     \
+      std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #cond);    \
+      ++g_fail;                                                        \
+    }                                                                  \
+  } while (0)
+
+// A circle of n nodes; `outward` false turns the normals inwards (a hole's
+// boundary seen from the domain outside it).
+static void add_circle(Boundary* b, int n, double cx, double cy, double r, bool outward) {
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    const double t = 2.0 * pi * i / n;
+    const double c = std::cos(t), s = std::sin(t);
+    b->points.push_back(cx + r * c);
+    b->points.push_back(cy + r * s);
+    b->normals.push_back(outward ? c : -c);
+    b->normals.push_back(outward ? s : -s);
+    b->weights.push_back(2.0 * pi * r / n);
+    b->curvatures.push_back(outward ? 1.0 / r : -1.0 / r);
+  }
+}
+
+// Data: a harmonic function (Laplace) or a Stokeslet's velocity (Stokes)
+// from a source at (2, 0.5), outside the domain.
+static void set_values(Boundary* b, bool stokes) {
+  const int n = (int)b->weights.size();
+  b->boundary_values = ie_Mat(stokes ? 2 * n : n, 1);
+  for (int i = 0; i < n; ++i) {
+    const double rx = b->points[2 * i] - 2.0, ry = b->points[2 * i + 1] - 0.5;
+    const double r2 = rx * rx + ry * ry;
+    if (!stokes) {
+      b->boundary_values.set(i, 0, 0.5 * std::log(r2));
+    } else {
+      b->boundary_values.set(2 * i, 0, -0.5 * std::log(r2) + rx * rx / r2);
+      b->boundary_values.set(2 * i + 1, 0, rx * ry / r2);
+    }
+  }
+}
+
+// ie_solver_test.cpp:29-96
+static void check_solve_err(const ie_solver_config& config, Boundary* boundary) {
+  QuadTree quadtree;
+  quadtree.set_gb300_options(config.max_leaf_dofs, config.num_proxy_points);
+  quadtree.initialize_tree(boundary, std::vector<double>(), config.solution_dimension,
+                           config.domain_dimension);
+  SkelFactorization skel_factorization(config.id_tol, config.is_strong_admissibility,
+                                       config.num_threads);
+  skel_factorization.precision = config.precision;
+  Kernel kernel(config.solution_dimension, config.domain_dimension, config.pde, boundary,
+                std::vector<double>());
+  std::vector<int> all_dofs;
+  for (int i = 0; i < config.solution_dimension * (int)boundary->weights.size(); ++i)
+    all_dofs.push_back(i);
+  if (!boundary->holes.empty()) {
+    ie_Mat U = initialize_U_mat(config.pde, boundary->holes, boundary->points);
+    ie_Mat Psi = initialize_Psi_mat(config.pde, boundary->holes, boundary);
+    quadtree.U = U;
+    quadtree.Psi = Psi;
+    skel_factorization.skeletonize(kernel, &quadtree);
+    ie_Mat mu, alpha(U.width(), 1);
+    linear_solve(skel_factorization, quadtree, boundary->boundary_values, &mu, &alpha);
+    ie_Mat stacked(mu.height() + alpha.height(), 1);
+    stacked.set_submatrix(0, mu.height(), 0, 1, mu);
+    stacked.set_submatrix(mu.height(), stacked.height(), 0, 1, alpha);
+    const int D = (int)all_dofs.size(), added = U.width();
+    ie_Mat dense(D + added, D + added), ident;
+    ident.eye(added);
+    dense.set_submatrix(0, D, 0, D, kernel(all_dofs, all_dofs));
+    dense.set_submatrix(0, D, D, D + added, U);
+    dense.set_submatrix(D, D + added, 0, D, Psi);
+    dense.set_submatrix(D, D + added, D, D + added, -ident);
+    ie_Mat out = dense * stacked;
+    const double e1 = (out(0, D, 0, 1) - boundary->boundary_values).max_entry_magnitude();
+    const double e2 = out(D, D + added, 0, 1).max_entry_magnitude();
+    std::printf("  holes %zu: backward error %.3e / %.3e (bound %.1e)\n", boundary->holes.size(),
+                e1, e2, 50 * config.id_tol);
+    EXPECT(e1 <= 50 * config.id_tol && e2 <= 50 * config.id_tol);
+  } else {
+    skel_factorization.skeletonize(kernel, &quadtree);
+    ie_Mat mu;
+    linear_solve(skel_factorization, quadtree, boundary->boundary_values, &mu);
+    const double e = (kernel(all_dofs, all_dofs) * mu - boundary->boundary_values).max_entry_magnitude();
+    std::printf("  backward error %.3e (bound %.1e)\n", e, 50 * config.id_tol);
+    EXPECT(e <= 50 * config.id_tol);
+  }
+}
+
+static void host_checks() {
+  // ie_Mat arithmetic
+  ie_Mat a(3, 2), b(2, 3);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 2; ++j) {
+      a.set(i, j, i + 10 * j);
+      b.set(j, i, 1.0 + i - j);
+    }
+  ie_Mat c = a * b;
+  EXPECT(c.height() == 3 && c.width() == 3);
+  EXPECT(c.get(2, 1) == a.get(2, 0) * b.get(0, 1) + a.get(2, 1) * b.get(1, 1));
+  ie_Mat t = a.transpose();
+  EXPECT(t.get(1, 2) == a.get(2, 1));
+  ie_Mat sub = a({2, 0}, {1});
+  EXPECT(sub.height() == 2 && sub.get(0, 0) == a.get(2, 1) && sub.get(1, 0) == a.get(0, 1));
+  ie_Mat z(3, 2);
+  z.set_submatrix(0, 3, 0, 2, a);
+  EXPECT((z - a).max_entry_magnitude() == 0.0);
+  // tree construction and the host mirror (no GPU needed)
+  Boundary circle;
+  add_circle(&circle, 4096, 0.0, 0.0, 1.0, true);
+  QuadTree tree;
+  tree.set_gb300_options(64, 64);
+  tree.initialize_tree(&circle, std::vector<double>(), 1, 2);
+  EXPECT(tree.root != nullptr && tree.levels.size() >= 5);
+  size_t leaf_dofs = 0;
+  for (QuadTreeLevel* l : tree.levels)
+    for (QuadTreeNode* nd : l->nodes) {
+      if (nd->is_leaf) leaf_dofs += nd->src_dof_lists.original_box.size();
+      for (int c = 0; c < 4 && !nd->is_leaf; ++c) EXPECT(nd->children[c]->parent == nd);
+    }
+  EXPECT(leaf_dofs == 4096);
+  EXPECT(tree.boundary != &circle && tree.boundary->weights.size() == 4096);
+}
+
+int main(int argc, char** argv) {
+  const bool host_only = argc > 1 && std::strcmp(argv[1], "--host") == 0;
+  host_checks();
+  if (host_only) {
+    // without a GPU the factorization reports it instead of falling back
+    Boundary circle;
+    add_circle(&circle, 512, 0.0, 0.0, 1.0, true);
+    set_values(&circle, false);
+    QuadTree tree;
+    tree.initialize_tree(&circle, std::vector<double>(), 1, 2);
+    SkelFactorization sf(1e-8, false, 1);
+    Kernel k(1, 2, ie_solver_config::LAPLACE, &circle, std::vector<double>());
+    bool threw = false;
+    try {
+      sf.skeletonize(k, &tree);
+    } catch (const rs_error& e) {
+      threw = e.code == RS_ERR_NO_DEVICE;
+    }
+    EXPECT(threw);
+  } else {
+    struct Case {
+      const char* name;
+      ie_solver_config::Pde pde;
+      int n;
+      bool hole;
+      rs_precision prec;
+    };
+    const Case cases[] = {{"laplace circle", ie_solver_config::LAPLACE, 1024, false, RS_FP64},
+                          {"stokes circle", ie_solver_config::STOKES, 512, false, RS_FP64},
+                          {"laplace annulus", ie_solver_config::LAPLACE, 1024, true, RS_FP64},
+                          {"stokes annulus", ie_solver_config::STOKES, 512, true, RS_FP64},
+                          {"laplace circle, FP32 + refinement", ie_solver_config::LAPLACE, 1024,
+                           false, RS_FP32_REFINE}};
+    for (const Case& cs : cases) {
+      std::printf("%s\n", cs.name);
+      ie_solver_config config;
+      config.pde = cs.pde;
+      config.solution_dimension = cs.pde == ie_solver_config::STOKES ? 2 : 1;
+      config.id_tol = 1e-8;
+      config.precision = cs.prec;
+      Boundary b;
+      add_circle(&b, cs.n, 0.0, 0.0, 1.0, true);
+      if (cs.hole) {
+        add_circle(&b, cs.n / 2, 0.2, -0.1, 0.3, false);
+        Hole h;
+        h.center = Vec2(0.2, -0.1);
+        h.radius = 0.3;
+        h.num_nodes = cs.n / 2;
+        b.holes.push_back(h);
+      }
+      set_values(&b, cs.pde == ie_solver_config::STOKES);
+      check_solve_err(config, &b);
+    }
+  }
+  std::printf(g_fail ? "%d FAILED\n" : "all passed\n", g_fail);
+  return g_fail ? 1 : 0;
+}
