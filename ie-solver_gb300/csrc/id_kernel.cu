@@ -553,7 +553,30 @@ size_t id_sketch_smem(int n) {
   return b;
 }
 
-template <int TS>
+// Leading dimension of a sketch held by one warp: n rounded up to 1 mod 32,
+// so that a column walk (fixed column, rows across lanes) and a row walk
+// (fixed row, columns across lanes) are both free of bank conflicts.
+__host__ __device__ inline int warp_ld(int n) { return n + (33 - n % 32) % 32; }
+
+size_t id_sketch_y_size(int n) { return (size_t)sketch_rows(n) * warp_ld(n); }
+
+// Shared memory of the sketch-only variant (no Y tile, no QR workspace).
+size_t id_sketch_split_smem(int n) {
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const int ld = layout_ld(n, team_size(n));
+  const int lp = (sketch_rows(n) + 3) & ~3;
+  size_t b = 0;
+  b += al(sizeof(float) * (size_t)kChunk * ld);   // C
+  b += al(sizeof(float) * (size_t)kChunk * lp);   // signs
+  b += dofs_bytes<float>(n) + dofs_bytes<float>(kChunk);
+  b += al(sizeof(int) * kChunk);
+  return b;
+}
+
+// kSplit = false: sketch, pivoted QR and Z in one CTA per box.
+// kSplit = true: the sketch only, written to p.sketch_y (row major, leading
+// dimension warp_ld(n)) for id_cpqr_warp_kernel.
+template <int TS, bool kSplit>
 __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   using Real = float;
   const IdTask t = p.tasks[blockIdx.x];
@@ -565,19 +588,28 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
   IdShared<Real> S;
-  S.R = carve<Real>(sp, ell * ld);  // holds the sketch Y (or A itself when m <= ell)
-  S.C = carve<Real>(sp, kChunk * ld);
-  Real* sg = carve<Real>(sp, kChunk * lp);
-  S.v = carve<Real>(sp, 3 * (ell > kChunk ? ell : kChunk) + 3 * 32 * 32);
-  S.vn1 = carve<double>(sp, n);
-  S.vn2 = carve<double>(sp, n);
-  S.perm = carve<int>(sp, n);
-  S.scal = carve<double>(sp, 8);
-  S.rs = carve<Real>(sp, 8);
-  S.is = carve<int>(sp, 8);
+  Real* sg;
+  if constexpr (kSplit) {
+    S.R = nullptr;
+    S.C = carve<Real>(sp, kChunk * ld);
+    sg = carve<Real>(sp, kChunk * lp);
+  } else {
+    S.R = carve<Real>(sp, ell * ld);  // holds the sketch Y (or A itself when m <= ell)
+    S.C = carve<Real>(sp, kChunk * ld);
+    sg = carve<Real>(sp, kChunk * lp);
+    S.v = carve<Real>(sp, 3 * (ell > kChunk ? ell : kChunk) + 3 * 32 * 32);
+    S.vn1 = carve<double>(sp, n);
+    S.vn2 = carve<double>(sp, n);
+    S.perm = carve<int>(sp, n);
+    S.scal = carve<double>(sp, 8);
+    S.rs = carve<Real>(sp, 8);
+    S.is = carve<int>(sp, 8);
+  }
   S.act = carve_dofs<Real>(sp, n);
   S.row = carve_dofs<Real>(sp, kChunk);
   S.kind = carve<int>(sp, kChunk);
+  const int wld = warp_ld(n);
+  Real* Yg = kSplit ? p.sketch_y + t.y_off : nullptr;
 
   const double ox = t.cx, oy = t.cy;
   for (int j = threadIdx.x; j < n; j += blockDim.x)
@@ -595,7 +627,8 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
       fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
       for (int e = threadIdx.x; e < cnt * n; e += blockDim.x) {
         const int i = e / n, j = e % n;
-        S.R[(size_t)(c0 + i) * ld + j] = S.C[(size_t)i * ld + j];
+        if constexpr (kSplit) Yg[(size_t)(c0 + i) * wld + j] = S.C[(size_t)i * ld + j];
+        else S.R[(size_t)(c0 + i) * ld + j] = S.C[(size_t)i * ld + j];
       }
       __syncthreads();
     }
@@ -648,10 +681,18 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
         const int r = r0 + e / 4, c = cc0 + e % 4;
-        if (r < ell && c < n) S.R[(size_t)r * ld + c] = acc[q][e];
+        if (r < ell && c < n) {
+          if constexpr (kSplit) Yg[(size_t)r * wld + c] = acc[q][e];
+          else S.R[(size_t)r * ld + c] = acc[q][e];
+        }
       }
     }
     __syncthreads();
+  }
+  if constexpr (kSplit) {
+    (void)clk_fill;
+    (void)clk_fold;
+    return;
   }
   clk0 = clock64();
   const int k = mr > 0 ? cpqr_rank<Real, TS>(n, mr, p.tol, L, S) : 0;
@@ -688,6 +729,171 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Second half of the split FP32 ID: one warp per box runs the column-pivoted
+// QR of the box's sketch (rows mr = min(m, ell)) held in its own slice of
+// shared memory, with no block-wide barrier: each lane owns the columns
+// lane + 32 c (c < CPL) for the reflector updates and norm downdates, the
+// pivot search and reflector norm are warp reductions.  Same rank rule,
+// pivot order (first maximal partial norm) and norm downdating as
+// cpqr_rank; then Z = R11^{-1} R12 by lane-local back substitution.
+// ---------------------------------------------------------------------------
+size_t id_cpqr_warp_bytes(int n) {
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const int ell = sketch_rows(n);
+  return al(sizeof(float) * (size_t)ell * warp_ld(n)) + al(sizeof(float) * ell) +
+         2 * al(sizeof(float) * n) + al(sizeof(int) * n);
+}
+
+template <int CPL>
+__global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int num_tasks,
+                                                                 int wbytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (ti >= num_tasks) return;  // warp-uniform; nothing below synchronises the block
+  const IdTask t = p.tasks[ti];
+  const int n = t.n;
+  const int ld = warp_ld(n);
+  const int ell = sketch_rows(n);
+  const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
+  const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+  const int mr = m <= ell ? m : ell;
+  unsigned char* sp = smem + (size_t)warp * wbytes;
+  float* A = carve<float>(sp, ell * ld);
+  float* v = carve<float>(sp, ell);
+  float* vn1 = carve<float>(sp, n);
+  float* vn2 = carve<float>(sp, n);
+  int* perm = carve<int>(sp, n);
+  const float* Y = p.sketch_y + t.y_off;
+  for (int e = lane; e < mr * ld; e += 32) A[e] = Y[e];
+  for (int j = lane; j < n; j += 32) perm[j] = j;
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    const int j = lane + 32 * c;
+    if (j < n) {
+      float s = 0.f;
+      for (int r = 0; r < mr; ++r) { const float a = A[(size_t)r * ld + j]; s += a * a; }
+      vn1[j] = sqrtf(s);
+      vn2[j] = vn1[j];
+    }
+  }
+  __syncwarp();
+  const float tol3z = 2.44140625e-4f;
+  const int kmax = n < mr ? n : mr;
+  int k = 0;
+  double thr = 0.0;
+  for (int i = 0; i < kmax; ++i) {
+    // pivot: first index of the largest partial norm
+    float best = -1.f;
+    int bi = n;
+    for (int j = i + lane; j < n; j += 32) {
+      const float val = vn1[j];
+      if (val > best) { best = val; bi = j; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (bi != i) {
+      for (int r = lane; r < mr; r += 32) {
+        const float a = A[(size_t)r * ld + bi];
+        A[(size_t)r * ld + bi] = A[(size_t)r * ld + i];
+        A[(size_t)r * ld + i] = a;
+      }
+      if (lane == 0) {
+        const int tp = perm[bi];
+        perm[bi] = perm[i];
+        perm[i] = tp;
+        vn1[bi] = vn1[i];
+        vn2[bi] = vn2[i];
+      }
+      __syncwarp();
+    }
+    // Householder reflector of column i (rows i..mr-1); |R_ii| sets the rank
+    double xs = 0.0;
+    for (int r = i + 1 + lane; r < mr; r += 32) {
+      const double a = (double)A[(size_t)r * ld + i];
+      xs += a * a;
+    }
+    xs = warp_sum(xs);
+    const double alpha = (double)A[(size_t)i * ld + i];
+    const double nrm = sqrt(alpha * alpha + xs);
+    if (i == 0) thr = fabs(p.tol * nrm);
+    else if (nrm < thr) { k = i; break; }
+    float tau = 0.f, scale = 0.f, beta = 0.f;
+    if (xs > 0.0) {
+      const float a = (float)alpha;
+      beta = -copysignf((float)nrm, a);
+      tau = (beta - a) / beta;
+      scale = 1.f / (a - beta);
+    }
+    for (int r = i + 1 + lane; r < mr; r += 32) v[r] = A[(size_t)r * ld + i] * scale;
+    __syncwarp();
+    if (lane == 0 && xs > 0.0) A[(size_t)i * ld + i] = beta;
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int j = lane + 32 * c;
+      if (j > i && j < n) {
+        float aij = A[(size_t)i * ld + j];
+        if (tau != 0.f) {
+          float w0 = aij, w1 = 0.f, w2 = 0.f, w3 = 0.f;
+          int r = i + 1;
+          for (; r + 3 < mr; r += 4) {
+            w0 += v[r] * A[(size_t)r * ld + j];
+            w1 += v[r + 1] * A[(size_t)(r + 1) * ld + j];
+            w2 += v[r + 2] * A[(size_t)(r + 2) * ld + j];
+            w3 += v[r + 3] * A[(size_t)(r + 3) * ld + j];
+          }
+          for (; r < mr; ++r) w0 += v[r] * A[(size_t)r * ld + j];
+          const float tw = tau * ((w0 + w1) + (w2 + w3));
+          for (int q = i + 1; q < mr; ++q) A[(size_t)q * ld + j] -= tw * v[q];
+          aij -= tw;
+        }
+        // partial norm downdate (dlaqp2), recomputed when it loses accuracy
+        const float v1 = vn1[j];
+        if (v1 != 0.f) {
+          const float v2 = vn2[j];
+          float x = v1 * v1 - aij * aij;
+          x = x < 0.f ? 0.f : x;
+          if (x <= tol3z * v2 * v2) {
+            float s2 = 0.f;
+            for (int q = i + 1; q < mr; ++q) { const float a = A[(size_t)q * ld + j]; s2 += a * a; }
+            vn1[j] = sqrtf(s2);
+            vn2[j] = vn1[j];
+          } else {
+            vn1[j] = sqrtf(x);
+          }
+        }
+        A[(size_t)i * ld + j] = aij;
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0) p.ranks[t.slot] = k;
+  for (int j = lane; j < n; j += 32) p.perm[t.act_off + j] = perm[j];
+  if (k > 0) {
+    // Z = R11^{-1} R12, one lane per column of R12
+    const int r = n - k;
+    float* T = reinterpret_cast<float*>(p.fac) + t.fac_off + fac_T(k, r);
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int col = lane + 32 * c;
+      if (col >= k && col < n) {
+        for (int row = k - 1; row >= 0; --row) {
+          const float z = A[(size_t)row * ld + col] / A[(size_t)row * ld + row];
+          A[(size_t)row * ld + col] = z;
+          for (int q = 0; q < row; ++q) A[(size_t)q * ld + col] -= z * A[(size_t)q * ld + row];
+        }
+        for (int row = 0; row < k; ++row) T[row + (size_t)k * (col - k)] = A[(size_t)row * ld + col];
+      }
+    }
+  }
+}
+
 template <class Real, int TS>
 static void launch_id_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
   set_smem_once<id_kernel<Real, TS>>();
@@ -696,19 +902,47 @@ static void launch_id_t(const IdParams& p, int num_tasks, size_t smem, cudaStrea
 
 template <int TS>
 static void launch_sketch_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
-  set_smem_once<id_sketch_kernel<TS>>();
-  id_sketch_kernel<TS><<<num_tasks, kThreads, smem, st>>>(p);
+  set_smem_once<id_sketch_kernel<TS, false>>();
+  id_sketch_kernel<TS, false><<<num_tasks, kThreads, smem, st>>>(p);
+}
+
+// Split FP32 ID: the sketch (one CTA per box), then the warp-per-box QR.
+template <int TS>
+static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
+  set_smem_once<id_sketch_kernel<TS, true>>();
+  id_sketch_kernel<TS, true><<<num_tasks, kThreads, id_sketch_split_smem(nmax), st>>>(p);
+  const int wbytes = (int)id_cpqr_warp_bytes(nmax);
+  int wpc = (int)((size_t)kSmemOptIn / wbytes);
+  wpc = wpc < 1 ? 1 : wpc > kWarps ? kWarps : wpc;
+  const int grid = (num_tasks + wpc - 1) / wpc;
+  if (nmax <= 64) {
+    set_smem_once<id_cpqr_warp_kernel<2>>();
+    id_cpqr_warp_kernel<2><<<grid, 32 * wpc, (size_t)wbytes * wpc, st>>>(p, num_tasks, wbytes);
+  } else {
+    set_smem_once<id_cpqr_warp_kernel<4>>();
+    id_cpqr_warp_kernel<4><<<grid, 32 * wpc, (size_t)wbytes * wpc, st>>>(p, num_tasks, wbytes);
+  }
 }
 
 bool id_sketch_ok(int nmax) {
   return nmax <= 128 && id_sketch_smem(nmax) <= 227 * 1024;
 }
 
+constexpr int kSplitMinTasks = 512;
+
 // All tasks of one launch use the team size of its largest box.
 void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
                cudaStream_t st) {
   if (num_tasks <= 0) return;
   const int ts = team_size(nmax);
+  // The warp-per-box QR pays off when a level has boxes enough to fill the
+  // GPU; small levels keep the lower-latency CTA-per-box QR.
+  if (fp32 && p.dense == nullptr && id_sketch_ok(nmax) && p.sketch_y != nullptr &&
+      num_tasks >= kSplitMinTasks) {
+    if (ts == 4) launch_split_t<4>(p, num_tasks, nmax, st);
+    else launch_split_t<2>(p, num_tasks, nmax, st);
+    return;
+  }
   if (fp32 && p.dense == nullptr && id_sketch_ok(nmax)) {
     const size_t sm = id_sketch_smem(nmax);
     if (ts == 4) launch_sketch_t<4>(p, num_tasks, sm, st);

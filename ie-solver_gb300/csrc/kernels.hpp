@@ -25,6 +25,7 @@ struct IdParams {
   const double* dense;  // matrices for rs_id_batched (column major)
   long long* phase_clk; // optional: per-task cycle counts {fill, fold, cpqr, z} (trace mode)
   int direct;           // 1: pivoted QR on the whole matrix in the task's global tile
+  float* sketch_y;      // FP32 randomized ID in two kernels: sketch, then warp-per-box QR
 };
 
 struct DecoupleParams {
@@ -67,6 +68,8 @@ size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);
 size_t id_direct_tile(int m, int n);
 size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
 
+// Floats of sketch storage one FP32 task of n columns needs (split ID).
+size_t id_sketch_y_size(int n);
 // Shared-memory attribute set-up of the FP64 ID kernels on the current device.
 cudaError_t id_noalloc_prepare();
 void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,

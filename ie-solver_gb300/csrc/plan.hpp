@@ -40,6 +40,7 @@ struct IdTask {
   int64_t dense_off;    // >= 0: rows come from a given dense matrix (rs_id_batched)
   int m_dense;          // rows of that matrix
   int pad;
+  int64_t y_off;        // FP32 split ID: the sketch (rows x warp leading dimension) at sketch_y[y_off]
 };
 
 // One elimination (skel_factorization.cpp:77-128) or, for boxes that are not

@@ -114,6 +114,7 @@ struct rs_solver {
   HostBuf<double> h_io;
 
   FmmPlan fmm;
+  DevBuf<float> sketch_y;  // FP32 split ID: per-level sketches
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
   rs_stats stats;
@@ -483,6 +484,16 @@ rs_status factor_impl(rs_solver* s) {
         scratch_need += (size_t)(t.n + 32) * (t.n + 64) + 64;
       }
     }
+    // FP32: sketches of the split randomized ID (boxes of at most 128 columns)
+    size_t y_need = 0;
+    for (IdTask& t : idt_s) {
+      t.y_off = -1;
+      if (f32 && t.n <= 128) {
+        t.y_off = (int64_t)y_need;
+        y_need += id_sketch_y_size(t.n);
+      }
+    }
+    if (y_need) CU(s->sketch_y.ensure(y_need));
     for (DecoupleTask& t : dct_s)
       if (decouple_kernel_smem(t.n, f32, true) > kSmemMax) {
         t.scratch_off = (int64_t)scratch_need;
@@ -526,6 +537,7 @@ rs_status factor_impl(rs_solver* s) {
     ip.scratch = F.scratch.p;
     ip.dense = nullptr;
     ip.direct = f32 ? 0 : 1;
+    ip.sketch_y = y_need ? s->sketch_y.p : nullptr;
     ip.phase_clk = nullptr;
     if (s->trace) {
       CU(s->clk.ensure(4 * std::max<size_t>(idt.size(), 1)));
