@@ -26,6 +26,7 @@
 #include "../../include/rskel.h"
 #include "border.hpp"
 #include "devbuf.hpp"
+#include "domain.hpp"
 #include "fmm.hpp"
 #include "kernels.hpp"
 #include "plan.hpp"
@@ -1401,6 +1402,67 @@ rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int
   CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
   CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, fp32 == 1, s->stream));
   CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+rs_status rs_domain_eval(rs_solver* s, int num_targets, const double* targets,
+                         const unsigned char* in_domain, const double* mu, const double* alpha,
+                         int nrhs, double* out) {
+  if (!s || num_targets < 0 || (num_targets > 0 && !targets) || !mu || !out || nrhs < 1)
+    return fail(s, RS_ERR_ARG, "bad domain evaluation arguments");
+  if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
+  const int nb = (s->nh > 0 && s->cfg.pde != kLaplaceNeumann)
+                     ? (s->cfg.pde == kStokes ? 3 * s->nh : s->nh) : 0;
+  if (nb > 0 && !alpha) return fail(s, RS_ERR_ARG, "holes need alpha");
+  if (num_targets == 0) return RS_OK;
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  rc = upload_geometry(s);
+  if (rc != RS_OK) return rc;
+  const int sd = s->sd, D = s->D, nt = num_targets;
+  std::vector<double> txy(2 * (size_t)nt);
+  for (int i = 0; i < nt; ++i) {
+    txy[i] = targets[2 * i];
+    txy[nt + i] = targets[2 * i + 1];
+  }
+  DevBuf<double> dt, dmu, dal, dhc, dout;
+  DevBuf<unsigned char> dmask;
+  CU(dt.ensure(2 * (size_t)nt));
+  CU(dmu.ensure((size_t)D * nrhs));
+  CU(dout.ensure((size_t)nt * sd * nrhs));
+  CU(cudaMemcpyAsync(dt.p, txy.data(), 2 * (size_t)nt * 8, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemcpyAsync(dmu.p, mu, (size_t)D * nrhs * 8, cudaMemcpyHostToDevice, s->stream));
+  if (in_domain) {
+    CU(dmask.ensure(nt));
+    CU(cudaMemcpyAsync(dmask.p, in_domain, nt, cudaMemcpyHostToDevice, s->stream));
+  }
+  if (nb > 0) {
+    CU(dal.ensure((size_t)nb * nrhs));
+    CU(dhc.ensure(2 * (size_t)s->nh));
+    CU(cudaMemcpyAsync(dal.p, alpha, (size_t)nb * nrhs * 8, cudaMemcpyHostToDevice, s->stream));
+    CU(cudaMemcpyAsync(dhc.p, s->hc.data(), 2 * (size_t)s->nh * 8, cudaMemcpyHostToDevice,
+                       s->stream));
+  }
+  DomainParams p{};
+  p.g = geo_of(s);
+  p.n = s->n;
+  p.sd = sd;
+  p.pde = s->cfg.pde;
+  p.tx = dt.p;
+  p.ty = dt.p + nt;
+  p.mask = in_domain ? dmask.p : nullptr;
+  p.nt = nt;
+  p.mu = dmu.p;
+  p.ldmu = D;
+  p.alpha = nb > 0 ? dal.p : nullptr;
+  p.ldal = nb;
+  p.hc = nb > 0 ? dhc.p : nullptr;
+  p.nh = nb > 0 ? s->nh : 0;
+  p.out = dout.p;
+  p.ldo = nt * sd;
+  CU(launch_domain_eval(p, nrhs, s->stream));
+  CU(cudaMemcpyAsync(out, dout.p, (size_t)nt * sd * nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   return RS_OK;
 }

@@ -25,7 +25,7 @@ STATUS = {0: "RS_OK", 1: "RS_ERR_ARG", 2: "RS_ERR_STATE", 3: "RS_ERR_CUDA",
 # Every function the C ABI exports (include/rskel.h).
 EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
-           "rs_matvec_fast",
+           "rs_matvec_fast", "rs_domain_eval",
            "rs_id_batched", "rs_id_noalloc", "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
            "rs_allskel", "rs_timer_start", "rs_timer_stop", "rs_synchronize", "rs_last_error"]
 
@@ -87,6 +87,8 @@ def lib():
         L.rs_matvec_fast.argtypes = [_vp, _dp, ctypes.c_int, _dp, ctypes.c_int]
         L.rs_id_batched.argtypes = [_vp, ctypes.c_int, _dp, _lp, _ip, _ip, ctypes.c_double, _ip,
                                     _ip, _lp, _dp, _lp]
+        L.rs_domain_eval.argtypes = [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_ubyte), _dp,
+                                     _dp, ctypes.c_int, _dp]
         L.rs_id_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double, _vp, _vp, _vp,
                                     _vp]
         L.rs_get_stats.argtypes = [_vp, ctypes.POINTER(RsStats)]
@@ -208,6 +210,29 @@ class Solver:
 
     def solve_device(self, f_ptr, nrhs, mu_ptr, alpha_ptr=0):
         self._check(lib().rs_solve_device(self.h, f_ptr, nrhs, mu_ptr, alpha_ptr))
+
+    def domain_eval(self, targets, mu, alpha=None, in_domain=None):
+        """rs_domain_eval: u at interleaved targets (2 nt,) from mu ((n sd) x nrhs)."""
+        t = np.ascontiguousarray(targets, dtype=np.float64)
+        mu = np.asfortranarray(mu, dtype=np.float64)
+        sq = mu.ndim == 1
+        if sq:
+            mu = mu[:, None]
+        nt = t.size // 2
+        out = np.zeros((nt * self.sd, mu.shape[1]), order="F")
+        mask = None
+        if in_domain is not None:
+            m = np.ascontiguousarray(in_domain, dtype=np.uint8)
+            mask = m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
+        al = None
+        if alpha is not None:
+            al = np.asfortranarray(alpha, dtype=np.float64)
+            if al.ndim == 1:
+                al = al[:, None]
+        self._check(lib().rs_domain_eval(self.h, nt, _d(t), mask, _d(mu),
+                                         _d(al) if al is not None else None, mu.shape[1],
+                                         _d(out)))
+        return out[:, 0] if sq else out
 
     def kernel_block(self, I, J):
         I = np.ascontiguousarray(I, dtype=np.int32)

@@ -20,8 +20,9 @@ Workloads (all seeded, no external data):
   a_k ~ U[0, 0.04], phi_k ~ U[0, 2 pi].
 * ``circle_with_ellipses(n_total, n_holes, rng)`` - outer unit circle plus
   seeded non-overlapping interior ellipses, semi-axes U[0.05, 0.15].
-* ``reference_circle(n)`` / ``reference_annulus(n)`` - the reference test
-  shapes (ie_solver/boundaries/circle.cpp:9-34, annulus.cpp:9-70).
+* ``reference_circle(n)`` / ``reference_annulus(n)`` / ``reference_donut(n)``
+  - the reference test shapes (ie_solver/boundaries/circle.cpp:9-34,
+  annulus.cpp:9-70, donut.cpp:9-52).
 """
 from __future__ import annotations
 
@@ -250,6 +251,33 @@ def reference_annulus(n: int) -> Geometry:
 # ---------------------------------------------------------------------------
 # Boundary data
 # ---------------------------------------------------------------------------
+
+def reference_donut(n: int) -> Geometry:
+    """ie_solver/boundaries/donut.cpp:9-52: unit circle around (0.5, 0.5) with
+    one concentric hole of radius 0.5 carrying n/5 nodes."""
+    t = np.arange(n) * 2.0 * math.pi / n
+    hn = n // 5
+    th = np.arange(hn) * 2.0 * math.pi / hn
+    x = np.concatenate([0.5 + np.cos(t), 0.5 + 0.5 * np.cos(th)])
+    y = np.concatenate([0.5 + np.sin(t), 0.5 + 0.5 * np.sin(th)])
+    nx = np.concatenate([np.cos(t), -np.cos(th)])
+    ny = np.concatenate([np.sin(t), -np.sin(th)])
+    p = np.empty(2 * x.shape[0])
+    p[0::2], p[1::2] = x, y
+    nr = np.empty(2 * x.shape[0])
+    nr[0::2], nr[1::2] = nx, ny
+    w = np.concatenate([np.full(n, 2 * math.pi / n), np.full(hn, 2 * 0.5 * math.pi / hn)])
+    k = np.concatenate([np.ones(n), np.full(hn, -2.0)])
+    return Geometry(p, nr, w, k, np.array([0.5, 0.5]), np.array([0.5]), n)
+
+
+def donut_neumann_data(geo: Geometry) -> np.ndarray:
+    """The donut's DEFAULT Neumann data (donut.cpp:54-61): 1 on the outer
+    circle, -1/r_hole on the hole; u = log|x - (0.5, 0.5)| + const solves it."""
+    f = np.ones(geo.n)
+    f[geo.num_outer:] = -1.0 / geo.hole_radii[0]
+    return f
+
 
 def laplace_point_source(geo: Geometry, src) -> np.ndarray:
     """f(x) = log|x - src| / (2 pi): harmonic inside the domain for an

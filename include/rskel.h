@@ -120,6 +120,20 @@ rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
  * (ie_solver_test.cpp:87-95). */
 rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int fp32);
 
+/* The solution at points off the boundary, as boundary_integral_solve
+ * assembles it (linear_solve.cpp:188-266, schur_solve 140-154):
+ * u = K_domain mu + U_forward alpha, with K_domain from
+ * Initialization::InitializeDomainKernel (initialization.cpp:11-135) and
+ * U_forward = initialize_U_mat at the targets (linear_solve.cpp:20-64).
+ * targets: interleaved (2*num_targets); in_domain: per-target flags
+ * (Boundary::is_in_domain in the reference; targets flagged 0 get 0), or
+ * NULL for all inside; mu: (num_points*sd) x nrhs; alpha: the hole unknowns
+ * from rs_solve (NULL without holes); out: (num_targets*sd) x nrhs.  Host
+ * memory, column major.  Evaluated directly in FP64 on the GPU. */
+rs_status rs_domain_eval(rs_solver* s, int num_targets, const double* targets,
+                         const unsigned char* in_domain, const double* mu, const double* alpha,
+                         int nrhs, double* out);
+
 /* ie_Mat::id (ie_mat.cpp:548-588) for a batch of matrices on the GPU.
  * mats: concatenated column-major m_i x n_i blocks (offsets a_off, in
  * doubles); ranks[i] gets k (0 = no compression); perm gets n_i 0-based

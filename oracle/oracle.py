@@ -223,3 +223,61 @@ class OracleSolver:
             res[key] = np.array(val, dtype=np.int32)
         res["level_sizes"] = level_sizes
         return res
+
+
+def domain_eval(geo, pde, targets, mu, alpha=None, in_domain=None):
+    """Restatement of the domain solution of boundary_integral_solve
+    (ie_solver/linear_solve.cpp:140-154, 188-266): K_domain mu + U_forward
+    alpha, K_domain per Initialization::InitializeDomainKernel
+    (ie_solver/initialization.cpp:11-135) with the off-boundary kernels of
+    ie_solver/kernel/kernel.cpp:29-104, U_forward per initialize_U_mat
+    (ie_solver/linear_solve.cpp:20-64); targets outside the domain give 0.
+    Dense numpy, FP64."""
+    pts = geo.points.reshape(-1, 2)
+    nrm = geo.normals.reshape(-1, 2)
+    w = geo.weights
+    t = np.asarray(targets, dtype=np.float64).reshape(-1, 2)
+    nt, n = t.shape[0], pts.shape[0]
+    mu = np.asarray(mu, dtype=np.float64)
+    if mu.ndim == 1:
+        mu = mu[:, None]
+    rx = t[:, 0:1] - pts[None, :, 0]
+    ry = t[:, 1:2] - pts[None, :, 1]
+    r2 = rx * rx + ry * ry
+    dot = rx * nrm[None, :, 0] + ry * nrm[None, :, 1]
+    if pde == 2:
+        c = w[None, :] / np.pi * dot / (r2 * r2)
+        out = np.zeros((2 * nt, mu.shape[1]))
+        m0, m1 = mu[0::2], mu[1::2]
+        for q in range(mu.shape[1]):
+            d = c * (rx * m0[None, :, q] + ry * m1[None, :, q])
+            out[0::2, q] = (rx * d).sum(1)
+            out[1::2, q] = (ry * d).sum(1)
+    elif pde == 1:
+        out = (w[None, :] / (2 * np.pi) * 0.5 * np.log(r2)) @ mu
+    else:
+        out = (-w[None, :] / (2 * np.pi) * dot / r2) @ mu
+    if alpha is not None and geo.num_holes > 0 and pde != 1:
+        alpha = np.asarray(alpha, dtype=np.float64)
+        if alpha.ndim == 1:
+            alpha = alpha[:, None]
+        hc = geo.hole_centers.reshape(-1, 2)
+        for h in range(hc.shape[0]):
+            hx = t[:, 0] - hc[h, 0]
+            hy = t[:, 1] - hc[h, 1]
+            h2 = hx * hx + hy * hy
+            if pde == 0:
+                out += np.outer(0.5 * np.log(h2), alpha[h])
+            else:
+                s = 1.0 / (4 * np.pi)
+                lg = -0.5 * np.log(h2)
+                a0, a1, a2 = alpha[3 * h], alpha[3 * h + 1], alpha[3 * h + 2]
+                out[0::2] += s * (np.outer(lg + hx * hx / h2, a0) + np.outer(hx * hy / h2, a1)
+                                  + np.outer(hy / h2, a2))
+                out[1::2] += s * (np.outer(hx * hy / h2, a0) + np.outer(lg + hy * hy / h2, a1)
+                                  - np.outer(hx / h2, a2))
+    if in_domain is not None:
+        keep = np.asarray(in_domain, dtype=bool)
+        sd = 2 if pde == 2 else 1
+        out[np.repeat(~keep, sd)] = 0.0
+    return out
