@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/rskel.h"
@@ -115,6 +116,8 @@ struct rs_solver {
   HostBuf<double> h_io;
 
   FmmPlan fmm;
+  bool incremental = false;      // next rs_factor keeps the boxes rs_perturb left compressed
+  size_t full_fac_used = 0;      // factor storage of the last full factorization
   DevBuf<float> sketch_y;  // FP32 split ID: per-level sketches
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
@@ -339,11 +342,22 @@ rs_status factor_impl(rs_solver* s) {
   Factor<Real>& F = factor_of<Real>(s);
   const int L = (int)s->tree.levels.size();
   const double tol = f32 ? std::max(s->cfg.id_tol, s->cfg.fp32_id_tol) : s->cfg.id_tol;
-  s->st.assign(s->tree.nodes.size(), NodeState());
+  // After rs_perturb the boxes still compressed keep their factors, E blocks
+  // and pivots where they are (skel_factorization.cpp:157 skips them); new
+  // ones are appended.  Once the appended storage reaches eight times a full
+  // factorization's, everything is factored afresh (which reclaims it).
+  const bool incr = s->incremental && F.fac_used > 0 && F.fac_used < 8 * s->full_fac_used + 1024;
+  if (s->trace)
+    std::fprintf(stderr, "[rskel] factor: incremental %d (requested %d, storage %zu of %zu)\n",
+                 (int)incr, (int)s->incremental, F.fac_used, s->full_fac_used);
+  s->incremental = false;
+  if (!incr) {
+    s->st.assign(s->tree.nodes.size(), NodeState());
+    F.fac_used = 0;
+    F.e_used = 0;
+    s->piv_used = 0;
+  }
   s->pool.clear();
-  F.fac_used = 0;
-  F.e_used = 0;
-  s->piv_used = 0;
   s->stats.id_flops = 0;
   s->stats.decouple_flops = 0;
   s->stats.id_ms = 0;
@@ -352,6 +366,7 @@ rs_status factor_impl(rs_solver* s) {
   s->stats.max_active = 0;
   s->stats.max_rank = 0;
   s->stats.max_rows = 0;
+  s->stats.boxes_factored = 0;
   CU(cudaMemsetAsync(s->status.p, 0, sizeof(int) * 4, s->stream));
   std::vector<IdTask> idt;
   std::vector<DecoupleTask> dct;
@@ -360,7 +375,7 @@ rs_status factor_impl(rs_solver* s) {
   std::vector<int> cand_ids, dc_ids;
   std::vector<int> m_of_slot;
   // Contents below these marks are live and survive buffer growth.
-  size_t fac_prev = 0, e_prev = 0, piv_prev = 0;
+  size_t fac_prev = F.fac_used, e_prev = F.e_used, piv_prev = s->piv_used;
   double t_plan = 0, t_wait = 0, t_post = 0;
   while ((int)s->lv_ev.size() < 3 * L) {
     cudaEvent_t e;
@@ -395,6 +410,7 @@ rs_status factor_impl(rs_solver* s) {
     const int prow = (s->cfg.pde == kStokes ? 2 : 1) * npp;
     for (int id : lvl) {
       NodeState& S = s->st[id];
+      if (S.compressed) continue;  // kept from before rs_perturb
       const TreeNode& nd = s->tree.nodes[id];
       const int n = (int)S.active.size();
       const bool cand = !S.compressed && n >= s->cfg.min_dofs_to_compress;
@@ -649,6 +665,7 @@ rs_status factor_impl(rs_solver* s) {
       S.e_ld = k;
       s->stats.max_rank = std::max(s->stats.max_rank, k);
       s->stats.decouple_flops += dec_flops(k, n - k);
+      ++s->stats.boxes_factored;
     }
     for (int id : dc_ids) {
       NodeState& S = s->st[id];
@@ -773,6 +790,7 @@ rs_status factor_impl(rs_solver* s) {
     ++s->launches;
   }
   CU(cudaGetLastError());
+  if (!incr) s->full_fac_used = F.fac_used;
   if (s->trace) std::fprintf(stderr, "[rskel] host: root + solve plan %.3f ms\n", now_ms() - h3);
   return RS_OK;
 }
@@ -1236,6 +1254,153 @@ rs_status rs_build_tree(rs_solver* s) {
   s->factored = false;
   s->st.assign(s->tree.nodes.size(), NodeState());
   s->stats.t_tree_ms = now_ms() - t0;
+  s->stats.num_levels = (int)s->tree.levels.size();
+  s->stats.num_nodes = (int)s->tree.nodes.size();
+  return RS_OK;
+}
+
+namespace {
+struct PointKey {
+  uint64_t x, y;
+  bool operator==(const PointKey& o) const { return x == o.x && y == o.y; }
+};
+struct PointKeyHash {
+  size_t operator()(const PointKey& k) const {
+    return (size_t)(k.x * 0x9E3779B97F4A7C15ull ^ (k.y + 0x7F4A7C159E3779B9ull + (k.x << 6)));
+  }
+};
+PointKey point_key(const double* p) {
+  PointKey k;
+  std::memcpy(&k.x, p, 8);
+  std::memcpy(&k.y, p + 1, 8);
+  return k;
+}
+}  // namespace
+
+rs_status rs_perturb(rs_solver* s, int num_points, const double* points, const double* normals,
+                     const double* weights, const double* curvatures, int num_holes,
+                     const double* hole_centers, const double* hole_radii) {
+  if (!s) return RS_ERR_ARG;
+  if (!s->tree_built)  // nothing to update
+    return rs_set_geometry(s, num_points, points, normals, weights, curvatures, num_holes,
+                           hole_centers, hole_radii);
+  const std::vector<double> old_pts = s->pts;
+  const int n_old = s->n, sd = s->sd;
+  rs_status rc = rs_set_geometry(s, num_points, points, normals, weights, curvatures, num_holes,
+                                 hole_centers, hole_radii);
+  if (rc != RS_OK) return rc;
+  // old point -> new point by exact coordinates (quadtree.cpp:529-561)
+  std::unordered_map<PointKey, int, PointKeyHash> where;
+  where.reserve(2 * (size_t)num_points);
+  for (int i = 0; i < num_points; ++i) where[point_key(points + 2 * i)] = i;
+  std::vector<int> old_to_new(n_old, -1);
+  for (int p = 0; p < n_old; ++p) {
+    auto it = where.find(point_key(old_pts.data() + 2 * p));
+    if (it != where.end()) old_to_new[p] = it->second;
+  }
+  std::vector<int> id_map;
+  std::vector<char> marked;
+  s->tree.perturb(old_pts.data(), points, num_points, old_to_new, &id_map, &marked);
+  // Boxes left compressed keep their factorization with renumbered DOF
+  // lists; everything else starts afresh.
+  std::vector<NodeState> st(s->tree.nodes.size());
+  std::vector<char> dropped(st.size(), 0);  // compressed before, refactored now
+  for (size_t old = 0; old < id_map.size() && old < s->st.size(); ++old) {
+    const int nw = id_map[old];
+    if (nw < 0 || !s->st[old].compressed) continue;
+    if (marked[nw]) {
+      dropped[nw] = 1;
+      continue;
+    }
+    NodeState& S = st[nw];
+    S = std::move(s->st[old]);
+    bool ok = true;
+    auto renumber = [&](std::vector<int>& v) {
+      for (int& d : v) {
+        const int q = old_to_new[d / sd];
+        if (q < 0) ok = false;
+        else d = sd * q + d % sd;
+      }
+    };
+    renumber(S.active);
+    renumber(S.skel);
+    renumber(S.red);
+    S.near_.clear();
+    S.rows.clear();
+    if (!ok) {
+      S = NodeState();
+      dropped[nw] = 1;
+    }
+  }
+  // A box's ID sees everything inside its proxy circle exactly (kernel.cpp:
+  // 360-394) and, at levels 1 and 2, every other box of its level
+  // (kernel.cpp:300-350).  Besides the reference's marking through neighbour
+  // lists, drop every kept box whose proxy circle holds a changed point (old
+  // or new position), and all of levels 1 and 2 when anything changed.
+  std::vector<double> changed;
+  for (int p = 0; p < n_old; ++p)
+    if (old_to_new[p] < 0) changed.insert(changed.end(), {old_pts[2 * p], old_pts[2 * p + 1]});
+  {
+    std::vector<char> found(num_points, 0);
+    for (int p = 0; p < n_old; ++p)
+      if (old_to_new[p] >= 0) found[old_to_new[p]] = 1;
+    for (int i = 0; i < num_points; ++i)
+      if (!found[i]) changed.insert(changed.end(), {points[2 * i], points[2 * i + 1]});
+  }
+  const size_t nch = changed.size() / 2;
+  if (nch > 0) {
+    // boxes of a level on a grid of their side; a changed point can only be
+    // inside the proxy circles of boxes within a few cells of its own
+    const TreeNode& rt = s->tree.nodes[s->tree.root];
+    const double x0 = rt.corners[0], y0 = rt.corners[1];
+    const int reach = (int)std::ceil(s->cfg.radius_ratio) + 1;
+    for (size_t lv = 0; lv < s->tree.levels.size(); ++lv) {
+      const std::vector<int>& lvl = s->tree.levels[lv];
+      if (lvl.empty()) continue;
+      const double side = s->tree.nodes[lvl[0]].side;
+      const double rad = s->cfg.radius_ratio * side * (1.0 + 1e-9);
+      std::unordered_map<int64_t, int> cell;
+      cell.reserve(2 * lvl.size());
+      auto key = [](int64_t ix, int64_t iy) { return (ix << 32) ^ (iy & 0xffffffffll); };
+      for (int id : lvl) {
+        const TreeNode& nd = s->tree.nodes[id];
+        cell[key((int64_t)std::floor((nd.corners[0] - x0) / side + 0.5),
+                 (int64_t)std::floor((nd.corners[1] - y0) / side + 0.5))] = id;
+      }
+      for (size_t q = 0; q < nch; ++q) {
+        const double px = changed[2 * q], py = changed[2 * q + 1];
+        const int64_t cx = (int64_t)std::floor((px - x0) / side);
+        const int64_t cy = (int64_t)std::floor((py - y0) / side);
+        for (int64_t dx = -reach; dx <= reach; ++dx)
+          for (int64_t dy = -reach; dy <= reach; ++dy) {
+            auto it = cell.find(key(cx + dx, cy + dy));
+            if (it == cell.end() || !st[it->second].compressed) continue;
+            const TreeNode& nd = s->tree.nodes[it->second];
+            const double ex = px - (nd.corners[0] + side / 2.0);
+            const double ey = py - (nd.corners[1] + side / 2.0);
+            if (lv <= 2 || ex * ex + ey * ey <= rad * rad) {
+              st[it->second] = NodeState();
+              dropped[it->second] = 1;
+            }
+          }
+      }
+      if (lv <= 2)
+        for (int id : lvl)
+          if (st[id].compressed) {
+            st[id] = NodeState();
+            dropped[id] = 1;
+          }
+    }
+  }
+  // a box whose factorization was dropped drops its ancestors' too
+  for (size_t id = 0; id < st.size(); ++id) {
+    if (!dropped[id]) continue;
+    for (int a = s->tree.nodes[id].parent; a >= 0; a = s->tree.nodes[a].parent)
+      if (st[a].compressed) st[a] = NodeState();
+  }
+  s->st.swap(st);
+  s->tree_built = true;
+  s->incremental = true;
   s->stats.num_levels = (int)s->tree.levels.size();
   s->stats.num_nodes = (int)s->tree.nodes.size();
   return RS_OK;

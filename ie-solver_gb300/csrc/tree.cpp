@@ -136,7 +136,15 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
   push_level(0, root);
   for (int i = 0; i < n; ++i) add(root, points[2 * i], points[2 * i + 1], i);
 
-  // quadtree.cpp:131-175
+  compute_neighbors();
+  number_levels();
+  pts_ = nullptr;
+  return true;
+}
+
+// quadtree.cpp:131-175
+void QuadTree::compute_neighbors() {
+  for (TreeNode& nd : nodes) nd.neighbors.clear();
   const double sqrt2 = std::sqrt(2.0);
   for (size_t lv = 0; lv < levels.size(); ++lv) {
     for (size_t k = 0; k < levels[lv].size(); ++k) {
@@ -171,6 +179,9 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
       }
     }
   }
+}
+
+void QuadTree::number_levels() {
   level_order.clear();
   level_rank.assign(nodes.size(), -1);
   for (const auto& lvl : levels)
@@ -178,8 +189,152 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
       level_rank[id] = static_cast<int>(level_order.size());
       level_order.push_back(id);
     }
+}
+
+// The leaf holding (x, y), by the midpoint rule of recursive_add.
+int QuadTree::find_leaf(double x, double y) const {
+  int cur = root;
+  while (!nodes[cur].is_leaf) {
+    const TreeNode& nd = nodes[cur];
+    const double midx = ((nd.corners[6] - nd.corners[0]) / 2.0) + nd.corners[0];
+    const double midy = ((nd.corners[3] - nd.corners[1]) / 2.0) + nd.corners[1];
+    if (x < midx && y < midy) cur = nd.bl;
+    else if (x < midx && y >= midy) cur = nd.tl;
+    else if (x >= midx && y < midy) cur = nd.br;
+    else cur = nd.tr;
+  }
+  return cur;
+}
+
+// quadtree.cpp:435-461
+void QuadTree::mark(int id, std::vector<char>* marked) const {
+  for (int cur = id; cur >= 0; cur = nodes[cur].parent) {
+    (*marked)[cur] = 1;
+    for (int nb : nodes[cur].neighbors) (*marked)[nb] = 1;
+  }
+}
+
+// quadtree.cpp:464-513: the subtree's leaf DOFs move into `id`, which
+// becomes a leaf; its descendants leave the tree.
+void QuadTree::consolidate(int id, std::vector<char>* dead) {
+  std::vector<int> queue(1, id), dofs;
+  for (size_t i = 0; i < queue.size(); ++i) {
+    const TreeNode& cur = nodes[queue[i]];
+    if (cur.is_leaf) dofs.insert(dofs.end(), cur.original.begin(), cur.original.end());
+    else
+      for (int c = 0; c < 4; ++c)
+        if (cur.children[c] >= 0) queue.push_back(cur.children[c]);
+    if (queue[i] != id) (*dead)[queue[i]] = 1;
+  }
+  TreeNode& nd = nodes[id];
+  nd.original = dofs;
+  nd.bl = nd.tl = nd.tr = nd.br = -1;
+  for (int c = 0; c < 4; ++c) nd.children[c] = -1;
+  nd.is_leaf = 1;
+}
+
+void QuadTree::perturb(const double* old_points, const double* new_points, int n_new,
+                       const std::vector<int>& old_to_new, std::vector<int>* id_map,
+                       std::vector<char>* marked) {
+  const int n_old = static_cast<int>(old_to_new.size());
+  std::vector<char> found(n_new, 0);
+  for (int p = 0; p < n_old; ++p)
+    if (old_to_new[p] >= 0) found[old_to_new[p]] = 1;
+  marked->assign(nodes.size(), 0);
+  // renumber the leaves' DOFs (quadtree.cpp:583-598)
+  for (TreeNode& nd : nodes) {
+    if (!nd.is_leaf) continue;
+    std::vector<int> ob;
+    for (int d : nd.original) {
+      const int q = old_to_new[d / sd];
+      if (q >= 0) ob.push_back(sd * q + d % sd);
+    }
+    nd.original.swap(ob);
+  }
+  // additions (quadtree.cpp:639-668)
+  std::vector<int> bursting;
+  for (int i = 0; i < n_new; ++i) {
+    if (found[i]) continue;
+    const int leaf = find_leaf(new_points[2 * i], new_points[2 * i + 1]);
+    for (int c = 0; c < sd; ++c) nodes[leaf].original.push_back(sd * i + c);
+    bursting.push_back(leaf);
+    mark(leaf, marked);
+  }
+  // DOFs below each box (quadtree.cpp:670-684)
+  std::vector<int> below(nodes.size(), 0);
+  for (int lv = static_cast<int>(levels.size()) - 1; lv >= 0; --lv)
+    for (int id : levels[lv]) {
+      if (nodes[id].is_leaf) below[id] = static_cast<int>(nodes[id].original.size());
+      const int par = nodes[id].parent;
+      if (par >= 0) below[par] += below[id];
+    }
+  // deletions (quadtree.cpp:686-715): the first box on the way down holding
+  // fewer than MAX_LEAF_DOFS DOFs is consolidated
+  std::vector<char> sparse(nodes.size(), 0);
+  for (int p = 0; p < n_old; ++p) {
+    if (old_to_new[p] >= 0) continue;
+    const double x = old_points[2 * p], y = old_points[2 * p + 1];
+    int cur = root;
+    bool path_marked = false;
+    while (!nodes[cur].is_leaf) {
+      if (below[cur] < leaf_ && !path_marked) {
+        path_marked = true;
+        sparse[cur] = 1;
+      }
+      const TreeNode& nd = nodes[cur];
+      const double midx = ((nd.corners[6] - nd.corners[0]) / 2.0) + nd.corners[0];
+      const double midy = ((nd.corners[3] - nd.corners[1]) / 2.0) + nd.corners[1];
+      if (x < midx && y < midy) cur = nd.bl;
+      else if (x < midx && y >= midy) cur = nd.tl;
+      else if (x >= midx && y < midy) cur = nd.br;
+      else cur = nd.tr;
+    }
+    mark(cur, marked);
+  }
+  // split bursting leaves (quadtree.cpp:727-733), new boxes start unmarked-
+  // less: they have no factorization
+  pts_ = new_points;
+  const size_t before = nodes.size();
+  for (int id : bursting)
+    if (nodes[id].is_leaf && static_cast<int>(nodes[id].original.size()) > leaf_) subdivide(id);
   pts_ = nullptr;
-  return true;
+  marked->resize(nodes.size(), 1);
+  for (size_t i = before; i < nodes.size(); ++i) (*marked)[i] = 1;
+  // consolidate sparse boxes (quadtree.cpp:737-739)
+  std::vector<char> dead(nodes.size(), 0);
+  for (size_t id = 0; id < sparse.size(); ++id)
+    if (sparse[id] && !dead[id]) consolidate(static_cast<int>(id), &dead);
+  // renumber without the removed boxes; levels keep their order
+  id_map->assign(nodes.size(), -1);
+  std::vector<TreeNode> kept;
+  std::vector<char> kmark;
+  for (size_t id = 0; id < nodes.size(); ++id) {
+    if (dead[id]) continue;
+    (*id_map)[id] = static_cast<int>(kept.size());
+    kept.push_back(nodes[id]);
+    kmark.push_back((*marked)[id]);
+  }
+  auto remap = [&](int v) { return v >= 0 ? (*id_map)[v] : -1; };
+  for (TreeNode& nd : kept) {
+    nd.parent = remap(nd.parent);
+    for (int c = 0; c < 4; ++c) nd.children[c] = remap(nd.children[c]);
+    nd.bl = remap(nd.bl);
+    nd.tl = remap(nd.tl);
+    nd.tr = remap(nd.tr);
+    nd.br = remap(nd.br);
+  }
+  for (auto& lvl : levels) {
+    std::vector<int> l2;
+    for (int id : lvl)
+      if (!dead[id]) l2.push_back((*id_map)[id]);
+    lvl.swap(l2);
+  }
+  while (!levels.empty() && levels.back().empty()) levels.pop_back();
+  root = remap(root);
+  nodes.swap(kept);
+  marked->swap(kmark);
+  compute_neighbors();  // quadtree.cpp:759-797, the same rules as the build
+  number_levels();
 }
 
 }  // namespace rskel

@@ -37,6 +37,20 @@ struct QuadTree {
 
   // points: interleaved (2n). Returns false on empty input.
   bool build(const double* points, int n, int sd, int max_leaf_dofs);
+
+  // QuadTree::perturb (quadtree.cpp:435-801) for a boundary whose points
+  // moved: old_to_new[p] is the new index of old point p (-1 if it is gone),
+  // points of the new boundary not in the old one are added.  Leaf DOF
+  // lists are renumbered, added points go to their leaves, emptied subtrees
+  // below MAX_LEAF_DOFS are consolidated, bursting leaves split, and the
+  // neighbour lists are rebuilt.  Nodes are then renumbered without the
+  // removed ones: id_map[old id] = new id or -1.  marked[new id] = 1 for the
+  // boxes whose factorization is dropped (mark_neighbors_and_parents: the
+  // leaves that gained or lost points, their neighbours, their ancestors and
+  // the ancestors' neighbours), and for new boxes.
+  void perturb(const double* old_points, const double* new_points, int n_new,
+               const std::vector<int>& old_to_new, std::vector<int>* id_map,
+               std::vector<char>* marked);
   // level-order numbering (level 0 first) <-> creation ids
   std::vector<int> level_order;   // level-order index -> node id
   std::vector<int> level_rank;    // node id -> level-order index
@@ -49,6 +63,11 @@ struct QuadTree {
   void add(int id, double x, double y, int point);
   void subdivide(int id);
   void descendant_neighbors(int big, int small);
+  void compute_neighbors();
+  void number_levels();
+  int find_leaf(double x, double y) const;
+  void mark(int id, std::vector<char>* marked) const;
+  void consolidate(int id, std::vector<char>* dead);
 };
 
 }  // namespace rskel

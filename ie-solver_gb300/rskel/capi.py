@@ -23,7 +23,8 @@ STATUS = {0: "RS_OK", 1: "RS_ERR_ARG", 2: "RS_ERR_STATE", 3: "RS_ERR_CUDA",
           7: "RS_ERR_NO_COMPRESSION"}
 
 # Every function the C ABI exports (include/rskel.h).
-EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_build_tree",
+EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_perturb",
+           "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
            "rs_matvec_fast", "rs_domain_eval",
            "rs_id_batched", "rs_id_noalloc", "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
@@ -54,6 +55,7 @@ class RsStats(ctypes.Structure):
                 ("refine_iters", ctypes.c_int), ("refine_residual", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int), ("host_plan_ms", ctypes.c_double),
                 ("host_wait_ms", ctypes.c_double), ("host_post_ms", ctypes.c_double),
+                ("boxes_factored", ctypes.c_int),
                 ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double)]
 
     def as_dict(self):
@@ -78,6 +80,7 @@ def lib():
         L.rs_create.argtypes = [ctypes.POINTER(RsConfig), ctypes.POINTER(_vp)]
         L.rs_destroy.argtypes = [_vp]
         L.rs_set_geometry.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
+        L.rs_perturb.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.rs_build_tree.argtypes = [_vp]
         L.rs_factor.argtypes = [_vp]
         L.rs_solve.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp]
@@ -157,8 +160,9 @@ class Solver:
         self.pde = pde
         self.set_geometry(geo)
 
-    def set_geometry(self, geo):
-        """rs_set_geometry: a new boundary for this handle (tree and factors reset)."""
+    def set_geometry(self, geo, perturb=False):
+        """rs_set_geometry: a new boundary for this handle (tree and factors
+        reset); with perturb=True rs_perturb, which keeps what it can."""
         self.n = geo.n
         self.D = geo.n * self.sd
         self.nh = geo.num_holes
@@ -168,8 +172,9 @@ class Solver:
                 (geo.points, geo.normals, geo.weights, geo.curvatures)]
         hc = np.ascontiguousarray(geo.hole_centers if geo.num_holes else np.zeros(2))
         hr = np.ascontiguousarray(geo.hole_radii if geo.num_holes else np.zeros(1))
-        self._check(lib().rs_set_geometry(self.h, geo.n, _d(arrs[0]), _d(arrs[1]), _d(arrs[2]),
-                                          _d(arrs[3]), geo.num_holes, _d(hc), _d(hr)))
+        fn = lib().rs_perturb if perturb else lib().rs_set_geometry
+        self._check(fn(self.h, geo.n, _d(arrs[0]), _d(arrs[1]), _d(arrs[2]), _d(arrs[3]),
+                       geo.num_holes, _d(hc), _d(hr)))
 
     def _check(self, rc, h="self"):
         if rc != 0:

@@ -252,6 +252,42 @@ def reference_annulus(n: int) -> Geometry:
 # Boundary data
 # ---------------------------------------------------------------------------
 
+def star_bump(n: int, center: float, height: float = 0.05, width: float = 0.3,
+              a: float = 0.3, k: int = 5) -> Geometry:
+    """The star r(t) = 1 + a cos(k t) plus a raised-cosine bump of the given
+    height on |t - center| < width (angles mod 2 pi).  Nodes outside the bump
+    are bit-identical to ``star(n, a, k)``'s, so moving the bump changes the
+    boundary locally, as the reference's update experiments do
+    (ie_solver_test.cpp:577-612)."""
+    def wrap(t):
+        return (t - center + math.pi) % (2 * math.pi) - math.pi
+
+    def bump(t):
+        u = wrap(t)
+        inside = np.abs(u) < width
+        return np.where(inside, height * 0.5 * (1 + np.cos(math.pi * u / width)), 0.0)
+
+    def dbump(t):
+        u = wrap(t)
+        inside = np.abs(u) < width
+        return np.where(inside, -height * 0.5 * math.pi / width * np.sin(math.pi * u / width), 0.0)
+
+    def ddbump(t):
+        u = wrap(t)
+        inside = np.abs(u) < width
+        return np.where(inside, -height * 0.5 * (math.pi / width) ** 2 * np.cos(math.pi * u / width),
+                        0.0)
+
+    pts, nrm, w, kappa = _radial(
+        n,
+        lambda t: (1.0 + a * np.cos(k * t)) + bump(t),
+        lambda t: (-a * k * np.sin(k * t)) + dbump(t),
+        lambda t: (-a * k * k * np.cos(k * t)) + ddbump(t),
+    )
+    hc, hr = _empty_holes()
+    return Geometry(pts, nrm, w, kappa, hc, hr, n)
+
+
 def reference_donut(n: int) -> Geometry:
     """ie_solver/boundaries/donut.cpp:9-52: unit circle around (0.5, 0.5) with
     one concentric hole of radius 0.5 carrying n/5 nodes."""

@@ -9,7 +9,8 @@
 //   Kernel                kernel/kernel.h:28-88 (construction, operator())
 //   QuadTree, nodes       quadtree/quadtree.h:16-139
 //   SkelFactorization     skel_factorization/skel_factorization.h:19-95
-//   linear_solve, initialize_U_mat, initialize_Psi_mat   linear_solve.h:26-35
+//   linear_solve, initialize_U_mat, initialize_Psi_mat, get_domain_points,
+//   boundary_integral_solve                               linear_solve.h:20-35
 // so a caller written against the reference compiles against this header.
 // The factorization itself runs on the GPU: QuadTree owns the solver handle
 // (rs_solver) that holds the tree and, after skeletonize, the factors; the
@@ -238,6 +239,9 @@ class Boundary {
   std::vector<Hole> holes;
   ie_Mat boundary_values;
   virtual ~Boundary() {}
+  // Which domain points boundary_integral_solve evaluates (the reference's
+  // shapes override it; every point by default).
+  virtual bool is_in_domain(const Vec2&) const { return true; }
 };
 
 namespace detail {
@@ -392,6 +396,24 @@ class QuadTree {
     initialize_tree(boundary_, domain_points, solution_dimension, domain_dimension);
   }
 
+  // quadtree.cpp:435-801: the boundary changed locally; the tree is updated
+  // and the next skeletonize refactors only the boxes near the change.
+  void perturb(const Boundary& perturbed_boundary) {
+    own_ = perturbed_boundary;
+    std::vector<double> hc, hr;
+    for (const Hole& h : own_.holes) {
+      hc.push_back(h.center.a[0]);
+      hc.push_back(h.center.a[1]);
+      hr.push_back(h.radius);
+    }
+    detail::check(rs_perturb(h_, (int)own_.weights.size(), own_.points.data(),
+                             own_.normals.data(), own_.weights.data(), own_.curvatures.data(),
+                             (int)own_.holes.size(), hc.data(), hr.data()),
+                  h_, "rs_perturb");
+    mirror();
+    perturbed_ = true;
+  }
+
   rs_solver* handle() const { return h_; }
   // Leaf size and proxy-point count of the tree and its factorization.
   void set_gb300_options(int max_leaf_dofs, int num_proxy_points) {
@@ -404,6 +426,7 @@ class QuadTree {
   Boundary own_;
   rs_solver* h_ = nullptr;
   int leaf_ = 32, npp_ = 128;
+  bool perturbed_ = false;   // the handle holds a factorization to update
 
   void clear() {
     for (QuadTreeLevel* l : levels) delete l;
@@ -482,6 +505,13 @@ class SkelFactorization {
   void skeletonize(const Kernel& K, QuadTree* tree) {
     if (strong_admissibility)
       throw rs_error(RS_ERR_ARG, "strong admissibility is not supported");
+    if (tree->perturbed_ && tree->h_) {
+      // after QuadTree::perturb: keep the compressed boxes (skel_factorization.cpp:157)
+      detail::check(rs_factor(tree->h_), tree->h_, "rs_factor");
+      tree->perturbed_ = false;
+      tree->mirror();
+      return;
+    }
     rs_solver* s = detail::make_handle(*tree->boundary, detail::to_pde(K.pde), id_tol,
                                        tree->leaf_, tree->npp_, precision);
     rs_status rc = rs_factor(s);
@@ -522,6 +552,47 @@ inline void linear_solve(const SkelFactorization& skel_factorization, const Quad
   } else {
     skel_factorization.multiply_connected_solve(quadtree, mu, alpha, f);
   }
+}
+
+// linear_solve.cpp:269-279: a size x size grid over [x_min, x_max] x
+// [y_min, y_max], x outer.
+inline void get_domain_points(int domain_size, std::vector<double>* points, double x_min,
+                              double x_max, double y_min, double y_max) {
+  for (int i = 0; i < domain_size; ++i) {
+    const double x = x_min + (double)i / (domain_size - 1) * (x_max - x_min);
+    for (int j = 0; j < domain_size; ++j) {
+      points->push_back(x);
+      points->push_back(y_min + (double)j / (domain_size - 1) * (y_max - y_min));
+    }
+  }
+}
+
+// linear_solve.cpp:188-266: factor, solve for the boundary's own data and
+// evaluate the solution (K_domain mu + U_forward alpha) at domain_points,
+// zero where boundary->is_in_domain is false.
+inline ie_Mat boundary_integral_solve(const ie_solver_config& config, QuadTree* quadtree,
+                                      const std::vector<double>& domain_points) {
+  Boundary* boundary = quadtree->boundary;
+  SkelFactorization sf(config.id_tol, config.is_strong_admissibility, config.num_threads);
+  sf.precision = config.precision;
+  Kernel kernel(config.solution_dimension, config.domain_dimension, config.pde, boundary,
+                domain_points);
+  sf.skeletonize(kernel, quadtree);
+  const int nb = boundary->holes.empty() || config.pde == ie_solver_config::LAPLACE_NEUMANN
+                     ? 0
+                     : (config.pde == ie_solver_config::STOKES ? 3 : 1) *
+                           (int)boundary->holes.size();
+  ie_Mat mu, alpha(nb, 1);
+  linear_solve(sf, *quadtree, boundary->boundary_values, &mu, nb ? &alpha : nullptr);
+  const int nt = (int)domain_points.size() / 2;
+  std::vector<unsigned char> inside(nt);
+  for (int i = 0; i < nt; ++i)
+    inside[i] = boundary->is_in_domain(Vec2(domain_points[2 * i], domain_points[2 * i + 1]));
+  ie_Mat out(nt * config.solution_dimension, 1);
+  detail::check(rs_domain_eval(quadtree->handle(), nt, domain_points.data(), inside.data(),
+                               mu.mat, nb ? alpha.mat : nullptr, 1, out.mat),
+                quadtree->handle(), "rs_domain_eval");
+  return out;
 }
 
 // linear_solve.cpp:20-64: U, the hole columns of the bordered operator.

@@ -87,6 +87,17 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
  * Host-side; needs no GPU. */
 rs_status rs_build_tree(rs_solver* s);
 
+/* QuadTree::perturb (quadtree/quadtree.cpp:435-801): the boundary changed
+ * (points matched to the old ones by exact coordinates).  The tree is
+ * updated in place, and the next rs_factor refactors only the boxes whose
+ * neighbourhood changed, keeping the others' factors, as skeletonize does
+ * after perturb (skel_factorization.cpp:157).  Arguments as rs_set_geometry;
+ * before rs_build_tree it is rs_set_geometry.  Host-side; needs no GPU. */
+rs_status rs_perturb(rs_solver* s, int num_points, const double* points,
+                     const double* normals, const double* weights,
+                     const double* curvatures, int num_holes,
+                     const double* hole_centers, const double* hole_radii);
+
 /* SkelFactorization::skeletonize (skel_factorization.cpp:140-310), including
  * the bordered system for holes (initialize_U_mat / initialize_Psi_mat,
  * linear_solve.cpp:20-112).  Builds the tree first when needed. */
@@ -177,6 +188,7 @@ typedef struct {
   double host_plan_ms, host_wait_ms, host_post_ms; /* last factor: host list building and
                                                       launches, waiting for ranks, and
                                                       bookkeeping after them */
+  int boxes_factored;                          /* boxes compressed by the last rs_factor */
   double residual64_ms, residual32_ms;         /* last RS_FP32_REFINE solve: CUDA-event time of
                                                   the FP64 residual products and of the FP32
                                                   correction products */

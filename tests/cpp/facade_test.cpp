@@ -143,6 +143,41 @@ static void host_checks() {
   EXPECT(tree.boundary != &circle && tree.boundary->weights.size() == 4096);
 }
 
+// ie_solver_test.cpp:404-416 (LaplaceCircleAnalyticAgreementElectron) through
+// boundary_integral_solve: the circle of the reference's tests (centre
+// (0.5, 0.5), radius 0.25) with log|x - (-3, -2)| data.
+struct RefCircle : Boundary {
+  bool is_in_domain(const Vec2& a) const override {
+    const double x = a.a[0] - 0.5, y = a.a[1] - 0.5;
+    return std::sqrt(x * x + y * y) + 1e-2 <= 0.25;
+  }
+};
+static void check_domain_solution() {
+  RefCircle b;
+  add_circle(&b, 512, 0.5, 0.5, 0.25, true);
+  const int n = (int)b.weights.size();
+  b.boundary_values = ie_Mat(n, 1);
+  for (int i = 0; i < n; ++i)
+    b.boundary_values.set(i, 0, std::log(std::hypot(b.points[2 * i] + 3, b.points[2 * i + 1] + 2)));
+  ie_solver_config config;
+  config.id_tol = 1e-6;
+  QuadTree tree;
+  tree.initialize_tree(&b, std::vector<double>(), 1, 2);
+  std::vector<double> dom;
+  get_domain_points(config.domain_size, &dom, tree.min, tree.max, tree.min, tree.max);
+  ie_Mat sol = boundary_integral_solve(config, &tree, dom);
+  double diff = 0, norm = 0;
+  for (size_t i = 0; i < dom.size(); i += 2) {
+    if (!b.is_in_domain(Vec2(dom[i], dom[i + 1]))) continue;
+    const double truth = std::log(std::hypot(dom[i] + 3, dom[i + 1] + 2));
+    diff += std::pow(sol.get((int)i / 2, 0) - truth, 2);
+    norm += truth * truth;
+  }
+  const double err = std::sqrt(diff / norm);
+  std::printf("  domain solution: relative error %.3e (bound %.1e)\n", err, 10 * config.id_tol);
+  EXPECT(norm > 0 && err <= 10 * config.id_tol);
+}
+
 int main(int argc, char** argv) {
   const bool host_only = argc > 1 && std::strcmp(argv[1], "--host") == 0;
   host_checks();
@@ -196,6 +231,8 @@ int main(int argc, char** argv) {
       set_values(&b, cs.pde == ie_solver_config::STOKES);
       check_solve_err(config, &b);
     }
+    std::printf("laplace circle, boundary_integral_solve\n");
+    check_domain_solution();
   }
   std::printf(g_fail ? "%d FAILED\n" : "all passed\n", g_fail);
   return g_fail ? 1 : 0;
