@@ -994,13 +994,19 @@ namespace {
 
 // r = f - K mu - U alpha;  rg = alpha - Psi mu  (bordered operator of
 // ie_solver_test.cpp:43-83, [K U; Psi -I]).
-// Multipole plan for the refinement residual (Laplace): FP64 order from the
-// configuration (default 32: ~1e-13 relative to the dense FP64 product on the
-// 65536-point star), FP32 order 16 for correction products.
-constexpr int kFmmOrderDefault = 32;
+// Multipole plan for the refinement residual (Laplace).  FP64 order from the
+// configuration, or matched to the refinement tolerance: on the 65536-point
+// star the product's relative error is about 10^(-0.36 p - 2.1) (order 20:
+// 1.2e-9, 28: 1.8e-12, 32: 6.5e-14), and the residual needs it ten times
+// below refine_tol.  FP32 order 16 for the correction products.
 constexpr int kFmmOrder32 = 16;
+int auto_fmm_order(double refine_tol) {
+  const double want = std::max(refine_tol, 1e-15) / 10.0;
+  const int p = (int)std::ceil((-std::log10(want) - 2.1) / 0.36);
+  return std::min(48, std::max(12, p));
+}
 rs_status build_fmm(rs_solver* s) {
-  const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : kFmmOrderDefault;
+  const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : auto_fmm_order(s->cfg.refine_tol);
   if (p > 64) return fail(s, RS_ERR_ARG, "fmm_order above 64");
   if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, kFmmOrder32, s->stream))
     return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
