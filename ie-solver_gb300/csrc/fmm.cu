@@ -1,6 +1,8 @@
 // Fast multipole kernels for the Laplace double-layer product; see fmm.hpp
-// for the formulation.  Templated on the arithmetic type R (double or
-// float); complex numbers are (re, im) pairs of R.
+// for the formulation.  Templated on the number type R: double, float, or
+// DF (float-float); complex numbers are (re, im) pairs of R.  Geometry comes
+// in as FP64 box centres and leaf-relative point coordinates, so only box
+// offsets (one per box pair) touch FP64.
 //
 // Scaled expansions for a box with centre z_B and side s_B:
 //   multipole  phi(z) = sum_k  M_k s^k / (z - z_B)^(k+1)
@@ -17,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "fmm.hpp"
 
@@ -28,6 +32,53 @@ constexpr int kFmmThreads = 128;
 constexpr int kMaxRhs = 8;  // right-hand sides per pass (larger batches loop)
 constexpr int kStage = 64;  // points staged in shared memory at a time
 constexpr int kEvalThreads = 128;
+
+// Float-float numbers: value = hi + lo with |lo| <= ulp(hi)/2, ~48-bit
+// significands.  Error-free transformations (Knuth's two-sum, and the
+// product error from an explicit fused multiply-add; Dekker 1971), so the
+// operations run on the FP32 pipes.
+struct DF {
+  float hi, lo;
+  DF() = default;
+  __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ explicit DF(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ explicit DF(int v) : DF((double)v) {}
+  __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ DF df_renorm(float s, float e) {
+  const float h = s + e;
+  return DF(h, e - (h - s));
+}
+__device__ __forceinline__ DF operator+(DF a, DF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
+  return df_renorm(s, e);
+}
+__device__ __forceinline__ DF operator-(DF a) { return DF(-a.hi, -a.lo); }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+__device__ __forceinline__ DF operator*(DF a, DF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_renorm(p, e);
+}
+__device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
+__device__ __forceinline__ DF& operator-=(DF& a, DF b) { return a = a - b; }
+__device__ __forceinline__ DF& operator*=(DF& a, DF b) { return a = a * b; }
+// 1/a: an FP32 reciprocal refined by one Newton step in float-float (the
+// float and double overloads come from common.cuh).
+using ::rskel::rcp;
+__device__ __forceinline__ DF rcp(DF a) {
+  const DF y(__frcp_rn(a.hi), 0.f);
+  const DF e = DF(1.f, 0.f) - a * y;
+  return y + y * e;
+}
+
+template <class R>
+__device__ __forceinline__ R to_r(double v) { return R(v); }
+template <>
+__device__ __forceinline__ float to_r<float>(double v) { return (float)v; }
 
 template <class R>
 struct Cx {
@@ -42,6 +93,10 @@ __device__ __forceinline__ Cx<R> cadd(Cx<R> a, Cx<R> b) {
   return {a.re + b.re, a.im + b.im};
 }
 template <class R>
+__device__ __forceinline__ Cx<R> csub(Cx<R> a, Cx<R> b) {
+  return {a.re - b.re, a.im - b.im};
+}
+template <class R>
 __device__ __forceinline__ Cx<R> cinv(Cx<R> a) {
   const R d = rcp(a.re * a.re + a.im * a.im);
   return {a.re * d, -a.im * d};
@@ -50,30 +105,47 @@ template <class R>
 __device__ __forceinline__ Cx<R> cscale(Cx<R> a, R s) {
   return {a.re * s, a.im * s};
 }
-// Positions: FP64 coordinates, or FP32 (hi, lo) pairs whose difference is
-// formed hi - hi (exact for nearby points) plus lo - lo.
+
+// Leaf-relative point positions: FP64, or a hi + lo float pair.
 template <class R>
-struct Pos;
+struct Pos {
+  float hx, lx, hy, ly;
+};
 template <>
 struct Pos<double> {
   double x, y;
 };
-template <>
-struct Pos<float> {
-  float hx, lx, hy, ly;
+__device__ __forceinline__ Cx<double> vec(Pos<double> a) { return {a.x, a.y}; }
+__device__ __forceinline__ Cx<float> vec(Pos<float> a) { return {a.hx + a.lx, a.hy + a.ly}; }
+__device__ __forceinline__ Cx<DF> vec(Pos<DF> a) { return {DF(a.hx, a.lx), DF(a.hy, a.ly)}; }
+// t - s - off for points t, s of leaves whose centres differ by off = c_s - c_t.
+// The near-field difference is a small remainder of O(side) terms, so the
+// FP32 variant forms it in float-float too and rounds once at the end.
+template <class R>
+struct OffT {
+  using type = DF;
 };
-__device__ __forceinline__ Cx<double> sub(Pos<double> a, Pos<double> b) {
-  return {a.x - b.x, a.y - b.y};
+template <>
+struct OffT<double> {
+  using type = double;
+};
+__device__ __forceinline__ Cx<double> diff(Pos<double> t, Pos<double> s, Cx<double> off) {
+  return {(t.x - s.x) - off.re, (t.y - s.y) - off.im};
 }
-__device__ __forceinline__ Cx<float> sub(Pos<float> a, Pos<float> b) {
-  return {(a.hx - b.hx) + (a.lx - b.lx), (a.hy - b.hy) + (a.ly - b.ly)};
+__device__ __forceinline__ Cx<DF> diff(Pos<DF> t, Pos<DF> s, Cx<DF> off) {
+  return {(DF(t.hx, t.lx) - DF(s.hx, s.lx)) - off.re, (DF(t.hy, t.ly) - DF(s.hy, s.ly)) - off.im};
+}
+__device__ __forceinline__ Cx<float> diff(Pos<float> t, Pos<float> s, Cx<DF> off) {
+  const DF x = (DF(t.hx, t.lx) - DF(s.hx, s.lx)) - off.re;
+  const DF y = (DF(t.hy, t.ly) - DF(s.hy, s.ly)) - off.im;
+  return {x.hi + x.lo, y.hi + y.lo};
 }
 
 template <class R>
 struct FmmArgs {
-  const double *cx, *cy, *zx, *zy;
-  const float *cxh, *cxl, *cyh, *cyl, *zxh, *zxl, *zyh, *zyl;
-  const R* side;
+  const double *cx, *cy, *side;
+  const double *rx, *ry;                  // FP64 variant
+  const float *rxh, *rxl, *ryh, *ryl;     // float and float-float variants
   const R* binom;
   const int *pstart, *pcount, *parent, *slot_pt, *children;
   const int *v_off, *v_idx, *w_off, *w_idx, *x_off, *x_idx, *u_off, *u_idx;
@@ -84,17 +156,27 @@ struct FmmArgs {
   R* local;
 };
 
-__device__ __forceinline__ Pos<double> box_pos(const FmmArgs<double>& a, int b) {
-  return {a.cx[b], a.cy[b]};
-}
-__device__ __forceinline__ Pos<float> box_pos(const FmmArgs<float>& a, int b) {
-  return {a.cxh[b], a.cxl[b], a.cyh[b], a.cyl[b]};
-}
 __device__ __forceinline__ Pos<double> pt_pos(const FmmArgs<double>& a, int s) {
-  return {a.zx[s], a.zy[s]};
+  return {a.rx[s], a.ry[s]};
 }
-__device__ __forceinline__ Pos<float> pt_pos(const FmmArgs<float>& a, int s) {
-  return {a.zxh[s], a.zxl[s], a.zyh[s], a.zyl[s]};
+template <class R>
+__device__ __forceinline__ Pos<R> pt_pos(const FmmArgs<R>& a, int s) {
+  return {a.rxh[s], a.rxl[s], a.ryh[s], a.ryl[s]};
+}
+// c_to - c_from in FP64, then in R
+template <class R>
+__device__ __forceinline__ Cx<R> box_off(const FmmArgs<R>& a, int from, int to) {
+  return {to_r<R>(a.cx[to] - a.cx[from]), to_r<R>(a.cy[to] - a.cy[from])};
+}
+// the same offset in the near-field difference's number type
+template <class R>
+__device__ __forceinline__ Cx<typename OffT<R>::type> p2p_off(const FmmArgs<R>& a, int from, int to) {
+  using T = typename OffT<R>::type;
+  return {T(a.cx[to] - a.cx[from]), T(a.cy[to] - a.cy[from])};
+}
+template <class R>
+__device__ __forceinline__ R side_of(const FmmArgs<R>& a, int b) {
+  return to_r<R>(a.side[b]);
 }
 
 template <class R>
@@ -127,8 +209,7 @@ __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
   const int b = a.boxes[blockIdx.x];
   const int s0 = a.pstart[b], cnt = a.pcount[b], p = a.p;
   Cx<R>* pw = reinterpret_cast<Cx<R>*>(smem);  // kStage x p
-  const Pos<R> c = box_pos(a, b);
-  const R is = rcp(a.side[b]);
+  const R is = rcp(side_of(a, b));
   constexpr int kPer = 4;  // (k, q) pairs per thread (p * nrhs <= 512)
   Cx<R> acc[kPer];
 #pragma unroll
@@ -137,7 +218,7 @@ __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
     const int jc = cnt - j0 < kStage ? cnt - j0 : kStage;
     __syncthreads();
     for (int j = threadIdx.x; j < jc; j += blockDim.x) {
-      const Cx<R> rho = cscale(sub(pt_pos(a, s0 + j0 + j), c), is);
+      const Cx<R> rho = cscale(vec(pt_pos(a, s0 + j0 + j)), is);
       Cx<R> v = {(R)1, (R)0};
       for (int k = 0; k < p; ++k) {
         pw[j * p + k] = v;
@@ -176,12 +257,12 @@ __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
   Cx<R>* dl = reinterpret_cast<Cx<R>*>(smem);  // 4 x p: d_c^l
   Cx<R>* gk = dl + 4 * p;                      // 4 x p: g_c^k
   Cx<R>* av = gk + 4 * p;                      // 4 x nrhs x p: M_k(c) g_c^k
-  const R isp = rcp(a.side[P]);
+  const R isp = rcp(side_of(a, P));
   if (threadIdx.x < 8) {
     const int c = threadIdx.x & 3;
     const int C = a.children[4 * P + c];
     if (C >= 0) {
-      const Cx<R> d = cscale(sub(box_pos(a, C), box_pos(a, P)), isp);
+      const Cx<R> d = cscale(box_off(a, P, C), isp);
       const Cx<R> base = threadIdx.x < 4 ? d : cinv(cscale(d, (R)2));
       Cx<R>* out = (threadIdx.x < 4 ? dl : gk) + c * p;
       Cx<R> v = {(R)1, (R)0};
@@ -226,8 +307,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   Cx<R>* av = reinterpret_cast<Cx<R>*>(smem);  // p x nrhs scaled source coefficients
   Cx<R>* vp = av + (size_t)p * nrhs;           // p: (-1)^l (s_B/d)^l / d
   Cx<R>* pw = vp + p;                          // kStage x p powers for P2L
-  const Pos<R> zb = box_pos(a, B);
-  const R sB = a.side[B];
+  const R sB = side_of(a, B);
   constexpr int kPer = 4;  // (l, q) pairs per thread (p * nrhs <= 512)
   Cx<R> acc[kPer];
 #pragma unroll
@@ -235,10 +315,10 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   for (int vi = a.v_off[B]; vi < a.v_off[B + 1]; ++vi) {
     const int C = a.v_idx[vi];
     if (threadIdx.x < 2) {
-      const Cx<R> id = cinv(sub(zb, box_pos(a, C)));
+      const Cx<R> id = cinv(box_off(a, C, B));
       // thread 0: u^k (u = s_C / d) into pw; thread 1: vp
       if (threadIdx.x == 0) {
-        const Cx<R> u = cscale(id, a.side[C]);
+        const Cx<R> u = cscale(id, side_of(a, C));
         Cx<R> v = {(R)1, (R)0};
         for (int k = 0; k < p; ++k) {
           pw[k] = v;
@@ -279,10 +359,11 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   for (int xi = a.x_off[B]; xi < a.x_off[B + 1]; ++xi) {
     const int S = a.x_idx[xi];
     const int s0 = a.pstart[S], cnt = a.pcount[S];
+    const Cx<R> offS = box_off(a, B, S);  // z_j - z_B = (z_j - c_S) + (c_S - c_B)
     for (int j0 = 0; j0 < cnt; j0 += kStage) {
       const int jc = cnt - j0 < kStage ? cnt - j0 : kStage;
       for (int j = threadIdx.x; j < jc; j += blockDim.x) {
-        const Cx<R> iw = cinv(sub(pt_pos(a, s0 + j0 + j), zb));
+        const Cx<R> iw = cinv(cadd(vec(pt_pos(a, s0 + j0 + j)), offS));
         const Cx<R> r = cscale(iw, sB);
         Cx<R> v = iw;  // 1/w * r^l
         for (int l = 0; l < p; ++l) {
@@ -328,7 +409,7 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
   Cx<R>* hm = el + p;                          // p: (2e)^-m
   Cx<R>* bv = hm + p;                          // nrhs x p: L_l(P) e^l
   if (threadIdx.x < 2) {
-    const Cx<R> e = cscale(sub(box_pos(a, C), box_pos(a, P)), rcp(a.side[P]));
+    const Cx<R> e = cscale(box_off(a, P, C), rcp(side_of(a, P)));
     const Cx<R> base = threadIdx.x == 0 ? e : cinv(cscale(e, (R)2));
     Cx<R>* out = threadIdx.x == 0 ? el : hm;
     Cx<R> v = {(R)1, (R)0};
@@ -374,8 +455,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
   Pos<R>* sp = reinterpret_cast<Pos<R>*>(smem);                 // staged source positions
   R* sc = reinterpret_cast<R*>(sp + kStage);                    // kStage x kMaxRhs complex
   double* red = reinterpret_cast<double*>(sc + 2 * kStage * kMaxRhs);  // blockDim x kMaxRhs
-  const Pos<R> zb = box_pos(a, B);
-  const R isB = rcp(a.side[B]);
+  const R isB = rcp(side_of(a, B));
   const int nsplit = (cnt > 0 && 2 * cnt <= (int)blockDim.x) ? (int)blockDim.x / cnt : 1;
   const int span = nsplit > 1 ? cnt : (int)blockDim.x;  // targets per pass
   const int part = threadIdx.x / span, tj = threadIdx.x % span;
@@ -389,7 +469,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
     if (act) {
       tp = pt_pos(a, s0 + j);
       // L2P
-      const Cx<R> rho = cscale(sub(tp, zb), isB);
+      const Cx<R> rho = cscale(vec(tp), isB);
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) {
         if (q < nrhs && q % nsplit == part) {
@@ -402,8 +482,8 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
       // M2P from the W list
       for (int wi = a.w_off[B]; wi < a.w_off[B + 1]; ++wi) {
         const int C = a.w_idx[wi];
-        const Cx<R> iw = cinv(sub(tp, box_pos(a, C)));
-        const Cx<R> t = cscale(iw, a.side[C]);
+        const Cx<R> iw = cinv(cadd(vec(tp), box_off(a, C, B)));  // z - c_C
+        const Cx<R> t = cscale(iw, side_of(a, C));
 #pragma unroll
         for (int q = 0; q < kMaxRhs; ++q) {
           if (q < nrhs && q % nsplit == part) {
@@ -419,6 +499,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
     for (int ui = a.u_off[B]; ui < a.u_off[B + 1]; ++ui) {
       const int D = a.u_idx[ui];
       const int d0 = a.pstart[D], dcnt = a.pcount[D];
+      const auto offD = p2p_off(a, B, D);
       for (int i0 = 0; i0 < dcnt; i0 += kStage) {
         const int ic = dcnt - i0 < kStage ? dcnt - i0 : kStage;
         __syncthreads();
@@ -433,7 +514,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
         if (act) {
           for (int i = part; i < ic; i += nsplit) {
             if (d0 + i0 + i == s0 + j) continue;  // self
-            const Cx<R> iv = cinv(sub(tp, sp[i]));
+            const Cx<R> iv = cinv(diff(tp, sp[i], offD));
 #pragma unroll
             for (int q = 0; q < kMaxRhs; ++q)
               if (q < nrhs)
@@ -474,7 +555,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
 template <class R>
 cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs, double* y,
                     double ya, double yb, cudaStream_t st) {
-  constexpr bool f32 = sizeof(R) == 4;
+  constexpr bool f32 = std::is_same<R, float>::value;
   const int p = f32 ? f.p32 : f.p;
   const int npts = f.npts, nb = f.nbox;
   if (p < 2 || p * kMaxRhs > 4 * kFmmThreads) return cudaErrorInvalidValue;
@@ -490,23 +571,16 @@ cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nr
   FmmArgs<R> a{};
   a.cx = f.cx.p;
   a.cy = f.cy.p;
-  a.zx = f.zx.p;
-  a.zy = f.zy.p;
-  a.cxh = f.cxh.p;
-  a.cxl = f.cxl.p;
-  a.cyh = f.cyh.p;
-  a.cyl = f.cyl.p;
-  a.zxh = f.zxh.p;
-  a.zxl = f.zxl.p;
-  a.zyh = f.zyh.p;
-  a.zyl = f.zyl.p;
-  if constexpr (f32) {
-    a.side = f.side32.p;
-    a.binom = f.binom32.p;
-  } else {
-    a.side = f.side.p;
-    a.binom = f.binom.p;
-  }
+  a.side = f.side.p;
+  a.rx = f.rx.p;
+  a.ry = f.ry.p;
+  a.rxh = f.rxh.p;
+  a.rxl = f.rxl.p;
+  a.ryh = f.ryh.p;
+  a.ryl = f.ryl.p;
+  if constexpr (f32) a.binom = f.binom32.p;
+  else if constexpr (std::is_same<R, DF>::value) a.binom = reinterpret_cast<const DF*>(f.binom_df.p);
+  else a.binom = f.binom.p;
   a.pstart = f.pstart.p;
   a.pcount = f.pcount.p;
   a.parent = f.parent.p;
@@ -575,10 +649,14 @@ cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nr
 }  // namespace
 
 cudaError_t fmm_laplace_apply(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs,
-                              double* y, double ya, double yb, bool fp32, cudaStream_t st) {
+                              double* y, double ya, double yb, int arith, cudaStream_t st) {
   if (!f.built) return cudaErrorInvalidValue;
-  return fp32 ? apply_t<float>(f, geo, mu, nrhs, y, ya, yb, st)
-              : apply_t<double>(f, geo, mu, nrhs, y, ya, yb, st);
+  switch (arith) {
+    case kFmmF64: return apply_t<double>(f, geo, mu, nrhs, y, ya, yb, st);
+    case kFmmF32: return apply_t<float>(f, geo, mu, nrhs, y, ya, yb, st);
+    case kFmmDF: return apply_t<DF>(f, geo, mu, nrhs, y, ya, yb, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace rskel

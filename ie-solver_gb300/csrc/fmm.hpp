@@ -13,11 +13,14 @@
 // overflows for small boxes.  Boxes holding no points are left out of every
 // list: their expansions are zero and they have no targets.
 //
-// Two arithmetic variants share one plan: FP64 (order p) for the first,
-// full residual, and FP32 (order p32) for products with refinement
-// corrections, whose size is already ~1e-6 of the solution's.  The FP32
-// variant keeps every coordinate as an unevaluated float pair (hi + lo), so
-// differences of nearby points are exact to FP32 rounding.
+// Three arithmetic variants share one plan: FP64; float-float ("double
+// single": an unevaluated pair of floats carrying ~48 bits, run on the FP32
+// pipes, which GB300 has ~58x more of than FP64) for the full FP64-accurate
+// residual; and FP32 (order p32) for products with refinement corrections,
+// whose size is already ~1e-6 of the solution's.  Every point is stored
+// relative to the centre of its leaf (as FP64, and as a hi + lo float
+// pair), and box-centre offsets are formed in FP64, so differences of nearby
+// points keep their relative accuracy in every variant.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -30,8 +33,10 @@
 
 namespace rskel {
 
+enum FmmArith : int { kFmmF64 = 0, kFmmF32 = 1, kFmmDF = 2 };
+
 struct FmmPlan {
-  int p = 0;          // expansion order, FP64 variant
+  int p = 0;          // expansion order, FP64 and float-float variants
   int p32 = 0;        // expansion order, FP32 variant
   int nbox = 0;
   int npts = 0;
@@ -39,14 +44,13 @@ struct FmmPlan {
   bool built = false;
   // per box (tree node id order)
   DevBuf<double> cx, cy, side;
-  DevBuf<float> cxh, cxl, cyh, cyl, side32;
   DevBuf<int> pstart, pcount;  // leaf point ranges in slot order (count 0: not a leaf)
   DevBuf<int> parent;
   DevBuf<int> children;        // 4 per box, -1 for leaves or empty children
   // slot order of points (leaf by leaf)
   DevBuf<int> slot_pt;         // slot -> point
-  DevBuf<double> zx, zy;       // slot coordinates
-  DevBuf<float> zxh, zxl, zyh, zyl;
+  DevBuf<double> rx, ry;       // slot coordinates relative to the leaf centre
+  DevBuf<float> rxh, rxl, ryh, ryl;  // the same as hi + lo float pairs
   // interaction lists (CSR over boxes)
   DevBuf<int> v_off, v_idx, w_off, w_idx, x_off, x_idx, u_off, u_idx;
   // non-empty boxes grouped by level (tree passes)
@@ -57,9 +61,10 @@ struct FmmPlan {
   std::vector<int> m2l_boxes_h;
   DevBuf<int> m2l_boxes;       // boxes with non-empty V or X lists
   DevBuf<double> binom;        // (2p) x (2p), binom[a * 2p + b] = C(a, b)
+  DevBuf<float> binom_df;      // the same table as hi + lo pairs
   DevBuf<float> binom32;       // (2 p32) x (2 p32)
   size_t v_pairs = 0, u_pairs = 0, w_pairs = 0, x_pairs = 0;
-  // work buffers (complex Real pairs; sized for FP64)
+  // work buffers (complex pairs of the variant's number type; sized for FP64)
   DevBuf<double> charge;       // 2 * (slot + npts * rhs)
   DevBuf<double> mpole, local; // 2 * (k + p * (rhs + nrhs * box))
 };
@@ -70,9 +75,9 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
                cudaStream_t st);
 
 // y[:, q] = ya * y[:, q] + yb * (K mu)[:, q] for the Laplace double layer
-// (device pointers, column major npts x nrhs; y is not read when ya == 0).
-// fp32 selects the FP32 variant.  geo holds the per-point boundary data.
+// (device pointers, column major npts x nrhs; y is not read when ya == 0),
+// in the arithmetic `arith` (FmmArith).  geo holds the per-point boundary data.
 cudaError_t fmm_laplace_apply(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs,
-                              double* y, double ya, double yb, bool fp32, cudaStream_t st);
+                              double* y, double ya, double yb, int arith, cudaStream_t st);
 
 }  // namespace rskel

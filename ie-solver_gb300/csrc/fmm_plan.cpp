@@ -139,15 +139,7 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
     *hi = (float)v;
     *lo = (float)(v - (double)*hi);
   };
-  std::vector<double> zx(npts), zy(npts), cx(nb), cy(nb), side(nb);
-  std::vector<float> zxh(npts), zxl(npts), zyh(npts), zyl(npts);
-  std::vector<float> cxh(nb), cxl(nb), cyh(nb), cyl(nb), side32(nb);
-  for (int s = 0; s < npts; ++s) {
-    zx[s] = points[2 * slot_pt[s]];
-    zy[s] = points[2 * slot_pt[s] + 1];
-    split(zx[s], &zxh[s], &zxl[s]);
-    split(zy[s], &zyh[s], &zyl[s]);
-  }
+  std::vector<double> cx(nb), cy(nb), side(nb);
   std::vector<int> parent(nb), children(4 * (size_t)nb, -1);
   for (int i = 0; i < nb; ++i) {
     if (!tree.nodes[i].is_leaf)
@@ -158,11 +150,18 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
     cx[i] = box[i].x0 + box[i].s / 2.0;
     cy[i] = box[i].y0 + box[i].s / 2.0;
     side[i] = box[i].s;
-    split(cx[i], &cxh[i], &cxl[i]);
-    split(cy[i], &cyh[i], &cyl[i]);
-    side32[i] = (float)side[i];
     parent[i] = tree.nodes[i].parent;
   }
+  // coordinates relative to the leaf centre
+  std::vector<double> rx(npts), ry(npts);
+  std::vector<float> rxh(npts), rxl(npts), ryh(npts), ryl(npts);
+  for (int leaf : f.leaves_h)
+    for (int s2 = pstart[leaf]; s2 < pstart[leaf] + pcount[leaf]; ++s2) {
+      rx[s2] = points[2 * slot_pt[s2]] - cx[leaf];
+      ry[s2] = points[2 * slot_pt[s2] + 1] - cy[leaf];
+      split(rx[s2], &rxh[s2], &rxl[s2]);
+      split(ry[s2], &ryh[s2], &ryl[s2]);
+    }
   // non-empty boxes by level
   f.nlevels = (int)tree.levels.size();
   std::vector<int> lvl_flat;
@@ -197,24 +196,24 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
   std::vector<double> binom, b32d;
   pascal(2 * p, &binom);
   pascal(2 * p32, &b32d);
-  std::vector<float> binom32(b32d.begin(), b32d.end());
+  std::vector<float> binom32(b32d.begin(), b32d.end()), binom_df(2 * binom.size());
+  for (size_t i = 0; i < binom.size(); ++i) split(binom[i], &binom_df[2 * i], &binom_df[2 * i + 1]);
   bool ok = upload(f.cx, cx) == cudaSuccess && upload(f.cy, cy) == cudaSuccess &&
-            upload(f.side, side) == cudaSuccess && upload(f.cxh, cxh) == cudaSuccess &&
-            upload(f.cxl, cxl) == cudaSuccess && upload(f.cyh, cyh) == cudaSuccess &&
-            upload(f.cyl, cyl) == cudaSuccess && upload(f.side32, side32) == cudaSuccess &&
-            upload(f.pstart, pstart) == cudaSuccess && upload(f.pcount, pcount) == cudaSuccess &&
-            upload(f.parent, parent) == cudaSuccess && upload(f.children, children) == cudaSuccess &&
-            upload(f.slot_pt, slot_pt) == cudaSuccess && upload(f.zx, zx) == cudaSuccess &&
-            upload(f.zy, zy) == cudaSuccess && upload(f.zxh, zxh) == cudaSuccess &&
-            upload(f.zxl, zxl) == cudaSuccess && upload(f.zyh, zyh) == cudaSuccess &&
-            upload(f.zyl, zyl) == cudaSuccess && upload(f.v_off, vo) == cudaSuccess &&
+            upload(f.side, side) == cudaSuccess && upload(f.pstart, pstart) == cudaSuccess &&
+            upload(f.pcount, pcount) == cudaSuccess && upload(f.parent, parent) == cudaSuccess &&
+            upload(f.children, children) == cudaSuccess &&
+            upload(f.slot_pt, slot_pt) == cudaSuccess && upload(f.rx, rx) == cudaSuccess &&
+            upload(f.ry, ry) == cudaSuccess && upload(f.rxh, rxh) == cudaSuccess &&
+            upload(f.rxl, rxl) == cudaSuccess && upload(f.ryh, ryh) == cudaSuccess &&
+            upload(f.ryl, ryl) == cudaSuccess && upload(f.v_off, vo) == cudaSuccess &&
             upload(f.v_idx, vi) == cudaSuccess && upload(f.w_off, wo) == cudaSuccess &&
             upload(f.w_idx, wi) == cudaSuccess && upload(f.x_off, xo) == cudaSuccess &&
             upload(f.x_idx, xi) == cudaSuccess && upload(f.u_off, uo) == cudaSuccess &&
             upload(f.u_idx, ui) == cudaSuccess && upload(f.lvl_boxes, lvl_flat) == cudaSuccess &&
             upload(f.leaves, f.leaves_h) == cudaSuccess &&
             upload(f.m2l_boxes, f.m2l_boxes_h) == cudaSuccess &&
-            upload(f.binom, binom) == cudaSuccess && upload(f.binom32, binom32) == cudaSuccess;
+            upload(f.binom, binom) == cudaSuccess && upload(f.binom_df, binom_df) == cudaSuccess &&
+            upload(f.binom32, binom32) == cudaSuccess;
   f.built = ok;
   return ok;
 }

@@ -1017,7 +1017,7 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
                    int nrhs, double* r, double* rg) {
   const int D = s->D;
   if (s->fmm.built) {
-    CU(fmm_laplace_apply(s->fmm, geo_of(s), mu, nrhs, r, 0.0, 1.0, false, s->stream));
+    CU(fmm_laplace_apply(s->fmm, geo_of(s), mu, nrhs, r, 0.0, 1.0, kFmmDF, s->stream));
     s->launches += 5 + 2 * s->fmm.nlevels;
   } else {
     launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, mu, nrhs, r, s->stream);
@@ -1040,12 +1040,12 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
 
 // Residual recurrence for a refinement correction (x, xa) of (mu, alpha):
 // r -= K x + U xa and rg -= Psi x - xa, with K x from the FP32 multipole
-// variant (the correction is ~1e-6 of the solution, so FP32 accuracy of the
+// variant (the full residual uses the float-float variant) (the correction is ~1e-6 of the solution, so FP32 accuracy of the
 // product leaves the residual exact to ~1e-13 of the data).
 rs_status residual_update(rs_solver* s, const double* x, const double* xa, int nrhs, double* r,
                           double* rg, double* g) {
   const int D = s->D;
-  CU(fmm_laplace_apply(s->fmm, geo_of(s), x, nrhs, r, 1.0, -1.0, true, s->stream));
+  CU(fmm_laplace_apply(s->fmm, geo_of(s), x, nrhs, r, 1.0, -1.0, kFmmF32, s->stream));
   s->launches += 5 + 2 * s->fmm.nlevels;
   if (s->nb > 0) {
     const int nb = s->nb;
@@ -1549,8 +1549,8 @@ rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y) {
   return RS_OK;
 }
 
-rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int fp32) {
-  if (!s || !x || !y || nrhs < 1 || fp32 < 0 || fp32 > 1)
+rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int arith) {
+  if (!s || !x || !y || nrhs < 1 || arith < 0 || arith > 2)
     return fail(s, RS_ERR_ARG, "bad matvec arguments");
   if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
   if (s->cfg.pde != kLaplace) return rs_matvec(s, x, nrhs, y);
@@ -1571,7 +1571,7 @@ rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int
   CU(dx.ensure(nd));
   CU(dy.ensure(nd));
   CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
-  CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, fp32 == 1, s->stream));
+  CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, arith, s->stream));
   CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   return RS_OK;

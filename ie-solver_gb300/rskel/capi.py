@@ -246,14 +246,17 @@ class Solver:
         self._check(lib().rs_kernel_block(self.h, _i(I), I.size, _i(J), J.size, _d(out)))
         return out
 
-    def matvec(self, x, fast=False, fp32=False):
+    def matvec(self, x, fast=False, fp32=False, arith=None):
+        """K x: dense FP64, or (fast=True) through the fast multipole method in
+        arithmetic `arith` (0 FP64, 1 FP32, 2 float-float; fp32=True is 1)."""
         x = np.asfortranarray(x, dtype=np.float64)
         sq = x.ndim == 1
         if sq:
             x = x[:, None]
         y = np.zeros_like(x, order="F")
         if fast:
-            self._check(lib().rs_matvec_fast(self.h, _d(x), x.shape[1], _d(y), int(fp32)))
+            a = (1 if fp32 else 0) if arith is None else int(arith)
+            self._check(lib().rs_matvec_fast(self.h, _d(x), x.shape[1], _d(y), a))
         else:
             self._check(lib().rs_matvec(self.h, _d(x), x.shape[1], _d(y)))
         return y[:, 0] if sq else y

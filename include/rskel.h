@@ -125,12 +125,13 @@ rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int 
 rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
 
 /* y = K x through the fast multipole method used by the refinement (Laplace);
- * falls back to rs_matvec for other kernels.  fp32 = 0: the FP64 variant of
- * the full residual (order rs_config.fmm_order); fp32 = 1: the FP32 variant
- * used for products with refinement corrections (~1e-7 relative).  No
- * reference counterpart: the reference applies K only densely in its tests
- * (ie_solver_test.cpp:87-95). */
-rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int fp32);
+ * falls back to rs_matvec for other kernels.  arith = 0: FP64; 2: float-float
+ * (pairs of floats, ~48-bit significands, on the FP32 pipes), the variant of
+ * the refinement's full residual; both at order rs_config.fmm_order.
+ * arith = 1: the FP32 variant used for products with refinement corrections
+ * (~1e-7 relative).  No reference counterpart: the reference applies K only
+ * densely in its tests (ie_solver_test.cpp:87-95). */
+rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int arith);
 
 /* The solution at points off the boundary, as boundary_integral_solve
  * assembles it (linear_solve.cpp:188-266, schur_solve 140-154):

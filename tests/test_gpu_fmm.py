@@ -1,10 +1,11 @@
 """GPU: the FP64 fast multipole Laplace double-layer product used for the
 refinement residual, against the dense FP64 product (rs_matvec).
 
-Tolerances: FP64 variant, max |y_fmm - y_dense| <= 1e-10 max |y_dense| per
-column at the default order (32; measured ~1e-13 on the 65536-point star);
-lower orders must be no more accurate than higher ones.  FP32 variant (used
-only for products with refinement corrections): <= 2e-6 of max |y_dense|.
+Tolerances: FP64 and float-float variants, max |y_fmm - y_dense| <= 1e-10
+max |y_dense| per column at the default order (31; measured ~1e-13 on the
+65536-point star); lower orders must be no more accurate than higher ones.
+FP32 variant (used only for products with refinement corrections): <= 2e-6
+of max |y_dense|.
 """
 import numpy as np
 import pytest
@@ -26,7 +27,9 @@ def test_fmm_matches_dense_golden(name, solver_lib):
     pde, sd, leaf, npp = (int(x) for x in d["meta"][:4])
     s = solver_lib.Solver(geo, pde, float(d["tol"][0]), leaf=leaf, npp=npp)
     x = np.random.default_rng(3).standard_normal((s.D, 3))
-    assert _rel(s.matvec(x, fast=True), s.matvec(x)) <= 1e-10
+    z = s.matvec(x)
+    assert _rel(s.matvec(x, fast=True), z) <= 1e-10
+    assert _rel(s.matvec(x, fast=True, arith=2), z) <= 1e-10
 
 
 def test_fmm_large_star_many_rhs(solver_lib):
@@ -37,6 +40,7 @@ def test_fmm_large_star_many_rhs(solver_lib):
     y = s.matvec(x, fast=True)
     z = s.matvec(x)
     assert _rel(y, z) <= 1e-10
+    assert _rel(s.matvec(x, fast=True, arith=2), z) <= 1e-10
     # column independence: the second pass equals a one-column product
     y9 = s.matvec(x[:, 9], fast=True)
     assert np.abs(y9 - y[:, 9]).max() <= 1e-13 * np.abs(y[:, 9]).max()
