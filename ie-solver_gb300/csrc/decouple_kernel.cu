@@ -134,8 +134,104 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     Msr[i + ld * j] = acc;
   }
   __syncthreads();
-  // 4) LU of X_rr with partial pivoting (dgetrf), in place.
   if (threadIdx.x == 0) scal[0] = 0.0;
+  if constexpr (sizeof(Real) == 4) {
+    // FP32 factorization: X_rr is inverted explicitly (Gauss-Jordan with
+    // partial pivoting), so that U_f, L_f and the solve's diagonal step are
+    // matrix products spread over the whole CTA instead of one warp-serial
+    // triangular solve per column.  The refinement absorbs the explicit
+    // inverse's slightly larger rounding error.
+    Real* colj = T;  // T is no longer needed; it holds >= r entries
+    __shared__ int s_p;
+    for (int j = 0; j < r; ++j) {
+      if (warp == 0) {
+        float best = -1.f;
+        int bi = r;
+        for (int i = j + lane; i < r; i += 32) {
+          const float v = fabsf(Mrr[i + ld * j]);
+          if (v > best || (v == best && i < bi)) { best = v; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) {
+          piv[j] = bi;
+          s_p = bi;
+          if (!(best > 0.f) || !isfinite(best)) scal[0] = 1.0;
+        }
+      }
+      __syncthreads();
+      const int pj = s_p;
+      if (pj != j) {
+        for (int c = threadIdx.x; c < r; c += blockDim.x) {
+          const Real tmp = Mrr[j + ld * c];
+          Mrr[j + ld * c] = Mrr[pj + ld * c];
+          Mrr[pj + ld * c] = tmp;
+        }
+        __syncthreads();
+      }
+      const Real d = Mrr[j + ld * j];
+      const Real inv = d != (Real)0 ? (Real)1 / d : (Real)0;
+      for (int i = threadIdx.x; i < r; i += blockDim.x) colj[i] = i == j ? (Real)0 : Mrr[i + ld * j];
+      __syncthreads();
+      for (int c = threadIdx.x; c < r; c += blockDim.x)
+        Mrr[j + ld * c] = (c == j ? (Real)1 : Mrr[j + ld * c]) * inv;
+      __syncthreads();
+      for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+        const int i = e % r, c = e / r;
+        if (i == j) continue;
+        const Real a = c == j ? (Real)0 : Mrr[i + ld * c];
+        Mrr[i + ld * c] = a - colj[i] * Mrr[j + ld * c];
+      }
+      __syncthreads();
+    }
+    // undo the row interchanges on the inverse's columns, last first
+    for (int j = r - 1; j >= 0; --j) {
+      const int pj = piv[j];
+      if (pj != j)
+        for (int i = threadIdx.x; i < r; i += blockDim.x) {
+          const Real tmp = Mrr[i + ld * j];
+          Mrr[i + ld * j] = Mrr[i + ld * pj];
+          Mrr[i + ld * pj] = tmp;
+        }
+      __syncthreads();
+    }
+    Real* Lo = fac + fac_L(k, r);
+    Real* Uo = fac + fac_U(k, r);
+    Real* Xo = fac + fac_X(k, r);
+    // U_f = X^{-1} K_r_sn (r x k) and L_f = K_sn_r X^{-1} (k x r), to the record
+    for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
+      const int i = e % r, j = e / r;
+      Real acc = 0;
+      for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
+      Uo[e] = acc;
+    }
+    for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
+      const int i = e % k, j = e / k;
+      Real acc = 0;
+      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrr[l + ld * j];
+      Lo[e] = acc;
+    }
+    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+      const int i = e % r, j = e / r;
+      Xo[e] = Mrr[i + ld * j];
+    }
+    __syncthreads();  // U_f is read back below (same CTA)
+    // E = Mss - K_sn_r U_f  (k x k)
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+      const int i = e % k, j = e / k;
+      Real acc = Mss[i + ld * j];
+      for (int l = 0; l < r; ++l) acc -= Msr[i + ld * l] * Uo[l + (size_t)r * j];
+      E_out[e] = acc;
+    }
+    for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = j;
+    if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
+    return;
+  }
+  // 4) LU of X_rr with partial pivoting (dgetrf), in place.
   for (int j = 0; j < r; ++j) {
     if (warp == 0) {
       double best = -1.0;

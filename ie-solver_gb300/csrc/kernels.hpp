@@ -60,7 +60,7 @@ struct SweepParams {
   void* x;          // Real, D x nrhs, column major
   int ld, nrhs;
   int mode;
-  int stage_x;      // set by launch_sweep: X_rr's LU factors staged in shared memory
+  int stage_fac;    // set by launch_sweep: each box's factor record staged in shared memory
 };
 
 size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem);

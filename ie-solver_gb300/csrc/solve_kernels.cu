@@ -41,26 +41,52 @@ __device__ void lu_solve_cols(const Real* X, const int* piv, int r, Real* y, int
   }
 }
 
+// x_r <- X_rr^{-1} x_r for cb columns: an LU solve with the FP64 factors
+// (the reference's apply_diag_inv_matrix, skel_factorization.cpp:419-426),
+// a product with the explicit inverse the FP32 factorization stores.
 template <class Real>
-__global__ void __launch_bounds__(kThreads) sweep_kernel(SweepParams p) {
+__device__ void diag_solve(const Real* X, const int* piv, int r, Real* xr, Real* xt, int cb) {
+  if constexpr (sizeof(Real) == 4) {
+    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {
+      const int i = e % r, c = e / r;
+      Real acc = 0;
+      for (int l = 0; l < r; ++l) acc += X[i + (size_t)r * l] * xr[l + r * c];
+      xt[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) xr[e] = xt[e];
+  } else {
+    (void)xt;
+    lu_solve_cols<Real>(X, piv, r, xr, r, cb);
+  }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   const SweepTask t = p.tasks[blockIdx.x];
   const int k = t.k, r = t.r;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
   Real* xs = carve<Real>(sp, k * kRhsBlock);
   Real* xr = carve<Real>(sp, r * kRhsBlock);
+  Real* xt = carve<Real>(sp, r * kRhsBlock);
   int* piv = carve<int>(sp, r);
   const Real* fac = reinterpret_cast<const Real*>(p.fac) + t.fac_off;
   const Real* T = fac + fac_T(k, r);
   const Real* L = fac + fac_L(k, r);
   const Real* U = fac + fac_U(k, r);
   const Real* X = fac + fac_X(k, r);
-  // The triangular solves with X_rr are chains of dependent steps: one bulk
-  // copy to shared memory replaces a global round trip per step.
-  if (p.stage_x && (p.mode == kUpSolve || p.mode == kDiagOnly)) {
-    Real* xsh = carve<Real>(sp, r * r);
-    for (int e = threadIdx.x; e < r * r; e += blockDim.x) xsh[e] = X[e];
-    X = xsh;
+  // The box's factor record (T, L, U and X_rr's LU, contiguous) is copied to
+  // shared memory in one coalesced pass: the products and the triangular
+  // solves below then read it without a global round trip per step.
+  if (p.stage_fac) {
+    const int len = (int)(fac_X(k, r) + (int64_t)r * r);
+    Real* fsh = carve<Real>(sp, len);
+    for (int e = threadIdx.x; e < len; e += blockDim.x) fsh[e] = fac[e];
+    T = fsh + fac_T(k, r);
+    L = fsh + fac_L(k, r);
+    U = fsh + fac_U(k, r);
+    X = fsh + fac_X(k, r);
   }
   Real* x = reinterpret_cast<Real*>(p.x);
   const int* sk = p.dofs + t.skel_off;
@@ -96,11 +122,11 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(SweepParams p) {
       }
       __syncthreads();
       if (p.mode == kUpSolve) {
-        lu_solve_cols<Real>(X, piv, r, xr, r, cb);
+        diag_solve<Real>(X, piv, r, xr, xt, cb);
         __syncthreads();
       }
     } else if (p.mode == kDiagOnly) {
-      lu_solve_cols<Real>(X, piv, r, xr, r, cb);
+      diag_solve<Real>(X, piv, r, xr, xt, cb);
       __syncthreads();
     } else {  // kDown
       for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {  // x_r -= U x_s
@@ -134,12 +160,12 @@ __global__ void __launch_bounds__(kThreads) sweep_kernel(SweepParams p) {
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st) {
   if (num_tasks <= 0) return;
   size_t es = fp32 ? sizeof(float) : sizeof(double);
-  size_t smem = 2 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
+  size_t smem = 3 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
                 ((sizeof(int) * nmax + 15) & ~size_t(15)) + 64;
   SweepParams q = p;
-  const size_t xb = ((size_t)nmax * nmax * es + 15) & ~size_t(15);
-  q.stage_x = (p.mode == kUpSolve || p.mode == kDiagOnly) && smem + xb <= (size_t)kSmemOptIn;
-  if (q.stage_x) smem += xb;
+  const size_t fb = ((size_t)fac_reserve(nmax) * es + 15) & ~size_t(15);
+  q.stage_fac = smem + fb <= (size_t)kSmemOptIn;
+  if (q.stage_fac) smem += fb;
   if (fp32) {
     set_smem_once<sweep_kernel<float>>();
     sweep_kernel<float><<<num_tasks, kThreads, smem, st>>>(q);

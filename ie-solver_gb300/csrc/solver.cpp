@@ -116,6 +116,8 @@ struct rs_solver {
   HostBuf<double> h_io;
 
   FmmPlan fmm;
+  HostBuf<unsigned char> stage;  // pinned staging of a factorization's host-to-device uploads
+  size_t stage_used = 0;
   bool incremental = false;      // next rs_factor keeps the boxes rs_perturb left compressed
   size_t full_fac_used = 0;      // factor storage of the last full factorization
   DevBuf<float> sketch_y;  // FP32 split ID: per-level sketches
@@ -282,13 +284,32 @@ void id_rows(rs_solver* s, int id, std::vector<int>* rows, int* use_proxy) {
   *use_proxy = 1;
 }
 
+// Host-to-device copy through the pinned staging buffer: a copy from pinned
+// memory is asynchronous, so a level's uploads no longer wait for the DMA.
+// Regions are handed out in order during one factorization (which ends with
+// a stream synchronisation), so no region is reused while its copy is in
+// flight; growing the buffer waits for the stream first.
+cudaError_t stage_copy(rs_solver* s, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return cudaSuccess;
+  size_t off = (s->stage_used + 255) & ~size_t(255);
+  if (off + bytes > s->stage.cap) {
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return e;
+    e = s->stage.ensure(std::max<size_t>(2 * s->stage.cap, bytes + 4096));
+    if (e != cudaSuccess) return e;
+    off = 0;
+  }
+  std::memcpy(s->stage.p + off, src, bytes);
+  s->stage_used = off + bytes;
+  return cudaMemcpyAsync(dst, s->stage.p + off, bytes, cudaMemcpyHostToDevice, s->stream);
+}
+
 rs_status upload_pool(rs_solver* s, size_t from) {
   size_t to = s->pool.size();
   if (to == from) return RS_OK;
   CU(s->dofs.ensure_keep(to, from, s->stream));
   CU(s->perm.ensure_keep(to, from, s->stream));
-  CU(cudaMemcpyAsync(s->dofs.p + from, s->pool.data() + from, (to - from) * sizeof(int),
-                     cudaMemcpyHostToDevice, s->stream));
+  CU(stage_copy(s, s->dofs.p + from, s->pool.data() + from, (to - from) * sizeof(int)));
   return RS_OK;
 }
 
@@ -357,6 +378,7 @@ rs_status factor_impl(rs_solver* s) {
     F.e_used = 0;
     s->piv_used = 0;
   }
+  s->stage_used = 0;
   s->pool.clear();
   s->stats.id_flops = 0;
   s->stats.decouple_flops = 0;
@@ -377,6 +399,7 @@ rs_status factor_impl(rs_solver* s) {
   // Contents below these marks are live and survive buffer growth.
   size_t fac_prev = F.fac_used, e_prev = F.e_used, piv_prev = s->piv_used;
   double t_plan = 0, t_wait = 0, t_post = 0;
+  double t_detail[4] = {0, 0, 0, 0};  // lists, task records, sorting/scratch, uploads+launches
   while ((int)s->lv_ev.size() < 3 * L) {
     cudaEvent_t e;
     CU(cudaEventCreate(&e));
@@ -388,10 +411,10 @@ rs_status factor_impl(rs_solver* s) {
     const std::vector<int>& lvl = s->tree.levels[lv];
     const int nl = (int)lvl.size();
     // Per-box list construction is independent across the boxes of a level.
-#pragma omp parallel for schedule(dynamic, 32) if (nl > 256)
+#pragma omp parallel for schedule(dynamic, 16) if (nl > 96)
     for (int q = 0; q < nl; ++q)
       if (!s->st[lvl[q]].compressed) compute_active(s, lvl[q]);
-#pragma omp parallel for schedule(dynamic, 32) if (nl > 256)
+#pragma omp parallel for schedule(dynamic, 16) if (nl > 96)
     for (int q = 0; q < nl; ++q) {
       const int id = lvl[q];
       compute_near(s, id);
@@ -399,6 +422,7 @@ rs_status factor_impl(rs_solver* s) {
       if (!S.compressed && (int)S.active.size() >= s->cfg.min_dofs_to_compress)
         id_rows(s, id, &S.rows, &S.use_proxy);
     }
+    const double h_lists = now_ms();
     idt.clear();
     dct.clear();
     blk.clear();
@@ -408,76 +432,116 @@ rs_status factor_impl(rs_solver* s) {
     const size_t seg0 = s->pool.size();
     const int npp = s->cfg.num_proxy_points;
     const int prow = (s->cfg.pde == kStokes ? 2 : 1) * npp;
-    for (int id : lvl) {
+    // Offsets first (a serial prefix pass), then the task records and the
+    // pool / block-reference copies, which are independent across boxes.
+    struct Slots {
+      int kind = 0;  // 0: nothing to do, 1: Schur assembly only, 2: ID + elimination
+      int slot = -1, dci = -1, blk_off = 0;
+      size_t act_off = 0, rows_off = 0;
+    };
+    std::vector<Slots> pl(nl);
+    size_t pool_end = seg0, blk_end = 0;
+    int nslots = 0, ndc = 0;
+    for (int q = 0; q < nl; ++q) {
+      const int id = lvl[q];
       NodeState& S = s->st[id];
       if (S.compressed) continue;  // kept from before rs_perturb
       const TreeNode& nd = s->tree.nodes[id];
       const int n = (int)S.active.size();
-      const bool cand = !S.compressed && n >= s->cfg.min_dofs_to_compress;
+      const bool cand = n >= s->cfg.min_dofs_to_compress;
       if (!cand && nd.is_leaf) {
         S.e_ld = 0;
         continue;
       }
-      const int act_off = (int)s->pool.size();
-      s->pool.insert(s->pool.end(), S.active.begin(), S.active.end());
+      Slots& P = pl[q];
+      P.kind = cand ? 2 : 1;
+      P.act_off = pool_end;
+      pool_end += n;
       S.fac_off = -1;
       S.slot = -1;
       if (cand) {
-        const std::vector<int>& rows = S.rows;
-        const int use_proxy = S.use_proxy;
-        const int rows_off = (int)s->pool.size();
-        s->pool.insert(s->pool.end(), rows.begin(), rows.end());
+        P.rows_off = pool_end;
+        pool_end += S.rows.size();
+        P.slot = nslots++;
+        S.slot = P.slot;
+        S.fac_off = (int64_t)F.fac_used;
+        F.fac_used += fac_reserve(n);
+      }
+      P.dci = ndc++;
+      P.blk_off = (int)blk_end;
+      blk_end += n;
+      S.piv_off = (int64_t)s->piv_used;
+      s->piv_used += n;
+      S.e_off = (int64_t)F.e_used;
+      F.e_used += (size_t)n * n;
+      s->stats.max_active = std::max(s->stats.max_active, n);
+    }
+    s->pool.resize(pool_end);
+    idt.resize(nslots);
+    m_of_slot.resize(nslots);
+    cand_ids.resize(nslots);
+    dct.resize(ndc);
+    dc_ids.resize(ndc);
+    blk.resize(blk_end);
+    int max_rows = s->stats.max_rows;
+#pragma omp parallel for schedule(dynamic, 16) reduction(max : max_rows) if (nl > 96)
+    for (int q = 0; q < nl; ++q) {
+      const Slots& P = pl[q];
+      if (P.kind == 0) continue;
+      const int id = lvl[q];
+      const NodeState& S = s->st[id];
+      const TreeNode& nd = s->tree.nodes[id];
+      const int n = (int)S.active.size();
+      std::copy(S.active.begin(), S.active.end(), s->pool.begin() + P.act_off);
+      if (P.kind == 2) {
+        std::copy(S.rows.begin(), S.rows.end(), s->pool.begin() + P.rows_off);
         IdTask t{};
         t.n = n;
-        t.act_off = act_off;
-        t.q = (int)rows.size();
-        t.rows_off = rows_off;
-        t.use_proxy = use_proxy;
-        t.slot = (int)idt.size();
+        t.act_off = (int)P.act_off;
+        t.q = (int)S.rows.size();
+        t.rows_off = (int)P.rows_off;
+        t.use_proxy = S.use_proxy;
+        t.slot = P.slot;
         t.cx = nd.corners[0] + nd.side / 2.0;
         t.cy = nd.corners[1] + nd.side / 2.0;
         t.pr = nd.side * s->cfg.radius_ratio;
-        t.fac_off = (int64_t)F.fac_used;
+        t.fac_off = S.fac_off;
         t.scratch_off = -1;
         t.dense_off = -1;
         t.m_dense = 0;
-        F.fac_used += fac_reserve(n);
-        S.slot = t.slot;
-        S.fac_off = t.fac_off;
-        const int m = 2 * t.q + (use_proxy ? 2 * prow : 0);
-        m_of_slot.push_back(m);
-        s->stats.max_rows = std::max(s->stats.max_rows, m);
-        idt.push_back(t);
-        cand_ids.push_back(id);
+        const int m = 2 * t.q + (S.use_proxy ? 2 * prow : 0);
+        m_of_slot[P.slot] = m;
+        max_rows = std::max(max_rows, m);
+        idt[P.slot] = t;
+        cand_ids[P.slot] = id;
       }
       DecoupleTask d{};
       d.n = n;
-      d.act_off = act_off;
-      d.blk_off = (int)blk.size();
+      d.act_off = (int)P.act_off;
+      d.blk_off = P.blk_off;
       d.slot = S.slot;
-      d.perm_off = act_off;
+      d.perm_off = (int)P.act_off;
       d.fac_off = S.fac_off;
-      d.piv_off = (int64_t)s->piv_used;
-      s->piv_used += n;
-      d.e_off = (int64_t)F.e_used;
-      F.e_used += (size_t)n * n;
+      d.piv_off = S.piv_off;
+      d.e_off = S.e_off;
       d.scratch_off = -1;
-      S.piv_off = d.piv_off;
-      S.e_off = d.e_off;
+      BlkRef* br = blk.data() + P.blk_off;
       if (nd.is_leaf) {
-        for (int j = 0; j < n; ++j) blk.push_back(BlkRef{0, j, 0, 0, -1});
+        for (int j = 0; j < n; ++j) br[j] = BlkRef{0, j, 0, 0, -1};
       } else {
+        int o = 0;
         for (int c = 0; c < 4; ++c) {
           const NodeState& C = s->st[nd.children[c]];
           const std::vector<int>& v = surviving(C);
           for (int j = 0; j < (int)v.size(); ++j)
-            blk.push_back(BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1});
+            br[o++] = BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1};
         }
       }
-      dct.push_back(d);
-      dc_ids.push_back(id);
-      s->stats.max_active = std::max(s->stats.max_active, n);
+      dct[P.dci] = d;
+      dc_ids[P.dci] = id;
     }
+    s->stats.max_rows = max_rows;
+    const double h_tasks = now_ms();
     if (dct.empty()) continue;
     // sort by size for binned launches (slots keep their identity)
     std::vector<size_t> oi(idt.size()), od(dct.size());
@@ -517,6 +581,7 @@ rs_status factor_impl(rs_solver* s) {
         scratch_need += (size_t)(t.n + 1) * (t.n + 1) * 2;
       }
     // upload
+    const double h_sort = now_ms();
     RSCHK(upload_pool(s, seg0));
     CU(F.fac.ensure_keep(F.fac_used, fac_prev, s->stream));
     CU(F.epool.ensure_keep(F.e_used, e_prev, s->stream));
@@ -529,14 +594,9 @@ rs_status factor_impl(rs_solver* s) {
     CU(s->dc_tasks.ensure(dct_s.size()));
     CU(s->blk.ensure(std::max<size_t>(blk.size(), 1)));
     CU(s->ranks.ensure(std::max<size_t>(idt_s.size(), 1)));
-    if (!idt_s.empty())
-      CU(cudaMemcpyAsync(s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask),
-                         cudaMemcpyHostToDevice, s->stream));
-    CU(cudaMemcpyAsync(s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask),
-                       cudaMemcpyHostToDevice, s->stream));
-    if (!blk.empty())
-      CU(cudaMemcpyAsync(s->blk.p, blk.data(), blk.size() * sizeof(BlkRef),
-                         cudaMemcpyHostToDevice, s->stream));
+    CU(stage_copy(s, s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask)));
+    CU(stage_copy(s, s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask)));
+    CU(stage_copy(s, s->blk.p, blk.data(), blk.size() * sizeof(BlkRef)));
     // ID launches
     IdParams ip{};
     ip.geo = geo_of(s);
@@ -610,6 +670,10 @@ rs_status factor_impl(rs_solver* s) {
     CU(cudaGetLastError());
     CU(cudaEventRecord(s->lv_ev[3 * lv + 2], s->stream));
     const double h1 = now_ms();
+    t_detail[0] += h_lists - h0;
+    t_detail[1] += h_tasks - h_lists;
+    t_detail[2] += h_sort - h_tasks;
+    t_detail[3] += h1 - h_sort;
     CU(cudaEventSynchronize(s->ev_c));
     const double h2 = now_ms();
     t_plan += h1 - h0;
@@ -677,8 +741,10 @@ rs_status factor_impl(rs_solver* s) {
   s->host_wait_ms = t_wait;
   s->host_post_ms = t_post;
   if (s->trace)
-    std::fprintf(stderr, "[rskel] host: plan+launch %.3f ms, wait %.3f ms, post %.3f ms\n", t_plan,
-                 t_wait, t_post);
+    std::fprintf(stderr,
+                 "[rskel] host: plan+launch %.3f ms (lists %.3f, tasks %.3f, sort %.3f, upload+launch "
+                 "%.3f), wait %.3f ms, post %.3f ms\n",
+                 t_plan, t_detail[0], t_detail[1], t_detail[2], t_detail[3], t_wait, t_post);
   const double h3 = now_ms();
   // remove_inactive_dofs_at_all_boxes (quadtree.cpp:989-995): only the root
   // (and level-0 bookkeeping) changes for a fresh factorization.
@@ -858,12 +924,35 @@ void sweep_levels(rs_solver* s, Real* x, int ld, int nrhs, int mode, bool up) {
   sp.ld = ld;
   sp.nrhs = nrhs;
   sp.mode = mode;
+  // trace mode: CUDA-event time of each level's launch
+  std::vector<std::pair<int, cudaEvent_t>> marks;
+  auto mark = [&](int lv) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) == cudaSuccess) {
+      cudaEventRecord(e, s->stream);
+      marks.emplace_back(lv, e);
+    }
+  };
   for (int step = 0; step < L - 1; ++step) {
     const int lv = up ? L - 1 - step : 1 + step;
     if (!s->sweep_cnt[lv]) continue;
+    if (s->trace) mark(lv);
     sp.tasks = s->sweep_dev.p + s->sweep_off[lv];
     launch_sweep(sp, s->sweep_cnt[lv], s->sweep_nmax[lv], sizeof(Real) == 4, s->stream);
     ++s->launches;
+  }
+  if (s->trace && !marks.empty()) {
+    mark(-1);
+    cudaEventSynchronize(marks.back().second);
+    std::fprintf(stderr, "[rskel] %s sweep (mode %d) per level:", up ? "up" : "down", mode);
+    for (size_t i = 0; i + 1 < marks.size(); ++i) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, marks[i].second, marks[i + 1].second);
+      std::fprintf(stderr, " L%d %d boxes %.1fus;", marks[i].first, s->sweep_cnt[marks[i].first],
+                   ms * 1e3);
+    }
+    std::fprintf(stderr, "\n");
+    for (auto& m : marks) cudaEventDestroy(m.second);
   }
 }
 
