@@ -535,6 +535,24 @@ __device__ __forceinline__ float sketch_sign(int r, int i) {
 
 __host__ __device__ inline int sketch_rows(int n) { return n + kOversample; }
 
+// Sketch rows of a task: the predicted size when there is one (never above
+// n + 16), the full n + 16 otherwise and in the redo pass.
+__device__ __forceinline__ int task_ell(const IdParams& p, const IdTask& t) {
+  const int full = sketch_rows(t.n);
+  if (p.redo == nullptr || p.redo_pass || t.ell <= 0 || t.ell >= full) return full;
+  return t.ell;
+}
+
+// A truncated sketch (mr = ell < m rows) settles the rank only when the rank
+// rule stopped with at least kMinSlack rows to spare; otherwise (no stop
+// within min(n, ell) pivots, or k > ell - kMinSlack) the box is redone.
+constexpr int kMinSlack = 8;
+__device__ __forceinline__ bool sketch_too_small(int k, int n, int m, int ell, int full) {
+  if (ell >= full || m <= ell) return false;
+  if (k == 0) return true;  // no stop: n <= ell would mean full rank, but ell < n + 16 here
+  return k > ell - kMinSlack;
+}
+
 size_t id_sketch_smem(int n) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const int ld = layout_ld(n, team_size(n));
@@ -580,10 +598,11 @@ template <int TS, bool kSplit>
 __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   using Real = float;
   const IdTask t = p.tasks[blockIdx.x];
+  if (p.redo_pass && p.redo[t.slot] == 0) return;  // block-uniform
   const int n = t.n;
   const Layout L = make_layout<TS>(n);
   const int ld = L.ld;
-  const int ell = sketch_rows(n);
+  const int ell = task_ell(p, t);
   const int lp = (ell + 3) & ~3;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
@@ -697,6 +716,11 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   clk0 = clock64();
   const int k = mr > 0 ? cpqr_rank<Real, TS>(n, mr, p.tol, L, S) : 0;
   const long long clk_cpqr = clock64() - clk0;
+  if (p.redo != nullptr && !p.redo_pass) {
+    const bool again = sketch_too_small(k, n, m, ell, sketch_rows(n));
+    if (threadIdx.x == 0) p.redo[t.slot] = again ? 1 : 0;
+    if (again) return;  // block-uniform
+  }
   if (threadIdx.x == 0) p.ranks[t.slot] = k;
   for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];
   if (k > 0) {
@@ -753,9 +777,10 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
   const int ti = blockIdx.x * (blockDim.x >> 5) + warp;
   if (ti >= num_tasks) return;  // warp-uniform; nothing below synchronises the block
   const IdTask t = p.tasks[ti];
+  if (p.redo_pass && p.redo[t.slot] == 0) return;  // warp-uniform
   const int n = t.n;
   const int ld = warp_ld(n);
-  const int ell = sketch_rows(n);
+  const int ell = task_ell(p, t);
   const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
   const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
   const int mr = m <= ell ? m : ell;
@@ -873,6 +898,11 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
     }
     __syncwarp();
   }
+  if (p.redo != nullptr && !p.redo_pass) {
+    const bool again = sketch_too_small(k, n, m, ell, sketch_rows(n));
+    if (lane == 0) p.redo[t.slot] = again ? 1 : 0;
+    if (again) return;  // warp-uniform
+  }
   if (lane == 0) p.ranks[t.slot] = k;
   for (int j = lane; j < n; j += 32) p.perm[t.act_off + j] = perm[j];
   if (k > 0) {
@@ -904,11 +934,16 @@ template <int TS>
 static void launch_sketch_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
   set_smem_once<id_sketch_kernel<TS, false>>();
   id_sketch_kernel<TS, false><<<num_tasks, kThreads, smem, st>>>(p);
+  if (p.redo != nullptr) {  // boxes whose predicted sketch was too small
+    IdParams q = p;
+    q.redo_pass = 1;
+    id_sketch_kernel<TS, false><<<num_tasks, kThreads, smem, st>>>(q);
+  }
 }
 
 // Split FP32 ID: the sketch (one CTA per box), then the warp-per-box QR.
 template <int TS>
-static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
+static void launch_split_pass(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
   set_smem_once<id_sketch_kernel<TS, true>>();
   id_sketch_kernel<TS, true><<<num_tasks, kThreads, id_sketch_split_smem(nmax), st>>>(p);
   const int wbytes = (int)id_cpqr_warp_bytes(nmax);
@@ -924,16 +959,28 @@ static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStrea
   }
 }
 
+template <int TS>
+static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
+  launch_split_pass<TS>(p, num_tasks, nmax, st);
+  if (p.redo != nullptr) {  // boxes whose predicted sketch was too small
+    IdParams q = p;
+    q.redo_pass = 1;
+    launch_split_pass<TS>(q, num_tasks, nmax, st);
+  }
+}
+
 bool id_sketch_ok(int nmax) {
   return nmax <= 128 && id_sketch_smem(nmax) <= 227 * 1024;
 }
 
 constexpr int kSplitMinTasks = 512;
 
-// All tasks of one launch use the team size of its largest box.
-void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
-               cudaStream_t st) {
-  if (num_tasks <= 0) return;
+// All tasks of one launch use the team size of its largest box.  Returns
+// the number of kernels launched.
+int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
+              cudaStream_t st) {
+  if (num_tasks <= 0) return 0;
+  const int passes = p.redo != nullptr ? 2 : 1;
   const int ts = team_size(nmax);
   // The warp-per-box QR pays off when a level has boxes enough to fill the
   // GPU; small levels keep the lower-latency CTA-per-box QR.
@@ -941,13 +988,13 @@ void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp3
       num_tasks >= kSplitMinTasks) {
     if (ts == 4) launch_split_t<4>(p, num_tasks, nmax, st);
     else launch_split_t<2>(p, num_tasks, nmax, st);
-    return;
+    return 2 * passes;
   }
   if (fp32 && p.dense == nullptr && id_sketch_ok(nmax)) {
     const size_t sm = id_sketch_smem(nmax);
     if (ts == 4) launch_sketch_t<4>(p, num_tasks, sm, st);
     else launch_sketch_t<2>(p, num_tasks, sm, st);
-    return;
+    return passes;
   }
   if (fp32) {
     if (ts == 4) launch_id_t<float, 4>(p, num_tasks, smem, st);
@@ -958,6 +1005,7 @@ void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp3
     else if (ts == 2) launch_id_t<double, 2>(p, num_tasks, smem, st);
     else launch_id_t<double, 1>(p, num_tasks, smem, st);
   }
+  return 1;
 }
 
 // Sets the dynamic shared-memory limit of the three FP64 ID kernel variants

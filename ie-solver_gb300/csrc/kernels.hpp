@@ -26,6 +26,12 @@ struct IdParams {
   long long* phase_clk; // optional: per-task cycle counts {fill, fold, cpqr, z} (trace mode)
   int direct;           // 1: pivoted QR on the whole matrix in the task's global tile
   float* sketch_y;      // FP32 randomized ID in two kernels: sketch, then warp-per-box QR
+  // Learned sketch sizes (IdTask::ell): per-slot flags set by a box whose
+  // truncated sketch could not settle its rank, and the second pass that
+  // redoes exactly those boxes with the full n + 16 rows.  nullptr: no
+  // learned sizes in this launch.
+  int* redo;
+  int redo_pass;
 };
 
 struct DecoupleParams {
@@ -72,7 +78,7 @@ size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
 size_t id_sketch_y_size(int n);
 // Shared-memory attribute set-up of the FP64 ID kernels on the current device.
 cudaError_t id_noalloc_prepare();
-void launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
+int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
                cudaStream_t st);
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
                      cudaStream_t st);

@@ -39,7 +39,7 @@ struct IdTask {
   int64_t scratch_off;  // >= 0: global-memory tile for boxes too large for shared memory
   int64_t dense_off;    // >= 0: rows come from a given dense matrix (rs_id_batched)
   int m_dense;          // rows of that matrix
-  int pad;
+  int ell;              // FP32 split ID: sketch rows from the rank predictor (0: n + 16)
   int64_t y_off;        // FP32 split ID: the sketch (rows x warp leading dimension) at sketch_y[y_off]
 };
 

@@ -31,6 +31,7 @@
 #include "fmm.hpp"
 #include "kernels.hpp"
 #include "plan.hpp"
+#include "rank_model.hpp"
 #include "tree.hpp"
 
 using namespace rskel;
@@ -121,6 +122,14 @@ struct rs_solver {
   bool incremental = false;      // next rs_factor keeps the boxes rs_perturb left compressed
   size_t full_fac_used = 0;      // factor storage of the last full factorization
   DevBuf<float> sketch_y;  // FP32 split ID: per-level sketches
+  // Learned sketch sizes: model weights on the device, a level's features
+  // (sorted task order), the redo flags per slot, and the last
+  // factorization's (features, k/n) samples for training.
+  bool rank_model_on = false;
+  DevBuf<float> rank_w, rank_feat;
+  DevBuf<int> redo;
+  HostBuf<int> h_redo;
+  std::vector<float> samp_feat, samp_target;
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
   rs_stats stats;
@@ -284,6 +293,52 @@ void id_rows(rs_solver* s, int id, std::vector<int>* rows, int* use_proxy) {
   *use_proxy = 1;
 }
 
+// Input features of the rank model for one box's ID (kRankFeatures values,
+// each of order one): sizes of the ID matrix, the box's place in the tree,
+// the tolerance and kernel, and the shape of the boundary piece the active
+// DOFs sample (curvature relative to the box, spread, quadrature mass).
+void rank_features(const rs_solver* s, const TreeNode& nd, const NodeState& S, int m, double tol,
+                   float* f) {
+  const int n = (int)S.active.size();
+  const double side = nd.side > 0 ? nd.side : 1.0;
+  const double root = s->tree.max > s->tree.min ? s->tree.max - s->tree.min : 1.0;
+  double ksum = 0, kmax = 0, wsum = 0, cx = 0, cy = 0;
+  double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+  for (int dof : S.active) {
+    const int p = dof / s->sd;
+    const double k = std::fabs(s->kap[p]) * side;
+    ksum += k;
+    kmax = std::max(kmax, k);
+    wsum += s->w[p];
+    const double x = s->pts[2 * p], y = s->pts[2 * p + 1];
+    cx += x;
+    cy += y;
+    x0 = std::min(x0, x);
+    x1 = std::max(x1, x);
+    y0 = std::min(y0, y);
+    y1 = std::max(y1, y);
+  }
+  const double inv = n > 0 ? 1.0 / n : 0.0;
+  const double kmean = ksum * inv;
+  const double bx = nd.corners[0] + side / 2, by = nd.corners[1] + side / 2;
+  f[0] = (float)(n / 128.0);
+  f[1] = (float)(std::log2(std::max(n, 1)) / 8.0);
+  f[2] = (float)(std::log2(std::max(m, 1)) / 12.0);
+  f[3] = (float)(std::min(8.0, (double)S.rows.size() / std::max(n, 1)) / 8.0);
+  f[4] = (float)S.use_proxy;
+  f[5] = (float)(nd.level / 16.0);
+  f[6] = (float)(std::log2(side / root) / 16.0);
+  f[7] = (float)(-std::log10(tol) / 16.0);
+  f[8] = (float)(s->cfg.pde / 2.0);
+  f[9] = (float)nd.is_leaf;
+  f[10] = (float)(kmean / (1.0 + kmean));
+  f[11] = (float)(kmax / (1.0 + kmax));
+  f[12] = (float)(std::min(4.0, wsum / (s->sd * side)) / 4.0);
+  f[13] = n > 0 ? (float)(std::max(x1 - x0, y1 - y0) / side) : 0.f;
+  f[14] = n > 0 ? (float)(std::hypot(cx * inv - bx, cy * inv - by) / side) : 0.f;
+  f[15] = (float)(std::log2(std::max(s->D, 1)) / 20.0);
+}
+
 // Host-to-device copy through the pinned staging buffer: a copy from pinned
 // memory is asynchronous, so a level's uploads no longer wait for the DMA.
 // Regions are handed out in order during one factorization (which ends with
@@ -396,6 +451,12 @@ rs_status factor_impl(rs_solver* s) {
   std::vector<int> rows;
   std::vector<int> cand_ids, dc_ids;
   std::vector<int> m_of_slot;
+  std::vector<float> feat, feat_s;  // rank-model features per slot, and in sorted order
+  const bool learned = f32 && s->rank_model_on;
+  s->samp_feat.clear();
+  s->samp_target.clear();
+  s->stats.rank_predicted = 0;
+  s->stats.rank_redo = 0;
   // Contents below these marks are live and survive buffer growth.
   size_t fac_prev = F.fac_used, e_prev = F.e_used, piv_prev = s->piv_used;
   double t_plan = 0, t_wait = 0, t_post = 0;
@@ -483,6 +544,7 @@ rs_status factor_impl(rs_solver* s) {
     dct.resize(ndc);
     dc_ids.resize(ndc);
     blk.resize(blk_end);
+    feat.resize((size_t)nslots * kRankFeatures);
     int max_rows = s->stats.max_rows;
 #pragma omp parallel for schedule(dynamic, 16) reduction(max : max_rows) if (nl > 96)
     for (int q = 0; q < nl; ++q) {
@@ -511,6 +573,7 @@ rs_status factor_impl(rs_solver* s) {
         t.m_dense = 0;
         const int m = 2 * t.q + (S.use_proxy ? 2 * prow : 0);
         m_of_slot[P.slot] = m;
+        rank_features(s, nd, S, m, tol, feat.data() + (size_t)P.slot * kRankFeatures);
         max_rows = std::max(max_rows, m);
         idt[P.slot] = t;
         cand_ids[P.slot] = id;
@@ -552,6 +615,12 @@ rs_status factor_impl(rs_solver* s) {
     std::vector<IdTask> idt_s(idt.size());
     std::vector<DecoupleTask> dct_s(dct.size());
     for (size_t i = 0; i < oi.size(); ++i) idt_s[i] = idt[oi[i]];
+    if (learned) {
+      feat_s.resize(feat.size());
+      for (size_t i = 0; i < oi.size(); ++i)
+        std::memcpy(feat_s.data() + i * kRankFeatures, feat.data() + oi[i] * kRankFeatures,
+                    sizeof(float) * kRankFeatures);
+    }
     for (size_t i = 0; i < od.size(); ++i) dct_s[i] = dct[od[i]];
     // global-memory tiles for boxes whose tiles do not fit in shared memory
     size_t scratch_need = 0;
@@ -597,6 +666,15 @@ rs_status factor_impl(rs_solver* s) {
     CU(stage_copy(s, s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask)));
     CU(stage_copy(s, s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask)));
     CU(stage_copy(s, s->blk.p, blk.data(), blk.size() * sizeof(BlkRef)));
+    if (learned && !idt_s.empty()) {
+      // predicted sketch sizes written into the uploaded task records
+      CU(s->rank_feat.ensure(feat_s.size()));
+      CU(s->redo.ensure(idt_s.size()));
+      CU(stage_copy(s, s->rank_feat.p, feat_s.data(), feat_s.size() * sizeof(float)));
+      CU(cudaMemsetAsync(s->redo.p, 0, idt_s.size() * sizeof(int), s->stream));
+      CU(rank_infer_ell(s->rank_w.p, s->rank_feat.p, s->id_tasks.p, (int)idt_s.size(), s->stream));
+      ++s->launches;
+    }
     // ID launches
     IdParams ip{};
     ip.geo = geo_of(s);
@@ -615,6 +693,8 @@ rs_status factor_impl(rs_solver* s) {
     ip.dense = nullptr;
     ip.direct = f32 ? 0 : 1;
     ip.sketch_y = y_need ? s->sketch_y.p : nullptr;
+    ip.redo = learned && !idt_s.empty() ? s->redo.p : nullptr;
+    ip.redo_pass = 0;
     ip.phase_clk = nullptr;
     if (s->trace) {
       CU(s->clk.ensure(4 * std::max<size_t>(idt.size(), 1)));
@@ -629,8 +709,7 @@ rs_status factor_impl(rs_solver* s) {
       IdParams q = ip;
       q.tasks = dt;
       bool in_smem = !ip.direct && id_kernel_smem(nmax, f32, true) <= kSmemMax;
-      launch_id(q, cnt, nmax, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
-      ++s->launches;
+      s->launches += launch_id(q, cnt, nmax, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
     });
     CU(cudaGetLastError());
     CU(cudaEventRecord(s->lv_ev[3 * lv + 1], s->stream));
@@ -642,6 +721,11 @@ rs_status factor_impl(rs_solver* s) {
     if (!idt.empty())
       CU(cudaMemcpyAsync(s->h_ranks.p, s->ranks.p, idt.size() * sizeof(int),
                          cudaMemcpyDeviceToHost, s->stream2));
+    if (ip.redo != nullptr) {
+      CU(s->h_redo.ensure(idt.size()));
+      CU(cudaMemcpyAsync(s->h_redo.p, s->redo.p, idt.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                         s->stream2));
+    }
     CU(cudaMemcpyAsync(s->h_perm.p, s->perm.p + seg0, (seg1 - seg0) * sizeof(int),
                        cudaMemcpyDeviceToHost, s->stream2));
     CU(cudaEventRecord(s->ev_c, s->stream2));
@@ -712,6 +796,13 @@ rs_status factor_impl(rs_solver* s) {
       NodeState& S = s->st[id];
       const int k = s->h_ranks.p[S.slot];
       const int n = (int)S.active.size();
+      s->samp_feat.insert(s->samp_feat.end(), feat.begin() + (size_t)S.slot * kRankFeatures,
+                          feat.begin() + (size_t)(S.slot + 1) * kRankFeatures);
+      s->samp_target.push_back(k > 0 ? (float)k / (float)n : 1.f);
+      if (ip.redo != nullptr && n <= 128) {
+        ++s->stats.rank_predicted;
+        s->stats.rank_redo += s->h_redo.p[S.slot] != 0;
+      }
       s->stats.id_flops += id_flops(m_of_slot[S.slot], n, k, s->cfg.pde);
       if (k <= 0) {
         S.e_ld = n;
@@ -1812,6 +1903,138 @@ rs_status rs_get_stats(const rs_solver* s, rs_stats* out) {
   out->host_post_ms = s->host_post_ms;
   out->residual64_ms = s->stats.residual64_ms;
   out->residual32_ms = s->stats.residual32_ms;
+  return RS_OK;
+}
+
+static_assert(kRankFeatures == RS_RANK_FEATURES && kRankWeights == RS_RANK_WEIGHTS,
+              "rank model sizes of rskel.h and rank_model.hpp differ");
+
+void rs_rank_model_init(uint64_t seed, float* weights) {
+  if (!weights) return;
+  uint64_t x = seed + 0x9E3779B97F4A7C15ull;
+  auto uni = [&x]() {  // splitmix64 -> uniform in [-1, 1)
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+  };
+  const int H = kRankHidden, F = kRankFeatures;
+  float* w = weights;
+  const float a1 = std::sqrt(6.f / F), a2 = std::sqrt(6.f / H), a3 = std::sqrt(1.f / H);
+  for (int e = 0; e < H * F; ++e) *w++ = a1 * uni();
+  for (int e = 0; e < H; ++e) *w++ = 0.f;
+  for (int e = 0; e < H * H; ++e) *w++ = a2 * uni();
+  for (int e = 0; e < H; ++e) *w++ = 0.f;
+  for (int e = 0; e < H; ++e) *w++ = a3 * uni();
+  *w++ = 0.f;
+}
+
+rs_status rs_set_rank_model(rs_solver* s, const float* weights) {
+  if (!s) return RS_ERR_ARG;
+  if (!weights) {
+    s->rank_model_on = false;
+    return RS_OK;
+  }
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  CU(cudaSetDevice(s->cfg.device));
+  CU(s->rank_w.ensure(kRankWeights));
+  CU(cudaMemcpyAsync(s->rank_w.p, weights, sizeof(float) * kRankWeights, cudaMemcpyHostToDevice,
+                     s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  s->rank_model_on = true;
+  return RS_OK;
+}
+
+rs_status rs_rank_samples(const rs_solver* s, float* features, float* targets, int cap,
+                          int* count) {
+  if (!s || !count || cap < 0 || (cap > 0 && (!features || !targets))) return RS_ERR_ARG;
+  const int n = (int)s->samp_target.size();
+  *count = n;
+  const int w = std::min(n, cap);
+  if (w > 0) {
+    std::memcpy(features, s->samp_feat.data(), sizeof(float) * kRankFeatures * (size_t)w);
+    std::memcpy(targets, s->samp_target.data(), sizeof(float) * (size_t)w);
+  }
+  return RS_OK;
+}
+
+// Device copies of a training set for the rank-model entry points.
+struct RankSet {
+  DevBuf<float> w, x, y, g, m, v, loss;
+};
+
+static rs_status rank_upload(rs_solver* s, RankSet& R, const float* weights,
+                             const float* features, const float* targets, int count) {
+  rs_status rc = ensure_device(s);
+  if (rc != RS_OK) return rc;
+  CU(cudaSetDevice(s->cfg.device));
+  CU(R.w.ensure(kRankWeights));
+  CU(R.g.ensure(kRankWeights));
+  CU(R.loss.ensure(1));
+  CU(R.x.ensure((size_t)count * kRankFeatures));
+  CU(cudaMemcpyAsync(R.w.p, weights, sizeof(float) * kRankWeights, cudaMemcpyHostToDevice,
+                     s->stream));
+  CU(cudaMemcpyAsync(R.x.p, features, sizeof(float) * kRankFeatures * (size_t)count,
+                     cudaMemcpyHostToDevice, s->stream));
+  if (targets) {
+    CU(R.y.ensure(count));
+    CU(cudaMemcpyAsync(R.y.p, targets, sizeof(float) * (size_t)count, cudaMemcpyHostToDevice,
+                       s->stream));
+  }
+  return RS_OK;
+}
+
+rs_status rs_rank_train(rs_solver* s, const float* features, const float* targets, int count,
+                        int epochs, float lr, float* weights, float* loss) {
+  if (!s || !features || !targets || !weights || count < 1 || epochs < 1 || !(lr > 0))
+    return RS_ERR_ARG;
+  RankSet R;
+  RSCHK(rank_upload(s, R, weights, features, targets, count));
+  CU(R.m.ensure(kRankWeights));
+  CU(R.v.ensure(kRankWeights));
+  CU(cudaMemsetAsync(R.m.p, 0, sizeof(float) * kRankWeights, s->stream));
+  CU(cudaMemsetAsync(R.v.p, 0, sizeof(float) * kRankWeights, s->stream));
+  for (int e = 1; e <= epochs; ++e) {
+    CU(rank_gradient(R.w.p, R.x.p, R.y.p, count, R.g.p, R.loss.p, s->stream));
+    CU(rank_adam(R.w.p, R.g.p, R.m.p, R.v.p, e, lr, s->stream));
+  }
+  float ls = 0;
+  CU(cudaMemcpyAsync(weights, R.w.p, sizeof(float) * kRankWeights, cudaMemcpyDeviceToHost,
+                     s->stream));
+  CU(cudaMemcpyAsync(&ls, R.loss.p, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  if (loss) *loss = ls / (float)count;
+  return RS_OK;
+}
+
+rs_status rs_rank_predict(rs_solver* s, const float* weights, const float* features, int count,
+                          float* out) {
+  if (!s || !weights || !features || !out || count < 0) return RS_ERR_ARG;
+  if (count == 0) return RS_OK;
+  RankSet R;
+  RSCHK(rank_upload(s, R, weights, features, nullptr, count));
+  CU(R.y.ensure(count));
+  CU(rank_predict(R.w.p, R.x.p, count, R.y.p, s->stream));
+  CU(cudaMemcpyAsync(out, R.y.p, sizeof(float) * (size_t)count, cudaMemcpyDeviceToHost,
+                     s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  return RS_OK;
+}
+
+rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* features,
+                           const float* targets, int count, float* grad, float* loss) {
+  if (!s || !weights || !features || !targets || !grad || count < 1) return RS_ERR_ARG;
+  RankSet R;
+  RSCHK(rank_upload(s, R, weights, features, targets, count));
+  CU(rank_gradient(R.w.p, R.x.p, R.y.p, count, R.g.p, R.loss.p, s->stream));
+  float ls = 0;
+  CU(cudaMemcpyAsync(grad, R.g.p, sizeof(float) * kRankWeights, cudaMemcpyDeviceToHost,
+                     s->stream));
+  CU(cudaMemcpyAsync(&ls, R.loss.p, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaStreamSynchronize(s->stream));
+  if (loss) *loss = ls / (float)count;
   return RS_OK;
 }
 

@@ -27,7 +27,9 @@ EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "r
            "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
            "rs_matvec_fast", "rs_domain_eval",
-           "rs_id_batched", "rs_id_noalloc", "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
+           "rs_id_batched", "rs_id_noalloc", "rs_rank_model_init", "rs_set_rank_model",
+           "rs_rank_samples", "rs_rank_train", "rs_rank_predict", "rs_rank_gradient",
+           "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
            "rs_allskel", "rs_timer_start", "rs_timer_stop", "rs_synchronize", "rs_last_error"]
 
 
@@ -56,7 +58,8 @@ class RsStats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int), ("host_plan_ms", ctypes.c_double),
                 ("host_wait_ms", ctypes.c_double), ("host_post_ms", ctypes.c_double),
                 ("boxes_factored", ctypes.c_int),
-                ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double)]
+                ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double),
+                ("rank_predicted", ctypes.c_int), ("rank_redo", ctypes.c_int)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -94,6 +97,15 @@ def lib():
                                      _dp, ctypes.c_int, _dp]
         L.rs_id_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double, _vp, _vp, _vp,
                                     _vp]
+        _fp = ctypes.POINTER(ctypes.c_float)
+        L.rs_rank_model_init.argtypes = [ctypes.c_uint64, _fp]
+        L.rs_rank_model_init.restype = None
+        L.rs_set_rank_model.argtypes = [_vp, _fp]
+        L.rs_rank_samples.argtypes = [_vp, _fp, _fp, ctypes.c_int, _ip]
+        L.rs_rank_train.argtypes = [_vp, _fp, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, _fp,
+                                    _fp]
+        L.rs_rank_predict.argtypes = [_vp, _fp, _fp, ctypes.c_int, _fp]
+        L.rs_rank_gradient.argtypes = [_vp, _fp, _fp, _fp, ctypes.c_int, _fp, _fp]
         L.rs_get_stats.argtypes = [_vp, ctypes.POINTER(RsStats)]
         L.rs_node_info.argtypes = [_vp, ctypes.c_int, _ip, _dp, _dp]
         L.rs_node_list.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip]
@@ -106,7 +118,7 @@ def lib():
         L.rs_last_error.restype = ctypes.c_char_p
         for fn in EXPORTS:
             f = getattr(L, fn)
-            if fn not in ("rs_config_default", "rs_last_error"):
+            if fn not in ("rs_config_default", "rs_last_error", "rs_rank_model_init"):
                 f.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -128,6 +140,34 @@ def _i(a):
 
 def _l(a):
     return a.ctypes.data_as(_lp)
+
+
+def _f(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+RANK_FEATURES, RANK_HIDDEN = 16, 64
+RANK_WEIGHTS = RANK_HIDDEN * RANK_FEATURES + RANK_HIDDEN + RANK_HIDDEN * RANK_HIDDEN + \
+    RANK_HIDDEN + RANK_HIDDEN + 1
+
+
+def rank_model_init(seed=0):
+    """rs_rank_model_init: deterministic initial weights of the rank model."""
+    w = np.zeros(RANK_WEIGHTS, dtype=np.float32)
+    lib().rs_rank_model_init(seed, _f(w))
+    return w
+
+
+def rank_unpack(w):
+    """Splits a weight vector into (W1 [64x16], b1, W2 [64x64], b2, w3, b3)."""
+    H, F = RANK_HIDDEN, RANK_FEATURES
+    o = 0
+    out = []
+    for shape in ((H, F), (H,), (H, H), (H,), (H,), (1,)):
+        sz = int(np.prod(shape))
+        out.append(np.asarray(w[o:o + sz]).reshape(shape))
+        o += sz
+    return out
 
 
 def default_config(**kw):
@@ -215,6 +255,54 @@ class Solver:
 
     def solve_device(self, f_ptr, nrhs, mu_ptr, alpha_ptr=0):
         self._check(lib().rs_solve_device(self.h, f_ptr, nrhs, mu_ptr, alpha_ptr))
+
+    # --- learned skeleton ranks (rs_rank_*) ---
+    def set_rank_model(self, weights):
+        """rs_set_rank_model: predicted sketch sizes for the FP32 ID from the
+        next factor() on; None switches them off."""
+        if weights is None:
+            self._check(lib().rs_set_rank_model(self.h, None))
+            return
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        assert w.size == RANK_WEIGHTS
+        self._check(lib().rs_set_rank_model(self.h, _f(w)))
+
+    def rank_samples(self):
+        """(features [count x 16], k/n [count]) of the last factorization."""
+        cnt = ctypes.c_int(0)
+        self._check(lib().rs_rank_samples(self.h, None, None, 0, ctypes.byref(cnt)))
+        X = np.zeros((cnt.value, RANK_FEATURES), dtype=np.float32)
+        y = np.zeros(cnt.value, dtype=np.float32)
+        if cnt.value:
+            self._check(lib().rs_rank_samples(self.h, _f(X), _f(y), cnt.value, ctypes.byref(cnt)))
+        return X, y
+
+    def rank_train(self, X, y, weights, epochs=1000, lr=3e-3):
+        """rs_rank_train: returns (trained weights, final mean loss)."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        w = np.array(weights, dtype=np.float32, copy=True)
+        loss = ctypes.c_float(0)
+        self._check(lib().rs_rank_train(self.h, _f(X), _f(y), len(y), epochs, lr, _f(w),
+                                        ctypes.byref(loss)))
+        return w, loss.value
+
+    def rank_predict(self, weights, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        out = np.zeros(len(X), dtype=np.float32)
+        self._check(lib().rs_rank_predict(self.h, _f(w), _f(X), len(X), _f(out)))
+        return out
+
+    def rank_gradient(self, weights, X, y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        g = np.zeros(RANK_WEIGHTS, dtype=np.float32)
+        loss = ctypes.c_float(0)
+        self._check(lib().rs_rank_gradient(self.h, _f(w), _f(X), _f(y), len(y), _f(g),
+                                           ctypes.byref(loss)))
+        return g, loss.value
 
     def domain_eval(self, targets, mu, alpha=None, in_domain=None):
         """rs_domain_eval: u at interleaved targets (2 nt,) from mu ((n sd) x nrhs)."""

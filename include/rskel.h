@@ -176,6 +176,44 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
 rs_status rs_id_noalloc(int m, int n, const double* A, double tol, int* rank, int* perm,
                         double* Z, void* stream);
 
+/* --- learned skeleton ranks (the RS_FP32_REFINE factorization's ID) ---
+ * No counterpart in the reference.  A 16 -> 64 -> 64 -> 1 multilayer
+ * perceptron (ReLU, ReLU, sigmoid) predicts each box's rank fraction k/n
+ * from RS_RANK_FEATURES features the host computes per box (ID matrix
+ * sizes, tree level and box size, tolerance, kernel, curvature and spread
+ * of the box's boundary piece).  The FP32 randomized ID of a box of at most
+ * 128 DOFs then sketches with ell = min(n + 16, ceil(1.15 n y) + 10) rows
+ * instead of n + 16.  A box whose truncated sketch does not settle its rank
+ * with 8 rows to spare is redone on the device with the full sketch, so a
+ * poor prediction costs time, not accuracy.
+ * Weights: W1 (64 x 16, row major), b1 (64), W2 (64 x 64), b2 (64), w3 (64),
+ * b3 (1), RS_RANK_WEIGHTS floats in all. */
+#define RS_RANK_FEATURES 16
+#define RS_RANK_WEIGHTS 5313
+/* Deterministic initial weights (He-scaled uniform, host only). */
+void rs_rank_model_init(uint64_t seed, float* weights);
+/* Uses `weights` (host, copied) for this handle's RS_FP32_REFINE
+ * factorizations from the next rs_factor on; NULL switches it off. */
+rs_status rs_set_rank_model(rs_solver* s, const float* weights);
+/* Training samples of the last rs_factor: per box that was tried for
+ * compression, its features (row major, RS_RANK_FEATURES per box) and the
+ * rank fraction it got (k/n; 1 when not compressed).  Writes up to cap
+ * samples; *count gets the number available. */
+rs_status rs_rank_samples(const rs_solver* s, float* features, float* targets, int cap,
+                          int* count);
+/* `epochs` full-batch Adam steps (lr; betas 0.9, 0.999) on the mean squared
+ * error of the predicted fractions, on the handle's device.  weights: host,
+ * in and out; *loss gets the mean loss at the last step's weights before
+ * its update. */
+rs_status rs_rank_train(rs_solver* s, const float* features, const float* targets, int count,
+                        int epochs, float lr, float* weights, float* loss);
+/* The inference kernel's fractions, and the gradient kernel's d(loss)/dW
+ * with the mean loss (host arrays). */
+rs_status rs_rank_predict(rs_solver* s, const float* weights, const float* features, int count,
+                          float* out);
+rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* features,
+                           const float* targets, int count, float* grad, float* loss);
+
 /* --- introspection (tree and factorization), for tests and tooling --- */
 typedef struct {
   int num_levels, num_nodes, num_compressed, num_skel_root;
@@ -194,6 +232,9 @@ typedef struct {
   double residual64_ms, residual32_ms;         /* last RS_FP32_REFINE solve: CUDA-event time of
                                                   the FP64 residual products and of the FP32
                                                   correction products */
+  int rank_predicted, rank_redo;               /* last rs_factor with a rank model: boxes whose
+                                                  sketch size was predicted, and those of them
+                                                  redone with the full sketch */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 

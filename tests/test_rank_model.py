@@ -1,0 +1,203 @@
+"""Learned skeleton ranks: the rank model's hand-written CUDA inference,
+gradient and Adam kernels against a PyTorch fp32 restatement of the same
+multilayer perceptron, and the FP32 factorization with predicted sketch
+sizes against the plain one.
+
+Tolerances: predicted fractions within 2e-6 of torch's (fp32 sums in
+another order); gradients within 1e-4 of max |grad| (the gradient kernel
+accumulates with atomics in fp32); a factorization with a rank model is
+refined to the same accuracy bar as without (1e-8 relative to the FP64
+solution), whatever the model predicts.
+"""
+import numpy as np
+import pytest
+
+RS_ERR_ARG = 1
+
+
+def _torch_mlp(torch, w, X):
+    from rskel import capi
+
+    W1, b1, W2, b2, w3, b3 = (torch.tensor(a, dtype=torch.float32, requires_grad=True)
+                              for a in capi.rank_unpack(w))
+    x = torch.tensor(X, dtype=torch.float32)
+    h1 = torch.relu(x @ W1.T + b1)
+    h2 = torch.relu(h1 @ W2.T + b2)
+    y = torch.sigmoid(h2 @ w3 + b3)
+    return y, (W1, b1, W2, b2, w3, b3)
+
+
+def _features(rng, count):
+    X = rng.uniform(0.0, 1.0, (count, 16)).astype(np.float32)
+    X[:, 6] = -X[:, 6]  # log box size relative to the root is negative
+    return X
+
+
+def test_init_is_deterministic_and_scaled(solver_lib):
+    capi = solver_lib
+    a, b, c = capi.rank_model_init(7), capi.rank_model_init(7), capi.rank_model_init(8)
+    assert a.size == capi.RANK_WEIGHTS == 5313
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    W1, b1, W2, b2, w3, b3 = capi.rank_unpack(a)
+    assert np.abs(W1).max() <= np.sqrt(6 / 16) and np.abs(W2).max() <= np.sqrt(6 / 64)
+    assert not b1.any() and not b2.any() and b3[0] == 0.0
+    assert W1.std() > 0.2 and W2.std() > 0.1
+
+
+def test_rank_entry_points_validate_arguments(solver_lib):
+    import ctypes
+
+    capi = solver_lib
+    L = capi.lib()
+    w = capi.rank_model_init(0)
+    X = np.zeros((4, 16), dtype=np.float32)
+    y = np.zeros(4, dtype=np.float32)
+    f = capi._f
+    # checks that come before any device call
+    assert L.rs_rank_train(None, f(X), f(y), 4, 10, 1e-3, f(w), None) == RS_ERR_ARG
+    assert L.rs_rank_predict(None, f(w), f(X), 4, f(y)) == RS_ERR_ARG
+    assert L.rs_rank_gradient(None, f(w), f(X), f(y), 4, f(w), None) == RS_ERR_ARG
+    cnt = ctypes.c_int(-1)
+    assert L.rs_rank_samples(None, None, None, 0, ctypes.byref(cnt)) == RS_ERR_ARG
+    assert L.rs_set_rank_model(None, f(w)) == RS_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_predict_matches_torch(solver_lib):
+    torch = pytest.importorskip("torch")
+    from rskel import geometry as g
+
+    capi = solver_lib
+    rng = np.random.default_rng(3)
+    w = capi.rank_model_init(5)
+    w[capi.RANK_HIDDEN * 16:capi.RANK_HIDDEN * 17] = rng.normal(0, 0.2, capi.RANK_HIDDEN)  # b1
+    w[-1] = 0.3
+    X = _features(rng, 1000)
+    s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
+    y = s.rank_predict(w, X)
+    yt, _ = _torch_mlp(torch, w, X)
+    assert np.abs(y - yt.detach().numpy()).max() <= 2e-6
+    assert s.rank_predict(w, X[:0]).size == 0
+
+
+@pytest.mark.gpu
+def test_gradient_matches_torch_autograd(solver_lib):
+    torch = pytest.importorskip("torch")
+    from rskel import geometry as g
+
+    capi = solver_lib
+    rng = np.random.default_rng(4)
+    w = capi.rank_model_init(9)
+    X = _features(rng, 777)
+    t = rng.uniform(0.05, 0.9, 777).astype(np.float32)
+    s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
+    grad, loss = s.rank_gradient(w, X, t)
+    yt, params = _torch_mlp(torch, w, X)
+    lt = ((yt - torch.tensor(t)) ** 2).mean()
+    lt.backward()
+    gt = np.concatenate([p.grad.numpy().ravel() for p in params])
+    assert abs(loss - lt.item()) <= 1e-5 * max(1.0, lt.item())
+    assert np.abs(grad - gt).max() <= 1e-4 * np.abs(gt).max()
+
+
+@pytest.mark.gpu
+def test_training_lowers_the_loss(solver_lib):
+    from rskel import geometry as g
+
+    capi = solver_lib
+    rng = np.random.default_rng(5)
+    X = _features(rng, 2048)
+    # a smooth rank-fraction-like target of the features
+    t = (0.15 + 0.5 * X[:, 0] * (1 - 0.5 * X[:, 7]) + 0.2 * X[:, 10] ** 2).astype(np.float32)
+    t = np.clip(t, 0.02, 0.98)
+    s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
+    w0 = capi.rank_model_init(1)
+    _, l0 = s.rank_gradient(w0, X, t)
+    w1, l1 = s.rank_train(X, t, w0, epochs=400, lr=3e-3)
+    _, l1b = s.rank_gradient(w1, X, t)
+    assert l1 < 0.1 * l0 and l1b < 0.1 * l0
+    assert np.abs(s.rank_predict(w1, X) - t).mean() < 0.05
+
+
+def _mixed(capi, geo, **kw):
+    return capi.Solver(geo, capi.RS_LAPLACE, 1e-8, leaf=64, npp=64,
+                       precision=capi.RS_FP32_REFINE, refine_tol=1e-11, refine_max_iters=8,
+                       fp32_id_tol=1e-6, **kw)
+
+
+def _rhs(geo):
+    from rskel import geometry as g
+
+    return np.stack([g.laplace_point_source(geo, (2.5 * np.cos(a), 2.5 * np.sin(a)))
+                     for a in (0.3, 2.0)], axis=1)
+
+
+@pytest.mark.gpu
+def test_learned_sketch_sizes_keep_the_solution(solver_lib):
+    from rskel import geometry as g
+
+    capi = solver_lib
+    # training samples: plain mixed-precision factorizations of other curves
+    Xs, ys = [], []
+    rng = np.random.default_rng(12)
+    for geo in (g.random_star(16384, rng), g.random_star(32768, rng), g.star(16384, a=0.2, k=7)):
+        s = _mixed(capi, geo)
+        s.factor()
+        X, y = s.rank_samples()
+        assert len(y) > 100 and np.all((y > 0) & (y <= 1))
+        assert X.shape == (len(y), 16) and np.isfinite(X).all()
+        Xs.append(X)
+        ys.append(y)
+        s.close()
+    X, y = np.concatenate(Xs), np.concatenate(ys)
+    t = _mixed(capi, g.star(32768))
+    w, loss = t.rank_train(X, y, capi.rank_model_init(0), epochs=1500, lr=3e-3)
+    assert loss < 0.01
+    # plain and learned factorizations of a new curve
+    F = _rhs(g.star(32768))
+    t.factor()
+    mu0, _ = t.solve(F)
+    st0 = t.stats()
+    assert st0["rank_predicted"] == 0
+    t.set_rank_model(w)
+    t.factor()
+    mu1, _ = t.solve(F)
+    st1 = t.stats()
+    assert st1["rank_predicted"] > 100
+    assert st1["rank_redo"] <= 0.25 * st1["rank_predicted"]
+    s64 = capi.Solver(g.star(32768), capi.RS_LAPLACE, 1e-8, leaf=64, npp=64)
+    s64.factor()
+    mu64, _ = s64.solve(F)
+    rel = np.linalg.norm(mu1 - mu64) / np.linalg.norm(mu64)
+    rel0 = np.linalg.norm(mu0 - mu64) / np.linalg.norm(mu64)
+    assert rel <= 1e-8 and rel0 <= 1e-8, (rel, rel0)
+    assert st1["refine_residual"] <= 1e-11
+    # switching the model off gives the plain factorization back
+    t.set_rank_model(None)
+    t.factor()
+    assert t.stats()["rank_predicted"] == 0
+
+
+@pytest.mark.gpu
+def test_too_small_predictions_fall_back_to_the_full_sketch(solver_lib):
+    from rskel import geometry as g
+
+    capi = solver_lib
+    geo = g.star(32768)
+    F = _rhs(geo)
+    s = _mixed(capi, geo)
+    s.factor()
+    mu0, _ = s.solve(F)
+    _, y0 = s.rank_samples()
+    # every prediction ~0: 12-row sketches, so every box of rank > 4 is redone
+    w = np.zeros(capi.RANK_WEIGHTS, dtype=np.float32)
+    w[-1] = -30.0
+    s.set_rank_model(w)
+    s.factor()
+    mu1, _ = s.solve(F)
+    st = s.stats()
+    _, y1 = s.rank_samples()
+    assert st["rank_predicted"] > 100 and st["rank_redo"] >= 0.9 * st["rank_predicted"]
+    # redone boxes get the plain factorization's ranks
+    assert np.abs(y1 - y0).max() <= 0.5 and np.mean(y1 == y0) >= 0.9
+    assert np.linalg.norm(mu1 - mu0) / np.linalg.norm(mu0) <= 1e-9
