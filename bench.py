@@ -8,10 +8,13 @@ solve of all 8 right-hand sides; DOFs/s = N / (t_factor + t_solve), as in
 the reference's timing protocol (linear_solve.cpp:156-185: tree build
 excluded), with the inputs resident on the device.
 
-Two arms run: plain FP64 (the reference's arithmetic) and FP32 factorization
-+ FP64 iterative refinement to a relative residual of 1e-11.  The headline is
-the refined arm when its solutions are within 1e-8 of the exact discrete
-solution (the FP64 oracle at tolerance 1e-12), else the plain FP64 arm.
+Three arms run: plain FP64 (the reference's arithmetic), FP32 factorization
++ FP64 iterative refinement to a relative residual of 1e-11, and the same
+with learned sketch sizes (the rank model trained, before timing, on ranks
+the plain FP32 factorization gets on 24 other seeded star and ellipse
+curves).  The headline is the learned refined arm when its solutions are
+within 1e-8 of the exact discrete solution (the FP64 oracle at tolerance
+1e-12), else the plain refined arm under the same test, else plain FP64.
 Errors against the oracle at the configuration's own tolerance 1e-8 are
 reported too (that oracle carries its own ~1e-8 ID error).
 
@@ -234,13 +237,45 @@ def fma_peaks(device):
     return {"fp32": f32.value, "fp64": f64.value}
 
 
-def make_solver(capi, geo, precision, device):
-    return capi.Solver(geo, capi.RS_LAPLACE, TOL, leaf=LEAF, npp=NPP, precision=precision,
-                       refine_tol=REFINE_TOL, refine_max_iters=8, fp32_id_tol=1e-6, device=device)
+def make_solver(capi, geo, precision, device, model=None):
+    s = capi.Solver(geo, capi.RS_LAPLACE, TOL, leaf=LEAF, npp=NPP, precision=precision,
+                    refine_tol=REFINE_TOL, refine_max_iters=8, fp32_id_tol=1e-6, device=device)
+    if model is not None:
+        s.set_rank_model(model)
+    return s
 
 
-def time_arm(capi, geo, F, precision, steps, warmup, cu, dist):
-    s = make_solver(capi, geo, precision, dist.local)
+TRAIN_CURVES, TRAIN_SEED, TRAIN_EPOCHS = 24, 5, 3000
+
+
+def train_rank_model(capi, device):
+    """Rank model for the learned arm: samples (box features, k/n) from plain
+    FP32 factorizations of seeded training curves (none of them the
+    benchmark's star), then full-batch Adam on the GPU.  Not timed."""
+    from rskel import geometry as g
+
+    t0 = time.perf_counter()
+    Xs, ys = [], []
+    for geo in g.rank_training_curves(TRAIN_CURVES, TRAIN_SEED):
+        s = make_solver(capi, geo, capi.RS_FP32_REFINE, device)
+        s.factor()
+        X, y = s.rank_samples()
+        Xs.append(X)
+        ys.append(y)
+        s.close()
+    X, y = np.concatenate(Xs), np.concatenate(ys)
+    t1 = time.perf_counter()
+    s = make_solver(capi, g.unit_circle(64), capi.RS_FP32_REFINE, device)
+    w, loss = s.rank_train(X, y, capi.rank_model_init(0), epochs=TRAIN_EPOCHS, lr=3e-3)
+    s.close()
+    info = {"curves": TRAIN_CURVES, "seed": TRAIN_SEED, "samples": int(len(y)),
+            "epochs": TRAIN_EPOCHS, "final_mse": loss, "collect_s": t1 - t0,
+            "train_s": time.perf_counter() - t1}
+    return w, info
+
+
+def time_arm(capi, geo, F, precision, steps, warmup, cu, dist, model=None):
+    s = make_solver(capi, geo, precision, dist.local, model)
     s.build_tree()
     d_f = cu.malloc(F.nbytes)
     d_mu = cu.malloc(F.nbytes)
@@ -270,10 +305,10 @@ def time_arm(capi, geo, F, precision, steps, warmup, cu, dist):
     return times, stats, mu, launches
 
 
-def e2e_arm(capi, geo, F, precision, steps, warmup, dist):
+def e2e_arm(capi, geo, F, precision, steps, warmup, dist, model=None):
     """Through the C ABI with host buffers, one handle reused as a caller
     would: rs_set_geometry, tree, factor, rs_solve from host f to host mu."""
-    s = make_solver(capi, geo, precision, dist.local)
+    s = make_solver(capi, geo, precision, dist.local, model)
     times = []
     for i in range(warmup + steps):
         dist.barrier()
@@ -338,23 +373,33 @@ def run_gpu(args):
     cores = os.cpu_count() or 1
     peaks = fma_peaks(dist.local)
     t64, st64, mu64, l64 = time_arm(capi, geo, F, capi.RS_FP64, args.steps, args.warmup, cu, dist)
+    model, train_info = train_rank_model(capi, dist.local)
+    t32p, st32p, mu32p, l32p = time_arm(capi, geo, F, capi.RS_FP32_REFINE, args.steps,
+                                        args.warmup, cu, dist)
     clk = ClockSampler(dist.local)
     clk.start()
     t32, st32, mu32, l32 = time_arm(capi, geo, F, capi.RS_FP32_REFINE, args.steps, args.warmup,
-                                    cu, dist)
+                                    cu, dist, model)
     clocks = clk.stop()
     # accuracy against the oracle (CPU): at the configuration's tolerance and
     # at 1e-12 (the exact discrete solution to ~1e-12)
     mu_cfg, _, _ = oracle_solution(geo, F, TOL, cores)
     mu_ex, _, _ = oracle_solution(geo, F, 1e-12, cores)
     acc = {"refined_vs_exact": rel_err(mu32, mu_ex), "refined_vs_oracle_tol1e-8": rel_err(mu32, mu_cfg),
+           "refined_plain_vs_exact": rel_err(mu32p, mu_ex),
            "fp64_vs_exact": rel_err(mu64, mu_ex), "fp64_vs_oracle_tol1e-8": rel_err(mu64, mu_cfg),
            "refine_iters": st32[-1]["refine_iters"], "refine_residual": st32[-1]["refine_residual"]}
-    refined_ok = acc["refined_vs_exact"] <= 1e-8
-    head = "fp32_refine" if refined_ok else "fp64"
-    times, stats, launches = (t32, st32, l32) if refined_ok else (t64, st64, l64)
+    learned_ok = acc["refined_vs_exact"] <= 1e-8
+    plain_ok = acc["refined_plain_vs_exact"] <= 1e-8
+    refined_ok = learned_ok or plain_ok
+    if learned_ok:
+        head, times, stats, launches, arm_model = "fp32_refine+learned", t32, st32, l32, model
+    elif plain_ok:
+        head, times, stats, launches, arm_model = "fp32_refine", t32p, st32p, l32p, None
+    else:
+        head, times, stats, launches, arm_model = "fp64", t64, st64, l64, None
     prec = capi.RS_FP32_REFINE if refined_ok else capi.RS_FP64
-    e2e_t, h2d, d2h = e2e_arm(capi, geo, F, prec, max(1, min(args.steps, 5)), 1, dist)
+    e2e_t, h2d, d2h = e2e_arm(capi, geo, F, prec, max(1, min(args.steps, 5)), 1, dist, arm_model)
     ms = dist.max(max(times))
     ms64 = dist.max(max(t64))
     e2e_ms = dist.max(statistics.median(e2e_t))
@@ -384,6 +429,15 @@ def run_gpu(args):
                        "ms_median": statistics.median(t64),
                        "breakdown_ms": breakdown(st64[-1], statistics.median(t64))},
         "speedup_vs_plain_fp64": ms64 / ms,
+        "fp32_refine_without_model": {
+            "value": dist.sum(dofs) / (dist.max(max(t32p)) * 1e-3),
+            "ms_per_step": dist.max(max(t32p)), "ms_median": statistics.median(t32p),
+            "breakdown_ms": breakdown(st32p[-1], statistics.median(t32p)),
+            "sketch_rows": st32p[-1]["sketch_rows"]},
+        "rank_model": dict(train_info, boxes_predicted=st32[-1]["rank_predicted"],
+                           boxes_redone=st32[-1]["rank_redo"],
+                           sketch_rows=st32[-1]["sketch_rows"],
+                           id_ms_with=st32[-1]["id_ms"], id_ms_without=st32p[-1]["id_ms"]),
         "ms_median": statistics.median(times),
         "step_breakdown_ms": bd,
         "host_ms": {"plan": st["host_plan_ms"], "wait": st["host_wait_ms"],

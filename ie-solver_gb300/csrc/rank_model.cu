@@ -100,10 +100,10 @@ __device__ __forceinline__ int ell_from_fraction(float y, int n) {
   return ell;
 }
 
-template <int kMode>  // 0: predict into out; 1: write tasks[i].ell
+template <int kMode>  // 0: predict into out; 1: write tasks[i].ell and ell_by_slot
 __global__ void __launch_bounds__(kMlpThreads) infer_kernel(const float* W, const float* feats,
                                                             int count, float* out,
-                                                            IdTask* tasks) {
+                                                            IdTask* tasks, int* ell_by_slot) {
   extern __shared__ __align__(16) float smem[];
   SharedMlp m;
   load_mlp(W, smem, &m, false);
@@ -117,8 +117,13 @@ __global__ void __launch_bounds__(kMlpThreads) infer_kernel(const float* W, cons
     __syncwarp();
     const float y = forward(m, xw, h1, h2);
     if (lane == 0) {
-      if (kMode == 0) out[i] = y;
-      else tasks[i].ell = ell_from_fraction(y, tasks[i].n);
+      if (kMode == 0) {
+        out[i] = y;
+      } else {
+        const int ell = ell_from_fraction(y, tasks[i].n);
+        tasks[i].ell = ell;
+        ell_by_slot[tasks[i].slot] = ell;
+      }
     }
     __syncwarp();
   }
@@ -205,18 +210,18 @@ int grid_for(int count) {
 }  // namespace
 
 cudaError_t rank_infer_ell(const float* weights, const float* features, IdTask* tasks,
-                           int num_tasks, cudaStream_t st) {
+                           int num_tasks, int* ell_by_slot, cudaStream_t st) {
   if (num_tasks <= 0) return cudaSuccess;
   infer_kernel<1><<<grid_for(num_tasks), kMlpThreads, mlp_smem(false), st>>>(
-      weights, features, num_tasks, nullptr, tasks);
+      weights, features, num_tasks, nullptr, tasks, ell_by_slot);
   return cudaGetLastError();
 }
 
 cudaError_t rank_predict(const float* weights, const float* features, int count, float* out,
                          cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
-  infer_kernel<0><<<grid_for(count), kMlpThreads, mlp_smem(false), st>>>(weights, features,
-                                                                         count, out, nullptr);
+  infer_kernel<0><<<grid_for(count), kMlpThreads, mlp_smem(false), st>>>(
+      weights, features, count, out, nullptr, nullptr);
   return cudaGetLastError();
 }
 

@@ -21,9 +21,9 @@ constexpr int kRankWeights = kRankHidden * kRankFeatures + kRankHidden +
                              kRankHidden * kRankHidden + kRankHidden + kRankHidden + 1;
 
 // Writes tasks[i].ell (sketch rows) for every task from its features
-// (num_tasks x 16, row major).
+// (num_tasks x 16, row major), and the same value to ell_by_slot[tasks[i].slot].
 cudaError_t rank_infer_ell(const float* weights, const float* features, IdTask* tasks,
-                           int num_tasks, cudaStream_t st);
+                           int num_tasks, int* ell_by_slot, cudaStream_t st);
 // out[i] = predicted rank fraction of sample i.
 cudaError_t rank_predict(const float* weights, const float* features, int count, float* out,
                          cudaStream_t st);

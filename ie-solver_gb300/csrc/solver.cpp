@@ -127,8 +127,8 @@ struct rs_solver {
   // factorization's (features, k/n) samples for training.
   bool rank_model_on = false;
   DevBuf<float> rank_w, rank_feat;
-  DevBuf<int> redo;
-  HostBuf<int> h_redo;
+  DevBuf<int> redo, ell_slot;
+  HostBuf<int> h_redo, h_ell;
   std::vector<float> samp_feat, samp_target;
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
@@ -374,6 +374,16 @@ double id_flops(int m, int n, int k, int pde) {
   return per * m * n + 4.0 * m * n * k - 2.0 * k * k * (m + n) + 4.0 * k * k * k / 3.0 +
          (double)k * k * r;
 }
+// One pass of the FP32 randomized ID of a box (ell sketch rows): the ID
+// matrix fill, the +-1 sketch (2 ell m n, none when the matrix is no taller
+// than ell and is factored itself), pivoted QR of the min(m, ell) x n tile
+// to the rank, and Z.
+double sketch_id_flops(int m, int n, int k, int ell, int pde) {
+  const double per = pde == kStokes ? 20.0 : 10.0;
+  const double mr = std::min(m, ell), r = n - k;
+  return per * m * n + (m > ell ? 2.0 * ell * m * n : 0.0) + 4.0 * mr * n * k -
+         2.0 * k * k * (mr + n) + 4.0 * k * k * k / 3.0 + (double)k * k * r;
+}
 double dec_flops(int k, int r) {
   const double K = k, R = r;
   return 2.0 * (R * K * K + 2 * R * R * K + R * K * K + K * K * R) + 2.0 / 3.0 * R * R * R +
@@ -457,6 +467,7 @@ rs_status factor_impl(rs_solver* s) {
   s->samp_target.clear();
   s->stats.rank_predicted = 0;
   s->stats.rank_redo = 0;
+  s->stats.sketch_rows = 0;
   // Contents below these marks are live and survive buffer growth.
   size_t fac_prev = F.fac_used, e_prev = F.e_used, piv_prev = s->piv_used;
   double t_plan = 0, t_wait = 0, t_post = 0;
@@ -670,9 +681,11 @@ rs_status factor_impl(rs_solver* s) {
       // predicted sketch sizes written into the uploaded task records
       CU(s->rank_feat.ensure(feat_s.size()));
       CU(s->redo.ensure(idt_s.size()));
+      CU(s->ell_slot.ensure(idt_s.size()));
       CU(stage_copy(s, s->rank_feat.p, feat_s.data(), feat_s.size() * sizeof(float)));
       CU(cudaMemsetAsync(s->redo.p, 0, idt_s.size() * sizeof(int), s->stream));
-      CU(rank_infer_ell(s->rank_w.p, s->rank_feat.p, s->id_tasks.p, (int)idt_s.size(), s->stream));
+      CU(rank_infer_ell(s->rank_w.p, s->rank_feat.p, s->id_tasks.p, (int)idt_s.size(),
+                        s->ell_slot.p, s->stream));
       ++s->launches;
     }
     // ID launches
@@ -725,6 +738,9 @@ rs_status factor_impl(rs_solver* s) {
       CU(s->h_redo.ensure(idt.size()));
       CU(cudaMemcpyAsync(s->h_redo.p, s->redo.p, idt.size() * sizeof(int), cudaMemcpyDeviceToHost,
                          s->stream2));
+      CU(s->h_ell.ensure(idt.size()));
+      CU(cudaMemcpyAsync(s->h_ell.p, s->ell_slot.p, idt.size() * sizeof(int),
+                         cudaMemcpyDeviceToHost, s->stream2));
     }
     CU(cudaMemcpyAsync(s->h_perm.p, s->perm.p + seg0, (seg1 - seg0) * sizeof(int),
                        cudaMemcpyDeviceToHost, s->stream2));
@@ -799,11 +815,24 @@ rs_status factor_impl(rs_solver* s) {
       s->samp_feat.insert(s->samp_feat.end(), feat.begin() + (size_t)S.slot * kRankFeatures,
                           feat.begin() + (size_t)(S.slot + 1) * kRankFeatures);
       s->samp_target.push_back(k > 0 ? (float)k / (float)n : 1.f);
-      if (ip.redo != nullptr && n <= 128) {
-        ++s->stats.rank_predicted;
-        s->stats.rank_redo += s->h_redo.p[S.slot] != 0;
+      const int m = m_of_slot[S.slot];
+      if (f32 && n <= 128) {
+        // rows the randomized ID sketched (m when the matrix is no taller)
+        const int full = n + 16;
+        int ell = full;
+        bool again = false;
+        if (ip.redo != nullptr) {
+          ++s->stats.rank_predicted;
+          again = s->h_redo.p[S.slot] != 0;
+          s->stats.rank_redo += again;
+          ell = std::min(s->h_ell.p[S.slot], full);
+        }
+        s->stats.sketch_rows += std::min(m, ell) + (again ? std::min(m, full) : 0);
+        s->stats.id_flops += sketch_id_flops(m, n, k, ell, s->cfg.pde) +
+                             (again ? sketch_id_flops(m, n, k, full, s->cfg.pde) : 0.0);
+      } else {
+        s->stats.id_flops += id_flops(m, n, k, s->cfg.pde);
       }
-      s->stats.id_flops += id_flops(m_of_slot[S.slot], n, k, s->cfg.pde);
       if (k <= 0) {
         S.e_ld = n;
         continue;

@@ -59,7 +59,8 @@ class RsStats(ctypes.Structure):
                 ("host_wait_ms", ctypes.c_double), ("host_post_ms", ctypes.c_double),
                 ("boxes_factored", ctypes.c_int),
                 ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double),
-                ("rank_predicted", ctypes.c_int), ("rank_redo", ctypes.c_int)]
+                ("rank_predicted", ctypes.c_int), ("rank_redo", ctypes.c_int),
+                ("sketch_rows", ctypes.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -150,6 +150,34 @@ def _ellipse(n, cx, cy, a, b, theta, orient):
     return _param_curve(n, x, y, dx, dy, ddx, ddy, orient)
 
 
+def ellipse(n: int, a: float, b: float, theta: float = 0.0) -> Geometry:
+    """Interior of the ellipse with semi-axes a, b rotated by theta, n nodes
+    equispaced in the parameter."""
+    pts, nrm, w, kappa = _ellipse(n, 0.0, 0.0, a, b, theta, 1.0)
+    hc, hr = _empty_holes()
+    return Geometry(pts, nrm, w, kappa, hc, hr, n)
+
+
+def rank_training_curves(count: int, seed: int, n_range=(8192, 65536)):
+    """Seeded star and ellipse boundaries for training the rank model:
+    random stars r(t) = 1 + sum_{k=2..8} a_k cos(kt + phi_k), stars
+    1 + a cos(kt) with a in [0.05, 0.35], k in 3..9, and ellipses with axis
+    ratio in [0.3, 1]; n uniform in n_range (multiples of 1024)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = 1024 * int(rng.integers(n_range[0] // 1024, n_range[1] // 1024 + 1))
+        kind = i % 3
+        if kind == 0:
+            out.append(random_star(n, rng))
+        elif kind == 1:
+            out.append(star(n, a=float(rng.uniform(0.05, 0.35)), k=int(rng.integers(3, 10))))
+        else:
+            out.append(ellipse(n, 1.0, float(rng.uniform(0.3, 1.0)),
+                               float(rng.uniform(0, math.pi))))
+    return out
+
+
 def _ellipse_perimeter(a, b):
     h = ((a - b) / (a + b)) ** 2
     return math.pi * (a + b) * (1 + 3 * h / (10 + math.sqrt(4 - 3 * h)))

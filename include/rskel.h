@@ -235,6 +235,9 @@ typedef struct {
   int rank_predicted, rank_redo;               /* last rs_factor with a rank model: boxes whose
                                                   sketch size was predicted, and those of them
                                                   redone with the full sketch */
+  double sketch_rows;                          /* last RS_FP32_REFINE rs_factor: rows of the
+                                                  randomized-ID sketches of boxes of <= 128 DOFs,
+                                                  summed (a redone box counts both sketches) */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 

@@ -1,16 +1,19 @@
 """Learned skeleton ranks: the rank model's hand-written CUDA inference,
-gradient and Adam kernels against a PyTorch fp32 restatement of the same
-multilayer perceptron, and the FP32 factorization with predicted sketch
-sizes against the plain one.
+gradient and Adam kernels against the oracle's float64 NumPy restatement
+(itself pinned by central finite differences) and a PyTorch fp32 autograd
+restatement of the same multilayer perceptron, and the FP32 factorization
+with predicted sketch sizes against the plain one.
 
-Tolerances: predicted fractions within 2e-6 of torch's (fp32 sums in
-another order); gradients within 1e-4 of max |grad| (the gradient kernel
-accumulates with atomics in fp32); a factorization with a rank model is
-refined to the same accuracy bar as without (1e-8 relative to the FP64
-solution), whatever the model predicts.
+Tolerances: predicted fractions within 2e-6 of the restatements (fp32 sums
+in another order); gradients within 1e-4 of max |grad| (the gradient kernel
+accumulates with atomics in fp32); Adam steps within 1e-6 of the oracle's;
+a factorization with a rank model is refined to the same accuracy bar as
+without (1e-8 relative to the FP64 solution), whatever the model predicts.
 """
 import numpy as np
 import pytest
+
+import rank_model as RM
 
 RS_ERR_ARG = 1
 
@@ -42,6 +45,30 @@ def test_init_is_deterministic_and_scaled(solver_lib):
     assert np.abs(W1).max() <= np.sqrt(6 / 16) and np.abs(W2).max() <= np.sqrt(6 / 64)
     assert not b1.any() and not b2.any() and b3[0] == 0.0
     assert W1.std() > 0.2 and W2.std() > 0.1
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    w = RM.pack([rng.normal(0, s, shape) for s, shape in
+                 zip((0.6, 0.1, 0.3, 0.1, 0.3, 0.1), RM.SHAPES)])
+    X = rng.uniform(-1, 1, (40, 16))
+    t = rng.uniform(0.05, 0.95, 40)
+    loss, g = RM.loss_and_gradient(w, X, t)
+    assert np.isclose(loss, np.mean((RM.forward(w, X) - t) ** 2))
+    idx = np.concatenate([rng.choice(RM.WEIGHTS, 60, replace=False), [RM.WEIGHTS - 1]])
+    h = 1e-6
+    for i in idx:
+        e = np.zeros(RM.WEIGHTS)
+        e[i] = h
+        fd = (RM.loss_and_gradient(w + e, X, t)[0] - RM.loss_and_gradient(w - e, X, t)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-7 + 1e-5 * abs(g[i]), (i, fd, g[i])
+
+
+def test_oracle_sketch_rows_rule():
+    n = np.array([16, 40, 64, 128, 128])
+    y = np.array([0.0, 0.5, 1.0, 0.25, 0.9])
+    # ceil(1.15 ceil(y n)) + 10, at least 12, at most n + 16
+    assert RM.sketch_rows(y, n).tolist() == [12, 33, 80, 47, 144]
 
 
 def test_rank_entry_points_validate_arguments(solver_lib):
@@ -77,6 +104,7 @@ def test_predict_matches_torch(solver_lib):
     y = s.rank_predict(w, X)
     yt, _ = _torch_mlp(torch, w, X)
     assert np.abs(y - yt.detach().numpy()).max() <= 2e-6
+    assert np.abs(y - RM.forward(w, X)).max() <= 2e-6
     assert s.rank_predict(w, X[:0]).size == 0
 
 
@@ -98,6 +126,36 @@ def test_gradient_matches_torch_autograd(solver_lib):
     gt = np.concatenate([p.grad.numpy().ravel() for p in params])
     assert abs(loss - lt.item()) <= 1e-5 * max(1.0, lt.item())
     assert np.abs(grad - gt).max() <= 1e-4 * np.abs(gt).max()
+    lo, go = RM.loss_and_gradient(w, X, t)
+    assert abs(loss - lo) <= 1e-5 * max(1.0, lo)
+    assert np.abs(grad - go).max() <= 1e-4 * np.abs(go).max()
+
+
+@pytest.mark.gpu
+def test_adam_kernel_matches_oracle(solver_lib):
+    from rskel import geometry as g
+
+    capi = solver_lib
+    rng = np.random.default_rng(6)
+    X = _features(rng, 300)
+    t = rng.uniform(0.1, 0.8, 300).astype(np.float32)
+    s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
+    w0 = capi.rank_model_init(2)
+    w3, _ = s.rank_train(X, t, w0, epochs=3, lr=1e-3)
+    # the same three full-batch steps in float64
+    w, m, v = w0.astype(np.float64), np.zeros(RM.WEIGHTS), np.zeros(RM.WEIGHTS)
+    g1 = None
+    for step in (1, 2, 3):
+        _, gr = RM.loss_and_gradient(w, X, t)
+        g1 = gr if g1 is None else g1
+        w, m, v = RM.adam_step(w, gr, m, v, step, 1e-3)
+    # Adam moves a weight by about lr per step whatever its gradient's size:
+    # compare the moves where the gradient's sign is well determined (fp32
+    # atomics may flip the sign of a gradient near zero), and bound the rest
+    sure = np.abs(g1) > 1e-3 * np.abs(g1).max()
+    assert sure.sum() > 1000
+    assert np.abs((w3 - w0) - (w - w0))[sure].max() <= 2e-5
+    assert np.abs(w3 - w0).max() <= 3.03e-3
 
 
 @pytest.mark.gpu
@@ -165,6 +223,9 @@ def test_learned_sketch_sizes_keep_the_solution(solver_lib):
     st1 = t.stats()
     assert st1["rank_predicted"] > 100
     assert st1["rank_redo"] <= 0.25 * st1["rank_predicted"]
+    # what the model gains: shorter sketches, less ID work
+    assert st1["sketch_rows"] <= 0.85 * st0["sketch_rows"], (st1["sketch_rows"], st0["sketch_rows"])
+    assert st1["id_flops"] <= 0.85 * st0["id_flops"]
     s64 = capi.Solver(g.star(32768), capi.RS_LAPLACE, 1e-8, leaf=64, npp=64)
     s64.factor()
     mu64, _ = s64.solve(F)
@@ -189,6 +250,7 @@ def test_too_small_predictions_fall_back_to_the_full_sketch(solver_lib):
     s.factor()
     mu0, _ = s.solve(F)
     _, y0 = s.rank_samples()
+    s0_rows = s.stats()["sketch_rows"]
     # every prediction ~0: 12-row sketches, so every box of rank > 4 is redone
     w = np.zeros(capi.RANK_WEIGHTS, dtype=np.float32)
     w[-1] = -30.0
@@ -198,6 +260,7 @@ def test_too_small_predictions_fall_back_to_the_full_sketch(solver_lib):
     st = s.stats()
     _, y1 = s.rank_samples()
     assert st["rank_predicted"] > 100 and st["rank_redo"] >= 0.9 * st["rank_predicted"]
+    assert st["sketch_rows"] > s0_rows
     # redone boxes get the plain factorization's ranks
     assert np.abs(y1 - y0).max() <= 0.5 and np.mean(y1 == y0) >= 0.9
     assert np.linalg.norm(mu1 - mu0) / np.linalg.norm(mu0) <= 1e-9
