@@ -90,11 +90,12 @@ constexpr size_t mlp_smem(bool need_w2) {
                           kWarpsPerBlock * (kF + 3 * kH));
 }
 
-// Sketch rows for a box from the predicted rank fraction: 15% headroom plus
-// ten rows of oversampling, never more than the plain n + 16.
-__device__ __forceinline__ int ell_from_fraction(float y, int n) {
+// Sketch rows for a box from the predicted rank fraction: headroom over the
+// predicted rank plus extra rows of oversampling, never more than the plain
+// n + 16.
+__device__ __forceinline__ int ell_from_fraction(float y, int n, float headroom, int extra) {
   const int k = (int)ceilf(y * (float)n);
-  int ell = (int)ceilf(1.15f * (float)k) + 10;
+  int ell = (int)ceilf(headroom * (float)k) + extra;
   if (ell < 12) ell = 12;
   if (ell > n + 16) ell = n + 16;
   return ell;
@@ -103,7 +104,8 @@ __device__ __forceinline__ int ell_from_fraction(float y, int n) {
 template <int kMode>  // 0: predict into out; 1: write tasks[i].ell and ell_by_slot
 __global__ void __launch_bounds__(kMlpThreads) infer_kernel(const float* W, const float* feats,
                                                             int count, float* out,
-                                                            IdTask* tasks, int* ell_by_slot) {
+                                                            IdTask* tasks, int* ell_by_slot,
+                                                            float headroom, int extra) {
   extern __shared__ __align__(16) float smem[];
   SharedMlp m;
   load_mlp(W, smem, &m, false);
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(kMlpThreads) infer_kernel(const float* W, cons
       if (kMode == 0) {
         out[i] = y;
       } else {
-        const int ell = ell_from_fraction(y, tasks[i].n);
+        const int ell = ell_from_fraction(y, tasks[i].n, headroom, extra);
         tasks[i].ell = ell;
         ell_by_slot[tasks[i].slot] = ell;
       }
@@ -210,10 +212,11 @@ int grid_for(int count) {
 }  // namespace
 
 cudaError_t rank_infer_ell(const float* weights, const float* features, IdTask* tasks,
-                           int num_tasks, int* ell_by_slot, cudaStream_t st) {
+                           int num_tasks, int* ell_by_slot, float headroom, int extra,
+                           cudaStream_t st) {
   if (num_tasks <= 0) return cudaSuccess;
   infer_kernel<1><<<grid_for(num_tasks), kMlpThreads, mlp_smem(false), st>>>(
-      weights, features, num_tasks, nullptr, tasks, ell_by_slot);
+      weights, features, num_tasks, nullptr, tasks, ell_by_slot, headroom, extra);
   return cudaGetLastError();
 }
 
@@ -221,7 +224,7 @@ cudaError_t rank_predict(const float* weights, const float* features, int count,
                          cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
   infer_kernel<0><<<grid_for(count), kMlpThreads, mlp_smem(false), st>>>(
-      weights, features, count, out, nullptr, nullptr);
+      weights, features, count, out, nullptr, nullptr, 0.f, 0);
   return cudaGetLastError();
 }
 

@@ -2,8 +2,8 @@
 // ReLU, sigmoid), FP32, predicting a box's ID rank as a fraction of its
 // active DOFs from geometric features of the box.  Trained on ranks the
 // plain factorization produces; the FP32 factorization uses the prediction
-// to size each box's randomized sketch (ell = 1.15 k_pred + 10 rows instead
-// of n + 16), and falls back to the full sketch for any box whose rank test
+// to size each box's randomized sketch (ell = 1.25 k_pred + 12 rows by
+// default instead of n + 16), and falls back to the full sketch for any box whose rank test
 // does not close inside the shorter sketch.  Training and inference are
 // hand-written kernels (rank_model.cu).
 #pragma once
@@ -21,9 +21,11 @@ constexpr int kRankWeights = kRankHidden * kRankFeatures + kRankHidden +
                              kRankHidden * kRankHidden + kRankHidden + kRankHidden + 1;
 
 // Writes tasks[i].ell (sketch rows) for every task from its features
-// (num_tasks x 16, row major), and the same value to ell_by_slot[tasks[i].slot].
+// (num_tasks x 16, row major), and the same value to ell_by_slot[tasks[i].slot]:
+// ell = ceil(headroom * ceil(y n)) + extra, within [12, n + 16].
 cudaError_t rank_infer_ell(const float* weights, const float* features, IdTask* tasks,
-                           int num_tasks, int* ell_by_slot, cudaStream_t st);
+                           int num_tasks, int* ell_by_slot, float headroom, int extra,
+                           cudaStream_t st);
 // out[i] = predicted rank fraction of sample i.
 cudaError_t rank_predict(const float* weights, const float* features, int count, float* out,
                          cudaStream_t st);

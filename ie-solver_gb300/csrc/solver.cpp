@@ -685,7 +685,8 @@ rs_status factor_impl(rs_solver* s) {
       CU(stage_copy(s, s->rank_feat.p, feat_s.data(), feat_s.size() * sizeof(float)));
       CU(cudaMemsetAsync(s->redo.p, 0, idt_s.size() * sizeof(int), s->stream));
       CU(rank_infer_ell(s->rank_w.p, s->rank_feat.p, s->id_tasks.p, (int)idt_s.size(),
-                        s->ell_slot.p, s->stream));
+                        s->ell_slot.p, (float)s->cfg.rank_headroom, s->cfg.rank_extra_rows,
+                        s->stream));
       ++s->launches;
     }
     // ID launches
@@ -1383,6 +1384,8 @@ void rs_config_default(rs_config* c) {
   c->fp32_id_tol = 1e-6;
   c->device = 0;
   c->fmm_order = 0;
+  c->rank_headroom = 1.25;
+  c->rank_extra_rows = 12;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -1396,6 +1399,9 @@ rs_status rs_create(const rs_config* cfg, rs_solver** out) {
     return RS_ERR_ARG;
   if (cfg->is_strong_admissibility) return RS_ERR_ARG;
   if (cfg->precision != RS_FP64 && cfg->precision != RS_FP32_REFINE) return RS_ERR_ARG;
+  if (!(cfg->rank_headroom >= 1.0 && cfg->rank_headroom <= 4.0) || cfg->rank_extra_rows < 0 ||
+      cfg->rank_extra_rows > 128)
+    return RS_ERR_ARG;
   rs_solver* s = new rs_solver();
   s->cfg = *cfg;
   const char* tr = std::getenv("RSKEL_TRACE");

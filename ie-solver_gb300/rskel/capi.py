@@ -41,7 +41,8 @@ class RsConfig(ctypes.Structure):
                 ("is_strong_admissibility", ctypes.c_int), ("precision", ctypes.c_int),
                 ("refine_tol", ctypes.c_double), ("refine_max_iters", ctypes.c_int),
                 ("fp32_id_tol", ctypes.c_double), ("device", ctypes.c_int),
-                ("fmm_order", ctypes.c_int)]
+                ("fmm_order", ctypes.c_int), ("rank_headroom", ctypes.c_double),
+                ("rank_extra_rows", ctypes.c_int)]
 
 
 class RsStats(ctypes.Structure):
@@ -187,14 +188,16 @@ class Solver:
     """One boundary problem: geometry -> quadtree -> factor -> solves."""
 
     def __init__(self, geo, pde, tol, leaf=64, npp=64, precision=RS_FP64, refine_tol=1e-12,
-                 refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16, fmm_order=0):
+                 refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16, fmm_order=0,
+                 rank_headroom=1.25, rank_extra_rows=12):
         self.sd = 2 if pde == RS_STOKES else 1
         self.cfg = default_config(pde=pde, solution_dimension=self.sd, id_tol=tol,
                                   max_leaf_dofs=leaf, num_proxy_points=npp,
                                   precision=precision, refine_tol=refine_tol,
                                   refine_max_iters=refine_max_iters, fp32_id_tol=fp32_id_tol,
                                   device=device, min_dofs_to_compress=min_dofs,
-                                  fmm_order=fmm_order)
+                                  fmm_order=fmm_order, rank_headroom=rank_headroom,
+                                  rank_extra_rows=rank_extra_rows)
         h = _vp()
         self._check(lib().rs_create(ctypes.byref(self.cfg), ctypes.byref(h)), None)
         self.h = h

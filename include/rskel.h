@@ -62,6 +62,10 @@ typedef struct {
   int fmm_order;             /* RS_FP32_REFINE, Laplace: multipole order of the
                                 FP64 residual, 2..64 (0 = matched to refine_tol:
                                 28 at 1e-11, 31 at 1e-12) */
+  double rank_headroom;      /* rank model (rs_set_rank_model): sketch rows
+                                ell = ceil(rank_headroom * k_pred) + rank_extra_rows,
+                                default 1.25 and 12 */
+  int rank_extra_rows;
 } rs_config;
 
 typedef struct rs_solver rs_solver;
@@ -182,7 +186,8 @@ rs_status rs_id_noalloc(int m, int n, const double* A, double tol, int* rank, in
  * from RS_RANK_FEATURES features the host computes per box (ID matrix
  * sizes, tree level and box size, tolerance, kernel, curvature and spread
  * of the box's boundary piece).  The FP32 randomized ID of a box of at most
- * 128 DOFs then sketches with ell = min(n + 16, ceil(1.15 n y) + 10) rows
+ * 128 DOFs then sketches with ell = min(n + 16, ceil(h ceil(n y)) + e) rows (h = rank_headroom, e =
+ * rank_extra_rows of rs_config)
  * instead of n + 16.  A box whose truncated sketch does not settle its rank
  * with 8 rows to spare is redone on the device with the full sketch, so a
  * poor prediction costs time, not accuracy.

@@ -74,8 +74,8 @@ def adam_step(w, g, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):
     return w - lr * mh / (np.sqrt(vh) + eps), m, v
 
 
-def sketch_rows(y, n):
+def sketch_rows(y, n, headroom=1.15, extra=10):
     """Sketch rows of a box of n DOFs for the predicted fraction y."""
     k = np.ceil(np.asarray(y) * n)
-    ell = np.maximum(np.ceil(1.15 * k) + 10, 12)
+    ell = np.maximum(np.ceil(headroom * k) + extra, 12)
     return np.minimum(ell, np.asarray(n) + 16).astype(int)

@@ -168,8 +168,10 @@ int run_id_mode(const char* in, const char* out) {
 
 int main(int argc, char** argv) {
   if (argc == 4 && std::string(argv[1]) == "--id") return run_id_mode(argv[2], argv[3]);
-  if (argc != 3) {
-    fprintf(stderr, "usage: %s problem.rsp result.rsr | --id in out\n", argv[0]);
+  // optional third argument --strong: SkelFactorization with strong admissibility
+  const bool strong = argc == 4 && std::string(argv[3]) == "--strong";
+  if (argc != 3 && !strong) {
+    fprintf(stderr, "usage: %s problem.rsp result.rsr [--strong] | --id in out\n", argv[0]);
     return 2;
   }
   Problem pr;
@@ -207,7 +209,7 @@ int main(int argc, char** argv) {
   std::vector<double> t_factor, t_solve;
   QuadTree* keep = nullptr;
   ie_Mat mu, alpha;
-  SkelFactorization sf(pr.tol, false, pr.threads);
+  SkelFactorization sf(pr.tol, strong, pr.threads);
   int reps = std::max(1, pr.repeats);
   for (int rep = 0; rep < reps; ++rep) {
     QuadTree* tree = new QuadTree();

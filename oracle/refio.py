@@ -62,7 +62,7 @@ def ref_binary(leaf, npp):
 
 
 def run_reference(geo, pde, sd, rhs, tol, leaf=64, npp=64, threads=1, repeats=1,
-                  dense_check=False, timeout=3600):
+                  dense_check=False, timeout=3600, strong=False):
     """Run the reference build on one problem; returns the result dict."""
     exe = ref_binary(leaf, npp)
     if exe is None:
@@ -73,7 +73,8 @@ def run_reference(geo, pde, sd, rhs, tol, leaf=64, npp=64, threads=1, repeats=1,
         pout = os.path.join(td, "r.rsr")
         write_problem(pin, geo, pde, sd, rhs, tol, leaf, npp, threads, repeats, dense_check)
         env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
-        subprocess.run([exe, pin, pout], check=True, timeout=timeout, env=env)
+        cmd = [exe, pin, pout] + (["--strong"] if strong else [])
+        subprocess.run(cmd, check=True, timeout=timeout, env=env)
         return read_result(pout)
 
 

@@ -89,3 +89,26 @@ def test_oracle_matches_live_reference(oracle_lib):
     for k in ("level_sizes", "node_parent", "nbr", "orig"):
         assert np.array_equal(t[k], r[k]), k
     assert np.linalg.norm(mu[:, 0] - r["mu"]) / np.linalg.norm(r["mu"]) < 1e-8
+
+
+def test_reference_strong_admissibility_gives_no_solution(oracle_lib):
+    """Why rs_create rejects is_strong_admissibility: the reference's own
+    strong-admissibility path (SkelFactorization(tol, true, nt)) returns no
+    solution of the system.  decouple (skel_factorization.cpp:87-127) forms
+    L and U from the (r, s) blocks only while solve (skel_factorization.cpp:
+    535-590) applies them over skel + near.  Run here from the reference's
+    sources: the backward error is of order one (or not finite), against
+    ~1e-15 for the weak path on the same problem."""
+    refio = pytest.importorskip("refio")
+    if refio.ref_binary(32, 128) is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    from rskel import geometry as g
+
+    geo = g.unit_circle(512)
+    f = g.laplace_cauchy(geo)[:, None]
+    weak = refio.run_reference(geo, 0, 1, f, 1e-10, leaf=32, npp=128, dense_check=True)
+    strong = refio.run_reference(geo, 0, 1, f, 1e-10, leaf=32, npp=128, dense_check=True,
+                                 strong=True)
+    assert np.abs(weak["dense_residual"]).max() <= 50 * 1e-10
+    res = np.abs(strong["dense_residual"])
+    assert not np.isfinite(res).all() or res.max() > 0.1
