@@ -150,7 +150,8 @@ struct FmmArgs {
   const int *pstart, *pcount, *parent, *slot_pt, *children;
   const int *v_off, *v_idx, *w_off, *w_idx, *x_off, *x_idx, *u_off, *u_idx;
   const int* boxes;
-  int p, npts, nrhs;
+  int p, npts, nrhs;  // nrhs: channels of this pass
+  int mode;           // FmmMode
   const R* charge;  // complex, 2 * (slot + npts * q)
   R* mpole;         // complex, 2 * (k + p * (q + nrhs * box))
   R* local;
@@ -202,6 +203,85 @@ __global__ void charges_kernel(Geo<double> g, const int* slot_pt, int npts, cons
   charge[2 * e + 1] = (R)(a * g.ny[pt]);
 }
 
+// Neumann (adjoint double layer, kernel.cpp:80-91): real charges
+// c_j = (w_j / 2pi) mu_j; (K mu)_i gets Re(nu_i sum_j c_j / (z_i - z_j)).
+template <class R>
+__global__ void neumann_charges_kernel(Geo<double> g, const int* slot_pt, int npts,
+                                       const double* mu, int nrhs, R* charge) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)npts * nrhs) return;
+  const int s = (int)(e % npts), q = (int)(e / npts);
+  const int pt = slot_pt[s];
+  charge[2 * e] = to_r<R>(g.w[pt] * (1.0 / (2.0 * CUDART_PI)) * mu[pt + (size_t)npts * q]);
+  charge[2 * e + 1] = to_r<R>(0.0);
+}
+
+// Stokes double layer in complex form.  With tau = z_i - z_j, nu_j the
+// normal and mu_j = mu_x + i mu_y the density, the off-diagonal part of
+// kernel.cpp:212-290, (w_j/pi) (r.n_j)(r.mu_j) r / |r|^4, is
+//   a_j / tau + b_j / conj(tau) + conj(a_j) tau / conj(tau)^2,
+//   a_j = (w_j / 4pi) nu_j mu_j,  b_j = (w_j / 2pi) Re(conj(nu_j) mu_j) (real).
+// Summed over j that is S_A + conj(S_B) - conj((conj(z) - conj(c)) S_A' + G')
+// for Cauchy sums S_A, S_B (charges a, b) and, about any centre c, the sum
+// G(z) = sum_j a_j (conj(c) - conj(z_j)) / (z - z_j).  Three channels per
+// density: A, B, and E with charges a_j conj(z_j - c_leaf) relative to the
+// source leaf's centre; translations turn E into G with conjugated box
+// offsets (M2M, M2L, L2L below), so no absolute coordinate enters.
+template <class R>
+__global__ void stokes_charges_kernel(Geo<double> g, const int* slot_pt, const double* rx,
+                                      const double* ry, int npts, const double* mu, int nq,
+                                      R* charge) {
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)npts * nq) return;
+  const int s = (int)(e % npts), q = (int)(e / npts);
+  const int pt = slot_pt[s];
+  const size_t D = 2 * (size_t)npts;
+  const double mx = mu[2 * (size_t)pt + D * q], my = mu[2 * (size_t)pt + 1 + D * q];
+  const double nx = g.nx[pt], ny = g.ny[pt], f = g.w[pt] * (1.0 / (4.0 * CUDART_PI));
+  const double ar = f * (nx * mx - ny * my), ai = f * (nx * my + ny * mx);
+  const double b = 2.0 * f * (nx * mx + ny * my);
+  const double er = ar * rx[s] + ai * ry[s], ei = ai * rx[s] - ar * ry[s];  // a conj(rel)
+  const double v[6] = {ar, ai, b, 0.0, er, ei};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t o = s + (size_t)npts * (3 * q + c);
+    charge[2 * o] = to_r<R>(v[2 * c]);
+    charge[2 * o + 1] = to_r<R>(v[2 * c + 1]);
+  }
+}
+
+// Per right-hand side, the rank-one part of the Neumann and Stokes operators:
+// sum_j w_j mu_j (Neumann, kernel.cpp:80-91) or sum_j w_j n_j . mu_j (Stokes,
+// the w n_t n_s term of kernel.cpp:212-290).  One block per right-hand side.
+__global__ void rank1_kernel(Geo<double> g, int npts, const double* mu, int mode, double* out) {
+  __shared__ double red[1024];
+  const int q = blockIdx.x;
+  double acc = 0.0;
+  if (mode == 1) {
+    for (int i = threadIdx.x; i < npts; i += blockDim.x) acc += g.w[i] * mu[i + (size_t)npts * q];
+  } else {
+    const size_t D = 2 * (size_t)npts;
+    for (int i = threadIdx.x; i < npts; i += blockDim.x)
+      acc += g.w[i] * (g.nx[i] * mu[2 * (size_t)i + D * q] + g.ny[i] * mu[2 * (size_t)i + 1 + D * q]);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[q] = red[0];
+}
+
+template <class R>
+__device__ __forceinline__ Cx<R> cconj(Cx<R> a) {
+  return {a.re, -a.im};
+}
+template <class R>
+__device__ __forceinline__ bool is_g(const FmmArgs<R>& a, int q) {
+  return a.mode == 2 && q % 3 == 2;
+}
+
 // P2M for every non-empty leaf (points staged kStage at a time).
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
@@ -248,6 +328,8 @@ __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
 // expansions.  With d = (z_C - z_P)/s_P and g = 1/(2d) the shift is
 //   M_l(P) = sum_C d^l sum_{k<=l} C(l,k) (M_k(C) g^k),
 // a real Pascal-matrix product between two diagonal complex scalings.
+// Stokes E channels re-centre their charges a_j conj(z_j - c) on the
+// parent: E(P) = shift(E(C)) + conj(z_C - z_P) shift(A(C)).
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -257,7 +339,12 @@ __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
   Cx<R>* dl = reinterpret_cast<Cx<R>*>(smem);  // 4 x p: d_c^l
   Cx<R>* gk = dl + 4 * p;                      // 4 x p: g_c^k
   Cx<R>* av = gk + 4 * p;                      // 4 x nrhs x p: M_k(c) g_c^k
+  Cx<R>* oc = av + 4 * p * nrhs;               // 4: conj(z_C - z_P)
   const R isp = rcp(side_of(a, P));
+  if (threadIdx.x < 4) {
+    const int C = a.children[4 * P + threadIdx.x];
+    if (C >= 0) oc[threadIdx.x] = cconj(box_off(a, P, C));
+  }
   if (threadIdx.x < 8) {
     const int c = threadIdx.x & 3;
     const int C = a.children[4 * P + c];
@@ -292,6 +379,16 @@ __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
         t.re += bk * ac[k].re;
         t.im += bk * ac[k].im;
       }
+      if (is_g(a, q)) {
+        const Cx<R>* aa = av + (size_t)p * (q - 2 + nrhs * c);
+        Cx<R> ta = {(R)0, (R)0};
+        for (int k = 0; k <= l; ++k) {
+          const R bk = a.binom[l * P2 + k];
+          ta.re += bk * aa[k].re;
+          ta.im += bk * aa[k].im;
+        }
+        t = cadd(t, cmul(oc[c], ta));
+      }
       acc = cadd(acc, cmul(dl[c * p + l], t));
     }
     st_c(a.mpole, l + (size_t)p * (q + nrhs * (size_t)P), acc);
@@ -299,6 +396,8 @@ __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
 }
 
 // M2L from the V list and P2L from the X list; writes the box's local expansion.
+// Stokes G channels: G(B) gets conj(c_B - c_C) M2L(A(C)) - M2L(E(C)) from a
+// V-list box, and charges -a_j conj(z_j - c_B) from an X-list box's points.
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -307,6 +406,8 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   Cx<R>* av = reinterpret_cast<Cx<R>*>(smem);  // p x nrhs scaled source coefficients
   Cx<R>* vp = av + (size_t)p * nrhs;           // p: (-1)^l (s_B/d)^l / d
   Cx<R>* pw = vp + p;                          // kStage x p powers for P2L
+  Cx<R>* ws = pw + kStage * (size_t)p;         // kStage: conj(z_j - c_B) (Stokes X list)
+  Cx<R>* dcs = ws + kStage;                    // 1: conj(c_B - c_C) (Stokes V list)
   const R sB = side_of(a, B);
   constexpr int kPer = 4;  // (l, q) pairs per thread (p * nrhs <= 512)
   Cx<R> acc[kPer];
@@ -318,6 +419,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
       const Cx<R> id = cinv(box_off(a, C, B));
       // thread 0: u^k (u = s_C / d) into pw; thread 1: vp
       if (threadIdx.x == 0) {
+        dcs[0] = cconj(box_off(a, C, B));
         const Cx<R> u = cscale(id, side_of(a, C));
         Cx<R> v = {(R)1, (R)0};
         for (int k = 0; k < p; ++k) {
@@ -352,6 +454,15 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
         s.re += bk * av[k + p * q].re;
         s.im += bk * av[k + p * q].im;
       }
+      if (is_g(a, q)) {
+        Cx<R> sa = {(R)0, (R)0};
+        for (int k = 0; k < p; ++k) {
+          const R bk = brow[(size_t)(k + l) * P2];
+          sa.re += bk * av[k + p * (q - 2)].re;
+          sa.im += bk * av[k + p * (q - 2)].im;
+        }
+        s = csub(cmul(dcs[0], sa), s);
+      }
       acc[t] = cadd(acc[t], cmul(vp[l], s));
     }
     __syncthreads();
@@ -363,7 +474,9 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
     for (int j0 = 0; j0 < cnt; j0 += kStage) {
       const int jc = cnt - j0 < kStage ? cnt - j0 : kStage;
       for (int j = threadIdx.x; j < jc; j += blockDim.x) {
-        const Cx<R> iw = cinv(cadd(vec(pt_pos(a, s0 + j0 + j)), offS));
+        const Cx<R> w = cadd(vec(pt_pos(a, s0 + j0 + j)), offS);
+        const Cx<R> iw = cinv(w);
+        ws[j] = cconj(w);
         const Cx<R> r = cscale(iw, sB);
         Cx<R> v = iw;  // 1/w * r^l
         for (int l = 0; l < p; ++l) {
@@ -377,10 +490,17 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
         const int e = threadIdx.x + t * blockDim.x;
         if (e >= p * nrhs) break;
         const int l = e % p, q = e / p;
-        for (int j = 0; j < jc; ++j) {
-          const Cx<R> v = cmul(ld_c(a.charge, s0 + j0 + j + (size_t)a.npts * q), pw[j * p + l]);
-          acc[t].re -= v.re;
-          acc[t].im -= v.im;
+        if (is_g(a, q)) {  // charges -a_j conj(w_j)
+          for (int j = 0; j < jc; ++j) {
+            const Cx<R> c = cmul(ld_c(a.charge, s0 + j0 + j + (size_t)a.npts * (q - 2)), ws[j]);
+            acc[t] = cadd(acc[t], cmul(c, pw[j * p + l]));
+          }
+        } else {
+          for (int j = 0; j < jc; ++j) {
+            const Cx<R> v = cmul(ld_c(a.charge, s0 + j0 + j + (size_t)a.npts * q), pw[j * p + l]);
+            acc[t].re -= v.re;
+            acc[t].im -= v.im;
+          }
         }
       }
       __syncthreads();
@@ -398,6 +518,8 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
 // L2L: each non-empty box of a level adds its parent's shifted local
 // expansion.  With e = (z_C - z_P)/s_P the shift is
 //   L_m(C) += (2e)^-m sum_{l>=m} C(l,m) (L_l(P) e^l).
+// Stokes G channels re-centre on the child: G(C) += shift(G(P)) +
+// conj(z_C - z_P) shift(A(P)).
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -408,6 +530,7 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
   Cx<R>* el = reinterpret_cast<Cx<R>*>(smem);  // p: e^l
   Cx<R>* hm = el + p;                          // p: (2e)^-m
   Cx<R>* bv = hm + p;                          // nrhs x p: L_l(P) e^l
+  const Cx<R> ocp = cconj(box_off(a, P, C));
   if (threadIdx.x < 2) {
     const Cx<R> e = cscale(box_off(a, P, C), rcp(side_of(a, P)));
     const Cx<R> base = threadIdx.x == 0 ? e : cinv(cscale(e, (R)2));
@@ -433,13 +556,24 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
       t.re += bl * bq[l].re;
       t.im += bl * bq[l].im;
     }
+    if (is_g(a, q)) {
+      const Cx<R>* ba = bv + (size_t)p * (q - 2);
+      Cx<R> ta = {(R)0, (R)0};
+      for (int l = m; l < p; ++l) {
+        const R bl = a.binom[l * P2 + m];
+        ta.re += bl * ba[l].re;
+        ta.im += bl * ba[l].im;
+      }
+      t = cadd(t, cmul(ocp, ta));
+    }
     const size_t o = m + (size_t)p * (q + nrhs * (size_t)C);
     st_c(a.local, o, cadd(ld_c(a.local, o), cmul(hm[m], t)));
   }
 }
 
 // Evaluation at a leaf's points: L2P + M2P (W list) + P2P (U list), then
-// y = ya * y + yb * (diag mu + phi).  A leaf holds ~30 points on average, so
+// y = ya * y + yb * (diag mu + phi) (Laplace double layer; for Neumann, phi
+// is Re of the target normal times the Cauchy sum, plus the rank-one sum).  A leaf holds ~30 points on average, so
 // each target is shared by nsplit = blockDim / cnt threads: they split the
 // right-hand sides of L2P / M2P and the sources of P2P (the t-th thread of a
 // target takes every nsplit-th one, starting at t), and their partial
@@ -447,7 +581,8 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
 template <class R>
 __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo<double> g,
                                                                const double* mu, double* y,
-                                                               double ya, double yb) {
+                                                               double ya, double yb,
+                                                               const double* r1) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = a.boxes[blockIdx.x];
   const int s0 = a.pstart[B], cnt = a.pcount[B];
@@ -466,6 +601,12 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
 #pragma unroll
     for (int q = 0; q < kMaxRhs; ++q) phi[q] = (R)0;
     Pos<R> tp{};
+    // Neumann: every Cauchy sum is multiplied by the target normal
+    Cx<R> tnu = {(R)1, (R)0};
+    if (act && a.mode == 1) {
+      const int pt = a.slot_pt[s0 + j];
+      tnu = {to_r<R>(g.nx[pt]), to_r<R>(g.ny[pt])};
+    }
     if (act) {
       tp = pt_pos(a, s0 + j);
       // L2P
@@ -476,7 +617,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
           const R* L = a.local + 2 * (size_t)p * (q + nrhs * (size_t)B);
           Cx<R> h = ld_c(L, p - 1);
           for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
-          phi[q] += h.re;
+          phi[q] += cmul(tnu, h).re;
         }
       }
       // M2P from the W list
@@ -490,7 +631,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
             const R* M = a.mpole + 2 * (size_t)p * (q + nrhs * (size_t)C);
             Cx<R> h = ld_c(M, p - 1);
             for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, t), ld_c(M, k));
-            phi[q] += cmul(h, iw).re;
+            phi[q] += cmul(tnu, cmul(h, iw)).re;
           }
         }
       }
@@ -514,7 +655,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
         if (act) {
           for (int i = part; i < ic; i += nsplit) {
             if (d0 + i0 + i == s0 + j) continue;  // self
-            const Cx<R> iv = cinv(diff(tp, sp[i], offD));
+            const Cx<R> iv = cmul(tnu, cinv(diff(tp, sp[i], offD)));
 #pragma unroll
             for (int q = 0; q < kMaxRhs; ++q)
               if (q < nrhs)
@@ -539,12 +680,13 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
     }
     if (act && part == 0) {
       const int pt = a.slot_pt[s0 + j];
-      const double diag = 0.5 + 0.5 * g.kap[pt] * g.w[pt] * (1.0 / (2.0 * CUDART_PI));
+      const double diag = (a.mode == 1 ? -0.5 : 0.5) +
+                          0.5 * g.kap[pt] * g.w[pt] * (1.0 / (2.0 * CUDART_PI));
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) {
         if (q < nrhs) {
           const size_t o = pt + (size_t)a.npts * q;
-          const double v = yb * (diag * mu[o] + tot[q]);
+          const double v = yb * (diag * mu[o] + tot[q] + (a.mode == 1 ? r1[q] : 0.0));
           y[o] = ya == 0.0 ? v : ya * y[o] + v;
         }
       }
@@ -552,9 +694,170 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
   }
 }
 
+// Stokes evaluation at a leaf's points (channels A, B, G of up to
+// kMaxDens densities): with rho = (z - c_B)/s_B,
+//   u = S_A + conj(S_B) - conj(conj(rho) dS_A/drho + dG/dz)   (local part)
+// plus, per W-list box C (w = z - c_C), S_A + conj(S_B) +
+// conj(S_E' - conj(w) S_A'), and per U-list source the direct
+// a/tau + b/conj(tau) + conj(a conj(tau) / tau^2); then the diagonal
+// -mu/2 + pot t (t . mu) (pot = -kappa w / 2pi, t the tangent) and the
+// rank-one n_i sum_j w_j n_j . mu_j of kernel.cpp:212-290.
+constexpr int kMaxDens = kMaxRhs / 3;
 template <class R>
-cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs, double* y,
-                    double ya, double yb, cudaStream_t st) {
+__global__ void __launch_bounds__(kEvalThreads, 4) stokes_eval_kernel(FmmArgs<R> a,
+                                                                      Geo<double> g,
+                                                                      const double* mu,
+                                                                      double* y, double ya,
+                                                                      double yb,
+                                                                      const double* r1) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int B = a.boxes[blockIdx.x];
+  const int s0 = a.pstart[B], cnt = a.pcount[B];
+  const int p = a.p, nch = a.nrhs, nq = nch / 3;
+  Pos<R>* sp = reinterpret_cast<Pos<R>*>(smem);
+  R* sc = reinterpret_cast<R*>(sp + kStage);                           // kStage x kMaxRhs complex
+  double* red = reinterpret_cast<double*>(sc + 2 * kStage * kMaxRhs);  // blockDim x 2 kMaxDens
+  const R isB = rcp(side_of(a, B));
+  const int nsplit = (cnt > 0 && 2 * cnt <= (int)blockDim.x) ? (int)blockDim.x / cnt : 1;
+  const int span = nsplit > 1 ? cnt : (int)blockDim.x;
+  const int part = threadIdx.x / span, tj = threadIdx.x % span;
+  for (int j0 = 0; j0 < cnt; j0 += span) {
+    const int j = j0 + tj;
+    const bool act = j < cnt && part < nsplit;
+    Cx<R> u[kMaxDens];
+#pragma unroll
+    for (int d = 0; d < kMaxDens; ++d) u[d] = {(R)0, (R)0};
+    Pos<R> tp{};
+    if (act) {
+      tp = pt_pos(a, s0 + j);
+      const Cx<R> rho = cscale(vec(tp), isB);
+#pragma unroll
+      for (int d = 0; d < kMaxDens; ++d) {
+        if (d < nq && d % nsplit == part) {
+          const R* LA = a.local + 2 * (size_t)p * (3 * d + nch * (size_t)B);
+          const R* LB = LA + 2 * (size_t)p;
+          const R* LG = LB + 2 * (size_t)p;
+          Cx<R> hA = ld_c(LA, p - 1), dA = {(R)0, (R)0};
+          Cx<R> hB = ld_c(LB, p - 1);
+          Cx<R> hG = ld_c(LG, p - 1), dG = {(R)0, (R)0};
+          for (int l = p - 2; l >= 0; --l) {
+            dA = cadd(cmul(dA, rho), hA);
+            hA = cadd(cmul(hA, rho), ld_c(LA, l));
+            hB = cadd(cmul(hB, rho), ld_c(LB, l));
+            dG = cadd(cmul(dG, rho), hG);
+            hG = cadd(cmul(hG, rho), ld_c(LG, l));
+          }
+          const Cx<R> c3 = cadd(cmul(cconj(rho), dA), cscale(dG, isB));
+          u[d] = cadd(u[d], csub(cadd(hA, cconj(hB)), cconj(c3)));
+        }
+      }
+      for (int wi = a.w_off[B]; wi < a.w_off[B + 1]; ++wi) {
+        const int C = a.w_idx[wi];
+        const Cx<R> w = cadd(vec(tp), box_off(a, C, B));  // z - c_C
+        const Cx<R> iw = cinv(w);
+        const Cx<R> t = cscale(iw, side_of(a, C));
+        const Cx<R> iw2 = cmul(iw, iw);
+#pragma unroll
+        for (int d = 0; d < kMaxDens; ++d) {
+          if (d < nq && d % nsplit == part) {
+            const R* MA = a.mpole + 2 * (size_t)p * (3 * d + nch * (size_t)C);
+            const R* MB = MA + 2 * (size_t)p;
+            const R* ME = MB + 2 * (size_t)p;
+            const R kp = to_r<R>((double)p);
+            Cx<R> hA = ld_c(MA, p - 1), kA = cscale(ld_c(MA, p - 1), kp);
+            Cx<R> hB = ld_c(MB, p - 1), kE = cscale(ld_c(ME, p - 1), kp);
+            for (int k = p - 2; k >= 0; --k) {
+              const R k1 = to_r<R>((double)(k + 1));
+              hA = cadd(cmul(hA, t), ld_c(MA, k));
+              kA = cadd(cmul(kA, t), cscale(ld_c(MA, k), k1));
+              hB = cadd(cmul(hB, t), ld_c(MB, k));
+              kE = cadd(cmul(kE, t), cscale(ld_c(ME, k), k1));
+            }
+            // S = iw h, S' = -iw^2 sum (k+1) M_k t^k
+            const Cx<R> SA = cmul(iw, hA), SB = cmul(iw, hB);
+            const Cx<R> dSA = cmul(iw2, kA), dSE = cmul(iw2, kE);  // -S'
+            // conj(S_E' - conj(w) S_A') = conj(conj(w) dSA - dSE)
+            const Cx<R> c3 = csub(cmul(cconj(w), dSA), dSE);
+            u[d] = cadd(u[d], cadd(cadd(SA, cconj(SB)), cconj(c3)));
+          }
+        }
+      }
+    }
+    for (int ui = a.u_off[B]; ui < a.u_off[B + 1]; ++ui) {
+      const int D = a.u_idx[ui];
+      const int d0 = a.pstart[D], dcnt = a.pcount[D];
+      const auto offD = p2p_off(a, B, D);
+      for (int i0 = 0; i0 < dcnt; i0 += kStage) {
+        const int ic = dcnt - i0 < kStage ? dcnt - i0 : kStage;
+        __syncthreads();
+        for (int e = threadIdx.x; e < ic; e += blockDim.x) sp[e] = pt_pos(a, d0 + i0 + e);
+        for (int e = threadIdx.x; e < ic * nch; e += blockDim.x) {
+          const int i = e % ic, q = e / ic;
+          const size_t src = d0 + i0 + i + (size_t)a.npts * q;
+          sc[2 * (i + kStage * q)] = a.charge[2 * src];
+          sc[2 * (i + kStage * q) + 1] = a.charge[2 * src + 1];
+        }
+        __syncthreads();
+        if (act) {
+          for (int i = part; i < ic; i += nsplit) {
+            if (d0 + i0 + i == s0 + j) continue;  // self
+            const Cx<R> tau = diff(tp, sp[i], offD);
+            const Cx<R> iv = cinv(tau);
+            const Cx<R> q2 = cmul(cconj(tau), cmul(iv, iv));  // conj(tau) / tau^2
+#pragma unroll
+            for (int d = 0; d < kMaxDens; ++d) {
+              if (d < nq) {
+                const Cx<R> av = {sc[2 * (i + kStage * 3 * d)], sc[2 * (i + kStage * 3 * d) + 1]};
+                const R bv = sc[2 * (i + kStage * (3 * d + 1))];
+                u[d] = cadd(u[d], cadd(cadd(cmul(av, iv), cscale(cconj(iv), bv)),
+                                       cconj(cmul(av, q2))));
+              }
+            }
+          }
+        }
+      }
+    }
+    double tot[2 * kMaxDens];
+#pragma unroll
+    for (int d = 0; d < kMaxDens; ++d) {
+      tot[2 * d] = (double)u[d].re;
+      tot[2 * d + 1] = (double)u[d].im;
+    }
+    if (nsplit > 1) {
+      __syncthreads();
+      if (act)
+#pragma unroll
+        for (int q = 0; q < 2 * kMaxDens; ++q) red[threadIdx.x * 2 * kMaxDens + q] = tot[q];
+      __syncthreads();
+      if (act && part == 0)
+        for (int t = 1; t < nsplit; ++t)
+#pragma unroll
+          for (int q = 0; q < 2 * kMaxDens; ++q) tot[q] += red[(t * span + tj) * 2 * kMaxDens + q];
+    }
+    if (act && part == 0) {
+      const int pt = a.slot_pt[s0 + j];
+      const double nx = g.nx[pt], ny = g.ny[pt], tx = -ny, ty = nx;
+      const double pot = -0.5 * g.kap[pt] * g.w[pt] * (1.0 / CUDART_PI);
+      const size_t D = 2 * (size_t)a.npts;
+#pragma unroll
+      for (int d = 0; d < kMaxDens; ++d) {
+        if (d < nq) {
+          const size_t o = 2 * (size_t)pt + D * d;
+          const double mx = mu[o], my = mu[o + 1];
+          const double tm = pot * (tx * mx + ty * my);
+          const double vx = yb * (-0.5 * mx + tm * tx + nx * r1[d] + tot[2 * d]);
+          const double vy = yb * (-0.5 * my + tm * ty + ny * r1[d] + tot[2 * d + 1]);
+          y[o] = ya == 0.0 ? vx : ya * y[o] + vx;
+          y[o + 1] = ya == 0.0 ? vy : ya * y[o + 1] + vy;
+        }
+      }
+    }
+  }
+}
+
+template <class R>
+cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* mu, int nrhs,
+                    double* y, double ya, double yb, cudaStream_t st) {
   constexpr bool f32 = std::is_same<R, float>::value;
   const int p = f32 ? f.p32 : f.p;
   const int npts = f.npts, nb = f.nbox;
@@ -568,6 +871,7 @@ cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nr
   if ((e = f.charge.ensure(2 * (size_t)npts * kMaxRhs)) != cudaSuccess) return e;
   if ((e = f.mpole.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
   if ((e = f.local.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
+  if ((e = f.r1.ensure(kMaxRhs)) != cudaSuccess) return e;
   FmmArgs<R> a{};
   a.cx = f.cx.p;
   a.cy = f.cy.p;
@@ -596,19 +900,32 @@ cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nr
   a.u_idx = f.u_idx.p;
   a.p = p;
   a.npts = npts;
+  a.mode = mode;
   R* charge = reinterpret_cast<R*>(f.charge.p);
   a.charge = charge;
   a.mpole = reinterpret_cast<R*>(f.mpole.p);
   a.local = reinterpret_cast<R*>(f.local.p);
   const unsigned nleaves = (unsigned)f.leaves_h.size();
-  for (int q0 = 0; q0 < nrhs; q0 += kMaxRhs) {
-    const int nq = nrhs - q0 < kMaxRhs ? nrhs - q0 : kMaxRhs;
-    a.nrhs = nq;
-    const double* muq = mu + (size_t)npts * q0;
-    double* yq = y + (size_t)npts * q0;
+  // densities per pass: one channel each (Laplace, Neumann) or three (Stokes)
+  const int per = mode == 2 ? kMaxDens : kMaxRhs;
+  const size_t dcol = (size_t)npts * (mode == 2 ? 2 : 1);
+  for (int q0 = 0; q0 < nrhs; q0 += per) {
+    const int nq = nrhs - q0 < per ? nrhs - q0 : per;
+    const int nch = mode == 2 ? 3 * nq : nq;
+    a.nrhs = nch;
+    const double* muq = mu + dcol * q0;
+    double* yq = y + dcol * q0;
     const size_t tot = (size_t)npts * nq;
-    charges_kernel<R><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(geo, f.slot_pt.p, npts, muq,
-                                                                     nq, charge);
+    const unsigned cg = (unsigned)((tot + 255) / 256);
+    if (mode == 0) {
+      charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq, charge);
+    } else if (mode == 1) {
+      neumann_charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq, charge);
+    } else {
+      stokes_charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, f.rx.p, f.ry.p, npts, muq,
+                                                   nq, charge);
+    }
+    if (mode != 0) rank1_kernel<<<nq, 1024, 0, st>>>(geo, npts, muq, mode, f.r1.p);
     // upward pass
     a.boxes = f.leaves.p;
     if (nleaves)
@@ -618,29 +935,33 @@ cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nr
       const int cnt = f.level_off[lv + 1] - f.level_off[lv];
       if (!cnt) continue;
       a.boxes = f.lvl_boxes.p + f.level_off[lv];
-      m2m_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (8 * (size_t)p + 4 * (size_t)p * nq), st>>>(a);
+      m2m_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (8 * (size_t)p + 4 * (size_t)p * nch + 4),
+                      st>>>(a);
     }
     // interactions and downward pass
-    if ((e = cudaMemsetAsync(f.local.p, 0, 2 * sizeof(R) * (size_t)p * nq * nb, st)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(f.local.p, 0, 2 * sizeof(R) * (size_t)p * nch * nb, st)) !=
+        cudaSuccess)
       return e;
     if (!f.m2l_boxes_h.empty()) {
       a.boxes = f.m2l_boxes.p;
       m2l_kernel<R><<<(unsigned)f.m2l_boxes_h.size(), kFmmThreads,
-                      sizeof(Cx<R>) * ((size_t)p * nq + p + kStage * (size_t)p), st>>>(a);
+                      sizeof(Cx<R>) * ((size_t)p * nch + p + kStage * (size_t)p + kStage + 1),
+                      st>>>(a);
     }
     // locals of levels <= 2 come only from M2L (level 0/1 locals are zero)
     for (int lv = 3; lv < f.nlevels; ++lv) {
       const int cnt = f.level_off[lv + 1] - f.level_off[lv];
       if (!cnt) continue;
       a.boxes = f.lvl_boxes.p + f.level_off[lv];
-      l2l_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (2 * (size_t)p + (size_t)p * nq), st>>>(a);
+      l2l_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (2 * (size_t)p + (size_t)p * nch), st>>>(a);
     }
     a.boxes = f.leaves.p;
-    if (nleaves)
-      eval_kernel<R><<<nleaves, kEvalThreads,
-                       sizeof(Pos<R>) * kStage + sizeof(Cx<R>) * kStage * kMaxRhs +
-                           sizeof(double) * kEvalThreads * kMaxRhs, st>>>(
-          a, geo, muq, yq, ya, yb);
+    const size_t esm = sizeof(Pos<R>) * kStage + sizeof(Cx<R>) * kStage * kMaxRhs +
+                       sizeof(double) * kEvalThreads * kMaxRhs;
+    if (nleaves && mode == 2)
+      stokes_eval_kernel<R><<<nleaves, kEvalThreads, esm, st>>>(a, geo, muq, yq, ya, yb, f.r1.p);
+    else if (nleaves)
+      eval_kernel<R><<<nleaves, kEvalThreads, esm, st>>>(a, geo, muq, yq, ya, yb, f.r1.p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -648,13 +969,22 @@ cudaError_t apply_t(FmmPlan& f, const Geo<double>& geo, const double* mu, int nr
 
 }  // namespace
 
-cudaError_t fmm_laplace_apply(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs,
-                              double* y, double ya, double yb, int arith, cudaStream_t st) {
-  if (!f.built) return cudaErrorInvalidValue;
+int fmm_launches(const FmmPlan& f, int pde, int nrhs) {
+  const int per = pde == 2 ? kMaxDens : kMaxRhs;
+  const int passes = (nrhs + per - 1) / per;
+  int k = 1 + (pde != 0) + (f.leaves_h.empty() ? 0 : 2) + (f.m2l_boxes_h.empty() ? 0 : 1);
+  for (int lv = f.nlevels - 2; lv >= 2; --lv) k += f.level_off[lv + 1] > f.level_off[lv];
+  for (int lv = 3; lv < f.nlevels; ++lv) k += f.level_off[lv + 1] > f.level_off[lv];
+  return passes * k;
+}
+
+cudaError_t fmm_apply(FmmPlan& f, int pde, const Geo<double>& geo, const double* mu, int nrhs,
+                      double* y, double ya, double yb, int arith, cudaStream_t st) {
+  if (!f.built || pde < 0 || pde > 2) return cudaErrorInvalidValue;
   switch (arith) {
-    case kFmmF64: return apply_t<double>(f, geo, mu, nrhs, y, ya, yb, st);
-    case kFmmF32: return apply_t<float>(f, geo, mu, nrhs, y, ya, yb, st);
-    case kFmmDF: return apply_t<DF>(f, geo, mu, nrhs, y, ya, yb, st);
+    case kFmmF64: return apply_t<double>(f, pde, geo, mu, nrhs, y, ya, yb, st);
+    case kFmmF32: return apply_t<float>(f, pde, geo, mu, nrhs, y, ya, yb, st);
+    case kFmmDF: return apply_t<DF>(f, pde, geo, mu, nrhs, y, ya, yb, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -1,5 +1,7 @@
-// Fast multipole evaluation of the Laplace double-layer operator, used for
-// the residual of the FP32 factorization's iterative refinement.
+// Fast multipole evaluation of the boundary operators (Laplace double layer,
+// Laplace-Neumann, Stokes double layer), used for the residual of the FP32
+// factorization's iterative refinement.  The Laplace formulation follows;
+// the Neumann and Stokes forms (further Cauchy sums) are in fmm.cu.
 //
 // In complex notation (z = x + iy, nu = n_x + i n_y) the double-layer kernel
 // of ie_solver/kernel/kernel.cpp:123-165 is
@@ -67,6 +69,7 @@ struct FmmPlan {
   // work buffers (complex pairs of the variant's number type; sized for FP64)
   DevBuf<double> charge;       // 2 * (slot + npts * rhs)
   DevBuf<double> mpole, local; // 2 * (k + p * (rhs + nrhs * box))
+  DevBuf<double> r1;           // per right-hand side: the rank-one sums (Neumann, Stokes)
 };
 
 // Builds the lists on the host from the tree (points interleaved, sd = 1).
@@ -74,10 +77,15 @@ struct FmmPlan {
 bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p, int p32,
                cudaStream_t st);
 
-// y[:, q] = ya * y[:, q] + yb * (K mu)[:, q] for the Laplace double layer
-// (device pointers, column major npts x nrhs; y is not read when ya == 0),
-// in the arithmetic `arith` (FmmArith).  geo holds the per-point boundary data.
-cudaError_t fmm_laplace_apply(FmmPlan& f, const Geo<double>& geo, const double* mu, int nrhs,
-                              double* y, double ya, double yb, int arith, cudaStream_t st);
+// y[:, q] = ya * y[:, q] + yb * (K mu)[:, q] for the operator of `pde`
+// (Pde: Laplace double layer, Laplace-Neumann, Stokes double layer with its
+// rank-one completion) as kernel_entry defines it; device pointers, column
+// major D x nrhs (D = npts, or 2 npts interleaved for Stokes); y is not read
+// when ya == 0.  Arithmetic `arith` (FmmArith); geo holds the per-point
+// boundary data.
+cudaError_t fmm_apply(FmmPlan& f, int pde, const Geo<double>& geo, const double* mu, int nrhs,
+                      double* y, double ya, double yb, int arith, cudaStream_t st);
+// Kernels one fmm_apply launches.
+int fmm_launches(const FmmPlan& f, int pde, int nrhs);
 
 }  // namespace rskel

@@ -1227,8 +1227,8 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
                    int nrhs, double* r, double* rg) {
   const int D = s->D;
   if (s->fmm.built) {
-    CU(fmm_laplace_apply(s->fmm, geo_of(s), mu, nrhs, r, 0.0, 1.0, kFmmDF, s->stream));
-    s->launches += 5 + 2 * s->fmm.nlevels;
+    CU(fmm_apply(s->fmm, s->cfg.pde, geo_of(s), mu, nrhs, r, 0.0, 1.0, kFmmDF, s->stream));
+    s->launches += fmm_launches(s->fmm, s->cfg.pde, nrhs);
   } else {
     launch_matvec(geo_of(s), s->cfg.pde, s->sd, s->n, mu, nrhs, r, s->stream);
   }
@@ -1255,8 +1255,8 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
 rs_status residual_update(rs_solver* s, const double* x, const double* xa, int nrhs, double* r,
                           double* rg, double* g) {
   const int D = s->D;
-  CU(fmm_laplace_apply(s->fmm, geo_of(s), x, nrhs, r, 1.0, -1.0, kFmmF32, s->stream));
-  s->launches += 5 + 2 * s->fmm.nlevels;
+  CU(fmm_apply(s->fmm, s->cfg.pde, geo_of(s), x, nrhs, r, 1.0, -1.0, kFmmF32, s->stream));
+  s->launches += fmm_launches(s->fmm, s->cfg.pde, nrhs);
   if (s->nb > 0) {
     const int nb = s->nb;
     for (int c = 0; c < nrhs; ++c) {
@@ -1638,7 +1638,7 @@ rs_status rs_factor(rs_solver* s) {
   CU(cudaSetDevice(s->cfg.device));
   rc = upload_geometry(s);
   if (rc != RS_OK) return rc;
-  if (s->fp32 && s->cfg.pde == kLaplace && !s->fmm.built) {
+  if (s->fp32 && !s->fmm.built) {
     rc = build_fmm(s);
     if (rc != RS_OK) return rc;
   }
@@ -1768,7 +1768,6 @@ rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int
   if (!s || !x || !y || nrhs < 1 || arith < 0 || arith > 2)
     return fail(s, RS_ERR_ARG, "bad matvec arguments");
   if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
-  if (s->cfg.pde != kLaplace) return rs_matvec(s, x, nrhs, y);
   rs_status rc = ensure_device(s);
   if (rc != RS_OK) return rc;
   rc = upload_geometry(s);
@@ -1786,7 +1785,7 @@ rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int
   CU(dx.ensure(nd));
   CU(dy.ensure(nd));
   CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
-  CU(fmm_laplace_apply(s->fmm, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, arith, s->stream));
+  CU(fmm_apply(s->fmm, s->cfg.pde, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, arith, s->stream));
   CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   return RS_OK;

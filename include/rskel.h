@@ -128,8 +128,9 @@ rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int 
  * inverse the factorization represents.  x, y: (num_points*sd) x nrhs. */
 rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
 
-/* y = K x through the fast multipole method used by the refinement (Laplace);
- * falls back to rs_matvec for other kernels.  arith = 0: FP64; 2: float-float
+/* y = K x through the fast multipole method used by the refinement (Laplace,
+ * Laplace-Neumann and Stokes operators as rs_kernel_block defines them).
+ * arith = 0: FP64; 2: float-float
  * (pairs of floats, ~48-bit significands, on the FP32 pipes), the variant of
  * the refinement's full residual; both at order rs_config.fmm_order.
  * arith = 1: the FP32 variant used for products with refinement corrections

@@ -1,5 +1,6 @@
-"""GPU: the FP64 fast multipole Laplace double-layer product used for the
-refinement residual, against the dense FP64 product (rs_matvec).
+"""GPU: the fast multipole products used for the refinement residual
+(Laplace double layer, Laplace-Neumann, Stokes double layer), against the
+dense FP64 product of the same kernel entries (rs_matvec).
 
 Tolerances: FP64 and float-float variants, max |y_fmm - y_dense| <= 1e-10
 max |y_dense| per column at the default order (31; measured ~1e-13 on the
@@ -67,9 +68,40 @@ def test_fmm_fp32_variant(name, solver_lib):
     assert _rel(s.matvec(x, fast=True, fp32=True), z) <= 2e-6
 
 
-def test_fmm_other_kernels_fall_back_to_dense(solver_lib):
-    d = load_golden("stokes_circle_512")
+@pytest.mark.parametrize("name", ["stokes_circle_512", "stokes_annulus_512",
+                                  "stokes_ellipses_4096"])
+def test_stokes_fmm_matches_dense(name, solver_lib):
+    """The Stokes double layer as three Cauchy sums per density (A, B and the
+    re-centred E/G channels) plus the rank-one term, against the dense
+    product of the same kernel entries."""
+    d = load_golden(name)
     geo = golden_geometry(d)
+    s = solver_lib.Solver(geo, solver_lib.RS_STOKES, 1e-8, leaf=int(d["meta"][2]),
+                          npp=int(d["meta"][3]))
+    x = np.random.default_rng(6).standard_normal((s.D, 5))  # passes of 2, 2 and 1 densities
+    z = s.matvec(x)
+    assert _rel(s.matvec(x, fast=True), z) <= 1e-10
+    assert _rel(s.matvec(x, fast=True, arith=2), z) <= 1e-10
+    assert _rel(s.matvec(x, fast=True, fp32=True), z) <= 2e-6
+
+
+def test_stokes_fmm_large_ellipses(solver_lib):
+    from rskel import geometry as G
+    geo = G.circle_with_ellipses(65536, 16, np.random.default_rng(3))
     s = solver_lib.Solver(geo, solver_lib.RS_STOKES, 1e-8)
-    x = np.random.default_rng(6).standard_normal((s.D, 2))
-    assert np.array_equal(s.matvec(x, fast=True), s.matvec(x))
+    x = np.random.default_rng(8).standard_normal((s.D, 2))
+    z = s.matvec(x)
+    assert _rel(s.matvec(x, fast=True), z) <= 1e-10
+    assert _rel(s.matvec(x, fast=True, arith=2), z) <= 1e-10
+    assert _rel(s.matvec(x, fast=True, fp32=True), z) <= 2e-6
+
+
+def test_neumann_fmm_matches_dense(solver_lib):
+    from rskel import geometry as G
+    for geo in (G.reference_donut(2048), G.star(16384)):
+        s = solver_lib.Solver(geo, solver_lib.RS_LAPLACE_NEUMANN, 1e-8)
+        x = np.random.default_rng(9).standard_normal((s.D, 3))
+        z = s.matvec(x)
+        assert _rel(s.matvec(x, fast=True), z) <= 1e-10
+        assert _rel(s.matvec(x, fast=True, arith=2), z) <= 1e-10
+        assert _rel(s.matvec(x, fast=True, fp32=True), z) <= 2e-6
