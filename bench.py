@@ -9,7 +9,7 @@ the reference's timing protocol (linear_solve.cpp:156-185: tree build
 excluded), with the inputs resident on the device.
 
 Three arms run: plain FP64 (the reference's arithmetic), FP32 factorization
-+ FP64 iterative refinement to a relative residual of 1e-11, and the same
++ FP64 iterative refinement to a relative residual of 1e-10 (confirmed by a fresh float-float residual), and the same
 with learned sketch sizes (the rank model trained, before timing, on ranks
 the plain FP32 factorization gets on 24 other seeded star and ellipse
 curves).  The headline is the learned refined arm when its solutions are
@@ -54,7 +54,7 @@ METRIC = ("factor+solve DOFs/s at rel err<=1e-8 vs FP64; mixed+learned vs plain 
 N_POINTS = 65536
 TOL = 1e-8
 NRHS = 8
-REFINE_TOL = 1e-11  # residual target of the refined arm: 1000x below the 1e-8 accuracy bar
+REFINE_TOL = 1e-10  # residual target of the refined arm: 100x below the 1e-8 accuracy bar
 LEAF = 64
 NPP = 64
 

@@ -24,6 +24,12 @@ void border_merge(Real* x, const Real* nv, const unsigned char* red_mask, int D,
                   const Real* y, int ns, cudaStream_t st);
 template <class Real>
 void transpose_to(const double* in, int rows, int cols, Real* out, cudaStream_t st);
+// U (D x nb) and Psi^T (D x nb), both column major, for h holes with centres
+// hc (2h) and radii hr (h) on the device: initialize_U_mat and
+// initialize_Psi_mat (linear_solve.cpp:20-112).  pde: 0 Laplace, 2 Stokes.
+void border_fill(const double* px, const double* py, const double* w, int n, int pde,
+                 const double* hc, const double* hr, int h, double* U, double* PsiT,
+                 cudaStream_t st);
 template <class Real>
 void convert_from_double(const double* in, Real* out, size_t n, cudaStream_t st);
 template <class Real>

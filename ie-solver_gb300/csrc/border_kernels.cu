@@ -189,4 +189,57 @@ void convert_to_double(const Real* in, double* out, size_t n, cudaStream_t st) {
 template void convert_to_double<double>(const double*, double*, size_t, cudaStream_t);
 template void convert_to_double<float>(const float*, double*, size_t, cudaStream_t);
 
+// One thread per point: the point's rows of U for every hole, and its Psi
+// entries for the first hole whose circle (radius + 1e-8) holds it.
+__global__ void border_fill_kernel(const double* px, const double* py, const double* w, int n,
+                                   int pde, const double* hc, const double* hr, int h, double* U,
+                                   double* PsiT) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool stokes = pde == 2;
+  const size_t D = stokes ? 2 * (size_t)n : (size_t)n;
+  const double x0 = px[i], x1 = py[i];
+  int member = -1;
+  for (int hi = 0; hi < h; ++hi) {
+    const double r0 = x0 - hc[2 * hi], r1 = x1 - hc[2 * hi + 1];
+    const double r2 = r0 * r0 + r1 * r1, rn = sqrt(r2);
+    if (member < 0 && rn < hr[hi] + 1e-8) member = hi;
+    if (!stokes) {
+      U[i + D * hi] = log(rn);
+      PsiT[i + D * hi] = 0.0;
+      continue;
+    }
+    // Stokeslet (two columns) and rotlet about the hole centre
+    const double scale = 1.0 / (4.0 * CUDART_PI), lg = log(1.0 / rn), ir2 = 1.0 / r2;
+    const size_t c0 = D * (3 * (size_t)hi), c1 = c0 + D, c2 = c1 + D;
+    U[2 * i + c0] = scale * (lg + ir2 * r0 * r0);
+    U[2 * i + 1 + c0] = scale * (ir2 * r1 * r0);
+    U[2 * i + c1] = scale * (ir2 * r0 * r1);
+    U[2 * i + 1 + c1] = scale * (lg + ir2 * r1 * r1);
+    U[2 * i + c2] = r1 * (scale * ir2);
+    U[2 * i + 1 + c2] = -r0 * (scale * ir2);
+    PsiT[2 * i + c0] = PsiT[2 * i + 1 + c0] = 0.0;
+    PsiT[2 * i + c1] = PsiT[2 * i + 1 + c1] = 0.0;
+    PsiT[2 * i + c2] = PsiT[2 * i + 1 + c2] = 0.0;
+  }
+  if (member < 0) return;
+  const double wi = w[i];
+  if (!stokes) {
+    PsiT[i + D * member] = wi;
+  } else {
+    const size_t c0 = D * (3 * (size_t)member), c1 = c0 + D, c2 = c1 + D;
+    PsiT[2 * i + c0] = wi;
+    PsiT[2 * i + 1 + c1] = wi;
+    PsiT[2 * i + c2] = wi * x1;
+    PsiT[2 * i + 1 + c2] = -wi * x0;
+  }
+}
+
+void border_fill(const double* px, const double* py, const double* w, int n, int pde,
+                 const double* hc, const double* hr, int h, double* U, double* PsiT,
+                 cudaStream_t st) {
+  if (n <= 0) return;
+  border_fill_kernel<<<(n + 255) / 256, 256, 0, st>>>(px, py, w, n, pde, hc, hr, h, U, PsiT);
+}
+
 }  // namespace rskel

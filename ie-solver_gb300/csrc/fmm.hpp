@@ -85,6 +85,9 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
 // boundary data.
 cudaError_t fmm_apply(FmmPlan& f, int pde, const Geo<double>& geo, const double* mu, int nrhs,
                       double* y, double ya, double yb, int arith, cudaStream_t st);
+// Sets the order of the FP64 and float-float variants (2..64; the plan's
+// lists do not depend on it).  Synchronous: call between products.
+bool fmm_set_order(FmmPlan& f, int p);
 // Kernels one fmm_apply launches.
 int fmm_launches(const FmmPlan& f, int pde, int nrhs);
 

@@ -49,14 +49,39 @@ void csr(const std::vector<std::vector<int>>& lists, std::vector<int>* off, std:
   }
 }
 
+// Pascal triangle, P2 x P2: t[a * P2 + b] = C(a, b)
+void pascal(int P2, std::vector<double>* t) {
+  t->assign((size_t)P2 * P2, 0.0);
+  for (int a = 0; a < P2; ++a) {
+    (*t)[(size_t)a * P2] = 1.0;
+    for (int b = 1; b <= a; ++b)
+      (*t)[(size_t)a * P2 + b] =
+          (*t)[(size_t)(a - 1) * P2 + b - 1] + (b < a ? (*t)[(size_t)(a - 1) * P2 + b] : 0.0);
+  }
+}
+
 }  // namespace
+
+bool fmm_set_order(FmmPlan& f, int p) {
+  if (p < 2 || p > 64) return false;
+  std::vector<double> binom;
+  pascal(2 * p, &binom);
+  std::vector<float> binom_df(2 * binom.size());
+  for (size_t i = 0; i < binom.size(); ++i) {
+    binom_df[2 * i] = (float)binom[i];
+    binom_df[2 * i + 1] = (float)(binom[i] - (double)binom_df[2 * i]);
+  }
+  if (upload(f.binom, binom) != cudaSuccess || upload(f.binom_df, binom_df) != cudaSuccess)
+    return false;
+  f.p = p;
+  return true;
+}
 
 bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p, int p32,
                cudaStream_t st) {
   (void)st;
   if (p < 2 || p > 64 || p32 < 2 || p32 > 64 || npts <= 0) return false;
   const int nb = (int)tree.nodes.size();
-  f.p = p;
   f.p32 = p32;
   f.nbox = nb;
   f.npts = npts;
@@ -183,22 +208,10 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
   f.w_pairs = wi.size();
   f.x_pairs = xi.size();
   f.u_pairs = ui.size();
-  // binomial tables (2p x 2p)
-  auto pascal = [](int P2, std::vector<double>* t) {
-    t->assign((size_t)P2 * P2, 0.0);
-    for (int a = 0; a < P2; ++a) {
-      (*t)[(size_t)a * P2] = 1.0;
-      for (int b = 1; b <= a; ++b)
-        (*t)[(size_t)a * P2 + b] =
-            (*t)[(size_t)(a - 1) * P2 + b - 1] + (b < a ? (*t)[(size_t)(a - 1) * P2 + b] : 0.0);
-    }
-  };
-  std::vector<double> binom, b32d;
-  pascal(2 * p, &binom);
+  std::vector<double> b32d;
   pascal(2 * p32, &b32d);
-  std::vector<float> binom32(b32d.begin(), b32d.end()), binom_df(2 * binom.size());
-  for (size_t i = 0; i < binom.size(); ++i) split(binom[i], &binom_df[2 * i], &binom_df[2 * i + 1]);
-  bool ok = upload(f.cx, cx) == cudaSuccess && upload(f.cy, cy) == cudaSuccess &&
+  std::vector<float> binom32(b32d.begin(), b32d.end());
+  bool ok = fmm_set_order(f, p) && upload(f.cx, cx) == cudaSuccess && upload(f.cy, cy) == cudaSuccess &&
             upload(f.side, side) == cudaSuccess && upload(f.pstart, pstart) == cudaSuccess &&
             upload(f.pcount, pcount) == cudaSuccess && upload(f.parent, parent) == cudaSuccess &&
             upload(f.children, children) == cudaSuccess &&
@@ -212,7 +225,6 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
             upload(f.u_idx, ui) == cudaSuccess && upload(f.lvl_boxes, lvl_flat) == cudaSuccess &&
             upload(f.leaves, f.leaves_h) == cudaSuccess &&
             upload(f.m2l_boxes, f.m2l_boxes_h) == cudaSuccess &&
-            upload(f.binom, binom) == cudaSuccess && upload(f.binom_df, binom_df) == cudaSuccess &&
             upload(f.binom32, binom32) == cudaSuccess;
   f.built = ok;
   return ok;

@@ -430,7 +430,10 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
   __syncthreads();
 
   const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
-  const int m = t.dense_off >= 0 ? t.m_dense : 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+  // direct == 2 (FP32 wide ID): a task with m_dense > 0 finds its m_dense-row
+  // sketch already in its tile; the others factor their ID matrix directly
+  const bool pre = p.direct == 2 && t.m_dense > 0;
+  const int m = (t.dense_off >= 0 || pre) ? t.m_dense : 2 * t.q + (t.use_proxy ? 2 * prow : 0);
   int step0 = 0;
   long long clk_fill = 0, clk_fold = 0, clk0 = clock64();
   int k = 0;
@@ -440,7 +443,7 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
     // calls it (ie_mat.cpp:556), minus the steps after the rank is known.
     Real* A = reinterpret_cast<Real*>(p.scratch) + t.scratch_off;
     Real* chunk_save = S.C;
-    for (int c0 = 0; c0 < m; c0 += kChunk) {
+    for (int c0 = 0; c0 < m && !pre; c0 += kChunk) {
       const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
       S.C = A + (size_t)c0 * L.ld;
       fill_chunk<Real>(p, t, S, L.ld, c0, cnt, ox, oy);
@@ -967,6 +970,131 @@ static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStrea
     q.redo_pass = 1;
     launch_split_pass<TS>(q, num_tasks, nmax, st);
   }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 wide ID: boxes of more than 128 columns (the top levels, whose ID
+// matrices have thousands of rows).  One CTA per (task, block of kWideCols
+// columns, range of rows) generates those rows of the ID matrix chunk by
+// chunk and accumulates the partial sketch Omega(:, rows) A(rows, cols)
+// (the same hashed signs as the other FP32 sketches); a second kernel sums
+// the row ranges in a fixed order into the task's global tile; the direct
+// pivoted QR (id_kernel, direct == 2) then runs on the ell x n sketch.
+// ---------------------------------------------------------------------------
+int id_sketch_rows(int n) { return sketch_rows(n); }
+size_t id_wide_tile(int m, int n) { return id_direct_tile(m, n); }
+
+constexpr int kWideMaxTiles = 5;  // 4x4 tiles per thread: ell <= 5 * 256 * 4 / kWideCols rows
+size_t id_wide_sketch_smem(int nmax) {
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const int lp = (sketch_rows(nmax) + 3) & ~3;
+  return al(sizeof(float) * kChunk * kWideCols) + al(sizeof(float) * (size_t)kChunk * lp) +
+         dofs_bytes<float>(kWideCols) + dofs_bytes<float>(kChunk) + al(sizeof(int) * kChunk);
+}
+
+__global__ void __launch_bounds__(kThreads) id_wide_sketch_kernel(IdParams p,
+                                                                  const WideItem* items,
+                                                                  float* part) {
+  const WideItem it = items[blockIdx.x];
+  const IdTask t = p.tasks[it.task];
+  const int n = t.n;
+  const int nc = n - it.j0 < kWideCols ? n - it.j0 : kWideCols;
+  const int ell = sketch_rows(n);
+  const int lp = (ell + 3) & ~3;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* sp = smem;
+  IdShared<float> S;
+  S.C = carve<float>(sp, kChunk * kWideCols);
+  float* sg = carve<float>(sp, kChunk * lp);
+  S.act = carve_dofs<float>(sp, kWideCols);
+  S.row = carve_dofs<float>(sp, kChunk);
+  S.kind = carve<int>(sp, kChunk);
+  const double ox = t.cx, oy = t.cy;
+  for (int j = threadIdx.x; j < nc; j += blockDim.x)
+    load_dof<float>(p.geo, p.sd, p.dofs[t.act_off + it.j0 + j], ox, oy, S.act, j);
+  for (int e = threadIdx.x; e < kChunk * kWideCols; e += blockDim.x) S.C[e] = 0.f;
+  __syncthreads();
+  IdTask tc = t;  // the column block as a task of nc columns
+  tc.n = nc;
+  constexpr int ncb = kWideCols / 4;
+  const int ntiles = (lp / 4) * ncb;
+  float acc[kWideMaxTiles][16];
+#pragma unroll
+  for (int q = 0; q < kWideMaxTiles; ++q)
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[q][e] = 0.f;
+  for (int c0 = it.r0; c0 < it.r1; c0 += kChunk) {
+    const int cnt = it.r1 - c0 < kChunk ? it.r1 - c0 : kChunk;
+    fill_chunk<float>(p, tc, S, kWideCols, c0, cnt, ox, oy);
+    for (int e = threadIdx.x; e < kChunk * lp; e += blockDim.x) {
+      const int ii = e / lp, r = e % lp;
+      sg[e] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kWideMaxTiles; ++q) {
+      const int tile = threadIdx.x + q * kThreads;
+      if (tile >= ntiles) break;
+      const int r0 = 4 * (tile / ncb), cc0 = 4 * (tile % ncb);
+      float* a = acc[q];
+#pragma unroll 4
+      for (int ii = 0; ii < kChunk; ++ii) {
+        const float4 cv = *reinterpret_cast<const float4*>(S.C + (size_t)ii * kWideCols + cc0);
+        const float4 sv = *reinterpret_cast<const float4*>(sg + (size_t)ii * lp + r0);
+        a[0] += sv.x * cv.x;  a[1] += sv.x * cv.y;  a[2] += sv.x * cv.z;  a[3] += sv.x * cv.w;
+        a[4] += sv.y * cv.x;  a[5] += sv.y * cv.y;  a[6] += sv.y * cv.z;  a[7] += sv.y * cv.w;
+        a[8] += sv.z * cv.x;  a[9] += sv.z * cv.y;  a[10] += sv.z * cv.z; a[11] += sv.z * cv.w;
+        a[12] += sv.w * cv.x; a[13] += sv.w * cv.y; a[14] += sv.w * cv.z; a[15] += sv.w * cv.w;
+      }
+    }
+    __syncthreads();
+  }
+  float* out = part + it.part_off;
+#pragma unroll
+  for (int q = 0; q < kWideMaxTiles; ++q) {
+    const int tile = threadIdx.x + q * kThreads;
+    if (tile >= ntiles) break;
+    const int r0 = 4 * (tile / ncb), cc0 = 4 * (tile % ncb);
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const int r = r0 + e / 4;
+      if (r < ell) out[(size_t)r * kWideCols + cc0 + e % 4] = acc[q][e];
+    }
+  }
+}
+
+// Sum of a task's partial sketches over its row ranges, in order, into the
+// row-major tile the direct pivoted QR reads (leading dimension as id_kernel
+// lays it out for the task's n).
+__global__ void __launch_bounds__(kThreads) id_wide_reduce_kernel(IdParams p, const float* part) {
+  const IdTask t = p.tasks[blockIdx.x];
+  if (t.m_dense <= 0) return;
+  const int n = t.n, ell = t.m_dense, ns = t.wide_split;
+  const int ld = layout_ld(n, team_size(n));
+  float* A = reinterpret_cast<float*>(p.scratch) + t.scratch_off;
+  const float* P = part + t.y_off;
+  for (int e = threadIdx.x; e < ell * n; e += blockDim.x) {
+    const int r = e / n, j = e % n, jb = j / kWideCols, jj = j % kWideCols;
+    float s = 0.f;
+    for (int q = 0; q < ns; ++q) s += P[((size_t)(jb * ns + q) * ell + r) * kWideCols + jj];
+    A[(size_t)r * ld + j] = s;
+  }
+}
+
+int launch_id_wide(const IdParams& p, int num_tasks, int nmax, const WideItem* items,
+                   int num_items, float* part, cudaStream_t st) {
+  if (num_tasks <= 0) return 0;
+  int k = 0;
+  if (num_items > 0) {
+    set_smem_once<id_wide_sketch_kernel>();
+    id_wide_sketch_kernel<<<num_items, kThreads, id_wide_sketch_smem(nmax), st>>>(p, items, part);
+    id_wide_reduce_kernel<<<num_tasks, kThreads, 0, st>>>(p, part);
+    k += 2;
+  }
+  IdParams q = p;
+  q.direct = 2;
+  launch_id_t<float, 1>(q, num_tasks, id_kernel_smem(nmax, true, false), st);
+  return k + 1;
 }
 
 bool id_sketch_ok(int nmax) {

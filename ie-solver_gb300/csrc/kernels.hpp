@@ -80,6 +80,14 @@ size_t id_sketch_y_size(int n);
 cudaError_t id_noalloc_prepare();
 int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,
                cudaStream_t st);
+// FP32 wide ID of num_tasks tasks (all of more than 128 columns; tasks with
+// m_dense > 0 are sketched through `items` into `part`, the others factor
+// their ID matrix directly): partial sketches, their sum into each task's
+// scratch tile, then pivoted QR and Z.  Returns the kernels launched.
+int launch_id_wide(const IdParams& p, int num_tasks, int nmax, const WideItem* items,
+                   int num_items, float* part, cudaStream_t st);
+size_t id_wide_tile(int m, int n);  // scratch floats of a wide task (m: rows factored)
+int id_sketch_rows(int n);
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
                      cudaStream_t st);
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st);
@@ -105,5 +113,20 @@ void launch_matvec(const Geo<double>& g, int pde, int sd, int npts, const double
 
 // Elementwise helpers.
 void launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);
+
+// Flexible GMRES block vectors (krylov.cu): nrhs vectors of the bordered
+// system stored as a D x nrhs block then an nb x nrhs block.
+constexpr int kKrylovMaxBasis = 32;
+int krylov_dot_blocks(int D, int nb);
+// h[c * kKrylovMaxBasis + j] = <V_j(c), w(c)> for j < nv; part holds
+// nrhs * krylov_dot_blocks(D, nb) * kKrylovMaxBasis partial sums.
+void launch_mdot(const double* V, size_t vstride, int nv, const double* w, int D, int nb, int nrhs,
+                 double* part, double* h, cudaStream_t st);
+// w += sign * sum_j h[c * kKrylovMaxBasis + j] V_j(c)
+void launch_maxpy(double* w, const double* V, size_t vstride, int nv, const double* h, double sign,
+                  int D, int nb, int nrhs, cudaStream_t st);
+// w(c) = x(c) * s[c]
+void launch_kscale(double* w, const double* x, const double* s, int D, int nb, int nrhs,
+                   cudaStream_t st);
 
 }  // namespace rskel

@@ -41,6 +41,20 @@ struct IdTask {
   int m_dense;          // rows of that matrix
   int ell;              // FP32 split ID: sketch rows from the rank predictor (0: n + 16)
   int64_t y_off;        // FP32 split ID: the sketch (rows x warp leading dimension) at sketch_y[y_off]
+                        // FP32 wide ID: first partial sketch of the task in the partial buffer
+  int wide_split;       // FP32 wide ID: row ranges the partial sketches are split into
+  int pad2;
+};
+
+// FP32 wide ID (boxes of more than 128 columns): one CTA per (task, block
+// of kWideCols columns, row range), each writing a partial sketch
+// (ell x kWideCols, row major) at part[part_off].
+constexpr int kWideCols = 32;
+struct WideItem {
+  int task;     // index in the launch's task array
+  int j0;       // first column
+  int r0, r1;   // ID matrix rows [r0, r1)
+  int64_t part_off;
 };
 
 // One elimination (skel_factorization.cpp:77-128) or, for boxes that are not

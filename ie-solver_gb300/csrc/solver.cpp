@@ -39,6 +39,7 @@ using namespace rskel;
 namespace {
 
 constexpr size_t kSmemMax = 227 * 1024;
+constexpr int kWideMaxN = 512;  // FP32 wide ID up to this many columns (wider: Householder fold)
 
 struct NodeState {
   int compressed = 0;
@@ -76,6 +77,7 @@ struct rs_solver {
   bool fp32 = false;
 
   bool dev_ready = false;
+  int num_sms = 152;  // of the handle's device; sizes the wide ID's work split
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;  // read-back of ranks while eliminations run
   cudaEvent_t ev_c = nullptr;
@@ -107,14 +109,17 @@ struct rs_solver {
 
   // bordered system
   int nb = 0;
-  std::vector<double> Uh, Psih;  // D x nb, nb x D (host)
-  DevBuf<double> U0, PsiT0, G, g1;
+  DevBuf<double> U0, PsiT0, G, g1, hole_dev;
   DevBuf<unsigned char> red_mask, skel_mask, ones_mask;
   DevBuf<int> S_piv;
 
   // solve buffers
   DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev, x64, xa64, g64;
   HostBuf<double> h_io;
+  // flexible GMRES: bases V, Z, work vector, right-hand side, dot partials,
+  // coefficients (device) and their host copies
+  DevBuf<double> kv, kz, kw, kb, kpart, kh;
+  HostBuf<double> hk_up, hk_dn;
 
   FmmPlan fmm;
   HostBuf<unsigned char> stage;  // pinned staging of a factorization's host-to-device uploads
@@ -122,6 +127,8 @@ struct rs_solver {
   bool incremental = false;      // next rs_factor keeps the boxes rs_perturb left compressed
   size_t full_fac_used = 0;      // factor storage of the last full factorization
   DevBuf<float> sketch_y;  // FP32 split ID: per-level sketches
+  DevBuf<WideItem> wide_items;  // FP32 wide ID: work items and partial sketches of a level
+  DevBuf<float> wide_part;
   // Learned sketch sizes: model weights on the device, a level's features
   // (sorted task order), the redo flags per slot, and the last
   // factorization's (features, k/n) samples for training.
@@ -168,6 +175,7 @@ rs_status ensure_device(rs_solver* s) {
     return fail(s, RS_ERR_NO_DEVICE, "no CUDA device available (there is no CPU fallback)");
   if (s->cfg.device < 0 || s->cfg.device >= count) return fail(s, RS_ERR_ARG, "bad device ordinal");
   CU(cudaSetDevice(s->cfg.device));
+  CU(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->cfg.device));
   CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   CU(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&s->ev_c, cudaEventDisableTiming));
@@ -635,7 +643,55 @@ rs_status factor_impl(rs_solver* s) {
     for (size_t i = 0; i < od.size(); ++i) dct_s[i] = dct[od[i]];
     // global-memory tiles for boxes whose tiles do not fit in shared memory
     size_t scratch_need = 0;
-    for (IdTask& t : idt_s) {
+    // FP32 wide ID: boxes of 129..kWideMaxN columns, a contiguous range of
+    // the size-sorted tasks.  Work items split each sketched box into
+    // column blocks and row ranges so that the level fills the GPU.
+    std::vector<WideItem> witems;
+    size_t w0 = idt_s.size(), w1 = idt_s.size(), part_need = 0;
+    if (f32) {
+      w0 = 0;
+      while (w0 < idt_s.size() && idt_s[w0].n <= 128) ++w0;
+      w1 = w0;
+      while (w1 < idt_s.size() && idt_s[w1].n <= kWideMaxN) ++w1;
+      int blocks = 0;
+      for (size_t i = w0; i < w1; ++i) {
+        const IdTask& t = idt_s[i];
+        const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+        if (m > id_sketch_rows(t.n)) blocks += (t.n + kWideCols - 1) / kWideCols;
+      }
+      const int want = blocks > 0 ? (2 * s->num_sms + blocks - 1) / blocks : 1;
+      for (size_t i = w0; i < w1; ++i) {
+        IdTask& t = idt_s[i];
+        const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0), ell = id_sketch_rows(t.n);
+        t.m_dense = m > ell ? ell : 0;
+        t.wide_split = 0;
+        t.scratch_off = (int64_t)scratch_need;
+        scratch_need += id_wide_tile(m > ell ? ell : m, t.n);
+        if (m <= ell) continue;
+        // row ranges of whole chunks, at least two chunks each
+        const int chunks = (m + 63) / 64;
+        int ns = std::max(1, std::min(want, chunks / 2));
+        const int per = (chunks + ns - 1) / ns;
+        ns = (chunks + per - 1) / per;
+        t.wide_split = ns;
+        t.y_off = (int64_t)part_need;
+        const int ncb = (t.n + kWideCols - 1) / kWideCols;
+        for (int jb = 0; jb < ncb; ++jb)
+          for (int q = 0; q < ns; ++q) {
+            WideItem it;
+            it.task = (int)(i - w0);
+            it.j0 = jb * kWideCols;
+            it.r0 = q * per * 64;
+            it.r1 = std::min(m, (q + 1) * per * 64);
+            it.part_off = t.y_off + ((int64_t)(jb * ns + q) * ell) * kWideCols;
+            witems.push_back(it);
+          }
+        part_need += (size_t)ncb * ns * ell * kWideCols;
+      }
+    }
+    for (size_t ti = 0; ti < idt_s.size(); ++ti) {
+      IdTask& t = idt_s[ti];
+      if (ti >= w0 && ti < w1) continue;  // wide: placed above
       if (!f32) {  // FP64: direct pivoted QR on the whole ID matrix
         const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
         t.scratch_off = (int64_t)scratch_need;
@@ -645,9 +701,12 @@ rs_status factor_impl(rs_solver* s) {
         scratch_need += (size_t)(t.n + 32) * (t.n + 64) + 64;
       }
     }
-    // FP32: sketches of the split randomized ID (boxes of at most 128 columns)
+    // FP32: sketches of the split randomized ID (boxes of at most 128
+    // columns); the wide tasks' y_off (their partial sketches) is set above
     size_t y_need = 0;
-    for (IdTask& t : idt_s) {
+    for (size_t ti = 0; ti < idt_s.size(); ++ti) {
+      IdTask& t = idt_s[ti];
+      if (ti >= w0 && ti < w1) continue;
       t.y_off = -1;
       if (f32 && t.n <= 128) {
         t.y_off = (int64_t)y_need;
@@ -677,6 +736,11 @@ rs_status factor_impl(rs_solver* s) {
     CU(stage_copy(s, s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask)));
     CU(stage_copy(s, s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask)));
     CU(stage_copy(s, s->blk.p, blk.data(), blk.size() * sizeof(BlkRef)));
+    if (!witems.empty()) {
+      CU(s->wide_items.ensure(witems.size()));
+      CU(s->wide_part.ensure(part_need));
+      CU(stage_copy(s, s->wide_items.p, witems.data(), witems.size() * sizeof(WideItem)));
+    }
     if (learned && !idt_s.empty()) {
       // predicted sketch sizes written into the uploaded task records
       CU(s->rank_feat.ensure(feat_s.size()));
@@ -719,12 +783,25 @@ rs_status factor_impl(rs_solver* s) {
     s->timed_levels.push_back(lv);
     auto id_fits = [&](int n) { return id_kernel_smem(n, f32, true) <= kSmemMax; };
     auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
-    launch_binned(idt_s, s->id_tasks.p, id_fits, [&](const IdTask* dt, int cnt, int nmax) {
+    auto id_launch = [&](const IdTask* dt, int cnt, int nmax) {
       IdParams q = ip;
       q.tasks = dt;
       bool in_smem = !ip.direct && id_kernel_smem(nmax, f32, true) <= kSmemMax;
       s->launches += launch_id(q, cnt, nmax, id_kernel_smem(nmax, f32, in_smem), f32, s->stream);
-    });
+    };
+    if (w0 < w1) {
+      // the three ranges: up to 128 columns, wide, wider
+      const std::vector<IdTask> lo(idt_s.begin(), idt_s.begin() + w0);
+      const std::vector<IdTask> hi(idt_s.begin() + w1, idt_s.end());
+      launch_binned(lo, s->id_tasks.p, id_fits, id_launch);
+      IdParams q = ip;
+      q.tasks = s->id_tasks.p + w0;
+      s->launches += launch_id_wide(q, (int)(w1 - w0), idt_s[w1 - 1].n, s->wide_items.p,
+                                    (int)witems.size(), s->wide_part.p, s->stream);
+      launch_binned(hi, s->id_tasks.p + w1, id_fits, id_launch);
+    } else {
+      launch_binned(idt_s, s->id_tasks.p, id_fits, id_launch);
+    }
     CU(cudaGetLastError());
     CU(cudaEventRecord(s->lv_ev[3 * lv + 1], s->stream));
     // ranks and pivots come back on the side stream while the eliminations run
@@ -817,7 +894,10 @@ rs_status factor_impl(rs_solver* s) {
                           feat.begin() + (size_t)(S.slot + 1) * kRankFeatures);
       s->samp_target.push_back(k > 0 ? (float)k / (float)n : 1.f);
       const int m = m_of_slot[S.slot];
-      if (f32 && n <= 128) {
+      if (f32 && n > 128 && n <= kWideMaxN) {
+        s->stats.sketch_rows += std::min(m, n + 16);
+        s->stats.id_flops += sketch_id_flops(m, n, k, n + 16, s->cfg.pde);
+      } else if (f32 && n <= 128) {
         // rows the randomized ID sketched (m when the matrix is no taller)
         const int full = n + 16;
         int ell = full;
@@ -990,49 +1070,6 @@ rs_status factor_impl(rs_solver* s) {
 // ---------------------------------------------------------------------------
 namespace {
 
-void build_border_host(rs_solver* s) {
-  const int h = s->nh, N = s->n, D = s->D;
-  s->nb = s->cfg.pde == kStokes ? 3 * h : h;
-  const int nb = s->nb;
-  s->Uh.assign((size_t)D * nb, 0.0);
-  s->Psih.assign((size_t)nb * D, 0.0);
-  for (int i = 0; i < N; ++i) {
-    const double x0 = s->pts[2 * i], x1 = s->pts[2 * i + 1];
-    for (int hi = 0; hi < h; ++hi) {
-      const double r0 = x0 - s->hc[2 * hi], r1 = x1 - s->hc[2 * hi + 1];
-      const double rn = std::sqrt(r0 * r0 + r1 * r1);
-      if (s->cfg.pde == kLaplace) {
-        s->Uh[i + (size_t)D * hi] = std::log(rn);
-      } else {
-        const double scale = 1.0 / (4 * M_PI);
-        const double r2 = rn * rn;
-        double* U = s->Uh.data();
-        U[2 * i + (size_t)D * (3 * hi)] = scale * (std::log(1 / rn) + (1.0 / r2) * r0 * r0);
-        U[2 * i + 1 + (size_t)D * (3 * hi)] = scale * ((1.0 / r2) * r1 * r0);
-        U[2 * i + (size_t)D * (3 * hi + 1)] = scale * ((1.0 / r2) * r0 * r1);
-        U[2 * i + 1 + (size_t)D * (3 * hi + 1)] = scale * (std::log(1 / rn) + (1.0 / r2) * r1 * r1);
-        U[2 * i + (size_t)D * (3 * hi + 2)] = r1 * (scale / r2);
-        U[2 * i + 1 + (size_t)D * (3 * hi + 2)] = -r0 * (scale / r2);
-      }
-    }
-    for (int hi = 0; hi < h; ++hi) {
-      const double r0 = x0 - s->hc[2 * hi], r1 = x1 - s->hc[2 * hi + 1];
-      if (std::sqrt(r0 * r0 + r1 * r1) < s->hr[hi] + 1e-8) {
-        const double wi = s->w[i];
-        if (s->cfg.pde == kLaplace) {
-          s->Psih[hi + (size_t)nb * i] = wi;
-        } else {
-          s->Psih[3 * hi + (size_t)nb * (2 * i)] = wi;
-          s->Psih[3 * hi + 1 + (size_t)nb * (2 * i + 1)] = wi;
-          s->Psih[3 * hi + 2 + (size_t)nb * (2 * i)] = wi * x1;
-          s->Psih[3 * hi + 2 + (size_t)nb * (2 * i + 1)] = -wi * x0;
-        }
-        break;
-      }
-    }
-  }
-}
-
 template <class Real>
 void sweep_levels(rs_solver* s, Real* x, int ld, int nrhs, int mode, bool up) {
   Factor<Real>& F = factor_of<Real>(s);
@@ -1080,7 +1117,7 @@ void sweep_levels(rs_solver* s, Real* x, int ld, int nrhs, int mode, bool up) {
 template <class Real>
 rs_status factor_border(rs_solver* s) {
   Factor<Real>& F = factor_of<Real>(s);
-  build_border_host(s);
+  s->nb = s->cfg.pde == kStokes ? 3 * s->nh : s->nh;
   const int D = s->D, nb = s->nb, ns = s->ns;
   std::vector<unsigned char> red(D, 1), sk(D, 0);
   for (int i : s->allskel) {
@@ -1092,26 +1129,21 @@ rs_status factor_border(rs_solver* s) {
   if (!any_red) return fail(s, RS_ERR_NO_COMPRESSION, "No compression possible");
   CU(s->red_mask.ensure(D));
   CU(s->skel_mask.ensure(D));
-  CU(cudaMemcpyAsync(s->red_mask.p, red.data(), D, cudaMemcpyHostToDevice, s->stream));
-  CU(cudaMemcpyAsync(s->skel_mask.p, sk.data(), D, cudaMemcpyHostToDevice, s->stream));
+  CU(stage_copy(s, s->red_mask.p, red.data(), D));
+  CU(stage_copy(s, s->skel_mask.p, sk.data(), D));
   CU(s->U0.ensure((size_t)D * nb));
   CU(s->PsiT0.ensure((size_t)D * nb));
-  CU(cudaMemcpyAsync(s->U0.p, s->Uh.data(), (size_t)D * nb * 8, cudaMemcpyHostToDevice,
-                     s->stream));
+  CU(s->hole_dev.ensure(3 * (size_t)s->nh));
+  CU(stage_copy(s, s->hole_dev.p, s->hc.data(), 2 * (size_t)s->nh * sizeof(double)));
+  CU(stage_copy(s, s->hole_dev.p + 2 * s->nh, s->hr.data(), (size_t)s->nh * sizeof(double)));
+  border_fill(s->gx.p, s->gy.p, s->gw.p, s->n, s->cfg.pde, s->hole_dev.p,
+              s->hole_dev.p + 2 * s->nh, s->nh, s->U0.p, s->PsiT0.p, s->stream);
   CU(F.mU.ensure((size_t)D * nb));
   CU(F.mP.ensure((size_t)D * nb));
   CU(F.tmp.ensure((size_t)D * nb));
   convert_from_double<Real>(s->U0.p, F.mU.p, (size_t)D * nb, s->stream);
-  // Psi (nb x D) staged through tmp storage, stored transposed (D x nb)
-  {
-    DevBuf<double> psi;
-    CU(psi.ensure((size_t)D * nb));
-    CU(cudaMemcpyAsync(psi.p, s->Psih.data(), (size_t)D * nb * 8, cudaMemcpyHostToDevice,
-                       s->stream));
-    transpose_to<double>(psi.p, nb, D, s->PsiT0.p, s->stream);
-    convert_from_double<Real>(s->PsiT0.p, F.mP.p, (size_t)D * nb, s->stream);
-    CU(cudaStreamSynchronize(s->stream));
-  }
+  convert_from_double<Real>(s->PsiT0.p, F.mP.p, (size_t)D * nb, s->stream);
+  s->launches += 3;
   // sweeps on U (with L) and Psi^T (with U^T), skel_factorization.cpp:229-266
   sweep_levels<Real>(s, F.mU.p, D, nb, kUpPlain, true);
   sweep_levels<Real>(s, F.mP.p, D, nb, kUpTransU, true);
@@ -1209,14 +1241,27 @@ namespace {
 // star the product's relative error is about 10^(-0.36 p - 2.1) (order 20:
 // 1.2e-9, 28: 1.8e-12, 32: 6.5e-14), and the residual needs it ten times
 // below refine_tol.  FP32 order 16 for the correction products.
+// The Stokes product also evaluates derivatives of the expansions (about
+// 30x the Laplace error at the same order on the 16-hole, 131072-point
+// geometry), so it takes four more terms.
 constexpr int kFmmOrder32 = 16;
-int auto_fmm_order(double refine_tol) {
+int auto_fmm_order(double refine_tol, int pde) {
   const double want = std::max(refine_tol, 1e-15) / 10.0;
-  const int p = (int)std::ceil((-std::log10(want) - 2.1) / 0.36);
+  const int p = (int)std::ceil((-std::log10(want) - 2.1) / 0.36) + (pde == kStokes ? 4 : 0);
   return std::min(48, std::max(12, p));
 }
+// Relative error of the FP32 product (order kFmmOrder32) on rough vectors,
+// with a factor 2 of margin over what it measures (65536-point star,
+// Laplace: 1.5e-8; 131072 points with 16 holes, Stokes: 7.8e-8).  The
+// refinement takes the FP32 product of a correction only while this times
+// the previous residual stays below half the refinement tolerance.
+double fmm32_error(int pde) { return pde == kStokes ? 1.6e-7 : 3e-8; }
+// Relative residual the inner GMRES of GMRES-IR aims for (its FP32
+// products and preconditioner are good to about 1e-7).
+constexpr double kGmresInnerTol = 1e-6;
 rs_status build_fmm(rs_solver* s) {
-  const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order : auto_fmm_order(s->cfg.refine_tol);
+  const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order
+                                     : auto_fmm_order(s->cfg.refine_tol, s->cfg.pde);
   if (p > 64) return fail(s, RS_ERR_ARG, "fmm_order above 64");
   if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, kFmmOrder32, s->stream))
     return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
@@ -1272,6 +1317,148 @@ rs_status residual_update(rs_solver* s, const double* x, const double* xa, int n
   return RS_OK;
 }
 
+// y = -(A z) for a block vector z (mu block, then alpha block) through the
+// FP32 multipole product: the bordered operator [K U; Psi -I] (the residual
+// recurrence's update applied to a zero residual).
+rs_status apply_neg_op(rs_solver* s, const double* z, int nrhs, double* y) {
+  const int D = s->D, nb = s->nb;
+  const size_t nd = (size_t)D * nrhs;
+  CU(cudaMemsetAsync(y, 0, (nd + (size_t)nb * nrhs) * 8, s->stream));
+  return residual_update(s, z, nb ? z + nd : nullptr, nrhs, y, nb ? y + nd : nullptr, s->g64.p);
+}
+
+// z = M^{-1} v with the FP32 factorization (block vectors; the alpha block
+// of v is the second-block right-hand side of the bordered solve).
+rs_status apply_prec(rs_solver* s, const double* v, int nrhs, double* z) {
+  Factor<float>& F = s->F32;
+  const int D = s->D, nb = s->nb;
+  const size_t nd = (size_t)D * nrhs;
+  launch_d2f(v, F.x.p, nd, s->stream);
+  rs_status rc = apply_inverse<float>(s, F.x.p, nrhs, F.tmp.p, nb ? v + nd : nullptr);
+  if (rc != RS_OK) return rc;
+  launch_f2d(F.x.p, z, nd, s->stream);
+  if (nb) launch_f2d(F.tmp.p, z + nd, (size_t)nb * nrhs, s->stream);
+  s->launches += nb ? 3 : 2;
+  return RS_OK;
+}
+
+// Flexible GMRES (Saad 1993) on A d = b for the block vector b: right
+// preconditioned by the FP32 factorization, FP32 multipole products, FP64
+// basis vectors orthogonalised by classical Gram-Schmidt applied twice, one
+// Krylov space per right-hand side advanced in lockstep.  Stops when every
+// right-hand side's residual estimate is below rtol of its |b|, or after m
+// steps (no restart: the refinement around it restarts from a fresh
+// residual).  d gets the correction; *steps the steps taken.
+rs_status fgmres(rs_solver* s, const double* b, int nrhs, double rtol, int m, double* d,
+                 int* steps) {
+  const int D = s->D, nb = s->nb;
+  const size_t nblk = ((size_t)D + nb) * nrhs;
+  m = std::max(1, std::min(m, kKrylovMaxBasis - 1));
+  CU(s->kv.ensure((size_t)(m + 1) * nblk));
+  CU(s->kz.ensure((size_t)m * nblk));
+  CU(s->kw.ensure(nblk));
+  CU(s->kpart.ensure((size_t)nrhs * krylov_dot_blocks(D, nb) * kKrylovMaxBasis));
+  CU(s->kh.ensure((size_t)kKrylovMaxBasis * nrhs));
+  CU(s->hk_up.ensure((size_t)kKrylovMaxBasis * nrhs));
+  CU(s->hk_dn.ensure((size_t)kKrylovMaxBasis * nrhs));
+  double *V = s->kv.p, *Z = s->kz.p, *W = s->kw.p, *kh = s->kh.p;
+  const int KB = kKrylovMaxBasis;
+  auto read_h = [&](int nv) -> rs_status {
+    CU(cudaMemcpyAsync(s->hk_dn.p, kh, sizeof(double) * KB * nrhs, cudaMemcpyDeviceToHost,
+                       s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+    (void)nv;
+    return RS_OK;
+  };
+  auto upload_scale = [&](const std::vector<double>& v) -> rs_status {
+    for (int c = 0; c < nrhs; ++c) s->hk_up.p[c] = v[c];
+    CU(cudaMemcpyAsync(kh, s->hk_up.p, sizeof(double) * nrhs, cudaMemcpyHostToDevice, s->stream));
+    return RS_OK;
+  };
+  // beta = |b| per right-hand side, v_0 = b / beta
+  launch_mdot(b, 0, 1, b, D, nb, nrhs, s->kpart.p, kh, s->stream);
+  RSCHK(read_h(1));
+  std::vector<double> beta(nrhs), inv(nrhs);
+  for (int c = 0; c < nrhs; ++c) {
+    beta[c] = std::sqrt(std::max(0.0, s->hk_dn.p[c * KB]));
+    inv[c] = beta[c] > 0 ? 1.0 / beta[c] : 0.0;
+  }
+  RSCHK(upload_scale(inv));
+  launch_kscale(V, b, kh, D, nb, nrhs, s->stream);
+  s->launches += 3;
+  // per right-hand side: Hessenberg columns (after rotations), Givens, rhs g
+  std::vector<double> H((size_t)nrhs * (m + 1) * m, 0.0), cs((size_t)nrhs * m), sn((size_t)nrhs * m),
+      g((size_t)nrhs * (m + 1), 0.0), h1((size_t)nrhs * KB);
+  auto Hc = [&](int c, int i, int j) -> double& { return H[((size_t)c * (m + 1) + i) * m + j]; };
+  for (int c = 0; c < nrhs; ++c) g[(size_t)c * (m + 1)] = beta[c];
+  int k = 0;
+  for (int j = 0; j < m; ++j) {
+    double* Vj = V + (size_t)j * nblk;
+    double* Zj = Z + (size_t)j * nblk;
+    RSCHK(apply_prec(s, Vj, nrhs, Zj));
+    RSCHK(apply_neg_op(s, Zj, nrhs, W));
+    // classical Gram-Schmidt, twice
+    launch_mdot(V, nblk, j + 1, W, D, nb, nrhs, s->kpart.p, kh, s->stream);
+    launch_maxpy(W, V, nblk, j + 1, kh, -1.0, D, nb, nrhs, s->stream);
+    RSCHK(read_h(j + 1));
+    std::copy(s->hk_dn.p, s->hk_dn.p + (size_t)KB * nrhs, h1.begin());
+    launch_mdot(V, nblk, j + 1, W, D, nb, nrhs, s->kpart.p, kh, s->stream);
+    launch_maxpy(W, V, nblk, j + 1, kh, -1.0, D, nb, nrhs, s->stream);
+    RSCHK(read_h(j + 1));
+    for (size_t e = 0; e < h1.size(); ++e) h1[e] += s->hk_dn.p[e];
+    launch_mdot(W, 0, 1, W, D, nb, nrhs, s->kpart.p, kh, s->stream);
+    RSCHK(read_h(1));
+    s->launches += 10;
+    bool done = true;
+    for (int c = 0; c < nrhs; ++c) {
+      const double wn = std::sqrt(std::max(0.0, s->hk_dn.p[c * KB]));
+      inv[c] = wn > 0 ? 1.0 / wn : 0.0;
+      // A z_j = sum_i (-h_i) v_i - |w| v_{j+1}  (w holds -A z_j)
+      for (int i = 0; i <= j; ++i) Hc(c, i, j) = -h1[(size_t)c * KB + i];
+      Hc(c, j + 1, j) = -wn;
+      for (int i = 0; i < j; ++i) {  // earlier rotations
+        const double a = Hc(c, i, j), bb = Hc(c, i + 1, j);
+        Hc(c, i, j) = cs[(size_t)c * m + i] * a + sn[(size_t)c * m + i] * bb;
+        Hc(c, i + 1, j) = -sn[(size_t)c * m + i] * a + cs[(size_t)c * m + i] * bb;
+      }
+      const double a = Hc(c, j, j), bb = Hc(c, j + 1, j);
+      const double r = std::hypot(a, bb);
+      const double cj = r > 0 ? a / r : 1.0, sj = r > 0 ? bb / r : 0.0;
+      cs[(size_t)c * m + j] = cj;
+      sn[(size_t)c * m + j] = sj;
+      Hc(c, j, j) = r;
+      Hc(c, j + 1, j) = 0.0;
+      const double gj = g[(size_t)c * (m + 1) + j];
+      g[(size_t)c * (m + 1) + j] = cj * gj;
+      g[(size_t)c * (m + 1) + j + 1] = -sj * gj;
+      if (beta[c] > 0 && std::fabs(g[(size_t)c * (m + 1) + j + 1]) > rtol * beta[c]) done = false;
+    }
+    k = j + 1;
+    if (done || j + 1 == m) break;
+    RSCHK(upload_scale(inv));
+    launch_kscale(V + (size_t)(j + 1) * nblk, W, kh, D, nb, nrhs, s->stream);
+    ++s->launches;
+  }
+  // y = R^{-1} g per right-hand side; d = Z y
+  for (int c = 0; c < nrhs; ++c) {
+    std::vector<double> y(k, 0.0);
+    for (int i = k - 1; i >= 0; --i) {
+      double t = g[(size_t)c * (m + 1) + i];
+      for (int l = i + 1; l < k; ++l) t -= Hc(c, i, l) * y[l];
+      y[i] = Hc(c, i, i) != 0.0 ? t / Hc(c, i, i) : 0.0;
+    }
+    for (int i = 0; i < KB; ++i) s->hk_up.p[(size_t)c * KB + i] = i < k ? y[i] : 0.0;
+  }
+  CU(cudaMemcpyAsync(kh, s->hk_up.p, sizeof(double) * KB * nrhs, cudaMemcpyHostToDevice,
+                     s->stream));
+  CU(cudaMemsetAsync(d, 0, nblk * 8, s->stream));
+  launch_maxpy(d, Z, nblk, k, kh, 1.0, D, nb, nrhs, s->stream);
+  ++s->launches;
+  *steps = k;
+  CU(cudaGetLastError());
+  return RS_OK;
+}
+
 rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu, double* alpha) {
   const int D = s->D, nb = s->nb;
   const size_t nd = (size_t)D * nrhs;
@@ -1284,6 +1471,7 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
     if (rc != RS_OK) return rc;
     CU(cudaMemcpyAsync(mu, F.x.p, nd * 8, cudaMemcpyDeviceToDevice, s->stream));
     s->stats.refine_iters = 0;
+    s->stats.krylov_steps = 0;
     return RS_OK;
   }
   // FP32 factorization + FP64 iterative refinement
@@ -1306,50 +1494,122 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   s->stats.residual64_ms = 0;
   s->stats.residual32_ms = 0;
   int it = 0;
-  double worst = 0;
+  double worst = 0, prev = 1.0;
   const int max_it = std::max(1, s->cfg.refine_max_iters);
   const bool recur = s->fmm.built;
+  const double eps32 = fmm32_error(s->cfg.pde);
   if (recur) {
     CU(s->x64.ensure(nd));
     CU(s->xa64.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
     CU(s->g64.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
   }
-  for (it = 0; it < max_it; ++it) {
-    launch_d2f(s->r64.p, F.x.p, nd, s->stream);
-    rs_status rc = apply_inverse<float>(s, F.x.p, nrhs, F.tmp.p, it == 0 || !nb ? nullptr : rg);
-    if (rc != RS_OK) return rc;
-    CU(cudaEventRecord(s->ev_a, s->stream));
-    const bool upd = recur && it > 0;
-    if (upd) {
-      launch_f2d(F.x.p, s->x64.p, nd, s->stream);
-      launch_axpby(mu, s->x64.p, 1.0, 1.0, nd, s->stream);
-      if (nb) {
-        launch_f2d(F.tmp.p, s->xa64.p, (size_t)nb * nrhs, s->stream);
-        launch_axpby(a64, s->xa64.p, 1.0, 1.0, (size_t)nb * nrhs, s->stream);
-      }
-      s->launches += 4;
-      rc = residual_update(s, s->x64.p, s->xa64.p, nrhs, s->r64.p, rg, s->g64.p);
-    } else {
-      launch_add_f2d(mu, F.x.p, nd, s->stream);
-      if (nb) launch_add_f2d(a64, F.tmp.p, (size_t)nb * nrhs, s->stream);
-      s->launches += 3;
-      rc = residual(s, f, mu, a64, nrhs, s->r64.p, rg);
-    }
-    if (rc != RS_OK) return rc;
+  // worst relative residual of r64 (and its event time into the given stat)
+  auto measure = [&](double* stat) -> rs_status {
     CU(cudaEventRecord(s->ev_b, s->stream));
     launch_col_norms(s->r64.p, D, nrhs, s->nrm_dev.p, s->stream);
     CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
     CU(cudaStreamSynchronize(s->stream));
     float ms_res = 0;
     CU(cudaEventElapsedTime(&ms_res, s->ev_a, s->ev_b));
-    (upd ? s->stats.residual32_ms : s->stats.residual64_ms) += ms_res;
+    if (stat) *stat += ms_res;
     worst = 0;
-    for (int c = 0; c < nrhs; ++c) {
-      double rel = fn[c] > 0 ? s->h_io.p[c] / fn[c] : s->h_io.p[c];
-      worst = std::max(worst, rel);
+    for (int c = 0; c < nrhs; ++c)
+      worst = std::max(worst, fn[c] > 0 ? s->h_io.p[c] / fn[c] : s->h_io.p[c]);
+    return RS_OK;
+  };
+  auto fresh = [&]() -> rs_status {
+    CU(cudaEventRecord(s->ev_a, s->stream));
+    RSCHK(residual(s, f, mu, a64, nrhs, s->r64.p, rg));
+    return measure(&s->stats.residual64_ms);
+  };
+  // GMRES-IR: the correction equation solved by flexible GMRES instead of
+  // one application of the FP32 factorization (refine_solver 2, or 0 once
+  // the stationary iteration contracts by less than a factor 10)
+  bool krylov = s->cfg.refine_solver == 2;
+  int ksteps = 0;
+  const size_t kbl = nd + (size_t)nb * nrhs;
+  if (nb) CU(cudaMemsetAsync(rg, 0, (size_t)nb * nrhs * 8, s->stream));
+  for (it = 0; it < max_it; ++it) {
+    const double before = prev;
+    bool upd = false;
+    if (krylov) {
+      CU(s->kb.ensure(kbl));
+      CU(s->x64.ensure(kbl));
+      CU(cudaMemcpyAsync(s->kb.p, s->r64.p, nd * 8, cudaMemcpyDeviceToDevice, s->stream));
+      if (nb)
+        CU(cudaMemcpyAsync(s->kb.p + nd, rg, (size_t)nb * nrhs * 8, cudaMemcpyDeviceToDevice,
+                           s->stream));
+      int steps = 0;
+      RSCHK(fgmres(s, s->kb.p, nrhs, kGmresInnerTol, kKrylovMaxBasis - 1, s->x64.p, &steps));
+      ksteps += steps;
+      launch_axpby(mu, s->x64.p, 1.0, 1.0, nd, s->stream);
+      if (nb) launch_axpby(a64, s->x64.p + nd, 1.0, 1.0, (size_t)nb * nrhs, s->stream);
+      s->launches += nb ? 2 : 1;
+      RSCHK(fresh());
+    } else {
+      launch_d2f(s->r64.p, F.x.p, nd, s->stream);
+      rs_status rc = apply_inverse<float>(s, F.x.p, nrhs, F.tmp.p, it == 0 || !nb ? nullptr : rg);
+      if (rc != RS_OK) return rc;
+      CU(cudaEventRecord(s->ev_a, s->stream));
+      // residual recurrence with the FP32 product of the correction (x ~
+      // prev relative to the data) only while its error, eps32 * prev, is
+      // below half the tolerance; otherwise a fresh float-float residual
+      upd = recur && it > 0 && eps32 * prev <= 0.5 * s->cfg.refine_tol;
+      if (upd) {
+        launch_f2d(F.x.p, s->x64.p, nd, s->stream);
+        launch_axpby(mu, s->x64.p, 1.0, 1.0, nd, s->stream);
+        if (nb) {
+          launch_f2d(F.tmp.p, s->xa64.p, (size_t)nb * nrhs, s->stream);
+          launch_axpby(a64, s->xa64.p, 1.0, 1.0, (size_t)nb * nrhs, s->stream);
+        }
+        s->launches += 4;
+        RSCHK(residual_update(s, s->x64.p, s->xa64.p, nrhs, s->r64.p, rg, s->g64.p));
+        RSCHK(measure(&s->stats.residual32_ms));
+      } else {
+        launch_add_f2d(mu, F.x.p, nd, s->stream);
+        if (nb) launch_add_f2d(a64, F.tmp.p, (size_t)nb * nrhs, s->stream);
+        s->launches += 3;
+        RSCHK(residual(s, f, mu, a64, nrhs, s->r64.p, rg));
+        RSCHK(measure(&s->stats.residual64_ms));
+      }
+    }
+    prev = worst;
+    if (s->trace)
+      std::fprintf(stderr, "[rskel] refine %d: %s, %s residual %.3e\n", it,
+                   krylov ? "GMRES" : "stationary", upd ? "recurrence" : "fresh", worst);
+    if (it == 0 && recur && s->cfg.fmm_order == 0) {
+      // The residual's multipole error scales with |mu| while the tolerance
+      // is relative to |f|: on an ill-conditioned system (|mu| >> |f|) the
+      // float-float product needs more terms.
+      launch_col_norms(mu, D, nrhs, s->nrm_dev.p, s->stream);
+      CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
+      CU(cudaStreamSynchronize(s->stream));
+      double amp = 0;
+      for (int c = 0; c < nrhs; ++c) amp = std::max(amp, fn[c] > 0 ? s->h_io.p[c] / fn[c] : 0.0);
+      const int want = auto_fmm_order(s->cfg.refine_tol / std::max(amp, 1.0), s->cfg.pde);
+      if (amp > 4.0 && want > s->fmm.p) {
+        if (!fmm_set_order(s->fmm, want)) return fail(s, RS_ERR_CUDA, "multipole order update failed");
+        if (s->trace)
+          std::fprintf(stderr, "[rskel] |mu|/|f| = %.1f: multipole order %d\n", amp, want);
+        RSCHK(fresh());
+        prev = worst;
+      }
+    }
+    if (worst <= s->cfg.refine_tol && upd && s->cfg.refine_verify) {
+      // the recurrence says converged: confirm with a fresh residual
+      RSCHK(fresh());
+      prev = worst;
     }
     if (worst <= s->cfg.refine_tol) { ++it; break; }
+    if (!krylov && s->cfg.refine_solver == 0 && recur && it >= 1 && worst > 0.1 * before) {
+      krylov = true;
+      if (upd) {  // GMRES works on the true residual
+        RSCHK(fresh());
+        prev = worst;
+      }
+    }
   }
+  s->stats.krylov_steps = ksteps;
   s->stats.refine_iters = it;
   s->stats.refine_residual = worst;
   return RS_OK;
@@ -1386,6 +1646,8 @@ void rs_config_default(rs_config* c) {
   c->fmm_order = 0;
   c->rank_headroom = 1.25;
   c->rank_extra_rows = 12;
+  c->refine_verify = 1;
+  c->refine_solver = 0;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -1400,7 +1662,7 @@ rs_status rs_create(const rs_config* cfg, rs_solver** out) {
   if (cfg->is_strong_admissibility) return RS_ERR_ARG;
   if (cfg->precision != RS_FP64 && cfg->precision != RS_FP32_REFINE) return RS_ERR_ARG;
   if (!(cfg->rank_headroom >= 1.0 && cfg->rank_headroom <= 4.0) || cfg->rank_extra_rows < 0 ||
-      cfg->rank_extra_rows > 128)
+      cfg->rank_extra_rows > 128 || cfg->refine_solver < 0 || cfg->refine_solver > 2)
     return RS_ERR_ARG;
   rs_solver* s = new rs_solver();
   s->cfg = *cfg;
@@ -1647,15 +1909,10 @@ rs_status rs_factor(rs_solver* s) {
   s->factored = false;
   rc = s->fp32 ? factor_impl<float>(s) : factor_impl<double>(s);
   if (rc != RS_OK) return rc;
-  if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann && s->fp32) {
-    // refinement residual needs the FP64 border matrices and an all-ones mask
-    std::vector<unsigned char> ones(s->D, 1);
+  if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann) {
+    // the residual's Psi product runs over every DOF: an all-ones mask
     CU(s->ones_mask.ensure(s->D));
-    CU(cudaMemcpyAsync(s->ones_mask.p, ones.data(), s->D, cudaMemcpyHostToDevice, s->stream));
-  } else if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann) {
-    std::vector<unsigned char> ones(s->D, 1);
-    CU(s->ones_mask.ensure(s->D));
-    CU(cudaMemcpyAsync(s->ones_mask.p, ones.data(), s->D, cudaMemcpyHostToDevice, s->stream));
+    CU(cudaMemsetAsync(s->ones_mask.p, 1, s->D, s->stream));
   }
   CU(cudaEventRecord(s->ev_f1, s->stream));
   CU(cudaMemcpyAsync(s->h_status.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));

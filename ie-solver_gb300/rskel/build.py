@@ -26,7 +26,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["id_kernel.cu", "decouple_kernel.cu", "solve_kernels.cu", "border_kernels.cu",
-              "fmm.cu", "id_noalloc.cu", "domain.cu", "rank_model.cu"]
+              "fmm.cu", "id_noalloc.cu", "domain.cu", "rank_model.cu",
+              "krylov.cu"]
 CPP_SOURCES = ["tree.cpp", "solver.cpp", "fmm_plan.cpp"]
 
 

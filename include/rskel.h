@@ -66,6 +66,16 @@ typedef struct {
                                 ell = ceil(rank_headroom * k_pred) + rank_extra_rows,
                                 default 1.25 and 12 */
   int rank_extra_rows;
+  int refine_verify;         /* RS_FP32_REFINE: 1 (default) = convergence of the residual
+                                recurrence (FP32 products of corrections) is confirmed by a
+                                fresh float-float residual, and refinement goes on while
+                                that is above refine_tol; 0 = trust the recurrence */
+  int refine_solver;         /* RS_FP32_REFINE correction equation: 0 (default) = one
+                                application of the FP32 factorization per step, switching to
+                                GMRES-IR when a step cuts the residual by less than 10x;
+                                1 = always the former; 2 = always GMRES-IR (flexible GMRES
+                                preconditioned by the FP32 factorization, FP32 multipole
+                                products, up to 31 steps per refinement step) */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
@@ -242,8 +252,9 @@ typedef struct {
                                                   sketch size was predicted, and those of them
                                                   redone with the full sketch */
   double sketch_rows;                          /* last RS_FP32_REFINE rs_factor: rows of the
-                                                  randomized-ID sketches of boxes of <= 128 DOFs,
+                                                  randomized-ID sketches of boxes of <= 512 DOFs,
                                                   summed (a redone box counts both sketches) */
+  int krylov_steps;                            /* last solve: GMRES steps of GMRES-IR */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 

@@ -281,3 +281,54 @@ def domain_eval(geo, pde, targets, mu, alpha=None, in_domain=None):
         sd = 2 if pde == 2 else 1
         out[np.repeat(~keep, sd)] = 0.0
     return out
+
+
+def border_matrices(geo, pde):
+    """U (D x nb) and Psi (nb x D) of the bordered system for a geometry with
+    holes, as initialize_U_mat and initialize_Psi_mat build them
+    (ie_solver/linear_solve.cpp:20-112): Laplace log|x - c_h| per hole;
+    Stokes a Stokeslet pair and a rotlet per hole; Psi the quadrature
+    weights of the hole's own points (first hole whose circle, radius
+    + 1e-8, holds the point), plus the moment row for Stokes.  pde: 0
+    Laplace, 2 Stokes."""
+    xy = np.asarray(geo.points, dtype=np.float64).reshape(-1, 2)
+    n = xy.shape[0]
+    hc = np.asarray(geo.hole_centers, dtype=np.float64).reshape(-1, 2)
+    hr = np.asarray(geo.hole_radii, dtype=np.float64).reshape(-1)
+    h = len(hr)
+    w = np.asarray(geo.weights, dtype=np.float64)
+    stokes = pde == 2
+    D = 2 * n if stokes else n
+    nb = 3 * h if stokes else h
+    U = np.zeros((D, nb))
+    P = np.zeros((nb, D))
+    member = -np.ones(n, dtype=int)
+    sc = 1.0 / (4.0 * np.pi)
+    for k in range(h):
+        r0 = xy[:, 0] - hc[k, 0]
+        r1 = xy[:, 1] - hc[k, 1]
+        r2 = r0 * r0 + r1 * r1
+        rn = np.sqrt(r2)
+        if stokes:
+            lg = np.log(1.0 / rn)
+            U[0::2, 3 * k] = sc * (lg + r0 * r0 / r2)
+            U[1::2, 3 * k] = sc * (r1 * r0 / r2)
+            U[0::2, 3 * k + 1] = sc * (r0 * r1 / r2)
+            U[1::2, 3 * k + 1] = sc * (lg + r1 * r1 / r2)
+            U[0::2, 3 * k + 2] = r1 * (sc / r2)
+            U[1::2, 3 * k + 2] = -r0 * (sc / r2)
+        else:
+            U[:, k] = np.log(rn)
+        sel = (member < 0) & (rn < hr[k] + 1e-8)
+        member[sel] = k
+    for i in np.nonzero(member >= 0)[0]:
+        k = member[i]
+        if stokes:
+            P[3 * k, 2 * i] = w[i]
+            P[3 * k + 1, 2 * i + 1] = w[i]
+            P[3 * k + 2, 2 * i] = w[i] * xy[i, 1]
+            P[3 * k + 2, 2 * i + 1] = -w[i] * xy[i, 0]
+        else:
+            P[k, i] = w[i]
+    return U, P
+
