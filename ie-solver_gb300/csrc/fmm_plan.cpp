@@ -98,9 +98,13 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
         for (int q = 0; q < 4; ++q) cnt[b] += cnt[nd.children[q]];
     }
   auto live = [&](int b) { return cnt[b] > 0; };
-  const double eps = 1e-9 * tree.nodes[tree.root].side;
+  // (a forest has one root per tree; lists never cross trees)
+  double root_side = 0;
+  for (int r : tree.roots) root_side = std::max(root_side, tree.nodes[r].side);
+  const double eps = 1e-9 * root_side;
   std::vector<std::vector<int>> coll(nb), V(nb), W(nb), X(nb), U(nb);
-  if (live(tree.root)) coll[tree.root].push_back(tree.root);
+  for (int r : tree.roots)
+    if (live(r)) coll[r].push_back(r);
   for (size_t lv = 1; lv < tree.levels.size(); ++lv) {
     for (int b : tree.levels[lv]) {
       if (!live(b)) continue;

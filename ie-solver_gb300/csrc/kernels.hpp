@@ -94,6 +94,20 @@ void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cuda
 
 // Dense LU with partial pivoting of an n x n column-major matrix (one CTA),
 // and the corresponding solve on gathered rows of x.
+// A forest's root blocks: E block at base[a_off] (n x n), pivots at
+// piv[piv_off], the block's DOFs at dofs[idx_off].
+struct RootTask {
+  int64_t a_off;
+  int n;
+  int piv_off;
+  int idx_off;
+  int pad;
+};
+void launch_dense_lu_batched(void* base, bool fp32, const RootTask* tasks, int count, int nmax,
+                             int* piv, int* status, cudaStream_t st);
+void launch_dense_solve_batched(const void* base, bool fp32, const RootTask* tasks, int count,
+                                int nmax, const int* piv, const int* dofs, void* x, int ld,
+                                int nrhs, cudaStream_t st);
 void launch_dense_lu(double* a, int n, int* piv, int* status, cudaStream_t st);
 void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st);
 // x[idx, :] = LU^{-1} x[idx, :] (idx == nullptr: rows 0..n-1); x is Real.

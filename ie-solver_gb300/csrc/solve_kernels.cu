@@ -182,9 +182,8 @@ void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cuda
 // reference calls it for the root, ie_mat.cpp:449-470).  With staged != 0
 // the block is held in shared memory for the whole factorization.
 template <class Real>
-__global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* Ag, int n, int* piv,
-                                                            int* status, int staged) {
-  extern __shared__ __align__(16) unsigned char smem[];
+__device__ void dense_lu_body(Real* Ag, int n, int* piv, int* status, int staged,
+                              unsigned char* smem) {
   __shared__ int s_piv;
   __shared__ int s_bad;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -241,6 +240,26 @@ __global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* Ag, int n, int
 }
 
 template <class Real>
+__global__ void __launch_bounds__(kThreads) dense_lu_kernel(Real* Ag, int n, int* piv,
+                                                            int* status, int staged) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  dense_lu_body<Real>(Ag, n, piv, status, staged, smem);
+}
+
+// One root block per CTA (a forest's trees); a block is staged in shared
+// memory when it fits in the launch's allocation.
+template <class Real>
+__global__ void __launch_bounds__(kThreads) dense_lu_batched_kernel(Real* base,
+                                                                    const RootTask* tasks,
+                                                                    int* piv, int* status,
+                                                                    size_t smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const RootTask t = tasks[blockIdx.x];
+  const int staged = sizeof(Real) * (size_t)t.n * t.n <= smem_bytes;
+  dense_lu_body<Real>(base + t.a_off, t.n, piv + t.piv_off, status, staged, smem);
+}
+
+template <class Real>
 static void launch_dense_lu_t(Real* a, int n, int* piv, int* status, cudaStream_t st) {
   if (n <= 0) return;
   const size_t bytes = sizeof(Real) * (size_t)n * n;
@@ -255,16 +274,30 @@ void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st
   launch_dense_lu_t<float>(a, n, piv, status, st);
 }
 
+void launch_dense_lu_batched(void* base, bool fp32, const RootTask* tasks, int count, int nmax,
+                             int* piv, int* status, cudaStream_t st) {
+  if (count <= 0 || nmax <= 0) return;
+  const size_t es = fp32 ? 4 : 8;
+  size_t smem = es * (size_t)nmax * nmax;
+  if (smem + 1024 > (size_t)kSmemOptIn) smem = (size_t)kSmemOptIn - 1024;
+  if (fp32) {
+    set_smem_once<dense_lu_batched_kernel<float>>();
+    dense_lu_batched_kernel<float><<<count, kThreads, smem, st>>>((float*)base, tasks, piv, status,
+                                                                  smem);
+  } else {
+    set_smem_once<dense_lu_batched_kernel<double>>();
+    dense_lu_batched_kernel<double><<<count, kThreads, smem, st>>>((double*)base, tasks, piv,
+                                                                   status, smem);
+  }
+}
+
 // x[idx, c] = LU^{-1} x[idx, c] for the root block (dgetrs), up to kWarps
 // columns per CTA, one warp per column.  staged: 0 = work on x and LU in
 // global memory; 1 = gathered columns in shared memory (n x cols); 2 = the
 // LU factors in shared memory too.
 template <class Real>
-__global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LUg, int n,
-                                                               const int* piv, const int* idx,
-                                                               Real* x, int ld, int nrhs,
-                                                               int staged) {
-  extern __shared__ __align__(16) unsigned char smem[];
+__device__ void dense_solve_body(const Real* LUg, int n, const int* piv, const int* idx, Real* x,
+                                 int ld, int nrhs, int staged, unsigned char* smem) {
   Real* sx = reinterpret_cast<Real*>(smem);
   Real* sl = sx + (size_t)n * nrhs;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -308,6 +341,55 @@ __global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LUg, 
       const int i = e % n, c = e / n;
       x[(idx ? idx[i] : i) + (size_t)ld * c] = sx[e];
     }
+  }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(kThreads) dense_solve_kernel(const Real* LUg, int n,
+                                                               const int* piv, const int* idx,
+                                                               Real* x, int ld, int nrhs,
+                                                               int staged) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  dense_solve_body<Real>(LUg, n, piv, idx, x, ld, nrhs, staged, smem);
+}
+
+// One root block per CTA, all right-hand sides in chunks of kWarps columns,
+// each chunk staged as far as the launch's allocation allows.
+template <class Real>
+__global__ void __launch_bounds__(kThreads) dense_solve_batched_kernel(const Real* base,
+                                                                       const RootTask* tasks,
+                                                                       const int* piv,
+                                                                       const int* dofs, Real* x,
+                                                                       int ld, int nrhs,
+                                                                       size_t smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const RootTask t = tasks[blockIdx.x];
+  for (int c0 = 0; c0 < nrhs; c0 += kWarps) {
+    const int cols = nrhs - c0 < kWarps ? nrhs - c0 : kWarps;
+    const size_t xb = sizeof(Real) * (size_t)t.n * cols, lb = sizeof(Real) * (size_t)t.n * t.n;
+    const int staged = xb + lb <= smem_bytes ? 2 : xb <= smem_bytes ? 1 : 0;
+    dense_solve_body<Real>(base + t.a_off, t.n, piv + t.piv_off, dofs + t.idx_off,
+                           x + (size_t)ld * c0, ld, cols, staged, smem);
+    __syncthreads();
+  }
+}
+
+void launch_dense_solve_batched(const void* base, bool fp32, const RootTask* tasks, int count,
+                                int nmax, const int* piv, const int* dofs, void* x, int ld,
+                                int nrhs, cudaStream_t st) {
+  if (count <= 0 || nmax <= 0 || nrhs <= 0) return;
+  const size_t es = fp32 ? 4 : 8;
+  const int cols = nrhs < kWarps ? nrhs : kWarps;
+  size_t smem = es * ((size_t)nmax * cols + (size_t)nmax * nmax);
+  if (smem > (size_t)kSmemOptIn) smem = (size_t)kSmemOptIn;
+  if (fp32) {
+    set_smem_once<dense_solve_batched_kernel<float>>();
+    dense_solve_batched_kernel<float><<<count, kThreads, smem, st>>>(
+        (const float*)base, tasks, piv, dofs, (float*)x, ld, nrhs, smem);
+  } else {
+    set_smem_once<dense_solve_batched_kernel<double>>();
+    dense_solve_batched_kernel<double><<<count, kThreads, smem, st>>>(
+        (const double*)base, tasks, piv, dofs, (double*)x, ld, nrhs, smem);
   }
 }
 
@@ -506,6 +588,32 @@ void launch_col_norms(const double* x, int rows, int cols, double* out, cudaStre
   double* part = out + cols;
   col_norms_partial_kernel<<<dim3(kNormBlocks, cols), 256, 0, st>>>(x, rows, part);
   col_norms_final_kernel<<<(cols + 7) / 8, 256, 0, st>>>(part, cols, out);
+}
+
+// out[q + np * c] = |x[seg[q] .. seg[q + 1]), column c|_2: the norm of each
+// boundary's part of a batch (one CTA per boundary and column).
+__global__ void seg_norms_kernel(const double* x, int rows, const int* seg, int np, double* out) {
+  __shared__ double red[kThreads / 32];
+  const int q = blockIdx.x, c = blockIdx.y;
+  double acc = 0.0;
+  for (int i = seg[q] + threadIdx.x; i < seg[q + 1]; i += blockDim.x) {
+    const double v = x[i + (size_t)rows * c];
+    acc += v * v;
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+    out[q + (size_t)np * c] = sqrt(t);
+  }
+}
+
+void launch_seg_norms(const double* x, int rows, int cols, const int* seg, int np, double* out,
+                      cudaStream_t st) {
+  if (cols <= 0 || np <= 0) return;
+  seg_norms_kernel<<<dim3(np, cols), kThreads, 0, st>>>(x, rows, seg, np, out);
 }
 
 // r[l] -= sum_j U[l, j] a[j]

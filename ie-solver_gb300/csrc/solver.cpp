@@ -104,8 +104,18 @@ struct rs_solver {
   int ns = 0;
   std::vector<int> allskel;
   int allskel_off = -1;
-  int64_t root_e_off = -1;
+  int64_t root_e_off = -1;  // the first root's E block (the bordered system uses it)
   DevBuf<int> root_piv;
+  // one root block per tree: the root tasks (E block, pivots, DOF list) of
+  // the dense LU and solve, and the largest root
+  std::vector<RootTask> roots_h;
+  DevBuf<RootTask> roots_dev;
+  int root_nmax = 0;
+  // boundaries held by the handle (rs_set_geometry_batch) and their point
+  // offsets; per-boundary DOF offsets on the device for the norms
+  int nprob = 1;
+  std::vector<int> prob_pt;
+  DevBuf<int> prob_dof;
 
   // bordered system
   int nb = 0;
@@ -273,14 +283,28 @@ void id_rows(rs_solver* s, int id, std::vector<int>* rows, int* use_proxy) {
   const int lv = nd.level;
   *use_proxy = 0;
   if (lv == 1 || lv == 2) {
-    for (int o : s->tree.levels[lv])
-      if (o != id) {
-        const std::vector<int>& v = s->st[o].active;
+    // (in a forest, the boxes of the same tree: a contiguous run of the
+    // level list, which holds the trees in order)
+    const int tid = nd.tree_id;
+    auto same_tree = [&](const std::vector<int>& lvl) {
+      const auto lo = std::partition_point(lvl.begin(), lvl.end(), [&](int o) {
+        return s->tree.nodes[o].tree_id < tid;
+      });
+      const auto hi = std::partition_point(lo, lvl.end(), [&](int o) {
+        return s->tree.nodes[o].tree_id == tid;
+      });
+      return std::make_pair(lo, hi);
+    };
+    const auto r = same_tree(s->tree.levels[lv]);
+    for (auto it = r.first; it != r.second; ++it)
+      if (*it != id) {
+        const std::vector<int>& v = s->st[*it].active;
         rows->insert(rows->end(), v.begin(), v.end());
       }
+    const auto r1 = same_tree(s->tree.levels[1]);
     if (lv == 2)
-      for (int o : s->tree.levels[1])
-        if (s->tree.nodes[o].is_leaf) {
+      for (auto it = r1.first; it != r1.second; ++it)
+        if (const int o = *it; s->tree.nodes[o].is_leaf) {
           const std::vector<int>& v = s->tree.nodes[o].original;
           rows->insert(rows->end(), v.begin(), v.end());
         }
@@ -948,31 +972,58 @@ rs_status factor_impl(rs_solver* s) {
                  t_plan, t_detail[0], t_detail[1], t_detail[2], t_detail[3], t_wait, t_post);
   const double h3 = now_ms();
   // remove_inactive_dofs_at_all_boxes (quadtree.cpp:989-995): only the root
-  // (and level-0 bookkeeping) changes for a fresh factorization.
-  {
-    const int root = s->tree.root;
-    compute_active(s, root);
-    compute_near(s, root);
+  // (and level-0 bookkeeping) changes for a fresh factorization.  A forest
+  // (a batch of boundaries) has one root per tree.
+  for (int r : s->tree.roots) {
+    compute_active(s, r);
+    compute_near(s, r);
   }
-  // root block (skel_factorization.cpp:174-186)
-  NodeState& R = s->st[s->tree.root];
-  s->allskel = R.active;
-  s->ns = (int)s->allskel.size();
+  // root blocks (skel_factorization.cpp:174-186), one per tree
   const size_t seg0 = s->pool.size();
   s->allskel_off = (int)seg0;
-  s->pool.insert(s->pool.end(), s->allskel.begin(), s->allskel.end());
+  s->allskel.clear();
+  s->roots_h.clear();
+  s->root_nmax = 0;
   std::vector<BlkRef> rblk;
-  const TreeNode& rn = s->tree.nodes[s->tree.root];
-  if (rn.is_leaf) {
-    for (int j = 0; j < s->ns; ++j) rblk.push_back(BlkRef{0, j, 0, 0, -1});
-  } else {
-    for (int c = 0; c < 4; ++c) {
-      const NodeState& C = s->st[rn.children[c]];
-      const std::vector<int>& v = surviving(C);
-      for (int j = 0; j < (int)v.size(); ++j)
-        rblk.push_back(BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1});
+  std::vector<DecoupleTask> rdt;
+  int piv_total = 0;
+  for (int r : s->tree.roots) {
+    const NodeState& R = s->st[r];
+    RootTask rt{};
+    rt.n = (int)R.active.size();
+    rt.idx_off = (int)s->pool.size();
+    rt.piv_off = piv_total;
+    rt.a_off = (int64_t)F.e_used;
+    s->pool.insert(s->pool.end(), R.active.begin(), R.active.end());
+    s->allskel.insert(s->allskel.end(), R.active.begin(), R.active.end());
+    if (rt.n == 0) continue;
+    piv_total += rt.n;
+    F.e_used += (size_t)rt.n * rt.n;
+    DecoupleTask d{};
+    d.n = rt.n;
+    d.act_off = rt.idx_off;
+    d.blk_off = (int)rblk.size();
+    d.slot = -1;
+    d.perm_off = rt.idx_off;
+    d.e_off = rt.a_off;
+    d.scratch_off = -1;
+    const TreeNode& rn = s->tree.nodes[r];
+    if (rn.is_leaf) {
+      for (int j = 0; j < rt.n; ++j) rblk.push_back(BlkRef{0, j, 0, 0, -1});
+    } else {
+      for (int c = 0; c < 4; ++c) {
+        const NodeState& C = s->st[rn.children[c]];
+        const std::vector<int>& v = surviving(C);
+        for (int j = 0; j < (int)v.size(); ++j)
+          rblk.push_back(BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1});
+      }
     }
+    rdt.push_back(d);
+    s->roots_h.push_back(rt);
+    s->root_nmax = std::max(s->root_nmax, rt.n);
   }
+  s->ns = (int)s->allskel.size();
+  s->root_e_off = s->roots_h.empty() ? 0 : s->roots_h[0].a_off;
   // solve plan: compressed boxes per level, skeleton / redundant lists
   s->sweeps.clear();
   s->sweep_off.assign(L, 0);
@@ -1002,30 +1053,23 @@ rs_status factor_impl(rs_solver* s) {
   if (!s->sweeps.empty())
     CU(cudaMemcpyAsync(s->sweep_dev.p, s->sweeps.data(), s->sweeps.size() * sizeof(SweepTask),
                        cudaMemcpyHostToDevice, s->stream));
-  s->root_e_off = (int64_t)F.e_used;
-  F.e_used += (size_t)s->ns * s->ns;
   CU(F.epool.ensure_keep(F.e_used, e_prev, s->stream));
-  if (s->ns > 0) {
-    DecoupleTask d{};
-    d.n = s->ns;
-    d.act_off = s->allskel_off;
-    d.blk_off = 0;
-    d.slot = -1;
-    d.perm_off = s->allskel_off;
-    d.fac_off = 0;
-    d.piv_off = 0;
-    d.e_off = s->root_e_off;
-    d.scratch_off = -1;
-    bool in_smem = decouple_kernel_smem(s->ns, f32, true) <= kSmemMax;
-    if (!in_smem) {
-      d.scratch_off = 0;
-      CU(F.scratch.ensure((size_t)(s->ns + 1) * (s->ns + 1) * 2));
-    }
+  if (!rdt.empty()) {
+    // root E blocks: the same assembly as a level's uncompressed boxes,
+    // every tree's root in one launch (binned by size)
+    std::stable_sort(rdt.begin(), rdt.end(),
+                     [](const DecoupleTask& a, const DecoupleTask& b) { return a.n < b.n; });
+    size_t rscratch = 0;
+    for (DecoupleTask& d : rdt)
+      if (decouple_kernel_smem(d.n, f32, true) > kSmemMax) {
+        d.scratch_off = (int64_t)rscratch;
+        rscratch += (size_t)(d.n + 1) * (d.n + 1) * 2;
+      }
+    if (rscratch) CU(F.scratch.ensure(rscratch));
     CU(s->blk.ensure(rblk.size()));
-    CU(cudaMemcpyAsync(s->blk.p, rblk.data(), rblk.size() * sizeof(BlkRef),
-                       cudaMemcpyHostToDevice, s->stream));
-    CU(s->dc_tasks.ensure(1));
-    CU(cudaMemcpyAsync(s->dc_tasks.p, &d, sizeof(d), cudaMemcpyHostToDevice, s->stream));
+    CU(s->dc_tasks.ensure(rdt.size()));
+    CU(stage_copy(s, s->blk.p, rblk.data(), rblk.size() * sizeof(BlkRef)));
+    CU(stage_copy(s, s->dc_tasks.p, rdt.data(), rdt.size() * sizeof(DecoupleTask)));
     DecoupleParams dp{};
     dp.geo = geo_of(s);
     dp.pde = s->cfg.pde;
@@ -1040,20 +1084,29 @@ rs_status factor_impl(rs_solver* s) {
     dp.epool = F.epool.p;
     dp.scratch = F.scratch.p;
     dp.status = s->status.p;
-    launch_decouple(dp, 1, decouple_kernel_smem(s->ns, f32, in_smem), f32, s->stream);
-    ++s->launches;
+    auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
+    launch_binned(rdt, s->dc_tasks.p, dc_fits, [&](const DecoupleTask* dt, int cnt, int nmax) {
+      DecoupleParams q = dp;
+      q.tasks = dt;
+      bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
+      launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream);
+      ++s->launches;
+    });
     CU(cudaGetLastError());
+  }
+  CU(s->root_piv.ensure(std::max(piv_total, 1)));
+  if (!s->roots_h.empty()) {
+    CU(s->roots_dev.ensure(s->roots_h.size()));
+    CU(stage_copy(s, s->roots_dev.p, s->roots_h.data(), s->roots_h.size() * sizeof(RootTask)));
   }
   s->nb = 0;
   if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann) {
     // bordered system, skel_factorization.cpp:188-305
     rs_status rc = factor_border<Real>(s);
     if (rc != RS_OK) return rc;
-  } else if (s->ns > 0) {
-    CU(s->root_piv.ensure(s->ns));
-    Real* a = F.epool.p + s->root_e_off;
-    if (f32) launch_dense_lu_f32((float*)a, s->ns, s->root_piv.p, s->status.p, s->stream);
-    else launch_dense_lu((double*)a, s->ns, s->root_piv.p, s->status.p, s->stream);
+  } else if (!s->roots_h.empty()) {
+    launch_dense_lu_batched(F.epool.p, f32, s->roots_dev.p, (int)s->roots_h.size(), s->root_nmax,
+                            s->root_piv.p, s->status.p, s->stream);
     ++s->launches;
   }
   CU(cudaGetLastError());
@@ -1204,10 +1257,10 @@ rs_status apply_inverse(rs_solver* s, Real* x, int nrhs, Real* alpha, const doub
   Factor<Real>& F = factor_of<Real>(s);
   if (s->nb == 0) {
     sweep_levels<Real>(s, x, s->D, nrhs, kUpSolve, true);
-    if (s->ns > 0) {
-      launch_dense_solve_gather(F.epool.p + s->root_e_off, sizeof(Real) == 4, s->ns,
-                                s->root_piv.p, s->dofs.p + s->allskel_off, x, s->D, nrhs,
-                                s->stream);
+    if (!s->roots_h.empty()) {
+      launch_dense_solve_batched(F.epool.p, sizeof(Real) == 4, s->roots_dev.p,
+                                 (int)s->roots_h.size(), s->root_nmax, s->root_piv.p, s->dofs.p,
+                                 x, s->D, nrhs, s->stream);
       ++s->launches;
     }
     sweep_levels<Real>(s, x, s->D, nrhs, kDown, false);
@@ -1229,6 +1282,8 @@ rs_status apply_inverse(rs_solver* s, Real* x, int nrhs, Real* alpha, const doub
 // ---------------------------------------------------------------------------
 namespace rskel {
 void launch_col_norms(const double* x, int rows, int cols, double* out, cudaStream_t st);
+void launch_seg_norms(const double* x, int rows, int cols, const int* seg, int np, double* out,
+                      cudaStream_t st);
 void launch_gemv_sub(double* r, const double* U, const double* a, int D, int nb, cudaStream_t st);
 }  // namespace rskel
 
@@ -1480,17 +1535,33 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   CU(F.tmp.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
   CU(s->r64.ensure(nd));
   CU(s->acc64.ensure(std::max<size_t>(2 * (size_t)nb * nrhs, 1)));
-  CU(s->nrm_dev.ensure(65 * (size_t)nrhs + 2));  // norms + partial sums
-  CU(s->h_io.ensure(4 * (size_t)nrhs + 4));
+  // Norms per column, or per boundary and column for a batch (each boundary
+  // is its own system): ncol entries into h_io.
+  const int np = s->nprob;
+  const int ncol = np * nrhs;
+  CU(s->nrm_dev.ensure(65 * (size_t)nrhs + 2 + (size_t)ncol));  // norms + partial sums
+  CU(s->h_io.ensure(4 * (size_t)nrhs + 4 + (size_t)ncol));
+  if (np > 1) {
+    std::vector<int> seg(np + 1);
+    for (int q = 0; q <= np; ++q) seg[q] = s->prob_pt[q] * s->sd;
+    CU(s->prob_dof.ensure(np + 1));
+    CU(cudaMemcpyAsync(s->prob_dof.p, seg.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                       s->stream));
+    CU(cudaStreamSynchronize(s->stream));
+  }
+  auto launch_norms = [&](const double* x) {
+    if (np > 1) launch_seg_norms(x, D, nrhs, s->prob_dof.p, np, s->nrm_dev.p, s->stream);
+    else launch_col_norms(x, D, nrhs, s->nrm_dev.p, s->stream);
+  };
   double* rg = s->acc64.p;
   double* a64 = alpha;
   CU(cudaMemsetAsync(mu, 0, nd * 8, s->stream));
   if (nb) CU(cudaMemsetAsync(a64, 0, (size_t)nb * nrhs * 8, s->stream));
   CU(cudaMemcpyAsync(s->r64.p, f, nd * 8, cudaMemcpyDeviceToDevice, s->stream));
-  launch_col_norms(f, D, nrhs, s->nrm_dev.p, s->stream);
-  CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
+  launch_norms(f);
+  CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, ncol * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
-  std::vector<double> fn(s->h_io.p, s->h_io.p + nrhs);
+  std::vector<double> fn(s->h_io.p, s->h_io.p + ncol);
   s->stats.residual64_ms = 0;
   s->stats.residual32_ms = 0;
   int it = 0;
@@ -1506,14 +1577,14 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   // worst relative residual of r64 (and its event time into the given stat)
   auto measure = [&](double* stat) -> rs_status {
     CU(cudaEventRecord(s->ev_b, s->stream));
-    launch_col_norms(s->r64.p, D, nrhs, s->nrm_dev.p, s->stream);
-    CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
+    launch_norms(s->r64.p);
+    CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, ncol * 8, cudaMemcpyDeviceToHost, s->stream));
     CU(cudaStreamSynchronize(s->stream));
     float ms_res = 0;
     CU(cudaEventElapsedTime(&ms_res, s->ev_a, s->ev_b));
     if (stat) *stat += ms_res;
     worst = 0;
-    for (int c = 0; c < nrhs; ++c)
+    for (int c = 0; c < ncol; ++c)
       worst = std::max(worst, fn[c] > 0 ? s->h_io.p[c] / fn[c] : s->h_io.p[c]);
     return RS_OK;
   };
@@ -1581,11 +1652,11 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
       // The residual's multipole error scales with |mu| while the tolerance
       // is relative to |f|: on an ill-conditioned system (|mu| >> |f|) the
       // float-float product needs more terms.
-      launch_col_norms(mu, D, nrhs, s->nrm_dev.p, s->stream);
-      CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, nrhs * 8, cudaMemcpyDeviceToHost, s->stream));
+      launch_norms(mu);
+      CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, ncol * 8, cudaMemcpyDeviceToHost, s->stream));
       CU(cudaStreamSynchronize(s->stream));
       double amp = 0;
-      for (int c = 0; c < nrhs; ++c) amp = std::max(amp, fn[c] > 0 ? s->h_io.p[c] / fn[c] : 0.0);
+      for (int c = 0; c < ncol; ++c) amp = std::max(amp, fn[c] > 0 ? s->h_io.p[c] / fn[c] : 0.0);
       const int want = auto_fmm_order(s->cfg.refine_tol / std::max(amp, 1.0), s->cfg.pde);
       if (amp > 4.0 && want > s->fmm.p) {
         if (!fmm_set_order(s->fmm, want)) return fail(s, RS_ERR_CUDA, "multipole order update failed");
@@ -1717,6 +1788,8 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
   s->w.assign(weights, weights + num_points);
   s->kap.assign(curvatures, curvatures + num_points);
   s->nh = num_holes;
+  s->nprob = 1;
+  s->prob_pt.assign({0, num_points});
   s->hc.assign(hole_centers ? hole_centers : points, hole_centers ? hole_centers + 2 * num_holes : points);
   s->hr.assign(hole_radii ? hole_radii : points, hole_radii ? hole_radii + num_holes : points);
   s->tree_built = false;
@@ -1726,12 +1799,45 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
   return RS_OK;
 }
 
+rs_status rs_set_geometry_batch(rs_solver* s, int count, const int* num_points,
+                                const double* points, const double* normals,
+                                const double* weights, const double* curvatures) {
+  if (!s || count < 1 || !num_points) return fail(s, RS_ERR_ARG, "bad batch arguments");
+  long long total = 0;
+  for (int t = 0; t < count; ++t) {
+    if (num_points[t] <= 0) return fail(s, RS_ERR_ARG, "empty boundary in batch");
+    total += num_points[t];
+  }
+  if (total > (1LL << 30) / s->sd) return fail(s, RS_ERR_CAPACITY, "batch too large");
+  rs_status rc = rs_set_geometry(s, (int)total, points, normals, weights, curvatures, 0, nullptr,
+                                 nullptr);
+  if (rc != RS_OK) return rc;
+  s->nprob = count;
+  s->prob_pt.assign(count + 1, 0);
+  for (int t = 0; t < count; ++t) s->prob_pt[t + 1] = s->prob_pt[t] + num_points[t];
+  return RS_OK;
+}
+
 rs_status rs_build_tree(rs_solver* s) {
   if (!s) return RS_ERR_ARG;
   if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
   double t0 = now_ms();
-  if (!s->tree.build(s->pts.data(), s->n, s->sd, s->cfg.max_leaf_dofs))
+  if (s->nprob > 1) {
+    // one tree per boundary, merged into a forest (independent problems)
+    std::vector<QuadTree> parts(s->nprob);
+    std::vector<int> dof_off(s->nprob);
+    bool ok = true;
+#pragma omp parallel for schedule(dynamic, 4) reduction(&& : ok)
+    for (int t = 0; t < s->nprob; ++t) {
+      const int p0 = s->prob_pt[t], np = s->prob_pt[t + 1] - p0;
+      ok = parts[t].build(s->pts.data() + 2 * (size_t)p0, np, s->sd, s->cfg.max_leaf_dofs) && ok;
+      dof_off[t] = p0 * s->sd;
+    }
+    if (!ok) return fail(s, RS_ERR_ARG, "tree build failed");
+    s->tree.merge(parts, dof_off);
+  } else if (!s->tree.build(s->pts.data(), s->n, s->sd, s->cfg.max_leaf_dofs)) {
     return fail(s, RS_ERR_ARG, "tree build failed");
+  }
   s->fmm.built = false;
   s->tree_built = true;
   s->factored = false;
@@ -1764,6 +1870,7 @@ rs_status rs_perturb(rs_solver* s, int num_points, const double* points, const d
                      const double* weights, const double* curvatures, int num_holes,
                      const double* hole_centers, const double* hole_radii) {
   if (!s) return RS_ERR_ARG;
+  if (s->nprob > 1) return fail(s, RS_ERR_ARG, "rs_perturb of a batch");
   if (!s->tree_built)  // nothing to update
     return rs_set_geometry(s, num_points, points, normals, weights, curvatures, num_holes,
                            hole_centers, hole_radii);
@@ -1900,6 +2007,8 @@ rs_status rs_factor(rs_solver* s) {
   CU(cudaSetDevice(s->cfg.device));
   rc = upload_geometry(s);
   if (rc != RS_OK) return rc;
+  if (s->fp32 && s->nprob > 1 && s->cfg.pde != kLaplace)
+    return fail(s, RS_ERR_ARG, "refinement of a batch supports the Laplace double layer only");
   if (s->fp32 && !s->fmm.built) {
     rc = build_fmm(s);
     if (rc != RS_OK) return rc;
@@ -2005,6 +2114,7 @@ rs_status rs_kernel_block(rs_solver* s, const int* I, int nI, const int* J, int 
 rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y) {
   if (!s || !x || !y || nrhs < 1) return fail(s, RS_ERR_ARG, "bad matvec arguments");
   if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
+  if (s->nprob > 1) return fail(s, RS_ERR_ARG, "dense product of a batch (use rs_matvec_fast)");
   rs_status rc = ensure_device(s);
   if (rc != RS_OK) return rc;
   rc = upload_geometry(s);
@@ -2054,6 +2164,7 @@ rs_status rs_domain_eval(rs_solver* s, int num_targets, const double* targets,
   if (!s || num_targets < 0 || (num_targets > 0 && !targets) || !mu || !out || nrhs < 1)
     return fail(s, RS_ERR_ARG, "bad domain evaluation arguments");
   if (s->n <= 0) return fail(s, RS_ERR_STATE, "no geometry");
+  if (s->nprob > 1) return fail(s, RS_ERR_ARG, "domain evaluation of a batch");
   const int nb = (s->nh > 0 && s->cfg.pde != kLaplaceNeumann)
                      ? (s->cfg.pde == kStokes ? 3 * s->nh : s->nh) : 0;
   if (nb > 0 && !alpha) return fail(s, RS_ERR_ARG, "holes need alpha");

@@ -138,8 +138,43 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
 
   compute_neighbors();
   number_levels();
+  roots.assign(1, root);
   pts_ = nullptr;
   return true;
+}
+
+void QuadTree::merge(const std::vector<QuadTree>& parts, const std::vector<int>& dof_offset) {
+  nodes.clear();
+  levels.clear();
+  roots.clear();
+  sd = parts.empty() ? 1 : parts[0].sd;
+  min = 0;
+  max = 0;
+  for (size_t t = 0; t < parts.size(); ++t) {
+    const QuadTree& q = parts[t];
+    const int o = static_cast<int>(nodes.size());
+    auto sh = [o](int id) { return id >= 0 ? id + o : -1; };
+    for (TreeNode nd : q.nodes) {
+      nd.parent = sh(nd.parent);
+      for (int c = 0; c < 4; ++c) nd.children[c] = sh(nd.children[c]);
+      nd.bl = sh(nd.bl);
+      nd.tl = sh(nd.tl);
+      nd.tr = sh(nd.tr);
+      nd.br = sh(nd.br);
+      for (int& nb : nd.neighbors) nb = sh(nb);
+      for (int& d : nd.original) d += dof_offset[t];
+      nd.tree_id = static_cast<int>(t);
+      nodes.push_back(std::move(nd));
+    }
+    if (levels.size() < q.levels.size()) levels.resize(q.levels.size());
+    for (size_t lv = 0; lv < q.levels.size(); ++lv)
+      for (int id : q.levels[lv]) levels[lv].push_back(id + o);
+    roots.push_back(q.root + o);
+    if (t == 0 || q.min < min) min = q.min;
+    if (t == 0 || q.max > max) max = q.max;
+  }
+  root = roots.empty() ? -1 : roots[0];
+  number_levels();
 }
 
 // quadtree.cpp:131-175
@@ -331,6 +366,7 @@ void QuadTree::perturb(const double* old_points, const double* new_points, int n
   }
   while (!levels.empty() && levels.back().empty()) levels.pop_back();
   root = remap(root);
+  roots.assign(1, root);
   nodes.swap(kept);
   marked->swap(kmark);
   compute_neighbors();  // quadtree.cpp:759-797, the same rules as the build

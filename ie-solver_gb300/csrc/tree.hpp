@@ -26,6 +26,7 @@ struct TreeNode {
   double side = 0;
   std::vector<int> neighbors;
   std::vector<int> original;  // DOF indices
+  int tree_id = 0;            // which tree of a forest (batch of boundaries) the box is in
 };
 
 struct QuadTree {
@@ -33,10 +34,16 @@ struct QuadTree {
   std::vector<std::vector<int>> levels;  // node ids per level, reference order
   double min = 0, max = 0;
   int root = -1;
+  std::vector<int> roots;  // every tree's root (a forest holds one tree per boundary)
   int sd = 1;
 
   // points: interleaved (2n). Returns false on empty input.
   bool build(const double* points, int n, int sd, int max_leaf_dofs);
+  // A forest of independent trees, one per boundary of a batch: the parts'
+  // nodes appended in order with their ids shifted, their DOF indices
+  // shifted by dof_offset[t], levels merged by depth (level l holds every
+  // tree's level-l boxes, tree by tree), neighbour lists within each tree.
+  void merge(const std::vector<QuadTree>& parts, const std::vector<int>& dof_offset);
 
   // QuadTree::perturb (quadtree.cpp:435-801) for a boundary whose points
   // moved: old_to_new[p] is the new index of old point p (-1 if it is gone),

@@ -24,6 +24,7 @@ STATUS = {0: "RS_OK", 1: "RS_ERR_ARG", 2: "RS_ERR_STATE", 3: "RS_ERR_CUDA",
 
 # Every function the C ABI exports (include/rskel.h).
 EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_perturb",
+           "rs_set_geometry_batch",
            "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
            "rs_matvec_fast", "rs_domain_eval",
@@ -87,6 +88,7 @@ def lib():
         L.rs_destroy.argtypes = [_vp]
         L.rs_set_geometry.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.rs_perturb.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
+        L.rs_set_geometry_batch.argtypes = [_vp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp]
         L.rs_build_tree.argtypes = [_vp]
         L.rs_factor.argtypes = [_vp]
         L.rs_solve.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp]
@@ -221,6 +223,22 @@ class Solver:
         fn = lib().rs_perturb if perturb else lib().rs_set_geometry
         self._check(fn(self.h, geo.n, _d(arrs[0]), _d(arrs[1]), _d(arrs[2]), _d(arrs[3]),
                        geo.num_holes, _d(hc), _d(hr)))
+
+    def set_geometry_batch(self, geos):
+        """rs_set_geometry_batch: independent boundaries (no holes) in one
+        handle; vectors are the boundaries' vectors concatenated in order."""
+        assert all(g.num_holes == 0 for g in geos)
+        counts = np.array([g.n for g in geos], dtype=np.int32)
+        self.n = int(counts.sum())
+        self.D = self.n * self.sd
+        self.nh = 0
+        self.nb = 0
+        self.batch = counts
+        arrs = [np.ascontiguousarray(np.concatenate([np.asarray(getattr(g, f)).ravel()
+                                                     for g in geos]), dtype=np.float64)
+                for f in ("points", "normals", "weights", "curvatures")]
+        self._check(lib().rs_set_geometry_batch(self.h, len(geos), _i(counts), _d(arrs[0]),
+                                                _d(arrs[1]), _d(arrs[2]), _d(arrs[3])))
 
     def _check(self, rc, h="self"):
         if rc != 0:

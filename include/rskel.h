@@ -98,6 +98,21 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
                           const double* curvatures, int num_holes,
                           const double* hole_centers, const double* hole_radii);
 
+/* A batch of independent boundaries without holes in one handle (no
+ * reference counterpart; the reference solves one boundary per
+ * SkelFactorization).  Boundary t has num_points[t] points; the arrays are
+ * the boundaries' data vectors concatenated in order, and right-hand sides
+ * and solutions are concatenated the same way (column of length
+ * sum(num_points) * sd).  rs_build_tree builds one quadtree per boundary
+ * and merges them into a forest: every tree level of every boundary is
+ * factored in the same launches, and each boundary keeps its own root
+ * block.  Refinement residuals are judged per boundary and column.
+ * Not available for a batch: holes, rs_perturb, rs_matvec (dense),
+ * rs_domain_eval, and RS_FP32_REFINE with other kernels than RS_LAPLACE. */
+rs_status rs_set_geometry_batch(rs_solver* s, int count, const int* num_points,
+                                const double* points, const double* normals,
+                                const double* weights, const double* curvatures);
+
 /* QuadTree::initialize_tree(boundary, {}, sd, 2) (quadtree/quadtree.cpp:39-180).
  * Host-side; needs no GPU. */
 rs_status rs_build_tree(rs_solver* s);
