@@ -363,6 +363,72 @@ def breakdown(st, total_ms):
     return b
 
 
+def other_configs(capi, dist, steps):
+    """The other configurations, measured with inputs resident on the device
+    (each a few steps; not the headline): a batch of 512 random stars in one
+    handle, and Stokes with 16 holes at 262144 DOFs."""
+    from rskel import geometry as g
+
+    out = {}
+    # 512 random stars r = 1 + sum_{k=2..8} a_k cos(k t + phi_k), N ~ U[1024, 16384]
+    rng = np.random.default_rng(4)
+    geos = [g.random_star(int(rng.integers(1024, 16385)), rng) for _ in range(512)]
+    F = np.concatenate([g.laplace_point_source(geo, (2.0 * math.cos(t), 2.0 * math.sin(t)))
+                        for geo, t in zip(geos, rng.uniform(0, 2 * math.pi, 512))])
+    for name, prec in (("fp64", capi.RS_FP64), ("fp32_refine", capi.RS_FP32_REFINE)):
+        s = capi.Solver(geos[0], capi.RS_LAPLACE, TOL, leaf=LEAF, npp=NPP, precision=prec,
+                        refine_tol=REFINE_TOL, device=dist.local)
+        s.set_geometry_batch(geos)
+        s.build_tree()
+        ts = []
+        for i in range(max(2, steps) + 1):
+            s.synchronize()
+            s.timer_start()
+            s.factor()
+            s.solve(F)
+            if i > 0:
+                ts.append(s.timer_stop())
+        st = s.stats()
+        out.setdefault("batch512_random_stars", {
+            "workload": "512 random stars, N~U[1024,16384], tol 1e-8, 1 rhs each",
+            "dofs": int(len(F))})["%s_ms_median" % name] = statistics.median(ts)
+        out["batch512_random_stars"]["%s_dofs_per_s" % name] = len(F) / (statistics.median(ts) * 1e-3)
+        if prec == capi.RS_FP32_REFINE:
+            out["batch512_random_stars"]["refine_residual"] = st["refine_residual"]
+            out["batch512_random_stars"]["kernel_launches_per_step"] = st["kernel_launches"]
+        s.close()
+    # Stokes, unit circle + 16 ellipses, 131072 points
+    geo = g.circle_with_ellipses(131072, 16, np.random.default_rng(3))
+    rng = np.random.default_rng(4)
+    Fs = np.zeros(2 * geo.n)
+    for c in np.asarray(geo.hole_centers).reshape(-1, 2)[:4]:
+        Fs += g.stokeslet_velocity(geo, c, rng.standard_normal(2))
+    Fs += g.stokeslet_velocity(geo, (1.7, 0.4), rng.standard_normal(2))
+    rec = {"workload": "Stokes DLP, unit circle + 16 ellipses, 131072 points, tol 1e-8",
+           "dofs": 2 * geo.n}
+    for name, prec in (("fp64", capi.RS_FP64), ("fp32_refine", capi.RS_FP32_REFINE)):
+        s = capi.Solver(geo, capi.RS_STOKES, TOL, leaf=LEAF, npp=NPP, precision=prec,
+                        refine_tol=REFINE_TOL, device=dist.local)
+        s.build_tree()
+        ts = []
+        for i in range(3 if prec == capi.RS_FP32_REFINE else 2):
+            s.synchronize()
+            s.timer_start()
+            s.factor()
+            s.solve(Fs)
+            if i > 0:
+                ts.append(s.timer_stop())
+        rec["%s_ms_median" % name] = statistics.median(ts)
+        rec["%s_dofs_per_s" % name] = 2 * geo.n / (statistics.median(ts) * 1e-3)
+        if prec == capi.RS_FP32_REFINE:
+            st = s.stats()
+            rec["refine_iters"] = st["refine_iters"]
+            rec["refine_residual"] = st["refine_residual"]
+        s.close()
+    out["stokes_16_ellipses_262144"] = rec
+    return out
+
+
 def run_gpu(args):
     from rskel import capi
 
@@ -457,6 +523,7 @@ def run_gpu(args):
                                    "restatement (OpenMP over boxes, all host cores), median"},
         "clocks": clocks,
         "gpu_launches": launches,
+        "other_configs": other_configs(capi, dist, args.steps) if not args.headline_only else None,
     }
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
@@ -508,6 +575,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the other configurations' timings")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

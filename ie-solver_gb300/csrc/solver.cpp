@@ -1305,12 +1305,15 @@ int auto_fmm_order(double refine_tol, int pde) {
   const int p = (int)std::ceil((-std::log10(want) - 2.1) / 0.36) + (pde == kStokes ? 4 : 0);
   return std::min(48, std::max(12, p));
 }
-// Relative error of the FP32 product (order kFmmOrder32) on rough vectors,
-// with a factor 2 of margin over what it measures (65536-point star,
-// Laplace: 1.5e-8; 131072 points with 16 holes, Stokes: 7.8e-8).  The
-// refinement takes the FP32 product of a correction only while this times
-// the previous residual stays below half the refinement tolerance.
-double fmm32_error(int pde) { return pde == kStokes ? 1.6e-7 : 3e-8; }
+// Error of the FP32 product (order kFmmOrder32) of a refinement correction,
+// relative to |mu|/|f| times the residual the correction came from, with a
+// margin over what refinement runs show: Laplace (65536-point star) 1.4e-8
+// -> 6e-8; Stokes (131072 points, 16 holes) 4.7e-7 -> 8e-7.  (On test
+// vectors the products measure 1.5e-8 rough / 1.4e-7 smooth for Laplace,
+// 7.8e-8 / 3.9e-7 for Stokes.)  The refinement takes the FP32 product of a
+// correction only while this bound stays below half the tolerance, and
+// sums the bounds.
+double fmm32_error(int pde) { return pde == kStokes ? 8e-7 : 6e-8; }
 // Relative residual the inner GMRES of GMRES-IR aims for (its FP32
 // products and preconditioner are good to about 1e-7).
 constexpr double kGmresInnerTol = 1e-6;
@@ -1568,7 +1571,10 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   double worst = 0, prev = 1.0;
   const int max_it = std::max(1, s->cfg.refine_max_iters);
   const bool recur = s->fmm.built;
-  const double eps32 = fmm32_error(s->cfg.pde);
+  // FP32 product error relative to the residual a correction came from: the
+  // product's own error times |delta| / |r|, which is about |mu| / |f| (set
+  // after the first step)
+  double eps32 = fmm32_error(s->cfg.pde);
   if (recur) {
     CU(s->x64.ensure(nd));
     CU(s->xa64.ensure(std::max<size_t>((size_t)nb * nrhs, 1)));
@@ -1598,6 +1604,7 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   // the stationary iteration contracts by less than a factor 10)
   bool krylov = s->cfg.refine_solver == 2;
   int ksteps = 0;
+  double rec_err = 0;  // bound on the recurrence's accumulated error (FP32 products)
   const size_t kbl = nd + (size_t)nb * nrhs;
   if (nb) CU(cudaMemsetAsync(rg, 0, (size_t)nb * nrhs * 8, s->stream));
   for (it = 0; it < max_it; ++it) {
@@ -1634,6 +1641,7 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
           launch_axpby(a64, s->xa64.p, 1.0, 1.0, (size_t)nb * nrhs, s->stream);
         }
         s->launches += 4;
+        rec_err += eps32 * prev;
         RSCHK(residual_update(s, s->x64.p, s->xa64.p, nrhs, s->r64.p, rg, s->g64.p));
         RSCHK(measure(&s->stats.residual32_ms));
       } else {
@@ -1648,17 +1656,19 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
     if (s->trace)
       std::fprintf(stderr, "[rskel] refine %d: %s, %s residual %.3e\n", it,
                    krylov ? "GMRES" : "stationary", upd ? "recurrence" : "fresh", worst);
-    if (it == 0 && recur && s->cfg.fmm_order == 0) {
-      // The residual's multipole error scales with |mu| while the tolerance
-      // is relative to |f|: on an ill-conditioned system (|mu| >> |f|) the
-      // float-float product needs more terms.
+    if (it == 0 && recur) {
+      // The multipole errors scale with |mu| while the tolerance is relative
+      // to |f|: on an ill-conditioned system (|mu| >> |f|) the float-float
+      // product needs more terms and FP32 products of corrections count for
+      // more.
       launch_norms(mu);
       CU(cudaMemcpyAsync(s->h_io.p, s->nrm_dev.p, ncol * 8, cudaMemcpyDeviceToHost, s->stream));
       CU(cudaStreamSynchronize(s->stream));
       double amp = 0;
       for (int c = 0; c < ncol; ++c) amp = std::max(amp, fn[c] > 0 ? s->h_io.p[c] / fn[c] : 0.0);
+      eps32 *= std::max(amp, 1.0);
       const int want = auto_fmm_order(s->cfg.refine_tol / std::max(amp, 1.0), s->cfg.pde);
-      if (amp > 4.0 && want > s->fmm.p) {
+      if (s->cfg.fmm_order == 0 && amp > 4.0 && want > s->fmm.p) {
         if (!fmm_set_order(s->fmm, want)) return fail(s, RS_ERR_CUDA, "multipole order update failed");
         if (s->trace)
           std::fprintf(stderr, "[rskel] |mu|/|f| = %.1f: multipole order %d\n", amp, want);
@@ -1666,10 +1676,14 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
         prev = worst;
       }
     }
-    if (worst <= s->cfg.refine_tol && upd && s->cfg.refine_verify) {
-      // the recurrence says converged: confirm with a fresh residual
+    if (worst <= s->cfg.refine_tol && upd &&
+        (s->cfg.refine_verify == 2 ||
+         (s->cfg.refine_verify == 1 && worst + rec_err > s->cfg.refine_tol))) {
+      // the recurrence says converged, but its error bound does not settle
+      // it (or confirmation is always asked for): confirm with a fresh residual
       RSCHK(fresh());
       prev = worst;
+      rec_err = 0;
     }
     if (worst <= s->cfg.refine_tol) { ++it; break; }
     if (!krylov && s->cfg.refine_solver == 0 && recur && it >= 1 && worst > 0.1 * before) {
@@ -1677,6 +1691,7 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
       if (upd) {  // GMRES works on the true residual
         RSCHK(fresh());
         prev = worst;
+        rec_err = 0;
       }
     }
   }

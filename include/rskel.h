@@ -66,10 +66,13 @@ typedef struct {
                                 ell = ceil(rank_headroom * k_pred) + rank_extra_rows,
                                 default 1.25 and 12 */
   int rank_extra_rows;
-  int refine_verify;         /* RS_FP32_REFINE: 1 (default) = convergence of the residual
-                                recurrence (FP32 products of corrections) is confirmed by a
-                                fresh float-float residual, and refinement goes on while
-                                that is above refine_tol; 0 = trust the recurrence */
+  int refine_verify;         /* RS_FP32_REFINE: convergence of the residual recurrence
+                                (FP32 products of corrections) is confirmed by a fresh
+                                float-float residual, refinement going on while that is
+                                above refine_tol: 1 (default) = when the recurrence's error
+                                bound (the FP32 products' error times the residuals they
+                                multiplied, summed) could take it above refine_tol;
+                                2 = always; 0 = never */
   int refine_solver;         /* RS_FP32_REFINE correction equation: 0 (default) = one
                                 application of the FP32 factorization per step, switching to
                                 GMRES-IR when a step cuts the residual by less than 10x;
