@@ -149,6 +149,18 @@ struct rs_solver {
   std::vector<float> samp_feat, samp_target;
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
+  // CUDA graph of the factorization's inverse (no holes): the level sweeps
+  // and the root solves, captured on first use for a (buffer, columns,
+  // precision) and replayed; dropped at every factorization.
+  struct InvGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* x = nullptr;
+    int nrhs = 0;
+    int fp32 = 0;
+    int kernels = 0;
+  };
+  InvGraph inv_graph;
+
   rs_stats stats;
   int launches = 0;
   bool trace = false;  // RSKEL_TRACE=1: per-level timing on stderr
@@ -1252,9 +1264,55 @@ rs_status solve_border_col(rs_solver* s, Real* x, Real* alpha, const double* g) 
 // Applies the factorization inverse in place to x (device, Real, D x nrhs);
 // alpha (device, Real, nb x nrhs) for bordered systems; g (device, double,
 // nb x nrhs) is the second-block right-hand side (null = 0).
+void drop_inverse_graph(rs_solver* s) {
+  if (s->inv_graph.exec) cudaGraphExecDestroy(s->inv_graph.exec);
+  s->inv_graph = rs_solver::InvGraph();
+}
+
+template <class Real>
+rs_status apply_inverse(rs_solver* s, Real* x, int nrhs, Real* alpha, const double* g);
+
+// The inverse without holes as one CUDA graph launch (cfg.use_graphs): the
+// first call for a buffer and column count captures the launches into a
+// graph, later calls replay it.
+template <class Real>
+rs_status apply_inverse_graph(rs_solver* s, Real* x, int nrhs) {
+  rs_solver::InvGraph& G = s->inv_graph;
+  const int fp32 = sizeof(Real) == 4;
+  if (!(G.exec && G.x == x && G.nrhs == nrhs && G.fp32 == fp32)) {
+    drop_inverse_graph(s);
+    const int before = s->launches;
+    CU(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    rs_status rc = apply_inverse<Real>(s, x, nrhs, nullptr, nullptr);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+    if (rc != RS_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CU(e);
+    const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CU(ei);
+    G.x = x;
+    G.nrhs = nrhs;
+    G.fp32 = fp32;
+    G.kernels = s->launches - before;
+    s->launches = before;
+  }
+  CU(cudaGraphLaunch(G.exec, s->stream));
+  s->launches += G.kernels;
+  return RS_OK;
+}
+
 template <class Real>
 rs_status apply_inverse(rs_solver* s, Real* x, int nrhs, Real* alpha, const double* g) {
   Factor<Real>& F = factor_of<Real>(s);
+  if (s->nb == 0 && s->cfg.use_graphs && !s->trace) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(s->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) return apply_inverse_graph<Real>(s, x, nrhs);
+  }
   if (s->nb == 0) {
     sweep_levels<Real>(s, x, s->D, nrhs, kUpSolve, true);
     if (!s->roots_h.empty()) {
@@ -1734,6 +1792,7 @@ void rs_config_default(rs_config* c) {
   c->rank_extra_rows = 12;
   c->refine_verify = 1;
   c->refine_solver = 0;
+  c->use_graphs = 1;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -1767,6 +1826,7 @@ rs_status rs_destroy(rs_solver* s) {
   if (s->dev_ready) {
     cudaSetDevice(s->cfg.device);
     cudaStreamSynchronize(s->stream);
+    drop_inverse_graph(s);
     cudaEventDestroy(s->ev_t0);
     cudaEventDestroy(s->ev_t1);
     cudaEventDestroy(s->ev_a);
@@ -1811,6 +1871,7 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
   s->factored = false;
   s->geo_on_dev = false;
   s->fmm.built = false;
+  if (s->dev_ready) drop_inverse_graph(s);
   return RS_OK;
 }
 
@@ -2029,6 +2090,7 @@ rs_status rs_factor(rs_solver* s) {
     if (rc != RS_OK) return rc;
   }
   double t0 = now_ms();
+  drop_inverse_graph(s);
   CU(cudaEventRecord(s->ev_f0, s->stream));
   s->factored = false;
   rc = s->fp32 ? factor_impl<float>(s) : factor_impl<double>(s);

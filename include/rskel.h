@@ -79,6 +79,9 @@ typedef struct {
                                 1 = always the former; 2 = always GMRES-IR (flexible GMRES
                                 preconditioned by the FP32 factorization, FP32 multipole
                                 products, up to 31 steps per refinement step) */
+  int use_graphs;            /* 1 (default): the factorization's inverse (no holes) runs as
+                                one CUDA graph launch, captured on first use after each
+                                rs_factor; 0: plain launches */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
