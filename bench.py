@@ -274,9 +274,11 @@ def train_rank_model(capi, device):
     return w, info
 
 
-def time_arm(capi, geo, F, precision, steps, warmup, cu, dist, model=None):
+def time_arm(capi, geo, F, precision, steps, warmup, cu, dist, model=None, tune=None):
     s = make_solver(capi, geo, precision, dist.local, model)
     s.build_tree()
+    if tune is not None:  # launch shapes from the autotuner, untimed
+        tune["split_min_tasks"], tune["wide_ctas_per_sm"] = s.autotune(reps=3)
     d_f = cu.malloc(F.nbytes)
     d_mu = cu.malloc(F.nbytes)
     cu.memcpy_htod(d_f, F)
@@ -444,8 +446,9 @@ def run_gpu(args):
                                         args.warmup, cu, dist)
     clk = ClockSampler(dist.local)
     clk.start()
+    tuned = {}
     t32, st32, mu32, l32 = time_arm(capi, geo, F, capi.RS_FP32_REFINE, args.steps, args.warmup,
-                                    cu, dist, model)
+                                    cu, dist, model, tune=tuned)
     clocks = clk.stop()
     # accuracy against the oracle (CPU): at the configuration's tolerance and
     # at 1e-12 (the exact discrete solution to ~1e-12)
@@ -500,6 +503,7 @@ def run_gpu(args):
             "ms_per_step": dist.max(max(t32p)), "ms_median": statistics.median(t32p),
             "breakdown_ms": breakdown(st32p[-1], statistics.median(t32p)),
             "sketch_rows": st32p[-1]["sketch_rows"]},
+        "autotuned": tuned,
         "rank_model": dict(train_info, boxes_predicted=st32[-1]["rank_predicted"],
                            boxes_redone=st32[-1]["rank_redo"],
                            sketch_rows=st32[-1]["sketch_rows"],

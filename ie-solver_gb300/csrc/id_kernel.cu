@@ -1101,7 +1101,6 @@ bool id_sketch_ok(int nmax) {
   return nmax <= 128 && id_sketch_smem(nmax) <= 227 * 1024;
 }
 
-constexpr int kSplitMinTasks = 512;
 
 // All tasks of one launch use the team size of its largest box.  Returns
 // the number of kernels launched.
@@ -1113,7 +1112,7 @@ int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32
   // The warp-per-box QR pays off when a level has boxes enough to fill the
   // GPU; small levels keep the lower-latency CTA-per-box QR.
   if (fp32 && p.dense == nullptr && id_sketch_ok(nmax) && p.sketch_y != nullptr &&
-      num_tasks >= kSplitMinTasks) {
+      num_tasks >= (p.split_min_tasks > 0 ? p.split_min_tasks : 512)) {
     if (ts == 4) launch_split_t<4>(p, num_tasks, nmax, st);
     else launch_split_t<2>(p, num_tasks, nmax, st);
     return 2 * passes;

@@ -32,6 +32,9 @@ struct IdParams {
   // learned sizes in this launch.
   int* redo;
   int redo_pass;
+  // FP32 sketched ID: levels of at least this many boxes run the pivoted QR
+  // one warp per box (id_cpqr_warp_kernel), smaller ones one CTA per box
+  int split_min_tasks;
 };
 
 struct DecoupleParams {

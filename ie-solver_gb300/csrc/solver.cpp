@@ -78,6 +78,11 @@ struct rs_solver {
 
   bool dev_ready = false;
   int num_sms = 152;  // of the handle's device; sizes the wide ID's work split
+  // launch shapes the autotuner (rs_autotune) picks: the level size from
+  // which the FP32 sketched ID's pivoted QR runs one warp per box, and the
+  // wide ID's CTAs per SM
+  int split_min_tasks = 512;
+  int wide_ctas_per_sm = 2;
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;  // read-back of ranks while eliminations run
   cudaEvent_t ev_c = nullptr;
@@ -695,7 +700,8 @@ rs_status factor_impl(rs_solver* s) {
         const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
         if (m > id_sketch_rows(t.n)) blocks += (t.n + kWideCols - 1) / kWideCols;
       }
-      const int want = blocks > 0 ? (2 * s->num_sms + blocks - 1) / blocks : 1;
+      const int want =
+          blocks > 0 ? (s->wide_ctas_per_sm * s->num_sms + blocks - 1) / blocks : 1;
       for (size_t i = w0; i < w1; ++i) {
         IdTask& t = idt_s[i];
         const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0), ell = id_sketch_rows(t.n);
@@ -809,6 +815,7 @@ rs_status factor_impl(rs_solver* s) {
     ip.sketch_y = y_need ? s->sketch_y.p : nullptr;
     ip.redo = learned && !idt_s.empty() ? s->redo.p : nullptr;
     ip.redo_pass = 0;
+    ip.split_min_tasks = s->split_min_tasks;
     ip.phase_clk = nullptr;
     if (s->trace) {
       CU(s->clk.ensure(4 * std::max<size_t>(idt.size(), 1)));
@@ -2382,6 +2389,53 @@ rs_status rs_get_stats(const rs_solver* s, rs_stats* out) {
   out->host_post_ms = s->host_post_ms;
   out->residual64_ms = s->stats.residual64_ms;
   out->residual32_ms = s->stats.residual32_ms;
+  return RS_OK;
+}
+
+rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm) {
+  if (!s || reps < 1) return RS_ERR_ARG;
+  // each candidate: the median device time of `reps` factorizations of the
+  // handle's geometry; one knob at a time, the other at its current value
+  auto time_factor = [&](double* ms) -> rs_status {
+    std::vector<double> t;
+    for (int r = 0; r < reps; ++r) {
+      rs_status rc = rs_factor(s);
+      if (rc != RS_OK) return rc;
+      t.push_back(s->stats.dev_factor_ms);
+    }
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return RS_OK;
+  };
+  rs_status rc = rs_factor(s);  // warm-up (plans, buffers, first launches)
+  if (rc != RS_OK) return rc;
+  double best = 1e300;
+  int best_split = s->split_min_tasks;
+  for (int cand : {128, 256, 512, 1024, 1 << 30}) {
+    s->split_min_tasks = cand;
+    double ms = 0;
+    RSCHK(time_factor(&ms));
+    if (ms < best) {
+      best = ms;
+      best_split = cand;
+    }
+  }
+  s->split_min_tasks = best_split;
+  best = 1e300;
+  int best_wide = s->wide_ctas_per_sm;
+  for (int cand : {1, 2, 4}) {
+    s->wide_ctas_per_sm = cand;
+    double ms = 0;
+    RSCHK(time_factor(&ms));
+    if (ms < best) {
+      best = ms;
+      best_wide = cand;
+    }
+  }
+  s->wide_ctas_per_sm = best_wide;
+  s->factored = false;  // the last candidate's factors are not the chosen shape's
+  if (split_min_tasks) *split_min_tasks = s->split_min_tasks;
+  if (wide_ctas_per_sm) *wide_ctas_per_sm = s->wide_ctas_per_sm;
   return RS_OK;
 }
 

@@ -24,7 +24,7 @@ STATUS = {0: "RS_OK", 1: "RS_ERR_ARG", 2: "RS_ERR_STATE", 3: "RS_ERR_CUDA",
 
 # Every function the C ABI exports (include/rskel.h).
 EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "rs_perturb",
-           "rs_set_geometry_batch",
+           "rs_set_geometry_batch", "rs_autotune",
            "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
            "rs_matvec_fast", "rs_domain_eval",
@@ -89,6 +89,7 @@ def lib():
         L.rs_set_geometry.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.rs_perturb.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.rs_set_geometry_batch.argtypes = [_vp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp]
+        L.rs_autotune.argtypes = [_vp, ctypes.c_int, _ip, _ip]
         L.rs_build_tree.argtypes = [_vp]
         L.rs_factor.argtypes = [_vp]
         L.rs_solve.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp]
@@ -240,6 +241,12 @@ class Solver:
                 for f in ("points", "normals", "weights", "curvatures")]
         self._check(lib().rs_set_geometry_batch(self.h, len(geos), _i(counts), _d(arrs[0]),
                                                 _d(arrs[1]), _d(arrs[2]), _d(arrs[3])))
+
+    def autotune(self, reps=3):
+        """rs_autotune: returns (split_min_tasks, wide_ctas_per_sm) chosen."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(lib().rs_autotune(self.h, reps, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def _check(self, rc, h="self"):
         if rc != 0:

@@ -251,6 +251,17 @@ rs_status rs_rank_predict(rs_solver* s, const float* weights, const float* featu
 rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* features,
                            const float* targets, int count, float* grad, float* loss);
 
+/* Autotuner (no reference counterpart): times factorizations of the
+ * handle's current geometry over the launch shapes that depend on the
+ * problem and keeps the fastest for this handle's later factorizations:
+ * the level size from which the FP32 sketched ID's pivoted QR runs one
+ * warp per box instead of one CTA per box (128, 256, 512 (default), 1024,
+ * never), then the wide ID's CTAs per SM (1, 2 (default), 4).  Each
+ * candidate is the median of `reps` factorizations.  The choices are
+ * returned (pointers may be NULL).  The handle must be factored again
+ * before solving. */
+rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm);
+
 /* --- introspection (tree and factorization), for tests and tooling --- */
 typedef struct {
   int num_levels, num_nodes, num_compressed, num_skel_root;
