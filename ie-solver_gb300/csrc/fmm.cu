@@ -645,21 +645,44 @@ __global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo
         const int ic = dcnt - i0 < kStage ? dcnt - i0 : kStage;
         __syncthreads();
         for (int e = threadIdx.x; e < ic; e += blockDim.x) sp[e] = pt_pos(a, d0 + i0 + e);
-        for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
-          const int i = e % ic, q = e / ic;
-          const size_t src = d0 + i0 + i + (size_t)a.npts * q;
-          sc[2 * (i + kStage * q)] = a.charge[2 * src];
-          sc[2 * (i + kStage * q) + 1] = a.charge[2 * src + 1];
+        // Laplace: a charge is b_j mu_j with b_j = -(w_j / 2pi) nu_j, so the
+        // pair term Re(b_j / tau) is formed once and scaled per right-hand
+        // side; staged as b (kStage complex) then the densities (kStage x
+        // nrhs).  Neumann: real charges.
+        R* sb = sc;
+        R* sdn = sc + 2 * kStage;
+        if (a.mode == 0) {
+          for (int e = threadIdx.x; e < ic; e += blockDim.x) {
+            const int pt = a.slot_pt[d0 + i0 + e];
+            const double f = -g.w[pt] * (1.0 / (2.0 * CUDART_PI));
+            sb[2 * e] = to_r<R>(f * g.nx[pt]);
+            sb[2 * e + 1] = to_r<R>(f * g.ny[pt]);
+          }
+          for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
+            const int i = e % ic, q = e / ic;
+            sdn[i + kStage * q] = to_r<R>(mu[a.slot_pt[d0 + i0 + i] + (size_t)a.npts * q]);
+          }
+        } else {
+          for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
+            const int i = e % ic, q = e / ic;
+            sc[i + kStage * q] = a.charge[2 * (d0 + i0 + i + (size_t)a.npts * q)];
+          }
         }
         __syncthreads();
         if (act) {
           for (int i = part; i < ic; i += nsplit) {
             if (d0 + i0 + i == s0 + j) continue;  // self
             const Cx<R> iv = cmul(tnu, cinv(diff(tp, sp[i], offD)));
+            if (a.mode == 0) {
+              const R t = sb[2 * i] * iv.re - sb[2 * i + 1] * iv.im;
 #pragma unroll
-            for (int q = 0; q < kMaxRhs; ++q)
-              if (q < nrhs)
-                phi[q] += sc[2 * (i + kStage * q)] * iv.re - sc[2 * (i + kStage * q) + 1] * iv.im;
+              for (int q = 0; q < kMaxRhs; ++q)
+                if (q < nrhs) phi[q] += sdn[i + kStage * q] * t;
+            } else {
+#pragma unroll
+              for (int q = 0; q < kMaxRhs; ++q)
+                if (q < nrhs) phi[q] += sc[i + kStage * q] * iv.re;
+            }
           }
         }
       }
