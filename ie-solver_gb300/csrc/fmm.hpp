@@ -70,7 +70,24 @@ struct FmmPlan {
   DevBuf<double> charge;       // 2 * (slot + npts * rhs)
   DevBuf<double> mpole, local; // 2 * (k + p * (rhs + nrhs * box))
   DevBuf<double> r1;           // per right-hand side: the rank-one sums (Neumann, Stokes)
+  HostBuf<unsigned char> stage;  // pinned staging of the plan's uploads
 };
+
+// The plan's host side: lists, slot order and leaf-relative coordinates,
+// built from the tree without touching the GPU (so that it can run on a
+// host thread while the factorization runs), then uploaded.
+struct FmmHostPlan {
+  bool ok = false;
+  int p = 0, p32 = 0, nbox = 0, npts = 0, nlevels = 0;
+  std::vector<double> cx, cy, side, rx, ry;
+  std::vector<float> rxh, rxl, ryh, ryl, binom32;
+  std::vector<int> pstart, pcount, parent, children, slot_pt, vo, vi, wo, wi, xo, xi, uo, ui,
+      lvl_flat, level_off, leaves_h, m2l_boxes_h;
+  size_t v_pairs = 0, u_pairs = 0, w_pairs = 0, x_pairs = 0;
+};
+bool fmm_plan_host(FmmHostPlan& h, const QuadTree& tree, const double* points, int npts, int p,
+                   int p32);
+bool fmm_plan_upload(FmmPlan& f, FmmHostPlan& h, cudaStream_t st);
 
 // Builds the lists on the host from the tree (points interleaved, sd = 1).
 // Orders 2..64 are supported for both variants.
@@ -87,7 +104,7 @@ cudaError_t fmm_apply(FmmPlan& f, int pde, const Geo<double>& geo, const double*
                       double* y, double ya, double yb, int arith, cudaStream_t st);
 // Sets the order of the FP64 and float-float variants (2..64; the plan's
 // lists do not depend on it).  Synchronous: call between products.
-bool fmm_set_order(FmmPlan& f, int p);
+bool fmm_set_order(FmmPlan& f, int p, cudaStream_t st);
 // Kernels one fmm_apply launches.
 int fmm_launches(const FmmPlan& f, int pde, int nrhs);
 

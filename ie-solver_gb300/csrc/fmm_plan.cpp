@@ -14,6 +14,7 @@
 // including its `y < top && y < bottom` condition (quadtree.cpp:209), so the
 // FMM recomputes adjacency from the box geometry instead.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
@@ -32,13 +33,33 @@ bool touch(const Box& a, const Box& b, double eps) {
          b.y0 <= a.y0 + a.s + eps;
 }
 
-template <class T>
-cudaError_t upload(DevBuf<T>& d, const std::vector<T>& h) {
-  cudaError_t e = d.ensure(std::max<size_t>(h.size(), 1));
-  if (e != cudaSuccess) return e;
-  if (h.empty()) return cudaSuccess;
-  return cudaMemcpy(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
-}
+// Plan arrays go to the device through the plan's pinned staging buffer
+// (asynchronous copies on the plan's stream; the build synchronises once
+// at its end, before the buffer can be written again).
+struct Uploader {
+  FmmPlan& f;
+  cudaStream_t st;
+  size_t used = 0;
+  cudaError_t err = cudaSuccess;
+  template <class T>
+  bool operator()(DevBuf<T>& d, const std::vector<T>& h) {
+    if (err != cudaSuccess) return false;
+    if ((err = d.ensure(std::max<size_t>(h.size(), 1))) != cudaSuccess) return false;
+    if (h.empty()) return true;
+    const size_t bytes = h.size() * sizeof(T), off = (used + 255) & ~size_t(255);
+    if (off + bytes > f.stage.cap) {  // full: wait for the copies in flight, start over
+      if ((err = cudaStreamSynchronize(st)) != cudaSuccess) return false;
+      if ((err = f.stage.ensure(std::max<size_t>(2 * f.stage.cap, bytes + 4096))) != cudaSuccess)
+        return false;
+      used = 0;
+      return (*this)(d, h);
+    }
+    std::memcpy(f.stage.p + off, h.data(), bytes);
+    used = off + bytes;
+    err = cudaMemcpyAsync(d.p, f.stage.p + off, bytes, cudaMemcpyHostToDevice, st);
+    return err == cudaSuccess;
+  }
+};
 
 void csr(const std::vector<std::vector<int>>& lists, std::vector<int>* off, std::vector<int>* idx) {
   off->assign(lists.size() + 1, 0);
@@ -62,7 +83,7 @@ void pascal(int P2, std::vector<double>* t) {
 
 }  // namespace
 
-bool fmm_set_order(FmmPlan& f, int p) {
+bool fmm_set_order(FmmPlan& f, int p, cudaStream_t st) {
   if (p < 2 || p > 64) return false;
   std::vector<double> binom;
   pascal(2 * p, &binom);
@@ -71,17 +92,19 @@ bool fmm_set_order(FmmPlan& f, int p) {
     binom_df[2 * i] = (float)binom[i];
     binom_df[2 * i + 1] = (float)(binom[i] - (double)binom_df[2 * i]);
   }
-  if (upload(f.binom, binom) != cudaSuccess || upload(f.binom_df, binom_df) != cudaSuccess)
-    return false;
+  Uploader up{f, st};
+  if (!up(f.binom, binom) || !up(f.binom_df, binom_df)) return false;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return false;
   f.p = p;
   return true;
 }
 
-bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p, int p32,
-               cudaStream_t st) {
-  (void)st;
+bool fmm_plan_host(FmmHostPlan& f, const QuadTree& tree, const double* points, int npts, int p,
+                   int p32) {
+  f.ok = false;
   if (p < 2 || p > 64 || p32 < 2 || p32 > 64 || npts <= 0) return false;
   const int nb = (int)tree.nodes.size();
+  f.p = p;
   f.p32 = p32;
   f.nbox = nb;
   f.npts = npts;
@@ -214,24 +237,66 @@ bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts,
   f.u_pairs = ui.size();
   std::vector<double> b32d;
   pascal(2 * p32, &b32d);
-  std::vector<float> binom32(b32d.begin(), b32d.end());
-  bool ok = fmm_set_order(f, p) && upload(f.cx, cx) == cudaSuccess && upload(f.cy, cy) == cudaSuccess &&
-            upload(f.side, side) == cudaSuccess && upload(f.pstart, pstart) == cudaSuccess &&
-            upload(f.pcount, pcount) == cudaSuccess && upload(f.parent, parent) == cudaSuccess &&
-            upload(f.children, children) == cudaSuccess &&
-            upload(f.slot_pt, slot_pt) == cudaSuccess && upload(f.rx, rx) == cudaSuccess &&
-            upload(f.ry, ry) == cudaSuccess && upload(f.rxh, rxh) == cudaSuccess &&
-            upload(f.rxl, rxl) == cudaSuccess && upload(f.ryh, ryh) == cudaSuccess &&
-            upload(f.ryl, ryl) == cudaSuccess && upload(f.v_off, vo) == cudaSuccess &&
-            upload(f.v_idx, vi) == cudaSuccess && upload(f.w_off, wo) == cudaSuccess &&
-            upload(f.w_idx, wi) == cudaSuccess && upload(f.x_off, xo) == cudaSuccess &&
-            upload(f.x_idx, xi) == cudaSuccess && upload(f.u_off, uo) == cudaSuccess &&
-            upload(f.u_idx, ui) == cudaSuccess && upload(f.lvl_boxes, lvl_flat) == cudaSuccess &&
-            upload(f.leaves, f.leaves_h) == cudaSuccess &&
-            upload(f.m2l_boxes, f.m2l_boxes_h) == cudaSuccess &&
-            upload(f.binom32, binom32) == cudaSuccess;
+  f.binom32.assign(b32d.begin(), b32d.end());
+  f.cx.swap(cx);
+  f.cy.swap(cy);
+  f.side.swap(side);
+  f.pstart.swap(pstart);
+  f.pcount.swap(pcount);
+  f.parent.swap(parent);
+  f.children.swap(children);
+  f.slot_pt.swap(slot_pt);
+  f.rx.swap(rx);
+  f.ry.swap(ry);
+  f.rxh.swap(rxh);
+  f.rxl.swap(rxl);
+  f.ryh.swap(ryh);
+  f.ryl.swap(ryl);
+  f.vo.swap(vo);
+  f.vi.swap(vi);
+  f.wo.swap(wo);
+  f.wi.swap(wi);
+  f.xo.swap(xo);
+  f.xi.swap(xi);
+  f.uo.swap(uo);
+  f.ui.swap(ui);
+  f.lvl_flat.swap(lvl_flat);
+  f.ok = true;
+  return true;
+}
+
+bool fmm_plan_upload(FmmPlan& f, FmmHostPlan& h, cudaStream_t st) {
+  f.built = false;
+  if (!h.ok) return false;
+  f.p32 = h.p32;
+  f.nbox = h.nbox;
+  f.npts = h.npts;
+  f.nlevels = h.nlevels;
+  f.level_off = h.level_off;
+  f.leaves_h = h.leaves_h;
+  f.m2l_boxes_h = h.m2l_boxes_h;
+  f.v_pairs = h.v_pairs;
+  f.w_pairs = h.w_pairs;
+  f.x_pairs = h.x_pairs;
+  f.u_pairs = h.u_pairs;
+  Uploader up{f, st};
+  bool ok = up(f.cx, h.cx) && up(f.cy, h.cy) && up(f.side, h.side) && up(f.pstart, h.pstart) &&
+            up(f.pcount, h.pcount) && up(f.parent, h.parent) && up(f.children, h.children) &&
+            up(f.slot_pt, h.slot_pt) && up(f.rx, h.rx) && up(f.ry, h.ry) && up(f.rxh, h.rxh) &&
+            up(f.rxl, h.rxl) && up(f.ryh, h.ryh) && up(f.ryl, h.ryl) && up(f.v_off, h.vo) &&
+            up(f.v_idx, h.vi) && up(f.w_off, h.wo) && up(f.w_idx, h.wi) && up(f.x_off, h.xo) &&
+            up(f.x_idx, h.xi) && up(f.u_off, h.uo) && up(f.u_idx, h.ui) &&
+            up(f.lvl_boxes, h.lvl_flat) && up(f.leaves, h.leaves_h) &&
+            up(f.m2l_boxes, h.m2l_boxes_h) && up(f.binom32, h.binom32) &&
+            cudaStreamSynchronize(st) == cudaSuccess && fmm_set_order(f, h.p, st);
   f.built = ok;
   return ok;
+}
+
+bool fmm_build(FmmPlan& f, const QuadTree& tree, const double* points, int npts, int p, int p32,
+               cudaStream_t st) {
+  FmmHostPlan h;
+  return fmm_plan_host(h, tree, points, npts, p, p32) && fmm_plan_upload(f, h, st);
 }
 
 }  // namespace rskel

@@ -20,7 +20,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <omp.h>
+
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -138,6 +141,7 @@ struct rs_solver {
 
   FmmPlan fmm;
   HostBuf<unsigned char> stage;  // pinned staging of a factorization's host-to-device uploads
+  HostBuf<double> geo_stage;     // pinned staging of the boundary data (upload_geometry)
   size_t stage_used = 0;
   bool incremental = false;      // next rs_factor keeps the boxes rs_perturb left compressed
   size_t full_fac_used = 0;      // factor storage of the last full factorization
@@ -218,40 +222,37 @@ rs_status ensure_device(rs_solver* s) {
   return RS_OK;
 }
 
+// The boundary data as six device arrays (x, y, n_x, n_y, w, kappa) and the
+// proxy-circle directions (kernel.cpp:432-441), gathered in a pinned buffer
+// and sent with one asynchronous copy each on the handle's stream.
 rs_status upload_geometry(rs_solver* s) {
   if (s->geo_on_dev) return RS_OK;
-  const int n = s->n;
-  std::vector<double> x(n), y(n), nx(n), ny(n);
+  const int n = s->n, npp = s->cfg.num_proxy_points;
+  CU(s->geo_stage.ensure(6 * (size_t)n + 2 * (size_t)npp));
+  double* h = s->geo_stage.p;
   for (int i = 0; i < n; ++i) {
-    x[i] = s->pts[2 * i];
-    y[i] = s->pts[2 * i + 1];
-    nx[i] = s->nrm[2 * i];
-    ny[i] = s->nrm[2 * i + 1];
+    h[i] = s->pts[2 * i];
+    h[n + i] = s->pts[2 * i + 1];
+    h[2 * n + i] = s->nrm[2 * i];
+    h[3 * n + i] = s->nrm[2 * i + 1];
   }
-  CU(s->gx.ensure(n));
-  CU(s->gy.ensure(n));
-  CU(s->gnx.ensure(n));
-  CU(s->gny.ensure(n));
-  CU(s->gw.ensure(n));
-  CU(s->gk.ensure(n));
-  CU(cudaMemcpy(s->gx.p, x.data(), n * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(s->gy.p, y.data(), n * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(s->gnx.p, nx.data(), n * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(s->gny.p, ny.data(), n * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(s->gw.p, s->w.data(), n * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(s->gk.p, s->kap.data(), n * 8, cudaMemcpyHostToDevice));
-  // proxy circle directions, kernel.cpp:432-441
-  const int npp = s->cfg.num_proxy_points;
-  std::vector<double> c(npp), sn(npp);
+  std::memcpy(h + 4 * (size_t)n, s->w.data(), n * 8);
+  std::memcpy(h + 5 * (size_t)n, s->kap.data(), n * 8);
   for (int i = 0; i < npp; ++i) {
-    double ang = 2 * M_PI * i * (1.0 / npp);
-    c[i] = std::cos(ang);
-    sn[i] = std::sin(ang);
+    const double ang = 2 * M_PI * i * (1.0 / npp);
+    h[6 * (size_t)n + i] = std::cos(ang);
+    h[6 * (size_t)n + npp + i] = std::sin(ang);
+  }
+  DevBuf<double>* dst[6] = {&s->gx, &s->gy, &s->gnx, &s->gny, &s->gw, &s->gk};
+  for (int a = 0; a < 6; ++a) {
+    CU(dst[a]->ensure(n));
+    CU(cudaMemcpyAsync(dst[a]->p, h + (size_t)a * n, n * 8, cudaMemcpyHostToDevice, s->stream));
   }
   CU(s->pxy_c.ensure(npp));
   CU(s->pxy_s.ensure(npp));
-  CU(cudaMemcpy(s->pxy_c.p, c.data(), npp * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(s->pxy_s.p, sn.data(), npp * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpyAsync(s->pxy_c.p, h + 6 * (size_t)n, npp * 8, cudaMemcpyHostToDevice, s->stream));
+  CU(cudaMemcpyAsync(s->pxy_s.p, h + 6 * (size_t)n + npp, npp * 8, cudaMemcpyHostToDevice,
+                     s->stream));
   s->geo_on_dev = true;
   return RS_OK;
 }
@@ -1382,9 +1383,11 @@ double fmm32_error(int pde) { return pde == kStokes ? 8e-7 : 6e-8; }
 // Relative residual the inner GMRES of GMRES-IR aims for (its FP32
 // products and preconditioner are good to about 1e-7).
 constexpr double kGmresInnerTol = 1e-6;
+int fmm_order_of(const rs_solver* s) {
+  return s->cfg.fmm_order > 0 ? s->cfg.fmm_order : auto_fmm_order(s->cfg.refine_tol, s->cfg.pde);
+}
 rs_status build_fmm(rs_solver* s) {
-  const int p = s->cfg.fmm_order > 0 ? s->cfg.fmm_order
-                                     : auto_fmm_order(s->cfg.refine_tol, s->cfg.pde);
+  const int p = fmm_order_of(s);
   if (p > 64) return fail(s, RS_ERR_ARG, "fmm_order above 64");
   if (!fmm_build(s->fmm, s->tree, s->pts.data(), s->n, p, kFmmOrder32, s->stream))
     return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
@@ -1734,7 +1737,8 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
       eps32 *= std::max(amp, 1.0);
       const int want = auto_fmm_order(s->cfg.refine_tol / std::max(amp, 1.0), s->cfg.pde);
       if (s->cfg.fmm_order == 0 && amp > 4.0 && want > s->fmm.p) {
-        if (!fmm_set_order(s->fmm, want)) return fail(s, RS_ERR_CUDA, "multipole order update failed");
+        if (!fmm_set_order(s->fmm, want, s->stream))
+          return fail(s, RS_ERR_CUDA, "multipole order update failed");
         if (s->trace)
           std::fprintf(stderr, "[rskel] |mu|/|f| = %.1f: multipole order %d\n", amp, want);
         RSCHK(fresh());
@@ -2092,10 +2096,28 @@ rs_status rs_factor(rs_solver* s) {
   if (rc != RS_OK) return rc;
   if (s->fp32 && s->nprob > 1 && s->cfg.pde != kLaplace)
     return fail(s, RS_ERR_ARG, "refinement of a batch supports the Laplace double layer only");
-  if (s->fp32 && !s->fmm.built) {
-    rc = build_fmm(s);
-    if (rc != RS_OK) return rc;
+  // The multipole plan is needed by the solve only: its host part is built
+  // on another thread while the factorization runs, and uploaded after.
+  FmmHostPlan fhp;
+  std::thread plan_thread;
+  const bool need_fmm = s->fp32 && !s->fmm.built;
+  // the factorization's OpenMP team leaves a core to the plan thread
+  const int omp_threads = omp_get_max_threads();
+  if (need_fmm && omp_threads > 2) omp_set_num_threads(omp_threads - 1);
+  if (need_fmm) {
+    if (fmm_order_of(s) > 64) return fail(s, RS_ERR_ARG, "fmm_order above 64");
+    plan_thread = std::thread([s, &fhp] {
+      fmm_plan_host(fhp, s->tree, s->pts.data(), s->n, fmm_order_of(s), kFmmOrder32);
+    });
   }
+  struct Joiner {
+    std::thread& t;
+    int omp_threads;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+      omp_set_num_threads(omp_threads);
+    }
+  } joiner{plan_thread, omp_threads};
   double t0 = now_ms();
   drop_inverse_graph(s);
   CU(cudaEventRecord(s->ev_f0, s->stream));
@@ -2108,6 +2130,11 @@ rs_status rs_factor(rs_solver* s) {
     CU(cudaMemsetAsync(s->ones_mask.p, 1, s->D, s->stream));
   }
   CU(cudaEventRecord(s->ev_f1, s->stream));
+  if (need_fmm) {
+    plan_thread.join();
+    if (!fmm_plan_upload(s->fmm, fhp, s->stream))
+      return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
+  }
   CU(cudaMemcpyAsync(s->h_status.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
   float ms = 0;
@@ -2599,7 +2626,10 @@ rs_status rs_node_list(const rs_solver* s, int node, int which, int* out, int ca
   const bool have = id < (int)s->st.size();
   static const std::vector<int> empty;
   switch (which) {
-    case 0: src = &nd.original; break;
+    case 0:
+      tmp = s->tree.box_dofs(id);
+      src = &tmp;
+      break;
     case 1: src = have ? &s->st[id].active : &empty; break;
     case 2: src = have ? &s->st[id].skel : &empty; break;
     case 3: src = have ? &s->st[id].red : &empty; break;

@@ -1,6 +1,7 @@
 // Host quadtree construction; see tree.hpp for the rules it reproduces.
 #include "tree.hpp"
 
+#include <algorithm>
 #include <cmath>
 
 namespace rskel {
@@ -15,22 +16,49 @@ void QuadTree::push_level(int level, int id) {
   levels[level].push_back(id);
 }
 
-// quadtree.cpp:230-269
+// quadtree.cpp:230-269.  The reference appends the point's DOFs to every
+// box on its path; here they go to the leaf only (a box's own list is the
+// ordered union of its leaves' lists, since every list is in point order,
+// and box_dofs forms it when asked): the tree, its creation order and every
+// leaf list come out the same.  The walk starts from the previous point's
+// box when the point lies in it: a box's edges are the very midpoints the
+// walk compares with (x < mid goes left), so the box test [x0, x1) x [y0, y1)
+// takes the same decisions as the walk from the root.
 void QuadTree::add(int id, double x, double y, int point) {
-  for (int c = 0; c < sd; ++c) nodes[id].original.push_back(sd * point + c);
-  const TreeNode& nd = nodes[id];
-  const double midx = ((nd.corners[6] - nd.corners[0]) / 2.0) + nd.corners[0];
-  const double midy = ((nd.corners[3] - nd.corners[1]) / 2.0) + nd.corners[1];
-  int child;
-  if (x < midx && y < midy) child = nd.bl;
-  else if (x < midx && y >= midy) child = nd.tl;
-  else if (x >= midx && y < midy) child = nd.br;
-  else child = nd.tr;
-  if (child >= 0) {
-    add(child, x, y, point);
-  } else if (nd.is_leaf && static_cast<int>(nd.original.size()) > leaf_) {
-    subdivide(id);
+  int cur = id;
+  if (hint_ >= 0) {
+    const TreeNode& h = nodes[hint_];
+    if (x >= h.corners[0] && x < h.corners[4] && y >= h.corners[1] && y < h.corners[3]) cur = hint_;
   }
+  while (!nodes[cur].is_leaf) {
+    const TreeNode& nd = nodes[cur];
+    const double midx = ((nd.corners[6] - nd.corners[0]) / 2.0) + nd.corners[0];
+    const double midy = ((nd.corners[3] - nd.corners[1]) / 2.0) + nd.corners[1];
+    if (x < midx && y < midy) cur = nd.bl;
+    else if (x < midx && y >= midy) cur = nd.tl;
+    else if (x >= midx && y < midy) cur = nd.br;
+    else cur = nd.tr;
+  }
+  for (int c = 0; c < sd; ++c) nodes[cur].original.push_back(sd * point + c);
+  hint_ = cur;
+  if (static_cast<int>(nodes[cur].original.size()) > leaf_) subdivide(cur);
+}
+
+std::vector<int> QuadTree::box_dofs(int id) const {
+  if (nodes[id].is_leaf) return nodes[id].original;
+  std::vector<int> out, stack(1, id);
+  while (!stack.empty()) {
+    const int b = stack.back();
+    stack.pop_back();
+    if (nodes[b].is_leaf) {
+      out.insert(out.end(), nodes[b].original.begin(), nodes[b].original.end());
+    } else {
+      for (int c = 0; c < 4; ++c)
+        if (nodes[b].children[c] >= 0) stack.push_back(nodes[b].children[c]);
+    }
+  }
+  std::sort(out.begin(), out.end());
+  return out;
 }
 
 // quadtree.cpp:275-432
@@ -65,7 +93,8 @@ void QuadTree::subdivide(int id) {
   TreeNode& nd = nodes[id];
   nd.bl = bl; nd.tl = tl; nd.tr = tr; nd.br = br;
   nd.children[0] = bl; nd.children[1] = tl; nd.children[2] = tr; nd.children[3] = br;
-  const std::vector<int> parent_dofs = nd.original;
+  std::vector<int> parent_dofs;
+  parent_dofs.swap(nd.original);  // a box above the leaves keeps no list (box_dofs)
   for (size_t idx = 0; idx < parent_dofs.size(); idx += sd) {
     const int mi = parent_dofs[idx];
     const int pv = (mi / sd) * 2;
@@ -83,12 +112,26 @@ void QuadTree::subdivide(int id) {
   if (static_cast<int>(nodes[br].original.size()) > leaf_) subdivide(br);
 }
 
-// quadtree.cpp:185-227
+// quadtree.cpp:185-227.  The reference walks the whole subtree of `small`;
+// a subtree whose box can hold no corner that passes either test (a corner
+// on big's top or bottom line inside its x range, or, by the reference's
+// condition, on its left or right line below its bottom) is skipped, with
+// a margin of 1e-12 around the 1e-14 tests: the walk order and the hits are
+// unchanged.
 void QuadTree::descendant_neighbors(int big, int small) {
   const double top = nodes[big].corners[3];
   const double bottom = nodes[big].corners[1];
   const double left = nodes[big].corners[0];
   const double right = nodes[big].corners[4];
+  {
+    const double* sc = nodes[small].corners;
+    const double sx0 = sc[0], sx1 = sc[4], sy0 = sc[1], sy1 = sc[3], m = 1e-12;
+    const bool near_row = (sy0 - m < top && top < sy1 + m) || (sy0 - m < bottom && bottom < sy1 + m);
+    const bool can_a = sx1 > left - m && sx0 < right + m && near_row;
+    const bool near_col = (sx0 - m < left && left < sx1 + m) || (sx0 - m < right && right < sx1 + m);
+    const bool can_b = sy0 < bottom + m && near_col;
+    if (!can_a && !can_b) return;
+  }
   for (int i = 0; i < 8; i += 2) {
     const double x = nodes[small].corners[i];
     const double y = nodes[small].corners[i + 1];
@@ -134,6 +177,7 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
   for (int i = 0; i < 8; ++i) r.corners[i] = rc[i];
   r.side = hi - lo;
   push_level(0, root);
+  hint_ = -1;
   for (int i = 0; i < n; ++i) add(root, points[2 * i], points[2 * i + 1], i);
 
   compute_neighbors();

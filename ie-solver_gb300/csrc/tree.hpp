@@ -25,7 +25,7 @@ struct TreeNode {
   double corners[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // {BL, TL, TR, BR} x,y pairs
   double side = 0;
   std::vector<int> neighbors;
-  std::vector<int> original;  // DOF indices
+  std::vector<int> original;  // DOF indices (leaves only; QuadTree::box_dofs for any box)
   int tree_id = 0;            // which tree of a forest (batch of boundaries) the box is in
 };
 
@@ -44,6 +44,9 @@ struct QuadTree {
   // shifted by dof_offset[t], levels merged by depth (level l holds every
   // tree's level-l boxes, tree by tree), neighbour lists within each tree.
   void merge(const std::vector<QuadTree>& parts, const std::vector<int>& dof_offset);
+  // A box's DOFs in point order: the leaf's list, or the ordered union of
+  // the leaves below it (original_box of the reference).
+  std::vector<int> box_dofs(int id) const;
 
   // QuadTree::perturb (quadtree.cpp:435-801) for a boundary whose points
   // moved: old_to_new[p] is the new index of old point p (-1 if it is gone),
@@ -69,6 +72,7 @@ struct QuadTree {
   void push_level(int level, int id);
   void add(int id, double x, double y, int point);
   void subdivide(int id);
+  int hint_ = -1;  // the box that took the previous point (build)
   void descendant_neighbors(int big, int small);
   void compute_neighbors();
   void number_levels();
