@@ -450,6 +450,10 @@ def run_gpu(args):
     t32, st32, mu32, l32 = time_arm(capi, geo, F, capi.RS_FP32_REFINE, args.steps, args.warmup,
                                     cu, dist, model, tune=tuned)
     clocks = clk.stop()
+    # the end-to-end arm of the expected headline runs before the CPU oracle
+    # (whose all-core OpenMP threads would otherwise still be spinning)
+    e2e_first = e2e_arm(capi, geo, F, capi.RS_FP32_REFINE, max(1, min(args.steps, 5)), 1, dist,
+                        model)
     # accuracy against the oracle (CPU): at the configuration's tolerance and
     # at 1e-12 (the exact discrete solution to ~1e-12)
     mu_cfg, _, _ = oracle_solution(geo, F, TOL, cores)
@@ -468,7 +472,11 @@ def run_gpu(args):
     else:
         head, times, stats, launches, arm_model = "fp64", t64, st64, l64, None
     prec = capi.RS_FP32_REFINE if refined_ok else capi.RS_FP64
-    e2e_t, h2d, d2h = e2e_arm(capi, geo, F, prec, max(1, min(args.steps, 5)), 1, dist, arm_model)
+    if learned_ok:
+        e2e_t, h2d, d2h = e2e_first
+    else:
+        e2e_t, h2d, d2h = e2e_arm(capi, geo, F, prec, max(1, min(args.steps, 5)), 1, dist,
+                                  arm_model)
     ms = dist.max(max(times))
     ms64 = dist.max(max(t64))
     e2e_ms = dist.max(statistics.median(e2e_t))
