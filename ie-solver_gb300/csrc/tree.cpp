@@ -1,6 +1,8 @@
 // Host quadtree construction; see tree.hpp for the rules it reproduces.
 #include "tree.hpp"
 
+#include <omp.h>
+
 #include <algorithm>
 #include <cmath>
 
@@ -16,34 +18,9 @@ void QuadTree::push_level(int level, int id) {
   levels[level].push_back(id);
 }
 
-// quadtree.cpp:230-269.  The reference appends the point's DOFs to every
-// box on its path; here they go to the leaf only (a box's own list is the
-// ordered union of its leaves' lists, since every list is in point order,
-// and box_dofs forms it when asked): the tree, its creation order and every
-// leaf list come out the same.  The walk starts from the previous point's
-// box when the point lies in it: a box's edges are the very midpoints the
-// walk compares with (x < mid goes left), so the box test [x0, x1) x [y0, y1)
-// takes the same decisions as the walk from the root.
-void QuadTree::add(int id, double x, double y, int point) {
-  int cur = id;
-  if (hint_ >= 0) {
-    const TreeNode& h = nodes[hint_];
-    if (x >= h.corners[0] && x < h.corners[4] && y >= h.corners[1] && y < h.corners[3]) cur = hint_;
-  }
-  while (!nodes[cur].is_leaf) {
-    const TreeNode& nd = nodes[cur];
-    const double midx = ((nd.corners[6] - nd.corners[0]) / 2.0) + nd.corners[0];
-    const double midy = ((nd.corners[3] - nd.corners[1]) / 2.0) + nd.corners[1];
-    if (x < midx && y < midy) cur = nd.bl;
-    else if (x < midx && y >= midy) cur = nd.tl;
-    else if (x >= midx && y < midy) cur = nd.br;
-    else cur = nd.tr;
-  }
-  for (int c = 0; c < sd; ++c) nodes[cur].original.push_back(sd * point + c);
-  hint_ = cur;
-  if (static_cast<int>(nodes[cur].original.size()) > leaf_) subdivide(cur);
-}
-
+// A box's own DOF list (the reference's original_box, which it appends to
+// every box on a point's path, quadtree.cpp:230-269) is the ordered union of
+// its leaves' lists, since every list is in point order: only leaves keep one.
 std::vector<int> QuadTree::box_dofs(int id) const {
   if (nodes[id].is_leaf) return nodes[id].original;
   std::vector<int> out, stack(1, id);
@@ -112,13 +89,14 @@ void QuadTree::subdivide(int id) {
   if (static_cast<int>(nodes[br].original.size()) > leaf_) subdivide(br);
 }
 
-// quadtree.cpp:185-227.  The reference walks the whole subtree of `small`;
-// a subtree whose box can hold no corner that passes either test (a corner
-// on big's top or bottom line inside its x range, or, by the reference's
-// condition, on its left or right line below its bottom) is skipped, with
-// a margin of 1e-12 around the 1e-14 tests: the walk order and the hits are
-// unchanged.
-void QuadTree::descendant_neighbors(int big, int small) {
+// quadtree.cpp:185-227: the boxes below `small` whose corners touch the
+// leaf `big`, in the reference's walk order, appended to *out.  The
+// reference walks the whole subtree of `small`; a subtree whose box can hold
+// no corner that passes either test (a corner on big's top or bottom line
+// inside its x range, or, by the reference's condition, on its left or
+// right line below its bottom) is skipped, with a margin of 1e-12 around the
+// 1e-14 tests: the walk order and the hits are unchanged.
+void QuadTree::descendant_neighbors(int big, int small, std::vector<int>* out) const {
   const double top = nodes[big].corners[3];
   const double bottom = nodes[big].corners[1];
   const double left = nodes[big].corners[0];
@@ -144,15 +122,234 @@ void QuadTree::descendant_neighbors(int big, int small) {
       if (std::fabs(x - left) < 1e-14 || std::fabs(x - right) < 1e-14) hit = true;
     }
     if (hit) {
-      nodes[big].neighbors.push_back(small);
-      nodes[small].neighbors.push_back(big);
+      out->push_back(small);
       break;
     }
   }
   for (int c = 0; c < 4; ++c) {
     const int ch = nodes[small].children[c];
-    if (ch >= 0) descendant_neighbors(big, ch);
+    if (ch >= 0) descendant_neighbors(big, ch, out);
   }
+}
+
+namespace {
+// A box of the partition before it is numbered.
+struct PBox {
+  double corners[8];
+  double side;
+  int level;
+  int parent;   // PBox index
+  int kids[4];  // PBox indices {bl, tl, tr, br}; -1 for a leaf
+  int a, b;     // its points: ord[a, b), ascending point index
+  int t;        // the point whose arrival splits it (boxes that split)
+};
+constexpr int kMaxTreeDepth = 256;  // boxes 2^-256 of the root: coincident points
+}  // namespace
+
+// The tree that inserting points 0..n-1 one at a time (add, subdivide)
+// makes, formed by recursive partition of the point indices with the same
+// midpoint comparisons.  A box splits iff more than cap = max_leaf_dofs / sd
+// of the points fall in it, and it splits when the (cap + 1)-th of them in
+// index order arrives.  The splits one point causes form a chain, from a box
+// down through the one child that holds all cap + 1 of its points, so ordering
+// the splits by (that point, depth) gives the order in which insertion creates
+// boxes; node ids and level lists follow it.  Leaf lists are in point order,
+// as insertion leaves them.  Returns false when points coincide so that
+// boxes split past kMaxTreeDepth levels (insertion would not end).
+bool QuadTree::partition_build(int n) {
+  const int cap = leaf_ / sd;
+  std::vector<int> ord(n), tmp(n);
+  std::vector<unsigned char> quad(n);
+  for (int i = 0; i < n; ++i) ord[i] = i;
+  std::vector<PBox> box(1);
+  {
+    PBox& r = box[0];
+    for (int i = 0; i < 8; ++i) r.corners[i] = nodes[root].corners[i];
+    r.side = nodes[root].side;
+    r.level = 0;
+    r.parent = -1;
+    r.kids[0] = r.kids[1] = r.kids[2] = r.kids[3] = -1;
+    r.a = 0;
+    r.b = n;
+    r.t = -1;
+  }
+  const double* pts = pts_;
+  int* const ordp = ord.data();
+  int* const tmpp = tmp.data();
+  unsigned char* const quadp = quad.data();
+  // quadrant of ord[j] (0 bl, 1 tl, 2 tr, 3 br: x < midx goes left, y < midy
+  // goes down, as in subdivide) into quad[j], counted into c[4]
+  auto classify = [pts, ordp, quadp](int j0, int j1, double midx, double midy, int* c) {
+    const int* __restrict o = ordp;
+    unsigned char* __restrict qd = quadp;
+    int c0 = 0, c1 = 0, c2 = 0;
+    for (int j = j0; j < j1; ++j) {
+      const size_t v = static_cast<size_t>(o[j]);
+      const double x = pts[2 * v], y = pts[2 * v + 1];
+      const int left = x < midx, low = y < midy;
+      const int q = left ? (low ? 0 : 1) : (low ? 3 : 2);
+      qd[j] = static_cast<unsigned char>(q);
+      c0 += q == 0;
+      c1 += q == 1;
+      c2 += q == 2;
+    }
+    c[0] = c0;
+    c[1] = c1;
+    c[2] = c2;
+    c[3] = (j1 - j0) - c0 - c1 - c2;
+  };
+  // stable scatter of ord[j0, j1) to tmp from the four write positions (in
+  // registers: an indexed position array would chain every store to the last)
+  auto scatter = [ordp, tmpp, quadp](int j0, int j1, const int* pos) {
+    const int* __restrict o = ordp;
+    const unsigned char* __restrict qd = quadp;
+    int* __restrict t = tmpp;
+    int p0 = pos[0], p1 = pos[1], p2 = pos[2], p3 = pos[3];
+    for (int j = j0; j < j1; ++j) {
+      const int v = o[j];
+      switch (qd[j]) {
+        case 0: t[p0++] = v; break;
+        case 1: t[p1++] = v; break;
+        case 2: t[p2++] = v; break;
+        default: t[p3++] = v; break;
+      }
+    }
+  };
+  const int nthreads = std::max(1, omp_get_max_threads());
+  constexpr int kChunked = 16384;  // boxes at least this large split over threads
+  std::vector<int> level_boxes(1, 0), split, splits, big_cnt;
+  std::vector<double> mid;
+  std::vector<int> cnt;
+  while (!level_boxes.empty()) {
+    split.clear();
+    for (int k : level_boxes)
+      if (box[k].b - box[k].a > cap) {
+        if (box[k].level >= kMaxTreeDepth) return false;
+        split.push_back(k);
+      }
+    if (split.empty()) break;
+    const int ns = static_cast<int>(split.size());
+    mid.resize(2 * (size_t)ns);
+    cnt.assign(4 * (size_t)ns, 0);
+    size_t work = 0;
+    for (int i = 0; i < ns; ++i) {
+      PBox& bx = box[split[i]];
+      const double* c = bx.corners;
+      mid[2 * i] = ((c[6] - c[0]) / 2.0) + c[0];
+      mid[2 * i + 1] = ((c[3] - c[1]) / 2.0) + c[1];
+      bx.t = ord[bx.a + cap];  // ord is ascending within a box
+      work += bx.b - bx.a;
+    }
+    // large boxes: chunks over the threads, offsets by prefix over chunks
+    for (int i = 0; i < ns; ++i) {
+      const PBox& bx = box[split[i]];
+      if (nthreads == 1 || bx.b - bx.a < kChunked) continue;
+      const int a = bx.a, b = bx.b, len = b - a;
+      big_cnt.assign(4 * (size_t)nthreads, 0);
+#pragma omp parallel num_threads(nthreads)
+      {
+        const int nt = omp_get_num_threads(), t = omp_get_thread_num();
+        const int chunk = (len + nt - 1) / nt;
+        const int j0 = std::min(b, a + t * chunk), j1 = std::min(b, j0 + chunk);
+        classify(j0, j1, mid[2 * i], mid[2 * i + 1], &big_cnt[4 * (size_t)t]);
+#pragma omp barrier
+        int pos[4];
+        for (int q = 0, base = a; q < 4; ++q) {
+          int before = 0, total = 0;
+          for (int u = 0; u < nt; ++u) {
+            if (u < t) before += big_cnt[4 * (size_t)u + q];
+            total += big_cnt[4 * (size_t)u + q];
+          }
+          pos[q] = base + before;
+          base += total;
+          if (t == 0) cnt[4 * (size_t)i + q] = total;
+        }
+        scatter(j0, j1, pos);
+#pragma omp barrier
+        std::copy(tmp.begin() + j0, tmp.begin() + j1, ord.begin() + j0);
+      }
+    }
+    // the other boxes: one thread each
+#pragma omp parallel for schedule(dynamic, 2) if (nthreads > 1 && work > 4096)
+    for (int i = 0; i < ns; ++i) {
+      const PBox& bx = box[split[i]];
+      if (nthreads > 1 && bx.b - bx.a >= kChunked) continue;
+      int* c = &cnt[4 * (size_t)i];
+      classify(bx.a, bx.b, mid[2 * i], mid[2 * i + 1], c);
+      const int pos[4] = {bx.a, bx.a + c[0], bx.a + c[0] + c[1], bx.a + c[0] + c[1] + c[2]};
+      scatter(bx.a, bx.b, pos);
+      std::copy(tmp.begin() + bx.a, tmp.begin() + bx.b, ord.begin() + bx.a);
+    }
+    // children, corners as in subdivide
+    level_boxes.clear();
+    for (int i = 0; i < ns; ++i) {
+      const int k = split[i];
+      double c[8];
+      for (int u = 0; u < 8; ++u) c[u] = box[k].corners[u];
+      const double midx = mid[2 * i], midy = mid[2 * i + 1];
+      const double cq[4][8] = {{c[0], c[1], c[2], midy, midx, midy, midx, c[7]},
+                               {c[0], midy, c[2], c[3], midx, c[5], midx, midy},
+                               {midx, midy, midx, c[3], c[4], c[5], c[6], midy},
+                               {midx, c[1], midx, midy, c[4], midy, c[6], c[7]}};
+      const double side = box[k].side / 2.0;
+      const int level = box[k].level + 1;
+      int start = box[k].a;
+      for (int q = 0; q < 4; ++q) {
+        PBox ch;
+        for (int u = 0; u < 8; ++u) ch.corners[u] = cq[q][u];
+        ch.side = side;
+        ch.level = level;
+        ch.parent = k;
+        ch.kids[0] = ch.kids[1] = ch.kids[2] = ch.kids[3] = -1;
+        ch.a = start;
+        ch.b = start + cnt[4 * (size_t)i + q];
+        ch.t = -1;
+        start = ch.b;
+        box[k].kids[q] = static_cast<int>(box.size());
+        level_boxes.push_back(static_cast<int>(box.size()));
+        box.push_back(ch);
+      }
+      splits.push_back(k);
+    }
+  }
+  std::stable_sort(splits.begin(), splits.end(), [&box](int u, int v) {
+    return box[u].t != box[v].t ? box[u].t < box[v].t : box[u].level < box[v].level;
+  });
+  std::vector<int> id(box.size(), -1);
+  id[0] = root;
+  int next = root + 1;
+  levels.assign(1, std::vector<int>(1, root));
+  for (int k : splits) {
+    for (int q = 0; q < 4; ++q) id[box[k].kids[q]] = next++;
+    const int lv = box[k].level + 1;
+    if (static_cast<int>(levels.size()) <= lv) levels.resize(lv + 1);
+    // level lists take the children as bl, br, tr, tl
+    for (int q : {0, 3, 2, 1}) levels[lv].push_back(id[box[k].kids[q]]);
+  }
+  nodes.resize(box.size());
+  const int nbox = static_cast<int>(box.size());
+#pragma omp parallel for schedule(dynamic, 64) if (nbox >= 1024)
+  for (int k = 0; k < nbox; ++k) {
+    const PBox& p = box[k];
+    TreeNode& nd = nodes[id[k]];
+    nd.level = p.level;
+    nd.parent = p.parent >= 0 ? id[p.parent] : -1;
+    nd.is_leaf = p.kids[0] < 0 ? 1 : 0;
+    for (int q = 0; q < 4; ++q) nd.children[q] = p.kids[q] >= 0 ? id[p.kids[q]] : -1;
+    nd.bl = nd.children[0];
+    nd.tl = nd.children[1];
+    nd.tr = nd.children[2];
+    nd.br = nd.children[3];
+    for (int i = 0; i < 8; ++i) nd.corners[i] = p.corners[i];
+    nd.side = p.side;
+    nd.original.clear();
+    if (nd.is_leaf) {
+      nd.original.reserve(static_cast<size_t>(p.b - p.a) * sd);
+      for (int j = p.a; j < p.b; ++j)
+        for (int c = 0; c < sd; ++c) nd.original.push_back(sd * ord[j] + c);
+    }
+  }
+  return true;
 }
 
 bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
@@ -176,10 +373,12 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
   const double rc[8] = {lo, lo, lo, hi, hi, hi, hi, lo};
   for (int i = 0; i < 8; ++i) r.corners[i] = rc[i];
   r.side = hi - lo;
-  push_level(0, root);
-  hint_ = -1;
-  for (int i = 0; i < n; ++i) add(root, points[2 * i], points[2 * i + 1], i);
-
+  if (!partition_build(n)) {
+    nodes.clear();
+    levels.clear();
+    pts_ = nullptr;
+    return false;
+  }
   compute_neighbors();
   number_levels();
   roots.assign(1, root);
@@ -221,42 +420,80 @@ void QuadTree::merge(const std::vector<QuadTree>& parts, const std::vector<int>&
   number_levels();
 }
 
-// quadtree.cpp:131-175
+// quadtree.cpp:131-175, level by level.  Within a level each box's own
+// list takes its siblings and cousins (reading only the coarser level's
+// finished lists), and each leaf finds the finer boxes touching it; the
+// boxes of a level are independent there and run in parallel.  The
+// leaf <-> finer-box links then go in sequentially, in level order, so
+// every list is in the reference's order.  (A leaf's walk reads only its own
+// same-level neighbours, and the links it adds are to finer boxes, whose
+// own sibling/cousin entries come after them, as in the reference.)
 void QuadTree::compute_neighbors() {
   for (TreeNode& nd : nodes) nd.neighbors.clear();
   const double sqrt2 = std::sqrt(2.0);
+  std::vector<std::vector<int>> hits;
+  std::vector<int> extra(nodes.size(), 0), touched;
   for (size_t lv = 0; lv < levels.size(); ++lv) {
-    for (size_t k = 0; k < levels[lv].size(); ++k) {
-      const int a = levels[lv][k];
-      const int par = nodes[a].parent;
+    const std::vector<int>& L = levels[lv];
+    const int m = static_cast<int>(L.size());
+    if (static_cast<int>(hits.size()) < m) hits.resize(m);
+#pragma omp parallel for schedule(dynamic, 16) if (m >= 256)
+    for (int k = 0; k < m; ++k) {
+      const int a = L[k];
+      TreeNode& na = nodes[a];
+      const int par = na.parent;
       if (par >= 0) {
+        const std::vector<int>& pn = nodes[par].neighbors;
+        na.neighbors.reserve(na.neighbors.size() + 3 + 4 * pn.size());
         for (int c = 0; c < 4; ++c) {
           const int sib = nodes[par].children[c];
-          if (sib != a) nodes[a].neighbors.push_back(sib);
+          if (sib != a) na.neighbors.push_back(sib);
         }
-        const std::vector<int>& pn = nodes[par].neighbors;
         for (size_t q = 0; q < pn.size(); ++q) {
           for (int c = 0; c < 4; ++c) {
             const int cousin = nodes[pn[q]].children[c];
-            if (cousin < 0 || nodes[cousin].level != nodes[a].level) continue;
-            const double dx = nodes[a].corners[0] - nodes[cousin].corners[0];
-            const double dy = nodes[a].corners[1] - nodes[cousin].corners[1];
+            if (cousin < 0 || nodes[cousin].level != na.level) continue;
+            const double dx = na.corners[0] - nodes[cousin].corners[0];
+            const double dy = na.corners[1] - nodes[cousin].corners[1];
             const double dist = std::sqrt(dx * dx + dy * dy);
-            if (dist < nodes[a].side * sqrt2 + 1e-5) nodes[a].neighbors.push_back(cousin);
+            if (dist < na.side * sqrt2 + 1e-5) na.neighbors.push_back(cousin);
           }
         }
       }
-      if (nodes[a].is_leaf) {
-        for (size_t q = 0; q < nodes[a].neighbors.size(); ++q) {
-          const int nb = nodes[a].neighbors[q];
-          if (nodes[nb].level != nodes[a].level) continue;
+      hits[k].clear();
+      if (na.is_leaf) {
+        for (size_t q = 0; q < na.neighbors.size(); ++q) {
+          const int nb = na.neighbors[q];
+          if (nodes[nb].level != na.level) continue;
           for (int c = 0; c < 4; ++c) {
             const int ch = nodes[nb].children[c];
-            if (ch >= 0) descendant_neighbors(a, ch);
+            if (ch >= 0) descendant_neighbors(a, ch, &hits[k]);
           }
         }
       }
     }
+    // room first (one allocation per list), then the links in order
+    touched.clear();
+    for (int k = 0; k < m; ++k)
+      for (int sm : hits[k])
+        if (extra[sm]++ == 0) touched.push_back(sm);
+    const int nt = static_cast<int>(touched.size());
+#pragma omp parallel for schedule(static) if (nt + m >= 512)
+    for (int u = 0; u < nt + m; ++u) {
+      if (u < nt) {
+        std::vector<int>& nb = nodes[touched[u]].neighbors;
+        nb.reserve(nb.size() + extra[touched[u]] + 12);  // + its siblings and cousins
+        extra[touched[u]] = 0;
+      } else {
+        std::vector<int>& nb = nodes[L[u - nt]].neighbors;
+        nb.reserve(nb.size() + hits[u - nt].size());
+      }
+    }
+    for (int k = 0; k < m; ++k)
+      for (int sm : hits[k]) {
+        nodes[L[k]].neighbors.push_back(sm);
+        nodes[sm].neighbors.push_back(L[k]);
+      }
   }
 }
 

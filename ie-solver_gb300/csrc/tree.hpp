@@ -70,10 +70,9 @@ struct QuadTree {
   int leaf_ = 32;
   int new_node();
   void push_level(int level, int id);
-  void add(int id, double x, double y, int point);
   void subdivide(int id);
-  int hint_ = -1;  // the box that took the previous point (build)
-  void descendant_neighbors(int big, int small);
+  bool partition_build(int n);
+  void descendant_neighbors(int big, int small, std::vector<int>* out) const;
   void compute_neighbors();
   void number_levels();
   int find_leaf(double x, double y) const;

@@ -111,3 +111,67 @@ def test_tree_edge_cases(solver_lib):
     s = solver_lib.Solver(g.unit_circle(17), solver_lib.RS_STOKES, 1e-6, leaf=32, npp=16)
     s.build_tree()
     assert s.stats()["num_levels"] >= 2
+
+
+def _cloud(n, rng, kind):
+    """Point sets for the tree alone (normals and weights are placeholders):
+    a uniform cloud, a cloud on an 8 x 8 lattice of clusters, and a thin
+    sliver, each in a seeded random order."""
+    from rskel.geometry import Geometry
+
+    if kind == "uniform":
+        xy = rng.random((n, 2))
+    elif kind == "clusters":
+        xy = np.floor(rng.random((n, 2)) * 8) / 8 + 1e-3 * rng.random((n, 2))
+    else:
+        t = rng.random(n) * 2 * np.pi
+        xy = np.stack([3 * np.cos(t), 0.01 * np.sin(t)], axis=1)
+    nrm = np.zeros_like(xy)
+    nrm[:, 0] = 1.0
+    return Geometry(points=xy.ravel().copy(), normals=nrm.ravel().copy(), weights=np.ones(n),
+                    curvatures=np.zeros(n), hole_centers=np.zeros(0), hole_radii=np.zeros(0),
+                    num_outer=n)
+
+
+def test_product_tree_matches_oracle_on_varied_geometries(solver_lib, oracle_lib):
+    """The product forms the tree by recursive partition of the point indices
+    and numbers the boxes in the order insertion would create them; the
+    oracle restates the reference's point-by-point insertion.  Trees, level
+    lists, leaf lists and neighbour lists agree on curves, holes and point
+    clouds, for one and two DOFs per point and several leaf sizes."""
+    from rskel import geometry as g
+
+    rng = np.random.default_rng(2024)
+    geos = [g.random_star(int(rng.integers(500, 20000)), rng) for _ in range(3)]
+    geos += [g.star(12000, 0.3, 7), g.reference_annulus(2048),
+             g.circle_with_ellipses(16000, 8, np.random.default_rng(3)),
+             g.ellipse(6000, 1.0, 0.05, 0.7)]
+    geos += [_cloud(int(rng.integers(200, 9000)), rng, k) for k in ("uniform", "clusters", "sliver")]
+    fields = ("level_sizes", "node_level", "node_leaf", "node_parent", "node_children",
+              "node_corners", "nbr_off", "nbr", "orig_off", "orig")
+    for geo in geos:
+        for pde, sd in ((0, 1), (2, 2)):
+            for leaf in (16, 33, 64):
+                s = solver_lib.Solver(geo, pde, 1e-8, leaf=leaf, npp=64)
+                s.build_tree()
+                mine = s.tree_dump()
+                o = oracle_lib.OracleSolver(geo, pde, sd, 1e-8, leaf, 64, 1)
+                o.build_tree()
+                ref = o.tree_dump()
+                for f in fields:
+                    assert np.array_equal(np.asarray(mine[f]), np.asarray(ref[f])), (geo.n, sd, leaf, f)
+                s.close()
+
+
+def test_coincident_points_are_refused(solver_lib):
+    """More coincident points than a leaf holds can never be separated (the
+    reference's insertion recursion would not end); the build reports an
+    argument error instead."""
+    from rskel import geometry as g
+
+    geo = g.unit_circle(256)
+    geo.points[2 * 10:2 * 60] = np.tile([0.25, 0.5], 50)
+    s = solver_lib.Solver(geo, solver_lib.RS_LAPLACE, 1e-6, leaf=16, npp=16)
+    with pytest.raises(solver_lib.RsError) as e:
+        s.build_tree()
+    assert e.value.code == 1
