@@ -199,6 +199,27 @@ rs_status fail(rs_solver* s, rs_status code, const std::string& msg) {
       return fail(s, RS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// Fresh per-box state for every box of the tree; the lists keep their
+// storage, so a handle that factors one geometry after another reallocates
+// nothing here.
+void reset_states(rs_solver* s) {
+  s->st.resize(s->tree.nodes.size());
+  for (NodeState& S : s->st) {
+    S.compressed = 0;
+    S.k = S.r = 0;
+    S.active.clear();
+    S.skel.clear();
+    S.red.clear();
+    S.near_.clear();
+    S.perm.clear();
+    S.rows.clear();
+    S.use_proxy = 0;
+    S.fac_off = S.piv_off = S.e_off = -1;
+    S.e_ld = 0;
+    S.slot = -1;
+  }
+}
+
 rs_status ensure_device(rs_solver* s) {
   if (s->dev_ready) return RS_OK;
   int count = 0;
@@ -488,7 +509,7 @@ rs_status factor_impl(rs_solver* s) {
                  (int)incr, (int)s->incremental, F.fac_used, s->full_fac_used);
   s->incremental = false;
   if (!incr) {
-    s->st.assign(s->tree.nodes.size(), NodeState());
+    reset_states(s);
     F.fac_used = 0;
     F.e_used = 0;
     s->piv_used = 0;
@@ -1928,7 +1949,7 @@ rs_status rs_build_tree(rs_solver* s) {
   s->fmm.built = false;
   s->tree_built = true;
   s->factored = false;
-  s->st.assign(s->tree.nodes.size(), NodeState());
+  reset_states(s);
   s->stats.t_tree_ms = now_ms() - t0;
   s->stats.num_levels = (int)s->tree.levels.size();
   s->stats.num_nodes = (int)s->tree.nodes.size();

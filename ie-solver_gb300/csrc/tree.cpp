@@ -342,6 +342,7 @@ bool QuadTree::partition_build(int n) {
     nd.br = nd.children[3];
     for (int i = 0; i < 8; ++i) nd.corners[i] = p.corners[i];
     nd.side = p.side;
+    nd.tree_id = 0;
     nd.original.clear();
     if (nd.is_leaf) {
       nd.original.reserve(static_cast<size_t>(p.b - p.a) * sd);
@@ -353,13 +354,17 @@ bool QuadTree::partition_build(int n) {
 }
 
 bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
-  nodes.clear();
   levels.clear();
-  if (n <= 0 || points == nullptr) return false;
+  if (n <= 0 || points == nullptr) {
+    nodes.clear();
+    return false;
+  }
   pts_ = points;
   sd = sd_;
   leaf_ = max_leaf_dofs;
-  nodes.reserve(static_cast<size_t>(8 * (n * sd_ / (max_leaf_dofs > 0 ? max_leaf_dofs : 1) + 1)));
+  // the previous tree's nodes are overwritten in place (partition_build),
+  // so their lists' storage is reused
+  if (nodes.empty()) nodes.emplace_back();
   double mn = points[0], mx = points[0];
   for (int i = 0; i < 2 * n; ++i) {
     if (points[i] < mn) mn = points[i];
@@ -368,7 +373,7 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
   min = mn;
   max = mx;
   const double lo = mn - 0.01, hi = mx + 0.01;
-  root = new_node();
+  root = 0;
   TreeNode& r = nodes[root];
   const double rc[8] = {lo, lo, lo, hi, hi, hi, hi, lo};
   for (int i = 0; i < 8; ++i) r.corners[i] = rc[i];
