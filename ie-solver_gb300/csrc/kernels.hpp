@@ -111,6 +111,14 @@ void launch_dense_lu_batched(void* base, bool fp32, const RootTask* tasks, int c
 void launch_dense_solve_batched(const void* base, bool fp32, const RootTask* tasks, int count,
                                 int nmax, const int* piv, const int* dofs, void* x, int ld,
                                 int nrhs, cudaStream_t st);
+// FP32 root blocks of at most kRootInvMax DOFs: explicit inverse in place
+// of the block (Gauss-Jordan with partial pivoting), then x[idx, :] =
+// A^{-1} x[idx, :] as one product per application.
+constexpr int kRootInvMax = 128;
+void launch_root_inverse(float* base, const RootTask* tasks, int count, int* status,
+                         cudaStream_t st);
+void launch_root_apply(const float* base, const RootTask* tasks, int count, const int* dofs,
+                       float* x, int ld, int nrhs, cudaStream_t st);
 void launch_dense_lu(double* a, int n, int* piv, int* status, cudaStream_t st);
 void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st);
 // x[idx, :] = LU^{-1} x[idx, :] (idx == nullptr: rows 0..n-1); x is Real.

@@ -393,6 +393,176 @@ void launch_dense_solve_batched(const void* base, bool fp32, const RootTask* tas
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 root blocks by explicit inverse.  The LU solve above is 2n dependent
+// steps per column on every application of the factorization; with the
+// inverse formed once per factorization, each application is one product.
+// Gauss-Jordan elimination with partial pivoting, one CTA per block, the
+// block in registers: thread (tc, ti) = (tid / 16, tid % 16) owns rows
+// ti + 16a and columns tc + 16b (a, b < 8), so a column's 128 rows sit in
+// one half-warp and its pivot search needs no barrier.  Rows are not
+// swapped: step j takes the unused row p_j with the largest |A(p_j, j)|
+// (the first on ties), and the in-place update leaves M with
+// A^{-1}(j, p_c) = M(p_j, c), which is written out unpermuted.
+// ---------------------------------------------------------------------------
+constexpr int kInvG = 16;             // thread grid 16 x 16
+constexpr int kInvR = kRootInvMax / kInvG;  // rows and columns per thread
+
+__global__ void __launch_bounds__(kInvG * kInvG) root_inverse_kernel(float* base,
+                                                                   const RootTask* tasks,
+                                                                   int* status) {
+  const RootTask t = tasks[blockIdx.x];
+  const int n = t.n;
+  float* Ag = base + t.a_off;
+  const int tid = threadIdx.x, tc = tid >> 4, ti = tid & 15;
+  __shared__ float colbuf[2][kRootInvMax];
+  __shared__ float rowbuf[2][kRootInvMax];
+  __shared__ int s_p[kRootInvMax];
+  __shared__ int s_pinv[kRootInvMax];
+  __shared__ float s_piv[2];
+  __shared__ int s_bad;
+  float M[kInvR][kInvR];
+#pragma unroll
+  for (int a = 0; a < kInvR; ++a)
+#pragma unroll
+    for (int b = 0; b < kInvR; ++b) {
+      const int i = ti + kInvG * a, c = tc + kInvG * b;
+      M[a][b] = i < n && c < n ? Ag[i + (size_t)n * c] : 0.f;
+    }
+  if (tid == 0) s_bad = 0;
+  unsigned used = 0;  // bit a: row ti + 16a has been a pivot row
+  const unsigned half = 0xffffu << (16 * (tc & 1));
+  for (int j = 0; j < n; ++j) {
+    const int buf = j & 1, jb = j >> 4;
+    if (tc == (j & 15)) {
+      // this half-warp holds column j: publish it and pick the pivot row
+      float best = -1.f, bv = 0.f;
+      int bi = kRootInvMax;
+#pragma unroll
+      for (int a = 0; a < kInvR; ++a) {
+        float v = 0.f;
+#pragma unroll
+        for (int b = 0; b < kInvR; ++b)
+          if (b == jb) v = M[a][b];
+        const int i = ti + kInvG * a;
+        colbuf[buf][i] = v;
+        if (i < n && !((used >> a) & 1u) && fabsf(v) > best) {
+          best = fabsf(v);
+          bv = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(half, best, o);
+        const float ov = __shfl_xor_sync(half, bv, o);
+        const int oi = __shfl_xor_sync(half, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (ti == 0) {
+        const bool ok = best > 0.f && isfinite(best) && bi < n;
+        s_p[j] = ok ? bi : 0;
+        s_piv[buf] = ok ? bv : 1.f;
+        if (!ok) s_bad = 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p[j];
+    const float piv = s_piv[buf];
+    if (ti == (p & 15)) {
+      // the owners of row p publish it scaled by the pivot
+      const int pa = p >> 4;
+      const float inv = 1.f / piv;
+      used |= 1u << pa;
+#pragma unroll
+      for (int b = 0; b < kInvR; ++b) {
+        float v = 0.f;
+#pragma unroll
+        for (int a = 0; a < kInvR; ++a)
+          if (a == pa) v = M[a][b];
+        const int c = tc + kInvG * b;
+        rowbuf[buf][c] = c == j ? inv : v * inv;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < kInvR; ++a) {
+      const int i = ti + kInvG * a;
+      const float ci = colbuf[buf][i];
+#pragma unroll
+      for (int b = 0; b < kInvR; ++b) {
+        const int c = tc + kInvG * b;
+        const float rc = rowbuf[buf][c];
+        const float m = c == j ? 0.f : M[a][b];
+        M[a][b] = i == p ? rc : m - ci * rc;
+      }
+    }
+  }
+  __syncthreads();
+  // (a singular block repeats pivot rows: the map then stays in range)
+  for (int r = tid; r < kRootInvMax; r += blockDim.x) s_pinv[r] = r;
+  __syncthreads();
+  for (int j = tid; j < n; j += blockDim.x) s_pinv[s_p[j]] = j;
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < kInvR; ++a)
+#pragma unroll
+    for (int b = 0; b < kInvR; ++b) {
+      const int r = ti + kInvG * a, c = tc + kInvG * b;
+      if (r < n && c < n) Ag[s_pinv[r] + (size_t)n * s_p[c]] = M[a][b];
+    }
+  if (tid == 0 && s_bad) atomicExch(status, 1);
+}
+
+// x[idx, c] <- A^{-1} x[idx, c] per root block, with the explicit inverse.
+__global__ void __launch_bounds__(kThreads) root_apply_kernel(const float* base,
+                                                              const RootTask* tasks,
+                                                              const int* dofs, float* x, int ld,
+                                                              int nrhs) {
+  const RootTask t = tasks[blockIdx.x];
+  const int n = t.n;
+  const float* Ai = base + t.a_off;
+  const int* idx = dofs + t.idx_off;
+  __shared__ float sx[kRootInvMax * kRhsBlock];
+  __shared__ float sy[kRootInvMax * kRhsBlock];
+  for (int c0 = 0; c0 < nrhs; c0 += kRhsBlock) {
+    const int cb = nrhs - c0 < kRhsBlock ? nrhs - c0 : kRhsBlock;
+    for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      sx[e] = x[idx[i] + (size_t)ld * (c0 + c)];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      float acc = 0.f;
+      for (int l = 0; l < n; ++l) acc += Ai[i + (size_t)n * l] * sx[l + n * c];
+      sy[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      x[idx[i] + (size_t)ld * (c0 + c)] = sy[e];
+    }
+    __syncthreads();
+  }
+}
+
+void launch_root_inverse(float* base, const RootTask* tasks, int count, int* status,
+                         cudaStream_t st) {
+  if (count <= 0) return;
+  root_inverse_kernel<<<count, kInvG * kInvG, 0, st>>>(base, tasks, status);
+}
+
+void launch_root_apply(const float* base, const RootTask* tasks, int count, const int* dofs,
+                       float* x, int ld, int nrhs, cudaStream_t st) {
+  if (count <= 0 || nrhs <= 0) return;
+  root_apply_kernel<<<count, kThreads, 0, st>>>(base, tasks, dofs, x, ld, nrhs);
+}
+
 template <class Real>
 static void launch_dense_solve_t(const Real* lu, int n, const int* piv, const int* idx, Real* x,
                                  int ld, int nrhs, cudaStream_t st) {

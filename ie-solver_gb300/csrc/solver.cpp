@@ -119,6 +119,7 @@ struct rs_solver {
   std::vector<RootTask> roots_h;
   DevBuf<RootTask> roots_dev;
   int root_nmax = 0;
+  bool root_inv = false;  // FP32 root blocks hold explicit inverses (else LU + pivots)
   // boundaries held by the handle (rs_set_geometry_batch) and their point
   // offsets; per-boundary DOF offsets on the device for the norms
   int nprob = 1;
@@ -1141,13 +1142,19 @@ rs_status factor_impl(rs_solver* s) {
     CU(stage_copy(s, s->roots_dev.p, s->roots_h.data(), s->roots_h.size() * sizeof(RootTask)));
   }
   s->nb = 0;
+  s->root_inv = false;
   if (s->nh > 0 && s->cfg.pde != kLaplaceNeumann) {
     // bordered system, skel_factorization.cpp:188-305
     rs_status rc = factor_border<Real>(s);
     if (rc != RS_OK) return rc;
   } else if (!s->roots_h.empty()) {
-    launch_dense_lu_batched(F.epool.p, f32, s->roots_dev.p, (int)s->roots_h.size(), s->root_nmax,
-                            s->root_piv.p, s->status.p, s->stream);
+    s->root_inv = f32 && s->root_nmax <= kRootInvMax;
+    if (s->root_inv)
+      launch_root_inverse((float*)F.epool.p, s->roots_dev.p, (int)s->roots_h.size(),
+                          s->status.p, s->stream);
+    else
+      launch_dense_lu_batched(F.epool.p, f32, s->roots_dev.p, (int)s->roots_h.size(),
+                              s->root_nmax, s->root_piv.p, s->status.p, s->stream);
     ++s->launches;
   }
   CU(cudaGetLastError());
@@ -1345,9 +1352,15 @@ rs_status apply_inverse(rs_solver* s, Real* x, int nrhs, Real* alpha, const doub
   if (s->nb == 0) {
     sweep_levels<Real>(s, x, s->D, nrhs, kUpSolve, true);
     if (!s->roots_h.empty()) {
-      launch_dense_solve_batched(F.epool.p, sizeof(Real) == 4, s->roots_dev.p,
-                                 (int)s->roots_h.size(), s->root_nmax, s->root_piv.p, s->dofs.p,
-                                 x, s->D, nrhs, s->stream);
+      if constexpr (sizeof(Real) == 4) {
+        if (s->root_inv)
+          launch_root_apply(F.epool.p, s->roots_dev.p, (int)s->roots_h.size(), s->dofs.p, x,
+                            s->D, nrhs, s->stream);
+      }
+      if (!s->root_inv || sizeof(Real) != 4)
+        launch_dense_solve_batched(F.epool.p, sizeof(Real) == 4, s->roots_dev.p,
+                                   (int)s->roots_h.size(), s->root_nmax, s->root_piv.p,
+                                   s->dofs.p, x, s->D, nrhs, s->stream);
       ++s->launches;
     }
     sweep_levels<Real>(s, x, s->D, nrhs, kDown, false);
