@@ -140,84 +140,86 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     // partial pivoting), so that U_f, L_f and the solve's diagonal step are
     // matrix products spread over the whole CTA instead of one warp-serial
     // triangular solve per column.  The refinement absorbs the explicit
-    // inverse's slightly larger rounding error.
-    Real* colj = T;  // T is no longer needed; it holds >= r entries
-    __shared__ int s_p;
+    // inverse's slightly larger rounding error.  Rows are not swapped: step
+    // j takes the unused row piv[j] with the largest |X(piv[j], j)| (the
+    // first on ties), and the in-place update leaves M with
+    // X^{-1}(a, b) = M(piv[a], pinv[b]).  Column j + 1 and the scaled pivot
+    // row go through double buffers, so a step takes two CTA barriers.  The
+    // assembly's index arrays are free by now and hold the buffers.
+    float* colbuf[2] = {reinterpret_cast<float*>(bchild), reinterpret_cast<float*>(bidx)};
+    float* rowbuf[2] = {reinterpret_cast<float*>(bld), reinterpret_cast<float*>(order)};
+    int* used = reinterpret_cast<int*>(bbase);
+    for (int i = threadIdx.x; i < r; i += blockDim.x) {
+      colbuf[0][i] = Mrr[i];
+      used[i] = 0;
+    }
+    __syncthreads();
     for (int j = 0; j < r; ++j) {
-      if (warp == 0) {
-        float best = -1.f;
-        int bi = r;
-        for (int i = j + lane; i < r; i += 32) {
-          const float v = fabsf(Mrr[i + ld * j]);
-          if (v > best || (v == best && i < bi)) { best = v; bi = i; }
-        }
+      const int buf = j & 1;
+      // every warp finds the pivot row itself (no barrier for a broadcast)
+      float best = -1.f;
+      int bi = r;
+      for (int i = lane; i < r; i += 32) {
+        const float v = fabsf(colbuf[buf][i]);
+        if (!used[i] && v > best) { best = v; bi = i; }
+      }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if (lane == 0) {
-          piv[j] = bi;
-          s_p = bi;
-          if (!(best > 0.f) || !isfinite(best)) scal[0] = 1.0;
-        }
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
       }
-      __syncthreads();
-      const int pj = s_p;
-      if (pj != j) {
-        for (int c = threadIdx.x; c < r; c += blockDim.x) {
-          const Real tmp = Mrr[j + ld * c];
-          Mrr[j + ld * c] = Mrr[pj + ld * c];
-          Mrr[pj + ld * c] = tmp;
-        }
-        __syncthreads();
+      const bool ok = best > 0.f && isfinite(best) && bi < r;
+      const int pr = ok ? bi : j;  // a singular block: any row, flagged
+      if (threadIdx.x == 0) {
+        piv[j] = pr;
+        if (!ok) scal[0] = 1.0;
       }
-      const Real d = Mrr[j + ld * j];
+      const Real d = Mrr[pr + ld * j];
       const Real inv = d != (Real)0 ? (Real)1 / d : (Real)0;
-      for (int i = threadIdx.x; i < r; i += blockDim.x) colj[i] = i == j ? (Real)0 : Mrr[i + ld * j];
-      __syncthreads();
       for (int c = threadIdx.x; c < r; c += blockDim.x)
-        Mrr[j + ld * c] = (c == j ? (Real)1 : Mrr[j + ld * c]) * inv;
+        rowbuf[buf][c] = c == j ? inv : Mrr[pr + ld * c] * inv;
       __syncthreads();
+      // (every warp has read `used` for this step by now)
+      if (threadIdx.x == 0) used[pr] = 1;
       for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
         const int i = e % r, c = e / r;
-        if (i == j) continue;
-        const Real a = c == j ? (Real)0 : Mrr[i + ld * c];
-        Mrr[i + ld * c] = a - colj[i] * Mrr[j + ld * c];
+        const Real m = c == j ? (Real)0 : Mrr[i + ld * c];
+        const Real v = i == pr ? rowbuf[buf][c] : m - colbuf[buf][i] * rowbuf[buf][c];
+        Mrr[i + ld * c] = v;
+        if (c == j + 1) colbuf[buf ^ 1][i] = v;
       }
       __syncthreads();
     }
-    // undo the row interchanges on the inverse's columns, last first
-    for (int j = r - 1; j >= 0; --j) {
-      const int pj = piv[j];
-      if (pj != j)
-        for (int i = threadIdx.x; i < r; i += blockDim.x) {
-          const Real tmp = Mrr[i + ld * j];
-          Mrr[i + ld * j] = Mrr[i + ld * pj];
-          Mrr[i + ld * pj] = tmp;
-        }
-      __syncthreads();
-    }
+    int* pinv = bchild;
+    for (int j = threadIdx.x; j < r; j += blockDim.x) pinv[j] = j;  // a singular block repeats rows
+    __syncthreads();
+    for (int j = threadIdx.x; j < r; j += blockDim.x) pinv[piv[j]] = j;
+    __syncthreads();
     Real* Lo = fac + fac_L(k, r);
     Real* Uo = fac + fac_U(k, r);
     Real* Xo = fac + fac_X(k, r);
-    // U_f = X^{-1} K_r_sn (r x k) and L_f = K_sn_r X^{-1} (k x r), to the record
+    // U_f = X^{-1} K_r_sn (r x k) and L_f = K_sn_r X^{-1} (k x r), to the
+    // record, with X^{-1}(a, b) = M(piv[a], pinv[b]):
+    //   U_f(i, j) = sum_c M(piv[i], c) K_r_sn(piv[c], j)
+    //   L_f(i, j) = sum_l K_sn_r(i, l) M(piv[l], pinv[j])
     for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
       const int i = e % r, j = e / r;
+      const Real* mrow = Mrr + piv[i];
       Real acc = 0;
-      for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
+      for (int c = 0; c < r; ++c) acc += mrow[ld * c] * Mrs[piv[c] + ld * j];
       Uo[e] = acc;
     }
     for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
       const int i = e % k, j = e / k;
+      const Real* mcol = Mrr + ld * pinv[j];
       Real acc = 0;
-      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrr[l + ld * j];
+      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * mcol[piv[l]];
       Lo[e] = acc;
     }
     for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
       const int i = e % r, j = e / r;
-      Xo[e] = Mrr[i + ld * j];
+      Xo[e] = Mrr[piv[i] + ld * pinv[j]];
     }
     __syncthreads();  // U_f is read back below (same CTA)
     // E = Mss - K_sn_r U_f  (k x k)

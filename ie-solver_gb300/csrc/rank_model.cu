@@ -131,9 +131,17 @@ __global__ void __launch_bounds__(kMlpThreads) infer_kernel(const float* W, cons
   }
 }
 
+// Gradient partials, deterministic: each warp owns a private gradient in
+// shared memory (within a warp every entry belongs to one lane, so no
+// atomics), the block sums its warps in order into partial[block], and
+// grad_reduce_kernel sums the blocks in order.  Samples go to warps by a
+// fixed rule, so the result does not depend on scheduling.
+constexpr int kGradBlocks = 152;
+constexpr int kPartial = kRankWeights + 1;  // a block's gradient, then its squared error
+
 __global__ void __launch_bounds__(kMlpThreads) grad_kernel(const float* W, const float* feats,
                                                            const float* targets, int count,
-                                                           float* grad, float* loss_sum) {
+                                                           float* partial) {
   extern __shared__ __align__(16) float smem[];
   SharedMlp m;
   load_mlp(W, smem, &m, true);
@@ -142,8 +150,10 @@ __global__ void __launch_bounds__(kMlpThreads) grad_kernel(const float* W, const
   float* h1 = xw + kF;
   float* h2 = h1 + kH;
   float* d2 = h2 + kH;  // dL/d(pre-activation of layer 2)
-  float* g = m.w3 + kH + kWarpsPerBlock * (kF + 3 * kH);  // block gradient, kRankWeights
-  for (int e = threadIdx.x; e < kRankWeights; e += blockDim.x) g[e] = 0.f;
+  float* gall = m.w3 + kH + kWarpsPerBlock * (kF + 3 * kH);  // kWarpsPerBlock gradients
+  float* g = gall + (size_t)warp * kRankWeights;
+  __shared__ float wl[kWarpsPerBlock];
+  for (int e = threadIdx.x; e < kWarpsPerBlock * kRankWeights; e += blockDim.x) gall[e] = 0.f;
   __syncthreads();
   float lsum = 0.f;
   const float scale = 1.f / (float)count;
@@ -154,22 +164,22 @@ __global__ void __launch_bounds__(kMlpThreads) grad_kernel(const float* W, const
     const float t = targets[i];
     lsum += (y - t) * (y - t);
     const float dz = 2.f * (y - t) * y * (1.f - y) * scale;
-    if (lane == 0) atomicAdd(&g[kOffB3], dz);
+    if (lane == 0) g[kOffB3] += dz;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
       const int u = lane + 32 * s;
-      atomicAdd(&g[kOffW3 + u], dz * h2[u]);
+      g[kOffW3 + u] += dz * h2[u];
       const float du = h2[u] > 0.f ? dz * m.w3[u] : 0.f;
       d2[u] = du;
-      atomicAdd(&g[kOffB2 + u], du);
+      g[kOffB2 + u] += du;
     }
     __syncwarp();
     // dW2[u][j] = d2[u] h1[j]: lane covers columns j = lane, lane + 32
     for (int u = 0; u < kH; ++u) {
       const float du = d2[u];
       if (du == 0.f) continue;
-      atomicAdd(&g[kOffW2 + u * kH + lane], du * h1[lane]);
-      atomicAdd(&g[kOffW2 + u * kH + lane + 32], du * h1[lane + 32]);
+      g[kOffW2 + u * kH + lane] += du * h1[lane];
+      g[kOffW2 + u * kH + lane + 32] += du * h1[lane + 32];
     }
     // d1[j] = sum_u W2[u][j] d2[u] (h1[j] > 0)
 #pragma unroll
@@ -178,16 +188,40 @@ __global__ void __launch_bounds__(kMlpThreads) grad_kernel(const float* W, const
       float a = 0.f;
       for (int u = 0; u < kH; ++u) a += m.w2[u * kH + j] * d2[u];
       const float d1 = h1[j] > 0.f ? a : 0.f;
-      atomicAdd(&g[kOffB1 + j], d1);
+      g[kOffB1 + j] += d1;
 #pragma unroll
-      for (int q = 0; q < kF; ++q) atomicAdd(&g[kOffW1 + j * kF + q], d1 * xw[q]);
+      for (int q = 0; q < kF; ++q) g[kOffW1 + j * kF + q] += d1 * xw[q];
     }
     __syncwarp();
   }
+  if (lane == 0) wl[warp] = lsum;  // every lane holds the warp's sum (y is on every lane)
   __syncthreads();
-  for (int e = threadIdx.x; e < kRankWeights; e += blockDim.x)
-    if (g[e] != 0.f) atomicAdd(&grad[e], g[e]);
-  if (lane == 0) atomicAdd(loss_sum, lsum);
+  float* out = partial + (size_t)blockIdx.x * kPartial;
+  for (int e = threadIdx.x; e < kRankWeights; e += blockDim.x) {
+    float a = 0.f;
+    for (int w = 0; w < kWarpsPerBlock; ++w) a += gall[(size_t)w * kRankWeights + e];
+    out[e] = a;
+  }
+  if (threadIdx.x == 0) {
+    float a = 0.f;
+    for (int w = 0; w < kWarpsPerBlock; ++w) a += wl[w];
+    out[kRankWeights] = a;
+  }
+}
+
+__global__ void grad_reduce_kernel(const float* partial, int blocks, float* grad,
+                                   float* loss_sum) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kPartial) return;
+  float a = 0.f;
+  for (int b = 0; b < blocks; ++b) a += partial[(size_t)b * kPartial + e];
+  if (e < kRankWeights) grad[e] = a;
+  else *loss_sum = a;
+}
+
+int grad_blocks(int count) {
+  const int g = (count + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  return g < 1 ? 1 : (g > kGradBlocks ? kGradBlocks : g);
 }
 
 __global__ void adam_kernel(float* W, const float* grad, float* m, float* v, float b1t, float b2t,
@@ -228,15 +262,20 @@ cudaError_t rank_predict(const float* weights, const float* features, int count,
   return cudaGetLastError();
 }
 
+size_t rank_gradient_scratch(int count) { return (size_t)grad_blocks(count) * kPartial; }
+
 cudaError_t rank_gradient(const float* weights, const float* features, const float* targets,
-                          int count, float* grad, float* loss_sum, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(float) * kRankWeights, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(loss_sum, 0, sizeof(float), st);
-  if (e != cudaSuccess || count <= 0) return e;
-  const size_t smem = mlp_smem(true) + sizeof(float) * kRankWeights;
+                          int count, float* grad, float* loss_sum, float* scratch,
+                          cudaStream_t st) {
+  if (count <= 0) {
+    cudaError_t e = cudaMemsetAsync(grad, 0, sizeof(float) * kRankWeights, st);
+    return e == cudaSuccess ? cudaMemsetAsync(loss_sum, 0, sizeof(float), st) : e;
+  }
+  const int blocks = grad_blocks(count);
+  const size_t smem = mlp_smem(true) + sizeof(float) * kWarpsPerBlock * kRankWeights;
   set_smem_once<grad_kernel>();
-  grad_kernel<<<grid_for(count), kMlpThreads, smem, st>>>(weights, features, targets, count, grad,
-                                                          loss_sum);
+  grad_kernel<<<blocks, kMlpThreads, smem, st>>>(weights, features, targets, count, scratch);
+  grad_reduce_kernel<<<(kPartial + 255) / 256, 256, 0, st>>>(scratch, blocks, grad, loss_sum);
   return cudaGetLastError();
 }
 

@@ -31,9 +31,12 @@ cudaError_t rank_predict(const float* weights, const float* features, int count,
                          cudaStream_t st);
 // Gradient of the mean squared error of the rank fraction over `count`
 // samples into grad (kRankWeights floats, overwritten) and the summed
-// squared error into *loss_sum (device pointer, overwritten).
+// squared error into *loss_sum (device pointer, overwritten).  Bit-for-bit
+// reproducible (no atomics).  scratch: rank_gradient_scratch(count) floats.
+size_t rank_gradient_scratch(int count);
 cudaError_t rank_gradient(const float* weights, const float* features, const float* targets,
-                          int count, float* grad, float* loss_sum, cudaStream_t st);
+                          int count, float* grad, float* loss_sum, float* scratch,
+                          cudaStream_t st);
 // One Adam step (step t >= 1) over the weights with moment buffers m, v.
 cudaError_t rank_adam(float* weights, const float* grad, float* m, float* v, int t, float lr,
                       cudaStream_t st);

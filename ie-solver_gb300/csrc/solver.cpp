@@ -2556,7 +2556,7 @@ rs_status rs_rank_samples(const rs_solver* s, float* features, float* targets, i
 
 // Device copies of a training set for the rank-model entry points.
 struct RankSet {
-  DevBuf<float> w, x, y, g, m, v, loss;
+  DevBuf<float> w, x, y, g, m, v, loss, part;
 };
 
 static rs_status rank_upload(rs_solver* s, RankSet& R, const float* weights,
@@ -2590,8 +2590,9 @@ rs_status rs_rank_train(rs_solver* s, const float* features, const float* target
   CU(R.v.ensure(kRankWeights));
   CU(cudaMemsetAsync(R.m.p, 0, sizeof(float) * kRankWeights, s->stream));
   CU(cudaMemsetAsync(R.v.p, 0, sizeof(float) * kRankWeights, s->stream));
+  CU(R.part.ensure(rank_gradient_scratch(count)));
   for (int e = 1; e <= epochs; ++e) {
-    CU(rank_gradient(R.w.p, R.x.p, R.y.p, count, R.g.p, R.loss.p, s->stream));
+    CU(rank_gradient(R.w.p, R.x.p, R.y.p, count, R.g.p, R.loss.p, R.part.p, s->stream));
     CU(rank_adam(R.w.p, R.g.p, R.m.p, R.v.p, e, lr, s->stream));
   }
   float ls = 0;
@@ -2622,7 +2623,8 @@ rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* feat
   if (!s || !weights || !features || !targets || !grad || count < 1) return RS_ERR_ARG;
   RankSet R;
   RSCHK(rank_upload(s, R, weights, features, targets, count));
-  CU(rank_gradient(R.w.p, R.x.p, R.y.p, count, R.g.p, R.loss.p, s->stream));
+  CU(R.part.ensure(rank_gradient_scratch(count)));
+  CU(rank_gradient(R.w.p, R.x.p, R.y.p, count, R.g.p, R.loss.p, R.part.p, s->stream));
   float ls = 0;
   CU(cudaMemcpyAsync(grad, R.g.p, sizeof(float) * kRankWeights, cudaMemcpyDeviceToHost,
                      s->stream));

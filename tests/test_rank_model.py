@@ -132,6 +132,26 @@ def test_gradient_matches_torch_autograd(solver_lib):
 
 
 @pytest.mark.gpu
+def test_gradient_and_training_are_reproducible(solver_lib):
+    """The gradient sums have a fixed order (no atomics): two calls, and two
+    trainings from the same start, give bit-identical results."""
+    from rskel import geometry as g
+
+    capi = solver_lib
+    rng = np.random.default_rng(8)
+    X = _features(rng, 5000)
+    t = rng.uniform(0.05, 0.9, 5000).astype(np.float32)
+    s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
+    w0 = capi.rank_model_init(3)
+    g1, l1 = s.rank_gradient(w0, X, t)
+    g2, l2 = s.rank_gradient(w0, X, t)
+    assert np.array_equal(g1, g2) and l1 == l2
+    wa, la = s.rank_train(X, t, w0, epochs=50, lr=3e-3)
+    wb, lb = s.rank_train(X, t, w0, epochs=50, lr=3e-3)
+    assert np.array_equal(wa, wb) and la == lb
+
+
+@pytest.mark.gpu
 def test_adam_kernel_matches_oracle(solver_lib):
     from rskel import geometry as g
 
@@ -150,8 +170,9 @@ def test_adam_kernel_matches_oracle(solver_lib):
         g1 = gr if g1 is None else g1
         w, m, v = RM.adam_step(w, gr, m, v, step, 1e-3)
     # Adam moves a weight by about lr per step whatever its gradient's size:
-    # compare the moves where the gradient's sign is well determined (fp32
-    # atomics may flip the sign of a gradient near zero), and bound the rest
+    # compare the moves where the gradient's sign is well determined (FP32
+    # sums in another order may flip the sign of a gradient near zero), and
+    # bound the rest
     sure = np.abs(g1) > 1e-3 * np.abs(g1).max()
     assert sure.sum() > 1000
     assert np.abs((w3 - w0) - (w - w0))[sure].max() <= 2e-5
