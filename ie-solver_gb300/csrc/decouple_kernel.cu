@@ -140,37 +140,45 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     // partial pivoting), so that U_f, L_f and the solve's diagonal step are
     // matrix products spread over the whole CTA instead of one warp-serial
     // triangular solve per column.  The refinement absorbs the explicit
-    // inverse's slightly larger rounding error.  Rows are not swapped: step
-    // j takes the unused row piv[j] with the largest |X(piv[j], j)| (the
-    // first on ties), and the in-place update leaves M with
-    // X^{-1}(a, b) = M(piv[a], pinv[b]).  Column j + 1 and the scaled pivot
-    // row go through double buffers, so a step takes two CTA barriers.  The
+    // inverse's slightly larger rounding error.  Rows are not moved: step j
+    // takes the row piv[j] with the largest |X(piv[j], j)| among those not
+    // yet pivot rows, and the in-place update leaves M with
+    // X^{-1}(a, b) = M(piv[a], pinv[b]).  Ties go to the row that
+    // dgetrf-style row interchanges would hold at the smallest position
+    // (pos[] tracks those positions), so the pivot sequence is that of
+    // elimination with explicit swaps.  Column j + 1 and the scaled pivot row
+    // go through double buffers, so a step takes two CTA barriers.  The
     // assembly's index arrays are free by now and hold the buffers.
     float* colbuf[2] = {reinterpret_cast<float*>(bchild), reinterpret_cast<float*>(bidx)};
     float* rowbuf[2] = {reinterpret_cast<float*>(bld), reinterpret_cast<float*>(order)};
-    int* used = reinterpret_cast<int*>(bbase);
+    int* pos = reinterpret_cast<int*>(bbase);  // row -> position (>= j: not yet a pivot row)
+    int* row_at = pos + n;                     // position -> row
     for (int i = threadIdx.x; i < r; i += blockDim.x) {
       colbuf[0][i] = Mrr[i];
-      used[i] = 0;
+      pos[i] = i;
+      row_at[i] = i;
     }
     __syncthreads();
     for (int j = 0; j < r; ++j) {
       const int buf = j & 1;
       // every warp finds the pivot row itself (no barrier for a broadcast)
       float best = -1.f;
-      int bi = r;
+      int bi = r, bp = r;
       for (int i = lane; i < r; i += 32) {
+        const int ps = pos[i];
+        if (ps < j) continue;
         const float v = fabsf(colbuf[buf][i]);
-        if (!used[i] && v > best) { best = v; bi = i; }
+        if (v > best || (v == best && ps < bp)) { best = v; bi = i; bp = ps; }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(0xffffffffu, best, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+        if (ov > best || (ov == best && op < bp)) { best = ov; bi = oi; bp = op; }
       }
       const bool ok = best > 0.f && isfinite(best) && bi < r;
-      const int pr = ok ? bi : j;  // a singular block: any row, flagged
+      const int pr = ok ? bi : row_at[j];  // a singular block: any row, flagged
       if (threadIdx.x == 0) {
         piv[j] = pr;
         if (!ok) scal[0] = 1.0;
@@ -180,8 +188,15 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
       for (int c = threadIdx.x; c < r; c += blockDim.x)
         rowbuf[buf][c] = c == j ? inv : Mrr[pr + ld * c] * inv;
       __syncthreads();
-      // (every warp has read `used` for this step by now)
-      if (threadIdx.x == 0) used[pr] = 1;
+      // (every warp has read pos for this step by now): the interchange of
+      // positions j and pos[pr]
+      if (threadIdx.x == 0) {
+        const int q = row_at[j], pp = pos[pr];
+        row_at[pp] = q;
+        pos[q] = pp;
+        row_at[j] = pr;
+        pos[pr] = j;
+      }
       for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
         const int i = e % r, c = e / r;
         const Real m = c == j ? (Real)0 : Mrr[i + ld * c];
@@ -199,27 +214,33 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     Real* Lo = fac + fac_L(k, r);
     Real* Uo = fac + fac_U(k, r);
     Real* Xo = fac + fac_X(k, r);
+    // X^{-1}(a, b) = M(piv[a], pinv[b]) to the record, then back over M in
+    // its own order (a CTA reads its own global writes after the barrier)
+    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+      const int i = e % r, j = e / r;
+      Xo[e] = Mrr[piv[i] + ld * pinv[j]];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+      const int i = e % r, j = e / r;
+      Mrr[i + ld * j] = Xo[e];
+    }
+    __syncthreads();
     // U_f = X^{-1} K_r_sn (r x k) and L_f = K_sn_r X^{-1} (k x r), to the
-    // record, with X^{-1}(a, b) = M(piv[a], pinv[b]):
-    //   U_f(i, j) = sum_c M(piv[i], c) K_r_sn(piv[c], j)
-    //   L_f(i, j) = sum_l K_sn_r(i, l) M(piv[l], pinv[j])
+    // record.  The sums run over the DOFs in their own order: in pivot order
+    // the Stokes x / y pairs no longer cancel early, and the FP32
+    // factorization loses accuracy.
     for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
       const int i = e % r, j = e / r;
-      const Real* mrow = Mrr + piv[i];
       Real acc = 0;
-      for (int c = 0; c < r; ++c) acc += mrow[ld * c] * Mrs[piv[c] + ld * j];
+      for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
       Uo[e] = acc;
     }
     for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
       const int i = e % k, j = e / k;
-      const Real* mcol = Mrr + ld * pinv[j];
       Real acc = 0;
-      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * mcol[piv[l]];
+      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrr[l + ld * j];
       Lo[e] = acc;
-    }
-    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-      const int i = e % r, j = e / r;
-      Xo[e] = Mrr[piv[i] + ld * pinv[j]];
     }
     __syncthreads();  // U_f is read back below (same CTA)
     // E = Mss - K_sn_r U_f  (k x k)
