@@ -76,17 +76,22 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   const Real* L = fac + fac_L(k, r);
   const Real* U = fac + fac_U(k, r);
   const Real* X = fac + fac_X(k, r);
-  // The box's factor record (T, L, U and X_rr's LU, contiguous) is copied to
-  // shared memory in one coalesced pass: the products and the triangular
-  // solves below then read it without a global round trip per step.
+  // The box's factor record (T, L, U, then X_rr) is copied to shared memory
+  // in one coalesced pass: the products and the triangular solves below then
+  // read it without a global round trip per step.  In FP32, X_rr (the
+  // record's largest block, an explicit inverse) stays in place: its product
+  // reads it coalesced, one row per thread and column step, and leaving it
+  // out lets more boxes of a level run at once.  The FP64 LU solve, a chain
+  // of dependent steps, reads it from shared memory.
+  constexpr bool kStageX = sizeof(Real) == 8;
   if (p.stage_fac) {
-    const int len = (int)(fac_X(k, r) + (int64_t)r * r);
+    const int len = (int)(fac_X(k, r) + (kStageX ? (int64_t)r * r : 0));
     Real* fsh = carve<Real>(sp, len);
     for (int e = threadIdx.x; e < len; e += blockDim.x) fsh[e] = fac[e];
     T = fsh + fac_T(k, r);
     L = fsh + fac_L(k, r);
     U = fsh + fac_U(k, r);
-    X = fsh + fac_X(k, r);
+    if (kStageX) X = fsh + fac_X(k, r);
   }
   Real* x = reinterpret_cast<Real*>(p.x);
   const int* sk = p.dofs + t.skel_off;
@@ -163,7 +168,9 @@ void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cuda
   size_t smem = 3 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
                 ((sizeof(int) * nmax + 15) & ~size_t(15)) + 64;
   SweepParams q = p;
-  const size_t fb = ((size_t)fac_reserve(nmax) * es + 15) & ~size_t(15);
+  // FP32 stages T, L, U (3 k r <= 3 n^2 / 4), FP64 the whole record
+  const size_t fe = fp32 ? 3 * (size_t)nmax * nmax / 4 + 8 : (size_t)fac_reserve(nmax);
+  const size_t fb = (fe * es + 15) & ~size_t(15);
   q.stage_fac = smem + fb <= (size_t)kSmemOptIn;
   if (q.stage_fac) smem += fb;
   if (fp32) {
