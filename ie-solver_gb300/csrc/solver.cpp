@@ -2472,7 +2472,7 @@ rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ct
   if (rc != RS_OK) return rc;
   double best = 1e300;
   int best_split = s->split_min_tasks;
-  for (int cand : {128, 256, 512, 1024, 1 << 30}) {
+  for (int cand : {1, 32, 128, 256, 512, 1024, 1 << 30}) {
     s->split_min_tasks = cand;
     double ms = 0;
     RSCHK(time_factor(&ms));
