@@ -326,28 +326,40 @@ __device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Re
       }
       __syncthreads();
     }
-    if (L.c0 == (i % L.cstep)) {
+    // The reflector of column i, by all of warp 0: its FP64 norm (which sets
+    // the rank) is a chain of mr - i - 1 conversions and FP64 multiply-adds,
+    // on the FP64 pipe's one warp instruction per 16 cycles per SM; over 32
+    // lanes instead of one team it is a few per lane and a shuffle tree.
+    if (warp == 0) {
       double xs = 0.0;
-      for (int r = i + 1 + t; r < mr; r += ts) { const double a = (double)A[(size_t)r * ld + i]; xs += a * a; }
-      xs = team_sum<TS>(xs);
+      for (int r = i + 1 + lane; r < mr; r += 32) {
+        const double a = (double)A[(size_t)r * ld + i];
+        xs += a * a;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, o);
       const double alpha = (double)A[(size_t)i * ld + i];
       const double nrm = sqrt(alpha * alpha + xs);  // |R_ii|, sets the rank
       int stop = 0;
       if (i == 0) {
-        if (t == 0) S.scal[2] = fabs(tol * nrm);
+        if (lane == 0) S.scal[2] = fabs(tol * nrm);
       } else if (nrm < S.scal[2]) {
         stop = 1;
       }
-      Real tau = 0, scale = 0;
+      Real tau = 0, scale = 0, beta = 0;
       if (!stop && xs > 0.0) {
         const Real a = (Real)alpha;
-        const Real beta = -copysign((Real)nrm, a);
+        beta = -copysign((Real)nrm, a);
         tau = (beta - a) / beta;
         scale = (Real)1 / (a - beta);
-        if (t == 0) A[(size_t)i * ld + i] = beta;
       }
-      for (int r = i + 1 + t; r < mr; r += ts) v[r] = A[(size_t)r * ld + i] * scale;
-      if (t == 0) { S.rs[0] = tau; S.is[0] = stop; }
+      for (int r = i + 1 + lane; r < mr; r += 32) v[r] = A[(size_t)r * ld + i] * scale;
+      __syncwarp();
+      if (lane == 0) {
+        if (!stop && xs > 0.0) A[(size_t)i * ld + i] = beta;
+        S.rs[0] = tau;
+        S.is[0] = stop;
+      }
     }
     __syncthreads();
     if (S.is[0] != 0) { k = i; break; }
