@@ -24,6 +24,30 @@
 
 namespace rskel {
 
+// The elements e = threadIdx.x, threadIdx.x + blockDim.x, ... of a
+// column-major rows x cols tile as (i, j) = (e % rows, e / rows), stepped
+// without an integer division per element (a division by a runtime value
+// is a long ALU sequence, and these loops run once per elimination step).
+// rows must be positive.
+struct TileWalk {
+  int i, j, di, dj, rows;
+  __device__ __forceinline__ explicit TileWalk(int rows_) : rows(rows_) {
+    i = (int)threadIdx.x % rows;
+    j = (int)threadIdx.x / rows;
+    di = (int)blockDim.x % rows;
+    dj = (int)blockDim.x / rows;
+  }
+  __device__ __forceinline__ int e() const { return i + rows * j; }
+  __device__ __forceinline__ void next() {
+    i += di;
+    j += dj;
+    if (i >= rows) {
+      i -= rows;
+      ++j;
+    }
+  }
+};
+
 template <class Real>
 __host__ __device__ size_t dec_smem_bytes(int n, bool tile_in_smem) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
@@ -82,17 +106,18 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   }
   __syncthreads();
   // Assemble Ktilde in skeleton-first order.
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    const int a = e % n, b = e / n;
-    const int ia = order[a], ib = order[b];
-    Real val;
-    if (bchild[ia] == bchild[ib] && bbase[ia] >= 0) {
-      val = E_in[bbase[ia] + bidx[ia] + (int64_t)bld[ia] * bidx[ib]];
-    } else {
-      val = kernel_dofs<Real>(p.pde, act, ia, act, ib);
+  if (n > 0)
+    for (TileWalk w(n); w.j < n; w.next()) {
+      const int a = w.i, b = w.j;
+      const int ia = order[a], ib = order[b];
+      Real val;
+      if (bchild[ia] == bchild[ib] && bbase[ia] >= 0) {
+        val = E_in[bbase[ia] + bidx[ia] + (int64_t)bld[ia] * bidx[ib]];
+      } else {
+        val = kernel_dofs<Real>(p.pde, act, ia, act, ib);
+      }
+      M[a + (size_t)n * b] = val;
     }
-    M[a + (size_t)n * b] = val;
-  }
   __syncthreads();
   Real* E_out = reinterpret_cast<Real*>(p.epool) + t.e_off;
   if (k == 0) {
@@ -108,31 +133,34 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   Real* Mrs = M + k;
   Real* Mrr = M + k + ld * k;
   // 1) K_r_sn = Mrs - T^T Mss  (r x k), in place
-  for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
-    const int i = e % r, j = e / r;
-    Real acc = Mrs[i + ld * j];
-    for (int l = 0; l < k; ++l) acc -= T[l + (size_t)k * i] * Mss[l + ld * j];
-    Mrs[i + ld * j] = acc;
-  }
+  if (r > 0)
+    for (TileWalk w(r); w.j < k; w.next()) {
+      const int i = w.i, j = w.j;
+      Real acc = Mrs[i + ld * j];
+      for (int l = 0; l < k; ++l) acc -= T[l + (size_t)k * i] * Mss[l + ld * j];
+      Mrs[i + ld * j] = acc;
+    }
   __syncthreads();
   // 2) X_rr = Mrr - T^T Msr - K_r_sn T  (r x r), in place
-  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-    const int i = e % r, j = e / r;
-    Real a1 = 0, a2 = 0;
-    for (int l = 0; l < k; ++l) {
-      a1 += T[l + (size_t)k * i] * Msr[l + ld * j];
-      a2 += Mrs[i + ld * l] * T[l + (size_t)k * j];
+  if (r > 0)
+    for (TileWalk w(r); w.j < r; w.next()) {
+      const int i = w.i, j = w.j;
+      Real a1 = 0, a2 = 0;
+      for (int l = 0; l < k; ++l) {
+        a1 += T[l + (size_t)k * i] * Msr[l + ld * j];
+        a2 += Mrs[i + ld * l] * T[l + (size_t)k * j];
+      }
+      Mrr[i + ld * j] = (Mrr[i + ld * j] - a1) - a2;
     }
-    Mrr[i + ld * j] = (Mrr[i + ld * j] - a1) - a2;
-  }
   __syncthreads();
   // 3) K_sn_r = Msr - Mss T  (k x r), in place
-  for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
-    const int i = e % k, j = e / k;
-    Real acc = Msr[i + ld * j];
-    for (int l = 0; l < k; ++l) acc -= Mss[i + ld * l] * T[l + (size_t)k * j];
-    Msr[i + ld * j] = acc;
-  }
+  if (k > 0)
+    for (TileWalk w(k); w.j < r; w.next()) {
+      const int i = w.i, j = w.j;
+      Real acc = Msr[i + ld * j];
+      for (int l = 0; l < k; ++l) acc -= Mss[i + ld * l] * T[l + (size_t)k * j];
+      Msr[i + ld * j] = acc;
+    }
   __syncthreads();
   if (threadIdx.x == 0) scal[0] = 0.0;
   if constexpr (sizeof(Real) == 4) {
@@ -197,13 +225,14 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
         row_at[j] = pr;
         pos[pr] = j;
       }
-      for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-        const int i = e % r, c = e / r;
-        const Real m = c == j ? (Real)0 : Mrr[i + ld * c];
-        const Real v = i == pr ? rowbuf[buf][c] : m - colbuf[buf][i] * rowbuf[buf][c];
-        Mrr[i + ld * c] = v;
-        if (c == j + 1) colbuf[buf ^ 1][i] = v;
-      }
+      if (r > 0)
+        for (TileWalk w(r); w.j < r; w.next()) {
+          const int i = w.i, c = w.j;
+          const Real m = c == j ? (Real)0 : Mrr[i + ld * c];
+          const Real v = i == pr ? rowbuf[buf][c] : m - colbuf[buf][i] * rowbuf[buf][c];
+          Mrr[i + ld * c] = v;
+          if (c == j + 1) colbuf[buf ^ 1][i] = v;
+        }
       __syncthreads();
     }
     int* pinv = bchild;
@@ -216,40 +245,50 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     Real* Xo = fac + fac_X(k, r);
     // X^{-1}(a, b) = M(piv[a], pinv[b]) to the record, then back over M in
     // its own order (a CTA reads its own global writes after the barrier)
-    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-      const int i = e % r, j = e / r;
-      Xo[e] = Mrr[piv[i] + ld * pinv[j]];
-    }
+    if (r > 0)
+      for (TileWalk w(r); w.j < r; w.next()) {
+        const int i = w.i, j = w.j;
+        const int e = w.e();
+        Xo[e] = Mrr[piv[i] + ld * pinv[j]];
+      }
     __syncthreads();
-    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-      const int i = e % r, j = e / r;
-      Mrr[i + ld * j] = Xo[e];
-    }
+    if (r > 0)
+      for (TileWalk w(r); w.j < r; w.next()) {
+        const int i = w.i, j = w.j;
+        const int e = w.e();
+        Mrr[i + ld * j] = Xo[e];
+      }
     __syncthreads();
     // U_f = X^{-1} K_r_sn (r x k) and L_f = K_sn_r X^{-1} (k x r), to the
     // record.  The sums run over the DOFs in their own order: in pivot order
     // the Stokes x / y pairs no longer cancel early, and the FP32
     // factorization loses accuracy.
-    for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
-      const int i = e % r, j = e / r;
-      Real acc = 0;
-      for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
-      Uo[e] = acc;
-    }
-    for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
-      const int i = e % k, j = e / k;
-      Real acc = 0;
-      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrr[l + ld * j];
-      Lo[e] = acc;
-    }
+    if (r > 0)
+      for (TileWalk w(r); w.j < k; w.next()) {
+        const int i = w.i, j = w.j;
+        const int e = w.e();
+        Real acc = 0;
+        for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
+        Uo[e] = acc;
+      }
+    if (k > 0)
+      for (TileWalk w(k); w.j < r; w.next()) {
+        const int i = w.i, j = w.j;
+        const int e = w.e();
+        Real acc = 0;
+        for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrr[l + ld * j];
+        Lo[e] = acc;
+      }
     __syncthreads();  // U_f is read back below (same CTA)
     // E = Mss - K_sn_r U_f  (k x k)
-    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
-      const int i = e % k, j = e / k;
-      Real acc = Mss[i + ld * j];
-      for (int l = 0; l < r; ++l) acc -= Msr[i + ld * l] * Uo[l + (size_t)r * j];
-      E_out[e] = acc;
-    }
+    if (k > 0)
+      for (TileWalk w(k); w.j < k; w.next()) {
+        const int i = w.i, j = w.j;
+        const int e = w.e();
+        Real acc = Mss[i + ld * j];
+        for (int l = 0; l < r; ++l) acc -= Msr[i + ld * l] * Uo[l + (size_t)r * j];
+        E_out[e] = acc;
+      }
     for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = j;
     if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
     return;
@@ -320,12 +359,13 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   }
   __syncthreads();
   // 6) E = Mss - K_sn_r U_f  (k x k), in place over Mss.
-  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
-    const int i = e % k, j = e / k;
-    Real acc = 0;
-    for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrs[l + ld * j];
-    Mss[i + ld * j] -= acc;
-  }
+  if (k > 0)
+    for (TileWalk w(k); w.j < k; w.next()) {
+      const int i = w.i, j = w.j;
+      Real acc = 0;
+      for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrs[l + ld * j];
+      Mss[i + ld * j] -= acc;
+    }
   __syncthreads();
   // 7) L_f = K_sn_r X^{-1}: solve X^T y = K_sn_r(i,:)^T per row (one warp per row).
   for (int i = warp; i < k; i += kWarps) {
@@ -353,20 +393,26 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   Real* Lo = fac + fac_L(k, r);
   Real* Uo = fac + fac_U(k, r);
   Real* Xo = fac + fac_X(k, r);
-  for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
-    const int i = e % k, j = e / k;
-    Lo[e] = Msr[i + ld * j];
-    const int i2 = e % r, j2 = e / r;
-    Uo[e] = Mrs[i2 + ld * j2];
-  }
-  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-    const int i = e % r, j = e / r;
-    Xo[e] = Mrr[i + ld * j];
-  }
-  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
-    const int i = e % k, j = e / k;
-    E_out[e] = Mss[i + ld * j];
-  }
+  if (k > 0)
+    for (TileWalk w(k); w.j < r; w.next()) {
+      const int i = w.i, j = w.j;
+      const int e = w.e();
+      Lo[e] = Msr[i + ld * j];
+      const int i2 = e % r, j2 = e / r;
+      Uo[e] = Mrs[i2 + ld * j2];
+    }
+  if (r > 0)
+    for (TileWalk w(r); w.j < r; w.next()) {
+      const int i = w.i, j = w.j;
+      const int e = w.e();
+      Xo[e] = Mrr[i + ld * j];
+    }
+  if (k > 0)
+    for (TileWalk w(k); w.j < k; w.next()) {
+      const int i = w.i, j = w.j;
+      const int e = w.e();
+      E_out[e] = Mss[i + ld * j];
+    }
   for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = piv[j];
   if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
 }
