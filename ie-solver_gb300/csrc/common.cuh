@@ -29,6 +29,30 @@ inline void set_smem_once() {
 }
 constexpr int kWarps = kThreads / 32;
 
+// The elements e = threadIdx.x, threadIdx.x + blockDim.x, ... of a
+// column-major rows x cols tile as (i, j) = (e % rows, e / rows), stepped
+// without an integer division per element (a division by a runtime value
+// is a long ALU sequence, and the kernels' tile loops run once per step).
+// rows must be positive.
+struct TileWalk {
+  int i, j, di, dj, rows;
+  __device__ __forceinline__ explicit TileWalk(int rows_) : rows(rows_) {
+    i = (int)threadIdx.x % rows;
+    j = (int)threadIdx.x / rows;
+    di = (int)blockDim.x % rows;
+    dj = (int)blockDim.x / rows;
+  }
+  __device__ __forceinline__ int e() const { return i + rows * j; }
+  __device__ __forceinline__ void next() {
+    i += di;
+    j += dj;
+    if (i >= rows) {
+      i -= rows;
+      ++j;
+    }
+  }
+};
+
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

@@ -24,30 +24,6 @@
 
 namespace rskel {
 
-// The elements e = threadIdx.x, threadIdx.x + blockDim.x, ... of a
-// column-major rows x cols tile as (i, j) = (e % rows, e / rows), stepped
-// without an integer division per element (a division by a runtime value
-// is a long ALU sequence, and these loops run once per elimination step).
-// rows must be positive.
-struct TileWalk {
-  int i, j, di, dj, rows;
-  __device__ __forceinline__ explicit TileWalk(int rows_) : rows(rows_) {
-    i = (int)threadIdx.x % rows;
-    j = (int)threadIdx.x / rows;
-    di = (int)blockDim.x % rows;
-    dj = (int)blockDim.x / rows;
-  }
-  __device__ __forceinline__ int e() const { return i + rows * j; }
-  __device__ __forceinline__ void next() {
-    i += di;
-    j += dj;
-    if (i >= rows) {
-      i -= rows;
-      ++j;
-    }
-  }
-};
-
 template <class Real>
 __host__ __device__ size_t dec_smem_bytes(int n, bool tile_in_smem) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };

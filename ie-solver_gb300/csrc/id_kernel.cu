@@ -167,8 +167,8 @@ __device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S
     S.kind[i] = kind;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < kChunk * n; e += blockDim.x) {
-    int i = e / n, j = e % n;
+  for (TileWalk w(n); w.j < kChunk; w.next()) {  // row i = w.j, column j = w.i
+    const int i = w.j, j = w.i;
     int kind = S.kind[i];
     Real val = (Real)0;
     if (kind == 0 || kind == 2) val = kernel_dofs<Real>(p.pde, S.row, i, S.act, j);
@@ -659,8 +659,8 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
     for (int c0 = 0; c0 < m; c0 += kChunk) {
       const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
       fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
-      for (int e = threadIdx.x; e < cnt * n; e += blockDim.x) {
-        const int i = e / n, j = e % n;
+      for (TileWalk w(n); w.j < cnt; w.next()) {
+        const int i = w.j, j = w.i;
         if constexpr (kSplit) Yg[(size_t)(c0 + i) * wld + j] = S.C[(size_t)i * ld + j];
         else S.R[(size_t)(c0 + i) * ld + j] = S.C[(size_t)i * ld + j];
       }
@@ -679,9 +679,9 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
     for (int c0 = 0; c0 < m; c0 += kChunk) {
       const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
       fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
-      for (int e = threadIdx.x; e < kChunk * lp; e += blockDim.x) {
-        const int ii = e / lp, r = e % lp;
-        sg[e] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
+      for (TileWalk w(lp); w.j < kChunk; w.next()) {
+        const int ii = w.j, r = w.i;
+        sg[w.e()] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
       }
       __syncthreads();
       const long long c1 = clock64();
@@ -1038,9 +1038,9 @@ __global__ void __launch_bounds__(kThreads) id_wide_sketch_kernel(IdParams p,
   for (int c0 = it.r0; c0 < it.r1; c0 += kChunk) {
     const int cnt = it.r1 - c0 < kChunk ? it.r1 - c0 : kChunk;
     fill_chunk<float>(p, tc, S, kWideCols, c0, cnt, ox, oy);
-    for (int e = threadIdx.x; e < kChunk * lp; e += blockDim.x) {
-      const int ii = e / lp, r = e % lp;
-      sg[e] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
+    for (TileWalk w(lp); w.j < kChunk; w.next()) {
+      const int ii = w.j, r = w.i;
+      sg[w.e()] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
     }
     __syncthreads();
 #pragma unroll
