@@ -47,12 +47,14 @@ __device__ void lu_solve_cols(const Real* X, const int* piv, int r, Real* y, int
 template <class Real>
 __device__ void diag_solve(const Real* X, const int* piv, int r, Real* xr, Real* xt, int cb) {
   if constexpr (sizeof(Real) == 4) {
-    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {
-      const int i = e % r, c = e / r;
-      Real acc = 0;
-      for (int l = 0; l < r; ++l) acc += X[i + (size_t)r * l] * xr[l + r * c];
-      xt[e] = acc;
-    }
+    if (r > 0)
+      for (TileWalk w(r); w.j < cb; w.next()) {
+        const int i = w.i, c = w.j;
+        const int e = w.e();
+        Real acc = 0;
+        for (int l = 0; l < r; ++l) acc += X[i + (size_t)r * l] * xr[l + r * c];
+        xt[e] = acc;
+      }
     __syncthreads();
     for (int e = threadIdx.x; e < r * cb; e += blockDim.x) xr[e] = xt[e];
   } else {
@@ -99,32 +101,36 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   for (int j = threadIdx.x; j < r; j += blockDim.x) piv[j] = p.piv[t.piv_off + j];
   for (int c0 = 0; c0 < p.nrhs; c0 += kRhsBlock) {
     const int cb = p.nrhs - c0 < kRhsBlock ? p.nrhs - c0 : kRhsBlock;
-    for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {
-      int i = e % k, c = e / k;
-      xs[i + k * c] = x[sk[i] + (size_t)p.ld * (c0 + c)];
-    }
-    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {
-      int i = e % r, c = e / r;
-      xr[i + r * c] = x[rd[i] + (size_t)p.ld * (c0 + c)];
-    }
+    if (k > 0)
+      for (TileWalk w(k); w.j < cb; w.next()) {
+        const int i = w.i, c = w.j;
+        xs[i + k * c] = x[sk[i] + (size_t)p.ld * (c0 + c)];
+      }
+    if (r > 0)
+      for (TileWalk w(r); w.j < cb; w.next()) {
+        const int i = w.i, c = w.j;
+        xr[i + r * c] = x[rd[i] + (size_t)p.ld * (c0 + c)];
+      }
     __syncthreads();
     if (p.mode == kUpSolve || p.mode == kUpPlain || p.mode == kUpTransU) {
-      for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {  // x_r -= T^T x_s
-        int i = e % r, c = e / r;
-        Real acc = 0;
-        for (int l = 0; l < k; ++l) acc += T[l + (size_t)k * i] * xs[l + k * c];
-        xr[i + r * c] -= acc;
-      }
+      if (r > 0)
+        for (TileWalk w(r); w.j < cb; w.next()) {  // x_r -= T^T x_s
+          const int i = w.i, c = w.j;
+          Real acc = 0;
+          for (int l = 0; l < k; ++l) acc += T[l + (size_t)k * i] * xs[l + k * c];
+          xr[i + r * c] -= acc;
+        }
       __syncthreads();
-      for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {
-        int i = e % k, c = e / k;
-        Real acc = 0;
-        if (p.mode == kUpTransU)  // x_s -= U^T x_r
-          for (int l = 0; l < r; ++l) acc += U[l + (size_t)r * i] * xr[l + r * c];
-        else  // x_s -= L x_r
-          for (int l = 0; l < r; ++l) acc += L[i + (size_t)k * l] * xr[l + r * c];
-        xs[i + k * c] -= acc;
-      }
+      if (k > 0)
+        for (TileWalk w(k); w.j < cb; w.next()) {
+          const int i = w.i, c = w.j;
+          Real acc = 0;
+          if (p.mode == kUpTransU)  // x_s -= U^T x_r
+            for (int l = 0; l < r; ++l) acc += U[l + (size_t)r * i] * xr[l + r * c];
+          else  // x_s -= L x_r
+            for (int l = 0; l < r; ++l) acc += L[i + (size_t)k * l] * xr[l + r * c];
+          xs[i + k * c] -= acc;
+        }
       __syncthreads();
       if (p.mode == kUpSolve) {
         diag_solve<Real>(X, piv, r, xr, xt, cb);
@@ -134,30 +140,34 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
       diag_solve<Real>(X, piv, r, xr, xt, cb);
       __syncthreads();
     } else {  // kDown
-      for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {  // x_r -= U x_s
-        int i = e % r, c = e / r;
-        Real acc = 0;
-        for (int l = 0; l < k; ++l) acc += U[i + (size_t)r * l] * xs[l + k * c];
-        xr[i + r * c] -= acc;
-      }
+      if (r > 0)
+        for (TileWalk w(r); w.j < cb; w.next()) {  // x_r -= U x_s
+          const int i = w.i, c = w.j;
+          Real acc = 0;
+          for (int l = 0; l < k; ++l) acc += U[i + (size_t)r * l] * xs[l + k * c];
+          xr[i + r * c] -= acc;
+        }
       __syncthreads();
-      for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {  // x_s -= T x_r
-        int i = e % k, c = e / k;
-        Real acc = 0;
-        for (int l = 0; l < r; ++l) acc += T[i + (size_t)k * l] * xr[l + r * c];
-        xs[i + k * c] -= acc;
-      }
+      if (k > 0)
+        for (TileWalk w(k); w.j < cb; w.next()) {  // x_s -= T x_r
+          const int i = w.i, c = w.j;
+          Real acc = 0;
+          for (int l = 0; l < r; ++l) acc += T[i + (size_t)k * l] * xr[l + r * c];
+          xs[i + k * c] -= acc;
+        }
       __syncthreads();
     }
     if (p.mode != kDiagOnly)
-      for (int e = threadIdx.x; e < k * cb; e += blockDim.x) {
-        int i = e % k, c = e / k;
-        x[sk[i] + (size_t)p.ld * (c0 + c)] = xs[i + k * c];
+      if (k > 0)
+        for (TileWalk w(k); w.j < cb; w.next()) {
+          const int i = w.i, c = w.j;
+          x[sk[i] + (size_t)p.ld * (c0 + c)] = xs[i + k * c];
+        }
+    if (r > 0)
+      for (TileWalk w(r); w.j < cb; w.next()) {
+        const int i = w.i, c = w.j;
+        x[rd[i] + (size_t)p.ld * (c0 + c)] = xr[i + r * c];
       }
-    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) {
-      int i = e % r, c = e / r;
-      x[rd[i] + (size_t)p.ld * (c0 + c)] = xr[i + r * c];
-    }
     __syncthreads();
   }
 }
