@@ -1003,6 +1003,12 @@ rs_status factor_impl(rs_solver* s) {
       if (S.slot < 0) S.e_ld = (int)S.active.size();
     }
     t_post += now_ms() - h2;
+    if (s->trace)
+      std::fprintf(stderr,
+                   "[rskel]   host level %2d: lists %.3f tasks %.3f sort %.3f launch %.3f wait %.3f "
+                   "post %.3f ms\n",
+                   lv, h_lists - h0, h_tasks - h_lists, h_sort - h_tasks, h1 - h_sort, h2 - h1,
+                   now_ms() - h2);
   }
   s->host_plan_ms = t_plan;
   s->host_wait_ms = t_wait;
@@ -1148,7 +1154,7 @@ rs_status factor_impl(rs_solver* s) {
     rs_status rc = factor_border<Real>(s);
     if (rc != RS_OK) return rc;
   } else if (!s->roots_h.empty()) {
-    s->root_inv = f32 && s->root_nmax <= kRootInvMax;
+    s->root_inv = f32 && s->cfg.root_inverse != 0 && s->root_nmax <= kRootInvMax;
     if (s->root_inv)
       launch_root_inverse((float*)F.epool.p, s->roots_dev.p, (int)s->roots_h.size(),
                           s->status.p, s->stream);
@@ -1838,6 +1844,7 @@ void rs_config_default(rs_config* c) {
   c->refine_verify = 1;
   c->refine_solver = 0;
   c->use_graphs = 1;
+  c->root_inverse = 1;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {

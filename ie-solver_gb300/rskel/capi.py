@@ -44,7 +44,8 @@ class RsConfig(ctypes.Structure):
                 ("fp32_id_tol", ctypes.c_double), ("device", ctypes.c_int),
                 ("fmm_order", ctypes.c_int), ("rank_headroom", ctypes.c_double),
                 ("rank_extra_rows", ctypes.c_int), ("refine_verify", ctypes.c_int),
-                ("refine_solver", ctypes.c_int), ("use_graphs", ctypes.c_int)]
+                ("refine_solver", ctypes.c_int), ("use_graphs", ctypes.c_int),
+                ("root_inverse", ctypes.c_int)]
 
 
 class RsStats(ctypes.Structure):
@@ -194,7 +195,7 @@ class Solver:
     def __init__(self, geo, pde, tol, leaf=64, npp=64, precision=RS_FP64, refine_tol=1e-12,
                  refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16, fmm_order=0,
                  rank_headroom=1.25, rank_extra_rows=12, refine_verify=1, refine_solver=0,
-                 use_graphs=1):
+                 use_graphs=1, root_inverse=1):
         self.sd = 2 if pde == RS_STOKES else 1
         self.cfg = default_config(pde=pde, solution_dimension=self.sd, id_tol=tol,
                                   max_leaf_dofs=leaf, num_proxy_points=npp,
@@ -203,7 +204,8 @@ class Solver:
                                   device=device, min_dofs_to_compress=min_dofs,
                                   fmm_order=fmm_order, rank_headroom=rank_headroom,
                                   rank_extra_rows=rank_extra_rows, refine_verify=refine_verify,
-                                  refine_solver=refine_solver, use_graphs=use_graphs)
+                                  refine_solver=refine_solver, use_graphs=use_graphs,
+                                  root_inverse=root_inverse)
         h = _vp()
         self._check(lib().rs_create(ctypes.byref(self.cfg), ctypes.byref(h)), None)
         self.h = h

@@ -82,6 +82,11 @@ typedef struct {
   int use_graphs;            /* 1 (default): the factorization's inverse (no holes) runs as
                                 one CUDA graph launch, captured on first use after each
                                 rs_factor; 0: plain launches */
+  int root_inverse;          /* RS_FP32_REFINE, root blocks of at most 128 DOFs: 1 (default)
+                                = inverted once per factorization (Gauss-Jordan with partial
+                                pivoting), one product per application; 0 = LU with partial
+                                pivoting and triangular solves (dgetrf/dgetrs, as FP64 and
+                                larger roots always do) */
 } rs_config;
 
 typedef struct rs_solver rs_solver;

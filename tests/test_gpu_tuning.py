@@ -46,3 +46,39 @@ def test_graph_inverse_is_bit_identical(solver_lib):
         assert np.array_equal(mu, mu2)
         out.append(mu)
     assert np.array_equal(out[0], out[1])
+
+
+def test_root_inverse_and_root_lu_agree(solver_lib):
+    """FP32 roots of at most 128 DOFs: the explicit inverse (Gauss-Jordan,
+    default) and LU with triangular solves give the same refined solution,
+    and the same FP32 preconditioner up to FP32 rounding (one refinement
+    step at most apart).  Also on a batch, where every tree has its own
+    root block."""
+    from rskel import geometry as g
+
+    capi = solver_lib
+    res = []
+    for ri in (1, 0):
+        s, F = _star(capi, g, root_inverse=ri, refine_max_iters=12)
+        s.factor()
+        mu, _ = s.solve(F)
+        st = s.stats()
+        assert st["num_skel_root"] <= 128
+        assert st["refine_residual"] <= 1e-10
+        res.append((mu, st["refine_iters"]))
+    (m1, i1), (m0, i0) = res
+    assert abs(i1 - i0) <= 1
+    assert np.linalg.norm(m1 - m0) / np.linalg.norm(m0) <= 1e-9
+    rng = np.random.default_rng(12)
+    geos = [g.random_star(int(rng.integers(1024, 4096)), rng) for _ in range(6)]
+    out = []
+    for ri in (1, 0):
+        s = capi.Solver(geos[0], capi.RS_LAPLACE, 1e-8, leaf=64, npp=64,
+                        precision=capi.RS_FP32_REFINE, refine_tol=1e-10, root_inverse=ri)
+        s.set_geometry_batch(geos)
+        F = np.concatenate([g.laplace_point_source(q, (2.0, 0.5)) for q in geos])
+        s.factor()
+        mu, _ = s.solve(F)
+        assert s.stats()["refine_residual"] <= 1e-10
+        out.append(mu)
+    assert np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[1]) <= 1e-9
