@@ -580,6 +580,189 @@ void launch_root_apply(const float* base, const RootTask* tasks, int count, cons
   root_apply_kernel<<<count, kThreads, 0, st>>>(base, tasks, dofs, x, ld, nrhs);
 }
 
+// ---------------------------------------------------------------------------
+// Explicit inverse of one large FP32 block (the bordered system's S, about
+// 1500 DOFs for 16 holes) by all SMs.  One CTA doing the whole LU in global
+// memory was most of a bordered solve's time.  Gauss-Jordan with partial
+// pivoting, the columns split over the CTAs of a cooperative launch: at step
+// j every CTA reads column j and picks the pivot row itself (the same
+// choice everywhere: the unused row with the largest |A(i, j)|, the first
+// on ties), reads the pivot row for its own columns, and after a grid
+// barrier updates its own columns; a second barrier closes the step.  Rows
+// are not moved, so A ends as M with A^{-1}(a, b) = M(piv[a], pinv[b]),
+// which the CTAs write out unpermuted.  Data other CTAs wrote are read past
+// L1 (ld.global.cg).  The grid barriers spin a bounded number of times:
+// on a timeout the kernel raises err and every CTA returns.
+// ---------------------------------------------------------------------------
+constexpr int kCoopThreads = 256;
+constexpr unsigned kBarrierSpins = 1u << 22;
+
+__device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    unsigned spins = 0;
+    int ok = 1;
+    while (*reinterpret_cast<volatile unsigned*>(count) < target) {
+      if (*reinterpret_cast<volatile int*>(err) != 0 || ++spins > kBarrierSpins) {
+        atomicExch(err, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+size_t coop_inverse_smem(int n, int grid) {
+  const int cols = (n + grid - 1) / grid;
+  return sizeof(float) * (size_t)n + 2 * sizeof(int) * (size_t)n + sizeof(float) * (size_t)cols;
+}
+
+__global__ void __launch_bounds__(kCoopThreads) coop_inverse_kernel(float* A, int n, float* Ainv,
+                                                                    unsigned* bar, int* err,
+                                                                    int* status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* col = reinterpret_cast<float*>(smem);     // column j, all rows
+  int* used = reinterpret_cast<int*>(col + n);      // row -> 1 once a pivot (then pinv)
+  int* piv = used + n;                              // step -> pivot row
+  float* rowv = reinterpret_cast<float*>(piv + n);  // scaled pivot row, own columns
+  __shared__ float red_v[kCoopThreads / 32];
+  __shared__ int red_i[kCoopThreads / 32];
+  __shared__ int s_p;
+  __shared__ float s_inv;
+  const int G = gridDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int per = (n + G - 1) / G;
+  const int c0 = blockIdx.x * per, c1 = min(n, c0 + per);
+  for (int i = tid; i < n; i += blockDim.x) used[i] = 0;
+  unsigned epoch = 0;
+  for (int j = 0; j < n; ++j) {
+    for (int i = tid; i < n; i += blockDim.x) col[i] = __ldcg(A + i + (size_t)n * j);
+    __syncthreads();
+    float best = -1.f;
+    int bi = n;
+    for (int i = tid; i < n; i += blockDim.x) {
+      const float v = fabsf(col[i]);
+      if (!used[i] && v > best) { best = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { red_v[warp] = best; red_i[warp] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < kCoopThreads / 32; ++w)
+        if (red_v[w] > best || (red_v[w] == best && red_i[w] < bi)) { best = red_v[w]; bi = red_i[w]; }
+      const bool ok = best > 0.f && isfinite(best) && bi < n;
+      if (!ok) {  // singular: flagged, continue with the first unused row
+        if (blockIdx.x == 0) atomicExch(status, 1);
+        bi = 0;
+        while (bi < n - 1 && used[bi]) ++bi;
+      }
+      s_p = bi;
+      const float d = col[bi];
+      s_inv = d != 0.f ? 1.f / d : 0.f;
+    }
+    __syncthreads();
+    const int p = s_p;
+    const float inv = s_inv;
+    for (int c = c0 + tid; c < c1; c += blockDim.x)
+      rowv[c - c0] = c == j ? inv : __ldcg(A + p + (size_t)n * c) * inv;
+    // every CTA has read column j and its part of row p
+    if (!grid_barrier(bar, ++epoch * (unsigned)G, err)) return;
+    if (tid == 0) {
+      used[p] = 1;
+      piv[j] = p;
+    }
+    for (int c = c0; c < c1; ++c) {
+      float* Ac = A + (size_t)n * c;
+      const float rc = rowv[c - c0];
+      for (int i = tid; i < n; i += blockDim.x) {
+        const float m = c == j ? 0.f : Ac[i];
+        Ac[i] = i == p ? rc : m - col[i] * rc;
+      }
+    }
+    if (!grid_barrier(bar, ++epoch * (unsigned)G, err)) return;
+  }
+  // pinv over used[] (no longer needed), then the own columns of A^{-1}
+  int* pinv = used;
+  for (int i = tid; i < n; i += blockDim.x) pinv[i] = i;  // a singular block repeats rows
+  __syncthreads();
+  for (int j = tid; j < n; j += blockDim.x) pinv[piv[j]] = j;
+  __syncthreads();
+  for (int b = c0; b < c1; ++b) {
+    const float* Mc = A + (size_t)n * pinv[b];
+    for (int a = tid; a < n; a += blockDim.x) Ainv[a + (size_t)n * b] = __ldcg(Mc + piv[a]);
+  }
+}
+
+// y[a] = sum_b Ainv(a, b) x[b], one thread per row, x staged in shared
+// memory a chunk at a time.
+__global__ void __launch_bounds__(128) dense_gemv_kernel(const float* Ainv, int n, const float* x,
+                                                         float* y) {
+  __shared__ float xs[1024];
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  float acc = 0.f;
+  for (int b0 = 0; b0 < n; b0 += 1024) {
+    const int nb = min(1024, n - b0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb; e += blockDim.x) xs[e] = x[b0 + e];
+    __syncthreads();
+    if (a < n)
+#pragma unroll 4
+      for (int b = 0; b < nb; ++b) acc += Ainv[a + (size_t)n * (b0 + b)] * xs[b];
+  }
+  if (a < n) y[a] = acc;
+}
+
+// CTAs of the cooperative launch: up to two per SM, as many as fit with the
+// shared memory n needs (0: n too large for it).
+int coop_inverse_grid(int n) {
+  int dev = 0, sms = 0, occ = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  const size_t smem = coop_inverse_smem(n, sms);  // at least what any grid of >= sms CTAs needs
+  if (smem + 1024 > (size_t)kSmemOptIn) return 0;
+  if (cudaFuncSetAttribute(coop_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, coop_inverse_kernel, kCoopThreads,
+                                                    smem) != cudaSuccess ||
+      occ < 1)
+    return 0;
+  return sms * (occ < 2 ? occ : 2);
+}
+
+cudaError_t launch_coop_inverse(float* a, int n, float* ainv, unsigned* bar, int* err,
+                                int* status, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  int grid = coop_inverse_grid(n);
+  if (grid <= 0) return cudaErrorInvalidValue;
+  if (grid > n) grid = n;
+  const size_t smem = coop_inverse_smem(n, grid);
+  cudaError_t e = cudaFuncSetAttribute(coop_inverse_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
+  void* args[] = {&a, &n, &ainv, &bar, &err, &status};
+  return cudaLaunchCooperativeKernel((const void*)coop_inverse_kernel, dim3(grid),
+                                     dim3(kCoopThreads), args, smem, st);
+}
+
+void launch_dense_gemv(const float* ainv, int n, const float* x, float* y, cudaStream_t st) {
+  if (n <= 0) return;
+  dense_gemv_kernel<<<(n + 127) / 128, 128, 0, st>>>(ainv, n, x, y);
+}
+
 template <class Real>
 static void launch_dense_solve_t(const Real* lu, int n, const int* piv, const int* idx, Real* x,
                                  int ld, int nrhs, cudaStream_t st) {

@@ -57,6 +57,7 @@ struct NodeState {
 template <class Real>
 struct Factor {
   DevBuf<Real> fac, epool, scratch, x, tmp, mU, mP, S, M, nv;
+  DevBuf<Real> Sinv, Mt;  // FP32 bordered system: S^{-1} and the product's output
   size_t fac_used = 0, e_used = 0;
 };
 
@@ -131,6 +132,8 @@ struct rs_solver {
   DevBuf<double> U0, PsiT0, G, g1, hole_dev;
   DevBuf<unsigned char> red_mask, skel_mask, ones_mask;
   DevBuf<int> S_piv;
+  DevBuf<unsigned> coop_bar;  // grid-barrier counter of the cooperative inverse
+  bool s_inv = false;         // the bordered system holds S^{-1} (FP32) instead of LU + pivots
 
   // solve buffers
   DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev, x64, xa64, g64;
@@ -1265,10 +1268,21 @@ rs_status factor_border(rs_solver* s) {
   assemble_s<Real>(F.S.p, ns, nb, F.epool.p + s->root_e_off, F.mU.p, F.mP.p, D,
                    s->dofs.p + s->allskel_off, s->G.p, s->stream);
   CU(s->S_piv.ensure(SN));
-  if (sizeof(Real) == 4)
-    launch_dense_lu_f32((float*)F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
-  else
-    launch_dense_lu((double*)F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+  s->s_inv = false;
+  if constexpr (sizeof(Real) == 4) {
+    // FP32: S^{-1} by all SMs; LU by one CTA only when S is too large for it
+    CU(F.Sinv.ensure((size_t)SN * SN));
+    CU(F.Mt.ensure(SN));
+    CU(s->coop_bar.ensure(1));
+    const cudaError_t e = launch_coop_inverse(F.S.p, SN, F.Sinv.p, s->coop_bar.p,
+                                              s->status.p + 1, s->status.p, s->stream);
+    if (e == cudaSuccess) s->s_inv = true;
+    else if (e != cudaErrorInvalidValue) CU(e);
+    else (void)cudaGetLastError();
+    if (!s->s_inv) launch_dense_lu_f32(F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+  } else {
+    launch_dense_lu(F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+  }
   s->launches += 4;
   CU(cudaGetLastError());
   return RS_OK;
@@ -1290,8 +1304,17 @@ rs_status solve_border_col(rs_solver* s, Real* x, Real* alpha, const double* g) 
   masked_cross<Real>(F.mP.p, D, nb, F.nv.p, D, 1, s->red_mask.p, D, s->g1.p, nb, s->stream);
   if (g) launch_axpby(s->g1.p, g, -1.0, 1.0, nb, s->stream);  // g1 <- g1 - g
   border_rhs<Real>(F.M.p, ns, nb, x, s->dofs.p + s->allskel_off, s->g1.p, s->stream);
-  launch_dense_solve_gather(F.S.p, sizeof(Real) == 4, SN, s->S_piv.p, nullptr, F.M.p, SN, 1,
-                            s->stream);
+  bool done = false;
+  if constexpr (sizeof(Real) == 4) {
+    if (s->s_inv) {
+      launch_dense_gemv(F.Sinv.p, SN, F.M.p, F.Mt.p, s->stream);
+      CU(cudaMemcpyAsync(F.M.p, F.Mt.p, SN * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
+      done = true;
+    }
+  }
+  if (!done)
+    launch_dense_solve_gather(F.S.p, sizeof(Real) == 4, SN, s->S_piv.p, nullptr, F.M.p, SN, 1,
+                              s->stream);
   CU(cudaMemcpyAsync(alpha, F.M.p + ns, nb * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
   border_sub<Real>(F.nv.p, x, F.mU.p, D, nb, alpha, s->red_mask.p, s->stream);
   sweep_levels<Real>(s, F.nv.p, D, 1, kDiagOnly, true);
@@ -2176,7 +2199,8 @@ rs_status rs_factor(rs_solver* s) {
     if (!fmm_plan_upload(s->fmm, fhp, s->stream))
       return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
   }
-  CU(cudaMemcpyAsync(s->h_status.p, s->status.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CU(cudaMemcpyAsync(s->h_status.p, s->status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                     s->stream));
   CU(cudaStreamSynchronize(s->stream));
   float ms = 0;
   cudaEventElapsedTime(&ms, s->ev_f0, s->ev_f1);
@@ -2195,6 +2219,7 @@ rs_status rs_factor(rs_solver* s) {
   for (const NodeState& S : s->st) nc += S.compressed;
   s->stats.num_compressed = nc;
   s->stats.num_skel_root = s->ns;
+  if (s->h_status.p[1] != 0) return fail(s, RS_ERR_CUDA, "grid barrier timed out");
   if (s->h_status.p[0] != 0) return fail(s, RS_ERR_NUMERIC, "singular or non-finite pivot");
   s->factored = true;
   return RS_OK;
