@@ -119,17 +119,20 @@ void launch_root_inverse(float* base, const RootTask* tasks, int count, int* sta
                          cudaStream_t st);
 void launch_root_apply(const float* base, const RootTask* tasks, int count, const int* dofs,
                        float* x, int ld, int nrhs, cudaStream_t st);
-// One large FP32 block (the bordered system's S): explicit inverse by all
-// SMs (cooperative launch, Gauss-Jordan with partial pivoting; a is
-// overwritten, ainv receives A^{-1}, column major).  bar: one unsigned of
-// scratch; err: raised if a grid barrier times out; status: raised for a
-// singular block.  Returns cudaErrorInvalidValue when n is too large for
-// the kernel's shared memory (the caller then factors with LU).
+// One large block (the bordered system's S): explicit inverse by all SMs
+// (cooperative launch, Gauss-Jordan with partial pivoting; a is overwritten,
+// ainv receives A^{-1}, column major).  bar: one unsigned of scratch; err:
+// raised if a grid barrier times out; status: raised for a singular block.
+// Returns cudaErrorInvalidValue when n is too large for the kernel's shared
+// memory (the caller then factors with LU).
 cudaError_t launch_coop_inverse(float* a, int n, float* ainv, unsigned* bar, int* err,
                                 int* status, cudaStream_t st);
-size_t coop_inverse_smem(int n, int grid);
+cudaError_t launch_coop_inverse(double* a, int n, double* ainv, unsigned* bar, int* err,
+                                int* status, cudaStream_t st);
+size_t coop_inverse_smem(int n, int grid, size_t elem_bytes);
 // y = ainv x (n x n column major, x and y distinct).
 void launch_dense_gemv(const float* ainv, int n, const float* x, float* y, cudaStream_t st);
+void launch_dense_gemv(const double* ainv, int n, const double* x, double* y, cudaStream_t st);
 void launch_dense_lu(double* a, int n, int* piv, int* status, cudaStream_t st);
 void launch_dense_lu_f32(float* a, int n, int* piv, int* status, cudaStream_t st);
 // x[idx, :] = LU^{-1} x[idx, :] (idx == nullptr: rows 0..n-1); x is Real.

@@ -581,8 +581,8 @@ void launch_root_apply(const float* base, const RootTask* tasks, int count, cons
 }
 
 // ---------------------------------------------------------------------------
-// Explicit inverse of one large FP32 block (the bordered system's S, about
-// 1500 DOFs for 16 holes) by all SMs.  One CTA doing the whole LU in global
+// Explicit inverse of one large block (the bordered system's S, about 1500
+// DOFs for 16 holes), FP32 or FP64, by all SMs.  One CTA doing the whole LU in global
 // memory was most of a bordered solve's time.  Gauss-Jordan with partial
 // pivoting, the columns split over the CTAs of a cooperative launch: at step
 // j every CTA reads column j and picks the pivot row itself (the same
@@ -620,40 +620,41 @@ __device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
   return s_ok != 0;
 }
 
-size_t coop_inverse_smem(int n, int grid) {
+size_t coop_inverse_smem(int n, int grid, size_t es) {
   const int cols = (n + grid - 1) / grid;
-  return sizeof(float) * (size_t)n + 2 * sizeof(int) * (size_t)n + sizeof(float) * (size_t)cols;
+  return es * (size_t)n + 2 * sizeof(int) * (size_t)n + es * (size_t)cols + 16;
 }
 
-__global__ void __launch_bounds__(kCoopThreads) coop_inverse_kernel(float* A, int n, float* Ainv,
+template <class Real>
+__global__ void __launch_bounds__(kCoopThreads) coop_inverse_kernel(Real* A, int n, Real* Ainv,
                                                                     unsigned* bar, int* err,
                                                                     int* status) {
   extern __shared__ __align__(16) unsigned char smem[];
-  float* col = reinterpret_cast<float*>(smem);     // column j, all rows
-  int* used = reinterpret_cast<int*>(col + n);      // row -> 1 once a pivot (then pinv)
+  Real* col = reinterpret_cast<Real*>(smem);        // column j, all rows
+  Real* rowv = col + n;                             // scaled pivot row, own columns
+  const int per = (n + gridDim.x - 1) / gridDim.x;
+  int* used = reinterpret_cast<int*>(rowv + per);   // row -> 1 once a pivot (then pinv)
   int* piv = used + n;                              // step -> pivot row
-  float* rowv = reinterpret_cast<float*>(piv + n);  // scaled pivot row, own columns
-  __shared__ float red_v[kCoopThreads / 32];
+  __shared__ Real red_v[kCoopThreads / 32];
   __shared__ int red_i[kCoopThreads / 32];
   __shared__ int s_p;
-  __shared__ float s_inv;
+  __shared__ Real s_inv;
   const int G = gridDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int per = (n + G - 1) / G;
   const int c0 = blockIdx.x * per, c1 = min(n, c0 + per);
   for (int i = tid; i < n; i += blockDim.x) used[i] = 0;
   unsigned epoch = 0;
   for (int j = 0; j < n; ++j) {
     for (int i = tid; i < n; i += blockDim.x) col[i] = __ldcg(A + i + (size_t)n * j);
     __syncthreads();
-    float best = -1.f;
+    Real best = -1;
     int bi = n;
     for (int i = tid; i < n; i += blockDim.x) {
-      const float v = fabsf(col[i]);
+      const Real v = fabs(col[i]);
       if (!used[i] && v > best) { best = v; bi = i; }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const Real ov = __shfl_xor_sync(0xffffffffu, best, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
       if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
     }
@@ -662,19 +663,19 @@ __global__ void __launch_bounds__(kCoopThreads) coop_inverse_kernel(float* A, in
     if (tid == 0) {
       for (int w = 1; w < kCoopThreads / 32; ++w)
         if (red_v[w] > best || (red_v[w] == best && red_i[w] < bi)) { best = red_v[w]; bi = red_i[w]; }
-      const bool ok = best > 0.f && isfinite(best) && bi < n;
+      const bool ok = best > (Real)0 && isfinite(best) && bi < n;
       if (!ok) {  // singular: flagged, continue with the first unused row
         if (blockIdx.x == 0) atomicExch(status, 1);
         bi = 0;
         while (bi < n - 1 && used[bi]) ++bi;
       }
       s_p = bi;
-      const float d = col[bi];
-      s_inv = d != 0.f ? 1.f / d : 0.f;
+      const Real d = col[bi];
+      s_inv = d != (Real)0 ? (Real)1 / d : (Real)0;
     }
     __syncthreads();
     const int p = s_p;
-    const float inv = s_inv;
+    const Real inv = s_inv;
     for (int c = c0 + tid; c < c1; c += blockDim.x)
       rowv[c - c0] = c == j ? inv : __ldcg(A + p + (size_t)n * c) * inv;
     // every CTA has read column j and its part of row p
@@ -684,10 +685,10 @@ __global__ void __launch_bounds__(kCoopThreads) coop_inverse_kernel(float* A, in
       piv[j] = p;
     }
     for (int c = c0; c < c1; ++c) {
-      float* Ac = A + (size_t)n * c;
-      const float rc = rowv[c - c0];
+      Real* Ac = A + (size_t)n * c;
+      const Real rc = rowv[c - c0];
       for (int i = tid; i < n; i += blockDim.x) {
-        const float m = c == j ? 0.f : Ac[i];
+        const Real m = c == j ? (Real)0 : Ac[i];
         Ac[i] = i == p ? rc : m - col[i] * rc;
       }
     }
@@ -700,18 +701,19 @@ __global__ void __launch_bounds__(kCoopThreads) coop_inverse_kernel(float* A, in
   for (int j = tid; j < n; j += blockDim.x) pinv[piv[j]] = j;
   __syncthreads();
   for (int b = c0; b < c1; ++b) {
-    const float* Mc = A + (size_t)n * pinv[b];
+    const Real* Mc = A + (size_t)n * pinv[b];
     for (int a = tid; a < n; a += blockDim.x) Ainv[a + (size_t)n * b] = __ldcg(Mc + piv[a]);
   }
 }
 
 // y[a] = sum_b Ainv(a, b) x[b], one thread per row, x staged in shared
 // memory a chunk at a time.
-__global__ void __launch_bounds__(128) dense_gemv_kernel(const float* Ainv, int n, const float* x,
-                                                         float* y) {
-  __shared__ float xs[1024];
+template <class Real>
+__global__ void __launch_bounds__(128) dense_gemv_kernel(const Real* Ainv, int n, const Real* x,
+                                                         Real* y) {
+  __shared__ Real xs[1024];
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  float acc = 0.f;
+  Real acc = 0;
   for (int b0 = 0; b0 < n; b0 += 1024) {
     const int nb = min(1024, n - b0);
     __syncthreads();
@@ -726,41 +728,56 @@ __global__ void __launch_bounds__(128) dense_gemv_kernel(const float* Ainv, int 
 
 // CTAs of the cooperative launch: up to two per SM, as many as fit with the
 // shared memory n needs (0: n too large for it).
+template <class Real>
 int coop_inverse_grid(int n) {
   int dev = 0, sms = 0, occ = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 0;
-  const size_t smem = coop_inverse_smem(n, sms);  // at least what any grid of >= sms CTAs needs
+  // at least what any grid of >= sms CTAs needs
+  const size_t smem = coop_inverse_smem(n, sms, sizeof(Real));
   if (smem + 1024 > (size_t)kSmemOptIn) return 0;
-  if (cudaFuncSetAttribute(coop_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, coop_inverse_kernel, kCoopThreads,
+  if (cudaFuncSetAttribute(coop_inverse_kernel<Real>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, coop_inverse_kernel<Real>, kCoopThreads,
                                                     smem) != cudaSuccess ||
       occ < 1)
     return 0;
   return sms * (occ < 2 ? occ : 2);
 }
 
-cudaError_t launch_coop_inverse(float* a, int n, float* ainv, unsigned* bar, int* err,
-                                int* status, cudaStream_t st) {
+template <class Real>
+static cudaError_t launch_coop_inverse_t(Real* a, int n, Real* ainv, unsigned* bar, int* err,
+                                         int* status, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  int grid = coop_inverse_grid(n);
+  int grid = coop_inverse_grid<Real>(n);
   if (grid <= 0) return cudaErrorInvalidValue;
   if (grid > n) grid = n;
-  const size_t smem = coop_inverse_smem(n, grid);
-  cudaError_t e = cudaFuncSetAttribute(coop_inverse_kernel,
+  const size_t smem = coop_inverse_smem(n, grid, sizeof(Real));
+  cudaError_t e = cudaFuncSetAttribute(coop_inverse_kernel<Real>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
   void* args[] = {&a, &n, &ainv, &bar, &err, &status};
-  return cudaLaunchCooperativeKernel((const void*)coop_inverse_kernel, dim3(grid),
+  return cudaLaunchCooperativeKernel((const void*)coop_inverse_kernel<Real>, dim3(grid),
                                      dim3(kCoopThreads), args, smem, st);
+}
+cudaError_t launch_coop_inverse(float* a, int n, float* ainv, unsigned* bar, int* err,
+                                int* status, cudaStream_t st) {
+  return launch_coop_inverse_t<float>(a, n, ainv, bar, err, status, st);
+}
+cudaError_t launch_coop_inverse(double* a, int n, double* ainv, unsigned* bar, int* err,
+                                int* status, cudaStream_t st) {
+  return launch_coop_inverse_t<double>(a, n, ainv, bar, err, status, st);
 }
 
 void launch_dense_gemv(const float* ainv, int n, const float* x, float* y, cudaStream_t st) {
   if (n <= 0) return;
-  dense_gemv_kernel<<<(n + 127) / 128, 128, 0, st>>>(ainv, n, x, y);
+  dense_gemv_kernel<float><<<(n + 127) / 128, 128, 0, st>>>(ainv, n, x, y);
+}
+void launch_dense_gemv(const double* ainv, int n, const double* x, double* y, cudaStream_t st) {
+  if (n <= 0) return;
+  dense_gemv_kernel<double><<<(n + 127) / 128, 128, 0, st>>>(ainv, n, x, y);
 }
 
 template <class Real>

@@ -57,7 +57,7 @@ struct NodeState {
 template <class Real>
 struct Factor {
   DevBuf<Real> fac, epool, scratch, x, tmp, mU, mP, S, M, nv;
-  DevBuf<Real> Sinv, Mt;  // FP32 bordered system: S^{-1} and the product's output
+  DevBuf<Real> Sinv, Mt;  // bordered system: S^{-1} and the product's output
   size_t fac_used = 0, e_used = 0;
 };
 
@@ -133,7 +133,7 @@ struct rs_solver {
   DevBuf<unsigned char> red_mask, skel_mask, ones_mask;
   DevBuf<int> S_piv;
   DevBuf<unsigned> coop_bar;  // grid-barrier counter of the cooperative inverse
-  bool s_inv = false;         // the bordered system holds S^{-1} (FP32) instead of LU + pivots
+  bool s_inv = false;         // the bordered system holds S^{-1} instead of LU + pivots
 
   // solve buffers
   DevBuf<double> f_dev, mu_dev, alpha_dev, r64, acc64, nrm_dev, x64, xa64, g64;
@@ -1268,20 +1268,23 @@ rs_status factor_border(rs_solver* s) {
   assemble_s<Real>(F.S.p, ns, nb, F.epool.p + s->root_e_off, F.mU.p, F.mP.p, D,
                    s->dofs.p + s->allskel_off, s->G.p, s->stream);
   CU(s->S_piv.ensure(SN));
+  // S^{-1} by all SMs (Gauss-Jordan with partial pivoting); LU with partial
+  // pivoting by one CTA (dgetrf, as the reference factors S) only when S is
+  // too large for the cooperative kernel's shared memory
   s->s_inv = false;
-  if constexpr (sizeof(Real) == 4) {
-    // FP32: S^{-1} by all SMs; LU by one CTA only when S is too large for it
-    CU(F.Sinv.ensure((size_t)SN * SN));
-    CU(F.Mt.ensure(SN));
-    CU(s->coop_bar.ensure(1));
-    const cudaError_t e = launch_coop_inverse(F.S.p, SN, F.Sinv.p, s->coop_bar.p,
-                                              s->status.p + 1, s->status.p, s->stream);
-    if (e == cudaSuccess) s->s_inv = true;
-    else if (e != cudaErrorInvalidValue) CU(e);
-    else (void)cudaGetLastError();
-    if (!s->s_inv) launch_dense_lu_f32(F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
-  } else {
-    launch_dense_lu(F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+  CU(F.Sinv.ensure((size_t)SN * SN));
+  CU(F.Mt.ensure(SN));
+  CU(s->coop_bar.ensure(1));
+  const cudaError_t ce = launch_coop_inverse(F.S.p, SN, F.Sinv.p, s->coop_bar.p,
+                                             s->status.p + 1, s->status.p, s->stream);
+  if (ce == cudaSuccess) s->s_inv = true;
+  else if (ce != cudaErrorInvalidValue) CU(ce);
+  else (void)cudaGetLastError();
+  if (!s->s_inv) {
+    if constexpr (sizeof(Real) == 4)
+      launch_dense_lu_f32(F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
+    else
+      launch_dense_lu(F.S.p, SN, s->S_piv.p, s->status.p, s->stream);
   }
   s->launches += 4;
   CU(cudaGetLastError());
@@ -1304,17 +1307,13 @@ rs_status solve_border_col(rs_solver* s, Real* x, Real* alpha, const double* g) 
   masked_cross<Real>(F.mP.p, D, nb, F.nv.p, D, 1, s->red_mask.p, D, s->g1.p, nb, s->stream);
   if (g) launch_axpby(s->g1.p, g, -1.0, 1.0, nb, s->stream);  // g1 <- g1 - g
   border_rhs<Real>(F.M.p, ns, nb, x, s->dofs.p + s->allskel_off, s->g1.p, s->stream);
-  bool done = false;
-  if constexpr (sizeof(Real) == 4) {
-    if (s->s_inv) {
-      launch_dense_gemv(F.Sinv.p, SN, F.M.p, F.Mt.p, s->stream);
-      CU(cudaMemcpyAsync(F.M.p, F.Mt.p, SN * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
-      done = true;
-    }
-  }
-  if (!done)
+  if (s->s_inv) {
+    launch_dense_gemv(F.Sinv.p, SN, F.M.p, F.Mt.p, s->stream);
+    CU(cudaMemcpyAsync(F.M.p, F.Mt.p, SN * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
+  } else {
     launch_dense_solve_gather(F.S.p, sizeof(Real) == 4, SN, s->S_piv.p, nullptr, F.M.p, SN, 1,
                               s->stream);
+  }
   CU(cudaMemcpyAsync(alpha, F.M.p + ns, nb * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
   border_sub<Real>(F.nv.p, x, F.mU.p, D, nb, alpha, s->red_mask.p, s->stream);
   sweep_levels<Real>(s, F.nv.p, D, 1, kDiagOnly, true);
