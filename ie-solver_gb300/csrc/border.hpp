@@ -7,9 +7,13 @@
 
 namespace rskel {
 
+// out(i, j) = sum_l mask[l] A(l, i) B(l, j) for A (D x na), B (D x nb),
+// in FP64; part: masked_cross_scratch(na, nb, D) doubles of scratch.
 template <class Real>
 void masked_cross(const Real* A, int lda, int na, const Real* B, int ldb, int nb,
-                  const unsigned char* mask, int D, double* out, int ldo, cudaStream_t st);
+                  const unsigned char* mask, int D, double* out, int ldo, double* part,
+                  cudaStream_t st);
+size_t masked_cross_scratch(int na, int nb, int D);
 template <class Real>
 void assemble_s(Real* S, int ns, int nb, const Real* root, const Real* mU, const Real* mP, int D,
                 const int* allskel, const double* G, cudaStream_t st);

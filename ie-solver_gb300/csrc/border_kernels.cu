@@ -9,22 +9,55 @@
 namespace rskel {
 
 // out(i, j) = sum_l mask[l] * A[l, i] * B[l, j]  (A: D x na, B: D x nb).
+// The sum over l (all DOFs, up to millions) is split into chunks: CTA
+// (i, group of 8 columns j, chunk) writes its partial sums, and a second
+// pass adds the chunks in order (the result does not depend on
+// scheduling).  Sums are FP64; in the FP32 variant the products of eight
+// consecutive terms of a thread are first added in FP32, so that FP64
+// additions (one FP64 instruction per 16 cycles per SM on this GPU) are an
+// eighth of the terms.
+constexpr int kCrossChunk = 16384;
+
 template <class Real>
-__global__ void __launch_bounds__(256) masked_cross_kernel(const Real* A, int lda, int na,
-                                                           const Real* B, int ldb, int nb,
-                                                           const unsigned char* mask, int D,
-                                                           double* out, int ldo) {
-  const int i = blockIdx.x;
-  const int j0 = blockIdx.y * 8;
+__global__ void __launch_bounds__(256) masked_cross_part_kernel(const Real* A, int lda,
+                                                                const Real* B, int ldb, int nb,
+                                                                const unsigned char* mask, int D,
+                                                                double* part) {
+  const int i = blockIdx.x, j0 = blockIdx.y * 8, na = gridDim.x;
+  const int l0 = blockIdx.z * kCrossChunk, l1 = min(D, l0 + kCrossChunk);
+  const int jn = min(8, nb - j0);
+  const Real* Ai = A + (size_t)lda * i;
   double acc[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-  for (int l = threadIdx.x; l < D; l += blockDim.x) {
-    if (!mask[l]) continue;
-    const double a = (double)A[l + (size_t)lda * i];
+  if constexpr (sizeof(Real) == 4) {
+    float f[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (j0 + q < nb) acc[q] += a * (double)B[l + (size_t)ldb * (j0 + q)];
+    for (int q = 0; q < 8; ++q) f[q] = 0.f;
+    int run = 0;
+    for (int l = l0 + threadIdx.x; l < l1; l += blockDim.x) {
+      const float a = mask[l] ? Ai[l] : 0.f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < jn) f[q] += a * B[l + (size_t)ldb * (j0 + q)];
+      if (++run == 8) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          acc[q] += (double)f[q];
+          f[q] = 0.f;
+        }
+        run = 0;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] += (double)f[q];
+  } else {
+    for (int l = l0 + threadIdx.x; l < l1; l += blockDim.x) {
+      const double a = mask[l] ? (double)Ai[l] : 0.0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < jn) acc[q] += a * (double)B[l + (size_t)ldb * (j0 + q)];
+    }
   }
   __shared__ double red[8][8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -34,24 +67,41 @@ __global__ void __launch_bounds__(256) masked_cross_kernel(const Real* A, int ld
     if (lane == 0) red[warp][q] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 8 && j0 + threadIdx.x < nb) {
-    double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
-    out[i + (size_t)ldo * (j0 + threadIdx.x)] = s;
+  if (threadIdx.x < jn) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+    part[((size_t)blockIdx.z * na + i) * nb + j0 + threadIdx.x] = v;
   }
+}
+
+__global__ void masked_cross_sum_kernel(const double* part, int chunks, int na, int nb,
+                                        double* out, int ldo) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= na * nb) return;
+  const int i = e % na, j = e / na;
+  double v = 0.0;
+  for (int c = 0; c < chunks; ++c) v += part[((size_t)c * na + i) * nb + j];
+  out[i + (size_t)ldo * j] = v;
+}
+
+size_t masked_cross_scratch(int na, int nb, int D) {
+  return (size_t)((D + kCrossChunk - 1) / kCrossChunk) * na * nb;
 }
 
 template <class Real>
 void masked_cross(const Real* A, int lda, int na, const Real* B, int ldb, int nb,
-                  const unsigned char* mask, int D, double* out, int ldo, cudaStream_t st) {
+                  const unsigned char* mask, int D, double* out, int ldo, double* part,
+                  cudaStream_t st) {
   if (na <= 0 || nb <= 0) return;
-  dim3 grid(na, (nb + 7) / 8);
-  masked_cross_kernel<Real><<<grid, 256, 0, st>>>(A, lda, na, B, ldb, nb, mask, D, out, ldo);
+  const int chunks = (D + kCrossChunk - 1) / kCrossChunk;
+  dim3 grid(na, (nb + 7) / 8, chunks);
+  masked_cross_part_kernel<Real><<<grid, 256, 0, st>>>(A, lda, B, ldb, nb, mask, D, part);
+  masked_cross_sum_kernel<<<(na * nb + 127) / 128, 128, 0, st>>>(part, chunks, na, nb, out, ldo);
 }
 template void masked_cross<double>(const double*, int, int, const double*, int, int,
-                                   const unsigned char*, int, double*, int, cudaStream_t);
+                                   const unsigned char*, int, double*, int, double*, cudaStream_t);
 template void masked_cross<float>(const float*, int, int, const float*, int, int,
-                                  const unsigned char*, int, double*, int, cudaStream_t);
+                                  const unsigned char*, int, double*, int, double*, cudaStream_t);
 
 // S = [Ktilde_root, mU(allskel, :); mP(allskel, :)^T, -I - G], SN = ns + nb.
 template <class Real>

@@ -133,6 +133,7 @@ struct rs_solver {
   DevBuf<unsigned char> red_mask, skel_mask, ones_mask;
   DevBuf<int> S_piv;
   DevBuf<unsigned> coop_bar;  // grid-barrier counter of the cooperative inverse
+  DevBuf<double> cross_part;  // partial sums of masked_cross
   bool s_inv = false;         // the bordered system holds S^{-1} instead of LU + pivots
 
   // solve buffers
@@ -1262,7 +1263,9 @@ rs_status factor_border(rs_solver* s) {
                      s->stream));
   sweep_levels<Real>(s, F.tmp.p, D, nb, kDiagOnly, true);
   CU(s->G.ensure((size_t)nb * nb));
-  masked_cross<Real>(F.mP.p, D, nb, F.tmp.p, D, nb, s->red_mask.p, D, s->G.p, nb, s->stream);
+  CU(s->cross_part.ensure(masked_cross_scratch(nb, nb, D)));
+  masked_cross<Real>(F.mP.p, D, nb, F.tmp.p, D, nb, s->red_mask.p, D, s->G.p, nb,
+                     s->cross_part.p, s->stream);
   const int SN = ns + nb;
   CU(F.S.ensure((size_t)SN * SN));
   assemble_s<Real>(F.S.p, ns, nb, F.epool.p + s->root_e_off, F.mU.p, F.mP.p, D,
@@ -1304,7 +1307,9 @@ rs_status solve_border_col(rs_solver* s, Real* x, Real* alpha, const double* g) 
   sweep_levels<Real>(s, x, D, 1, kUpPlain, true);
   CU(cudaMemcpyAsync(F.nv.p, x, D * sizeof(Real), cudaMemcpyDeviceToDevice, s->stream));
   sweep_levels<Real>(s, F.nv.p, D, 1, kDiagOnly, true);
-  masked_cross<Real>(F.mP.p, D, nb, F.nv.p, D, 1, s->red_mask.p, D, s->g1.p, nb, s->stream);
+  CU(s->cross_part.ensure(masked_cross_scratch(nb, nb, D)));
+  masked_cross<Real>(F.mP.p, D, nb, F.nv.p, D, 1, s->red_mask.p, D, s->g1.p, nb,
+                     s->cross_part.p, s->stream);
   if (g) launch_axpby(s->g1.p, g, -1.0, 1.0, nb, s->stream);  // g1 <- g1 - g
   border_rhs<Real>(F.M.p, ns, nb, x, s->dofs.p + s->allskel_off, s->g1.p, s->stream);
   if (s->s_inv) {
@@ -1471,8 +1476,9 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
     const int nb = s->nb;
     for (int c = 0; c < nrhs; ++c) {
       launch_gemv_sub(r + (size_t)D * c, s->U0.p, alpha + (size_t)nb * c, D, nb, s->stream);
+      CU(s->cross_part.ensure(masked_cross_scratch(nb, nb, D)));
       masked_cross<double>(s->PsiT0.p, D, nb, mu + (size_t)D * c, D, 1, s->ones_mask.p, D,
-                           rg + (size_t)nb * c, nb, s->stream);
+                           rg + (size_t)nb * c, nb, s->cross_part.p, s->stream);
       launch_axpby(rg + (size_t)nb * c, alpha + (size_t)nb * c, 1.0, -1.0, nb, s->stream);
       s->launches += 3;
     }
@@ -1494,8 +1500,9 @@ rs_status residual_update(rs_solver* s, const double* x, const double* xa, int n
     const int nb = s->nb;
     for (int c = 0; c < nrhs; ++c) {
       launch_gemv_sub(r + (size_t)D * c, s->U0.p, xa + (size_t)nb * c, D, nb, s->stream);
+      CU(s->cross_part.ensure(masked_cross_scratch(nb, nb, D)));
       masked_cross<double>(s->PsiT0.p, D, nb, x + (size_t)D * c, D, 1, s->ones_mask.p, D,
-                           g + (size_t)nb * c, nb, s->stream);
+                           g + (size_t)nb * c, nb, s->cross_part.p, s->stream);
       launch_axpby(rg + (size_t)nb * c, g + (size_t)nb * c, -1.0, 1.0, nb, s->stream);
       launch_axpby(rg + (size_t)nb * c, xa + (size_t)nb * c, 1.0, 1.0, nb, s->stream);
       s->launches += 4;
