@@ -18,6 +18,7 @@
 // factorization then runs on the small n x n tile only, and stops as soon as
 // the rank is known.  Norms and the rank decision are accumulated in double
 // for both element types.
+#include <algorithm>
 #include <cstdio>
 
 #include "common.cuh"
@@ -996,10 +997,12 @@ static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStrea
 int id_sketch_rows(int n) { return sketch_rows(n); }
 size_t id_wide_tile(int m, int n) { return id_direct_tile(m, n); }
 
-constexpr int kWideMaxTiles = 5;  // 4x4 tiles per thread: ell <= 5 * 256 * 4 / kWideCols rows
+constexpr int kWideMaxTiles = 5;  // 4x4 tiles per thread: <= 5 * 256 * 4 / kWideCols sketch rows
 size_t id_wide_sketch_smem(int nmax) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
-  const int lp = (sketch_rows(nmax) + 3) & ~3;
+  // the largest block any task of up to nmax columns uses (wide_sketch_block
+  // is not monotonic: up to 640 rows whole, above that in blocks of <= 512)
+  const int lp = std::min((sketch_rows(nmax) + 3) & ~3, 640);
   return al(sizeof(float) * kChunk * kWideCols) + al(sizeof(float) * (size_t)kChunk * lp) +
          dofs_bytes<float>(kWideCols) + dofs_bytes<float>(kChunk) + al(sizeof(int) * kChunk);
 }
@@ -1011,8 +1014,8 @@ __global__ void __launch_bounds__(kThreads) id_wide_sketch_kernel(IdParams p,
   const IdTask t = p.tasks[it.task];
   const int n = t.n;
   const int nc = n - it.j0 < kWideCols ? n - it.j0 : kWideCols;
-  const int ell = sketch_rows(n);
-  const int lp = (ell + 3) & ~3;
+  const int sb = it.s1 - it.s0;  // this item's sketch rows, s0 + [0, sb)
+  const int lp = (sb + 3) & ~3;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
   IdShared<float> S;
@@ -1040,7 +1043,7 @@ __global__ void __launch_bounds__(kThreads) id_wide_sketch_kernel(IdParams p,
     fill_chunk<float>(p, tc, S, kWideCols, c0, cnt, ox, oy);
     for (TileWalk w(lp); w.j < kChunk; w.next()) {
       const int ii = w.j, r = w.i;
-      sg[w.e()] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
+      sg[w.e()] = (r < sb && ii < cnt) ? sketch_sign(it.s0 + r, c0 + ii) : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -1070,7 +1073,7 @@ __global__ void __launch_bounds__(kThreads) id_wide_sketch_kernel(IdParams p,
 #pragma unroll
     for (int e = 0; e < 16; ++e) {
       const int r = r0 + e / 4;
-      if (r < ell) out[(size_t)r * kWideCols + cc0 + e % 4] = acc[q][e];
+      if (r < sb) out[(size_t)(it.s0 + r) * kWideCols + cc0 + e % 4] = acc[q][e];
     }
   }
 }

@@ -54,8 +54,16 @@ struct WideItem {
   int task;     // index in the launch's task array
   int j0;       // first column
   int r0, r1;   // ID matrix rows [r0, r1)
+  int s0, s1;   // sketch rows [s0, s1)
   int64_t part_off;
 };
+// Sketch rows one wide item forms: all of them up to 640 (the register
+// tiles' limit), else blocks of at most 512.
+inline int wide_sketch_block(int ell) {
+  if (ell <= 640) return ell;
+  const int nb = (ell + 511) / 512;
+  return (((ell + nb - 1) / nb) + 3) & ~3;
+}
 
 // One elimination (skel_factorization.cpp:77-128) or, for boxes that are not
 // compressed, the assembly of the box's Schur-complemented block.

@@ -42,7 +42,7 @@ using namespace rskel;
 namespace {
 
 constexpr size_t kSmemMax = 227 * 1024;
-constexpr int kWideMaxN = 512;  // FP32 wide ID up to this many columns (wider: Householder fold)
+constexpr int kWideMaxN = 1024;  // FP32 wide ID up to this many columns (wider: Householder fold)
 
 struct NodeState {
   int compressed = 0;
@@ -745,16 +745,20 @@ rs_status factor_impl(rs_solver* s) {
         t.wide_split = ns;
         t.y_off = (int64_t)part_need;
         const int ncb = (t.n + kWideCols - 1) / kWideCols;
+        const int sbk = wide_sketch_block(ell);
         for (int jb = 0; jb < ncb; ++jb)
-          for (int q = 0; q < ns; ++q) {
-            WideItem it;
-            it.task = (int)(i - w0);
-            it.j0 = jb * kWideCols;
-            it.r0 = q * per * 64;
-            it.r1 = std::min(m, (q + 1) * per * 64);
-            it.part_off = t.y_off + ((int64_t)(jb * ns + q) * ell) * kWideCols;
-            witems.push_back(it);
-          }
+          for (int q = 0; q < ns; ++q)
+            for (int s0 = 0; s0 < ell; s0 += sbk) {
+              WideItem it;
+              it.task = (int)(i - w0);
+              it.j0 = jb * kWideCols;
+              it.r0 = q * per * 64;
+              it.r1 = std::min(m, (q + 1) * per * 64);
+              it.s0 = s0;
+              it.s1 = std::min(ell, s0 + sbk);
+              it.part_off = t.y_off + ((int64_t)(jb * ns + q) * ell) * kWideCols;
+              witems.push_back(it);
+            }
         part_need += (size_t)ncb * ns * ell * kWideCols;
       }
     }
