@@ -306,10 +306,11 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     }
     __syncthreads();
     const int rem = r - j - 1;
-    for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
-      const int i = j + 1 + e % rem, c = j + 1 + e / rem;
-      Mrr[i + ld * c] -= Mrr[i + ld * j] * Mrr[j + ld * c];
-    }
+    if (rem > 0)
+      for (TileWalk w(rem); w.j < rem; w.next()) {
+        const int i = j + 1 + w.i, c = j + 1 + w.j;
+        Mrr[i + ld * c] -= Mrr[i + ld * j] * Mrr[j + ld * c];
+      }
     __syncthreads();
   }
   // 5) U_f = X^{-1} K_r_sn, in place over Mrs (one warp per column).
@@ -372,10 +373,12 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   if (k > 0)
     for (TileWalk w(k); w.j < r; w.next()) {
       const int i = w.i, j = w.j;
-      const int e = w.e();
-      Lo[e] = Msr[i + ld * j];
-      const int i2 = e % r, j2 = e / r;
-      Uo[e] = Mrs[i2 + ld * j2];
+      Lo[w.e()] = Msr[i + ld * j];
+    }
+  if (r > 0)
+    for (TileWalk w(r); w.j < k; w.next()) {
+      const int i = w.i, j = w.j;
+      Uo[w.e()] = Mrs[i + ld * j];
     }
   if (r > 0)
     for (TileWalk w(r); w.j < r; w.next()) {
