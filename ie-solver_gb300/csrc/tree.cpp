@@ -437,7 +437,8 @@ void QuadTree::compute_neighbors() {
   for (TreeNode& nd : nodes) nd.neighbors.clear();
   const double sqrt2 = std::sqrt(2.0);
   std::vector<std::vector<int>> hits;
-  std::vector<int> extra(nodes.size(), 0), touched;
+  std::vector<int> extra(nodes.size(), 0), slot(nodes.size(), 0), touched, group, group_off,
+      group_fill;
   for (size_t lv = 0; lv < levels.size(); ++lv) {
     const std::vector<int>& L = levels[lv];
     const int m = static_cast<int>(L.size());
@@ -477,28 +478,38 @@ void QuadTree::compute_neighbors() {
         }
       }
     }
-    // room first (one allocation per list), then the links in order
+    // The links, in the reference's order, with the list appends in
+    // parallel: each leaf of the level appends its own hits, and each finer
+    // box appends the leaves that found it in level order (grouped by a
+    // counting pass over the hits, which keeps that order).
     touched.clear();
     for (int k = 0; k < m; ++k)
       for (int sm : hits[k])
         if (extra[sm]++ == 0) touched.push_back(sm);
     const int nt = static_cast<int>(touched.size());
-#pragma omp parallel for schedule(static) if (nt + m >= 512)
+    group_off.resize(nt + 1);
+    group_off[0] = 0;
+    for (int u = 0; u < nt; ++u) {
+      slot[touched[u]] = u;
+      group_off[u + 1] = group_off[u] + extra[touched[u]];
+    }
+    group.resize(group_off[nt]);
+    group_fill.assign(group_off.begin(), group_off.end() - 1);
+    for (int k = 0; k < m; ++k)
+      for (int sm : hits[k]) group[group_fill[slot[sm]]++] = L[k];
+#pragma omp parallel for schedule(dynamic, 32) if (nt + m >= 512)
     for (int u = 0; u < nt + m; ++u) {
       if (u < nt) {
         std::vector<int>& nb = nodes[touched[u]].neighbors;
-        nb.reserve(nb.size() + extra[touched[u]] + 12);  // + its siblings and cousins
+        nb.reserve(nb.size() + (group_off[u + 1] - group_off[u]) + 12);  // + siblings, cousins
+        nb.insert(nb.end(), group.begin() + group_off[u], group.begin() + group_off[u + 1]);
         extra[touched[u]] = 0;
       } else {
-        std::vector<int>& nb = nodes[L[u - nt]].neighbors;
-        nb.reserve(nb.size() + hits[u - nt].size());
+        const int k = u - nt;
+        std::vector<int>& nb = nodes[L[k]].neighbors;
+        nb.insert(nb.end(), hits[k].begin(), hits[k].end());
       }
     }
-    for (int k = 0; k < m; ++k)
-      for (int sm : hits[k]) {
-        nodes[L[k]].neighbors.push_back(sm);
-        nodes[sm].neighbors.push_back(L[k]);
-      }
   }
 }
 
