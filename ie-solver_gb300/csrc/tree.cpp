@@ -280,8 +280,11 @@ bool QuadTree::partition_build(int n) {
       scatter(bx.a, bx.b, pos);
       std::copy(tmp.begin() + bx.a, tmp.begin() + bx.b, ord.begin() + bx.a);
     }
-    // children, corners as in subdivide
-    level_boxes.clear();
+    // children, corners as in subdivide: box i's four at base + 4 i + q
+    const int base = static_cast<int>(box.size());
+    box.resize(box.size() + 4 * (size_t)ns);
+    level_boxes.resize(4 * (size_t)ns);
+#pragma omp parallel for schedule(static) if (nthreads > 1 && ns >= 256)
     for (int i = 0; i < ns; ++i) {
       const int k = split[i];
       double c[8];
@@ -295,7 +298,8 @@ bool QuadTree::partition_build(int n) {
       const int level = box[k].level + 1;
       int start = box[k].a;
       for (int q = 0; q < 4; ++q) {
-        PBox ch;
+        const int idx = base + 4 * i + q;
+        PBox& ch = box[idx];
         for (int u = 0; u < 8; ++u) ch.corners[u] = cq[q][u];
         ch.side = side;
         ch.level = level;
@@ -305,12 +309,11 @@ bool QuadTree::partition_build(int n) {
         ch.b = start + cnt[4 * (size_t)i + q];
         ch.t = -1;
         start = ch.b;
-        box[k].kids[q] = static_cast<int>(box.size());
-        level_boxes.push_back(static_cast<int>(box.size()));
-        box.push_back(ch);
+        box[k].kids[q] = idx;
+        level_boxes[4 * (size_t)i + q] = idx;
       }
-      splits.push_back(k);
     }
+    splits.insert(splits.end(), split.begin(), split.end());
   }
   std::stable_sort(splits.begin(), splits.end(), [&box](int u, int v) {
     return box[u].t != box[v].t ? box[u].t < box[v].t : box[u].level < box[v].level;
