@@ -1935,12 +1935,15 @@ rs_status rs_set_geometry(rs_solver* s, int num_points, const double* points,
     return fail(s, RS_ERR_ARG, "bad geometry arguments");
   if (num_holes > 0 && (!hole_centers || !hole_radii))
     return fail(s, RS_ERR_ARG, "holes need centres and radii");
-  for (int i = 0; i < 2 * num_points; ++i)
-    if (!std::isfinite(points[i]) || !std::isfinite(normals[i]))
-      return fail(s, RS_ERR_NUMERIC, "non-finite point or normal");
-  for (int i = 0; i < num_points; ++i)
-    if (!std::isfinite(weights[i]) || !std::isfinite(curvatures[i]))
-      return fail(s, RS_ERR_NUMERIC, "non-finite weight or curvature");
+  int bad_xy = 0, bad_wk = 0;  // validated before anything of the handle changes
+#pragma omp parallel for reduction(| : bad_xy, bad_wk) if (num_points >= 16384)
+  for (int i = 0; i < num_points; ++i) {
+    bad_xy |= !std::isfinite(points[2 * i]) || !std::isfinite(points[2 * i + 1]) ||
+              !std::isfinite(normals[2 * i]) || !std::isfinite(normals[2 * i + 1]);
+    bad_wk |= !std::isfinite(weights[i]) || !std::isfinite(curvatures[i]);
+  }
+  if (bad_xy) return fail(s, RS_ERR_NUMERIC, "non-finite point or normal");
+  if (bad_wk) return fail(s, RS_ERR_NUMERIC, "non-finite weight or curvature");
   s->n = num_points;
   s->D = num_points * s->sd;
   s->pts.assign(points, points + 2 * (size_t)num_points);
