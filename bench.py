@@ -531,7 +531,8 @@ def run_gpu(args):
                      "peak_source": "CUDA-core FMA chains measured now on this GPU "
                                     "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
                      "work": "algorithmic flops per factorization: ID fill + CPQR to rank + Z, "
-                             "or Schur eliminations (formulas in DESIGN.md)"},
+                             "or Schur eliminations (per box: sketch_id_flops, id_flops, dec_flops "
+                             "in solver.cpp)"},
         "fma_peaks_tflops": peaks,
         "cpu_baseline": {"value": cpu_v, "unit": "DOFs/s", "cores": cores, "kind": "port",
                          "sample": "10 factor + 8-RHS solves of the full workload by the oracle "
