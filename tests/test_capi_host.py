@@ -32,6 +32,27 @@ def test_config_defaults_are_the_reference_defaults(solver_lib):
     assert c.id_tol == 1e-6 and c.max_leaf_dofs == 32 and c.num_proxy_points == 128
     assert c.radius_ratio == 1.5 and c.min_dofs_to_compress == 16
     assert c.is_strong_admissibility == 0 and c.solution_dimension == 1
+    # fields beyond the reference's configuration
+    assert c.precision == solver_lib.RS_FP64 and c.refine_verify == 1 and c.refine_solver == 0
+    assert c.use_graphs == 1 and c.root_inverse == 1
+
+
+def test_geometry_checks_leave_the_handle_unchanged(solver_lib):
+    """A rejected geometry (non-finite weight) leaves the handle's previous
+    geometry and tree in place: the check runs before anything changes."""
+    from rskel import geometry as g
+
+    s = solver_lib.Solver(g.unit_circle(20000), solver_lib.RS_LAPLACE, 1e-6)
+    s.build_tree()
+    before = s.tree_dump()
+    bad = g.unit_circle(20000)
+    bad.weights[123] = np.inf
+    with pytest.raises(solver_lib.RsError) as e:
+        s.set_geometry(bad)
+    assert e.value.code == 6
+    after = s.tree_dump()
+    for k in ("level_sizes", "node_parent", "nbr", "orig"):
+        assert np.array_equal(before[k], after[k]), k
 
 
 def test_argument_validation(solver_lib):
