@@ -368,7 +368,8 @@ bool QuadTree::build(const double* points, int n, int sd_, int max_leaf_dofs) {
   // the previous tree's nodes are overwritten in place (partition_build),
   // so their lists' storage is reused
   if (nodes.empty()) nodes.emplace_back();
-  double mn = points[0], mx = points[0];
+  double mn = points[0], mx = points[0];  // min and max are exact in any order
+#pragma omp parallel for reduction(min : mn) reduction(max : mx) if (n >= 16384)
   for (int i = 0; i < 2 * n; ++i) {
     if (points[i] < mn) mn = points[i];
     if (points[i] > mx) mx = points[i];
