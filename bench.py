@@ -503,7 +503,8 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if refined_ok else "f64",
         "data": "synthetic (seeded star curve, exterior point-source data)",
-        "config": dict(config(dist.ws), arm=head),
+        "config": config(dist.ws),
+        "arm": head,
         "accuracy": acc,
         "plain_fp64": {"value": dist.sum(dofs) / (ms64 * 1e-3), "ms_per_step": ms64,
                        "ms_median": statistics.median(t64),
