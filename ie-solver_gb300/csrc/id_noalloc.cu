@@ -12,6 +12,14 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // arrays' device addresses with cudaGetSymbolAddress and sets the kernel's
 // shared-memory attribute; make that first call before any stream capture.
+// The addresses are kept for the life of the process, so a process that
+// resets a device (cudaDeviceReset) must not call this entry point on that
+// device afterwards: the kept addresses belong to the destroyed context.
+//
+// Errors: a CUDA error already pending in the calling thread (left by the
+// caller's earlier work) is reported as RS_ERR_CUDA without being cleared,
+// and nothing is launched; each of this call's two launches is checked on
+// its own right after it.
 //
 // Sharing: every call on a device uses the same arrays, so calls that overlap
 // in time (on different streams, or from different host threads) race and
@@ -83,6 +91,8 @@ extern "C" rs_status rs_id_noalloc(int m, int n, const double* A, double tol, in
   DeviceSlots* d = nullptr;
   rs_status rc = setup_device(dev, &d);
   if (rc != RS_OK) return rc;
+  // not this call's error: leave it pending for its owner, launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return RS_ERR_CUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   IdTask t{};
   t.n = n;
@@ -93,6 +103,7 @@ extern "C" rs_status rs_id_noalloc(int m, int n, const double* A, double tol, in
   t.dense_off = 0;
   t.m_dense = m;
   put_task_kernel<<<1, 1, 0, st>>>(t, d->task);
+  if (cudaGetLastError() != cudaSuccess) return RS_ERR_CUDA;
   IdParams ip{};
   ip.sd = 1;
   ip.npp = 1;

@@ -7,6 +7,10 @@
 // is one launch with one CTA per box; the per-box work is a gather of the
 // box's skeleton / redundant rows of x, a few small matrix products with the
 // box's factors and a scatter back.
+#include <algorithm>
+#include <vector>
+
+#include "../../include/rskel.h"
 #include "common.cuh"
 #include "kernels.hpp"
 
@@ -597,7 +601,8 @@ void launch_root_apply(const float* base, const RootTask* tasks, int count, cons
 constexpr int kCoopThreads = 256;
 constexpr unsigned kBarrierSpins = 1u << 22;
 
-__device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
+__device__ bool grid_barrier(unsigned* count, unsigned target, int* err,
+                             unsigned max_spins = kBarrierSpins) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -606,7 +611,7 @@ __device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
     unsigned spins = 0;
     int ok = 1;
     while (*reinterpret_cast<volatile unsigned*>(count) < target) {
-      if (*reinterpret_cast<volatile int*>(err) != 0 || ++spins > kBarrierSpins) {
+      if (*reinterpret_cast<volatile int*>(err) != 0 || ++spins > max_spins) {
         atomicExch(err, 1);
         ok = 0;
         break;
@@ -618,6 +623,23 @@ __device__ bool grid_barrier(unsigned* count, unsigned target, int* err) {
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// Self-test of the bounded grid barrier: `rounds` barriers over a
+// cooperative grid of one CTA per SM.  CTA `skip` (none when skip < 0)
+// returns before its first arrival, so the other CTAs' waits run out after
+// `spins` polls; they raise *err and return.  passed[b] = the barriers CTA b
+// got through (the skipped CTA writes nothing).
+__global__ void __launch_bounds__(128) barrier_probe_kernel(unsigned* bar, int* err, int skip,
+                                                            unsigned spins, int rounds,
+                                                            int* passed) {
+  if ((int)blockIdx.x == skip) return;  // block-uniform
+  int k = 0;
+  for (int r = 0; r < rounds; ++r) {
+    if (!grid_barrier(bar, (unsigned)(r + 1) * gridDim.x, err, spins)) break;
+    ++k;
+  }
+  if (threadIdx.x == 0) passed[blockIdx.x] = k;
 }
 
 size_t coop_inverse_smem(int n, int grid, size_t es) {
@@ -1017,3 +1039,61 @@ void launch_gemv_sub(double* r, const double* U, const double* a, int D, int nb,
 }
 
 }  // namespace rskel
+
+// ---------------------------------------------------------------------------
+// C ABI: rs_barrier_selftest (include/rskel.h)
+// ---------------------------------------------------------------------------
+extern "C" rs_status rs_barrier_selftest(int device, int skip_block, unsigned spins, int rounds,
+                                         int* err, int* passed_min, int* passed_max, float* ms) {
+  using namespace rskel;
+  if (!err || !passed_min || !passed_max || !ms || rounds < 1 || rounds > 64 || spins < 1 ||
+      spins > kBarrierSpins)
+    return RS_ERR_ARG;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return RS_ERR_NO_DEVICE;
+  if (device < 0 || device >= count) return RS_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return RS_ERR_CUDA;
+  int grid = 0;
+  if (cudaDeviceGetAttribute(&grid, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return RS_ERR_CUDA;
+  if (skip_block >= grid) return RS_ERR_ARG;
+  unsigned* bar = nullptr;
+  int* d_err = nullptr;
+  int* passed = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  rs_status rc = RS_ERR_CUDA;
+  std::vector<int> h(grid);
+  void* args[] = {&bar, &d_err, &skip_block, &spins, &rounds, &passed};
+  if (cudaMalloc(&bar, sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&d_err, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&passed, sizeof(int) * grid) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
+      cudaMemset(bar, 0, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(d_err, 0, sizeof(int)) != cudaSuccess ||
+      cudaMemset(passed, 0xff, sizeof(int) * grid) != cudaSuccess)
+    goto done;
+  if (cudaEventRecord(e0, nullptr) != cudaSuccess ||
+      cudaLaunchCooperativeKernel((const void*)barrier_probe_kernel, dim3(grid), dim3(128), args,
+                                  0, nullptr) != cudaSuccess ||
+      cudaEventRecord(e1, nullptr) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(err, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(h.data(), passed, sizeof(int) * grid, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)
+    goto done;
+  *passed_min = rounds;
+  *passed_max = 0;
+  for (int b = 0; b < grid; ++b)
+    if (b != skip_block) {
+      *passed_min = std::min(*passed_min, h[b]);
+      *passed_max = std::max(*passed_max, h[b]);
+    }
+  rc = RS_OK;
+done:
+  if (rc != RS_OK) (void)cudaGetLastError();
+  cudaFree(bar);
+  cudaFree(d_err);
+  cudaFree(passed);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return rc;
+}

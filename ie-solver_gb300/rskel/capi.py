@@ -28,7 +28,7 @@ EXPORTS = ["rs_config_default", "rs_create", "rs_destroy", "rs_set_geometry", "r
            "rs_build_tree",
            "rs_factor", "rs_solve", "rs_solve_device", "rs_kernel_block", "rs_matvec",
            "rs_matvec_fast", "rs_domain_eval",
-           "rs_id_batched", "rs_id_noalloc", "rs_rank_model_init", "rs_set_rank_model",
+           "rs_id_batched", "rs_id_noalloc", "rs_barrier_selftest", "rs_rank_model_init", "rs_set_rank_model",
            "rs_rank_samples", "rs_rank_train", "rs_rank_predict", "rs_rank_gradient",
            "rs_get_stats", "rs_node_info", "rs_node_list", "rs_tree_bounds",
            "rs_allskel", "rs_timer_start", "rs_timer_stop", "rs_synchronize", "rs_last_error"]
@@ -104,6 +104,8 @@ def lib():
                                      _dp, ctypes.c_int, _dp]
         L.rs_id_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_double, _vp, _vp, _vp,
                                     _vp]
+        L.rs_barrier_selftest.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.c_int,
+                                          _ip, _ip, _ip, ctypes.POINTER(ctypes.c_float)]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.rs_rank_model_init.argtypes = [ctypes.c_uint64, _fp]
         L.rs_rank_model_init.restype = None
@@ -487,3 +489,14 @@ def id_batched(solver, mats, tol):
         z = Z[z_off[i]:z_off[i] + k * (n[i] - k)].reshape((k, n[i] - k), order="F") if k else None
         out.append((k, p, z))
     return out
+
+
+def barrier_selftest(device=0, skip_block=-1, spins=1 << 16, rounds=8):
+    """rs_barrier_selftest: returns (err, passed_min, passed_max, ms)."""
+    err, pmin, pmax = ctypes.c_int(-1), ctypes.c_int(-1), ctypes.c_int(-1)
+    ms = ctypes.c_float(0)
+    rc = lib().rs_barrier_selftest(device, skip_block, spins, rounds, ctypes.byref(err),
+                                   ctypes.byref(pmin), ctypes.byref(pmax), ctypes.byref(ms))
+    if rc != 0:
+        raise RsError(rc, "barrier self-test failed")
+    return err.value, pmin.value, pmax.value, ms.value

@@ -201,7 +201,12 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
  * `stream` (a cudaStream_t; NULL = the legacy default stream) of the current
  * device, with no device allocation.  No counterpart in the reference: it is
  * rs_id_batched's kernel with its global scratch tile taken from a fixed
- * 4 MiB file-scope device array instead of cudaMalloc.
+ * 4 MiB file-scope device array instead of cudaMalloc.  It is meant for
+ * callers that cannot allocate device memory: a process whose device memory
+ * is owned by another caching allocator (PyTorch's, for instance), or a
+ * stream pipeline that cannot take cudaMalloc/cudaFree's implicit device
+ * synchronisation.  The array stays resident on every device that loads the
+ * library until the process exits.
  * Outputs (device pointers): *rank = k (0 = no compression), perm = n
  * 0-based column indices, Z = k x (n - k) column major (reserve n*n/4 + 1
  * doubles).  Asynchronous: results are ready when `stream` is.
@@ -211,11 +216,28 @@ rs_status rs_id_batched(rs_solver* s, int count, const double* mats, const int64
  * 227 KB; larger sizes return RS_ERR_CAPACITY without touching the device.
  * The first call on a device sets up the device (symbol addresses and the
  * kernel's shared-memory attribute): make it before any stream capture.
+ * The set-up is kept for the life of the process: after a cudaDeviceReset
+ * of a device, do not call this entry point on that device again.
  * All calls on a device share the scratch array: calls that overlap in time
  * race and must be serialised by the caller.  Nothing needs to start at
- * zero. */
+ * zero.  A CUDA error already pending in the calling thread is returned as
+ * RS_ERR_CUDA (and left pending) without launching anything. */
 rs_status rs_id_noalloc(int m, int n, const double* A, double tol, int* rank, int* perm,
                         double* Z, void* stream);
+
+/* Self-test of the bounded grid barrier that the cooperative kernels (the
+ * bordered system's S inverse) synchronise with.  No counterpart in the
+ * reference, which has no GPU code.  Runs `rounds` (1..64) grid barriers on
+ * `device` over one CTA per SM, each wait limited to `spins` polls (at most
+ * the production limit of 2^22).  CTA `skip_block` (-1: none) leaves
+ * without arriving, so the other CTAs' waits run out: they raise the error
+ * flag and return, the way a barrier timeout surfaces in rs_factor as
+ * RS_ERR_CUDA "grid barrier timed out", with the context still usable.
+ * Outputs: *err = the flag (0 or 1), the fewest and most barriers passed by
+ * the CTAs that ran them, and the kernel's device time in ms.  Allocates a
+ * few bytes of device memory per call. */
+rs_status rs_barrier_selftest(int device, int skip_block, unsigned spins, int rounds, int* err,
+                              int* passed_min, int* passed_max, float* ms);
 
 /* --- learned skeleton ranks (the RS_FP32_REFINE factorization's ID) ---
  * No counterpart in the reference.  A 16 -> 64 -> 64 -> 1 multilayer

@@ -4,10 +4,20 @@ the same matrices.
 
 This file is collected last so that its GPU test also runs after every other
 GPU test of the session (the static scratch then holds whatever the earlier
-calls left in it).  Tolerances: equal rank and pivot order on matrices with a
-clear singular-value gap; |Z - Z_batched| <= 1e-9 max(1, |Z|) (the two paths
-order the same FP64 operations differently); ID reconstruction error within
-100 tol |A|, as for rs_id_batched against the reference's ID matrices.
+calls left in it).  The largest documented sizes run first (m = 2048 with
+n = 222 and m = 1024 with n = 478 fill the 524288-double array to within
+2 %), so every later, smaller call starts on a scratch array holding a
+full-size tile's values, which it must overwrite before reading.
+
+Tolerances: equal rank and pivot order on matrices with a clear
+singular-value gap; |Z - Z_batched| <= 1e-9 max(1, |Z|) (the two paths order
+the same FP64 operations differently); ID reconstruction error within
+100 tol |A|, as for rs_id_batched against the reference's ID matrices.  On
+those matrices the rank may differ by one: rs_id_batched folds the rows
+into an n x n triangle by Householder reflections before the pivoted QR,
+while this entry point runs the pivoted QR on the whole m x n tile, so the
+two compute |R_ii| with different roundings, and the reference's matrices
+have singular values that decay smoothly through the threshold tol |R_00|.
 """
 import os
 
@@ -61,20 +71,24 @@ def test_noalloc_matches_batched_two_calls_in_a_row(solver_lib):
     s = capi.Solver(g.unit_circle(64), capi.RS_LAPLACE, 1e-8)
     rng = np.random.default_rng(11)
     tol = 1e-8
-    # two calls in a row, the second smaller than the first, then the first again
+    # the two largest documented sizes, then two calls in a row, the second
+    # smaller than the first, then the first again
+    full = [_gapped(rng, 2048, 222, 60), _gapped(rng, 1024, 478, 60)]
     cases = [_gapped(rng, 640, 200, 40), _gapped(rng, 150, 48, 12)]
     first = None
-    for A in cases + [cases[0]]:
+    for A in full + cases + [cases[0]]:
         k, perm, Z = _noalloc(capi, torch, A, tol)
         (kb, pb, zb), = capi.id_batched(s, [A], tol)
         assert k == kb and np.array_equal(perm, pb), (k, kb)
         assert np.abs(Z - zb).max() <= 1e-9 * max(1.0, np.abs(zb).max())
         err = np.linalg.norm(A[:, perm[k:]] - A[:, perm[:k]] @ Z, 2)
         assert err <= 100 * tol * np.linalg.norm(A, 2)
-        if first is None:
-            first = (k, perm, Z)
-        elif A is cases[0]:
-            assert first[0] == k and np.array_equal(first[1], perm) and np.array_equal(first[2], Z)
+        if A is cases[0]:
+            if first is None:
+                first = (k, perm, Z)
+            else:  # the repeated call gives the same result bit for bit
+                assert first[0] == k and np.array_equal(first[1], perm)
+                assert np.array_equal(first[2], Z)
     # the reference's own ID matrices (rank within one of rs_id_batched's)
     d = np.load(os.path.join(os.path.dirname(__file__), "golden", "id_cases.npz"))
     for i in range(len(d["ranks"])):
