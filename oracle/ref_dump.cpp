@@ -132,6 +132,47 @@ void dense_residual(const Kernel& kernel, int ndofs, const ie_Mat& mu, const ie_
   }
 }
 
+// The tree in level order: node fields, DOF lists and neighbour lists.
+void write_tree(Writer& w, QuadTree& tree) {
+  std::unordered_map<const QuadTreeNode*, int> gid;
+  std::vector<const QuadTreeNode*> order;
+  std::vector<int32_t> level_sizes;
+  for (QuadTreeLevel* lvl : tree.levels) {
+    level_sizes.push_back((int32_t)lvl->nodes.size());
+    for (QuadTreeNode* nd : lvl->nodes) { gid[nd] = (int)order.size(); order.push_back(nd); }
+  }
+  std::vector<int32_t> lev, leaf, parent, children, compressed, nbr_off, nbr, orig_off, orig,
+      act_off, act, skel_off, skel, red_off, red, near_off, near;
+  std::vector<double> corners, side;
+  for (const QuadTreeNode* nd : order) {
+    lev.push_back(nd->level);
+    leaf.push_back(nd->is_leaf ? 1 : 0);
+    parent.push_back(nd->parent ? gid[nd->parent] : -1);
+    for (int c = 0; c < 4; ++c) children.push_back(nd->children[c] ? gid[nd->children[c]] : -1);
+    compressed.push_back(nd->compressed ? 1 : 0);
+    for (int c = 0; c < 8; ++c) corners.push_back(nd->corners[c]);
+    side.push_back(nd->side_length);
+    std::vector<int> nb;
+    for (QuadTreeNode* x : nd->neighbors) nb.push_back(gid[x]);
+    csr_append(&nbr_off, &nbr, nb);
+    csr_append(&orig_off, &orig, nd->src_dof_lists.original_box);
+    csr_append(&act_off, &act, nd->src_dof_lists.active_box);
+    csr_append(&skel_off, &skel, nd->src_dof_lists.skel);
+    csr_append(&red_off, &red, nd->src_dof_lists.redundant);
+    csr_append(&near_off, &near, nd->src_dof_lists.near);
+  }
+  w.i32("level_sizes", level_sizes);
+  w.i32("node_level", lev); w.i32("node_leaf", leaf); w.i32("node_parent", parent);
+  w.i32("node_children", children); w.i32("node_compressed", compressed);
+  w.f64("node_corners", corners); w.f64("node_side", side);
+  w.i32("nbr_off", nbr_off); w.i32("nbr", nbr);
+  w.i32("orig_off", orig_off); w.i32("orig", orig);
+  w.i32("active_off", act_off); w.i32("active", act);
+  w.i32("skel_off", skel_off); w.i32("skel", skel);
+  w.i32("red_off", red_off); w.i32("red", red);
+  w.i32("near_off", near_off); w.i32("near", near);
+}
+
 int run_id_mode(const char* in, const char* out) {
   // "ID mode": read matrices (int32 count; per matrix int32 m, n; double tol;
   // double a[m*n] column major), run ie_Mat::id on each, write rank/perm/Z.
@@ -164,10 +205,52 @@ int run_id_mode(const char* in, const char* out) {
   return 0;
 }
 
+DataBoundary boundary_of(const Problem& pr) {
+  DataBoundary bnd;
+  bnd.boundary_shape = Boundary::BoundaryShape::CIRCLE;
+  bnd.points = pr.pts; bnd.normals = pr.nrm; bnd.weights = pr.w; bnd.curvatures = pr.curv;
+  for (int i = 0; i < pr.h; ++i) {
+    Hole hole;
+    hole.center = Vec2(pr.hc[2 * i], pr.hc[2 * i + 1]);
+    hole.radius = pr.hr[i];
+    hole.num_nodes = 0;
+    bnd.holes.push_back(hole);
+  }
+  return bnd;
+}
+
+int run_perturb_mode(int count, char** in, const char* out) {
+  // "perturb mode": QuadTree::initialize_tree on the first problem's
+  // boundary, then QuadTree::perturb (quadtree.cpp:520-801) with each later
+  // problem's boundary in turn; writes the final tree.  No factorization:
+  // the tree update does not depend on which boxes are compressed.
+  std::vector<Problem> prs(count);
+  for (int i = 0; i < count; ++i)
+    if (!read_problem(in[i], &prs[i])) { fprintf(stderr, "bad problem file\n"); return 2; }
+  if (prs[0].leaf != MAX_LEAF_DOFS) {
+    fprintf(stderr, "this binary is built for leaf %d\n", MAX_LEAF_DOFS);
+    return 3;
+  }
+  DataBoundary first = boundary_of(prs[0]);
+  QuadTree tree;
+  tree.initialize_tree(&first, std::vector<double>(), prs[0].sd, 2);
+  for (int i = 1; i < count; ++i) {
+    DataBoundary next = boundary_of(prs[i]);
+    tree.perturb(next);
+  }
+  Writer w(out);
+  if (!w.f) return 4;
+  write_tree(w, tree);
+  w.f64("tree_minmax", std::vector<double>{tree.min, tree.max});
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc == 4 && std::string(argv[1]) == "--id") return run_id_mode(argv[2], argv[3]);
+  if (argc >= 5 && std::string(argv[1]) == "--perturb")
+    return run_perturb_mode(argc - 3, argv + 2, argv[argc - 1]);
   // optional third argument --strong: SkelFactorization with strong admissibility
   const bool strong = argc == 4 && std::string(argv[3]) == "--strong";
   if (argc != 3 && !strong) {
@@ -229,43 +312,7 @@ int main(int argc, char** argv) {
   Writer w(argv[2]);
   if (!w.f) return 4;
   QuadTree& tree = *keep;
-  std::unordered_map<const QuadTreeNode*, int> gid;
-  std::vector<const QuadTreeNode*> order;
-  std::vector<int32_t> level_sizes;
-  for (QuadTreeLevel* lvl : tree.levels) {
-    level_sizes.push_back((int32_t)lvl->nodes.size());
-    for (QuadTreeNode* nd : lvl->nodes) { gid[nd] = (int)order.size(); order.push_back(nd); }
-  }
-  std::vector<int32_t> lev, leaf, parent, children, compressed, nbr_off, nbr, orig_off, orig,
-      act_off, act, skel_off, skel, red_off, red, near_off, near;
-  std::vector<double> corners, side;
-  for (const QuadTreeNode* nd : order) {
-    lev.push_back(nd->level);
-    leaf.push_back(nd->is_leaf ? 1 : 0);
-    parent.push_back(nd->parent ? gid[nd->parent] : -1);
-    for (int c = 0; c < 4; ++c) children.push_back(nd->children[c] ? gid[nd->children[c]] : -1);
-    compressed.push_back(nd->compressed ? 1 : 0);
-    for (int c = 0; c < 8; ++c) corners.push_back(nd->corners[c]);
-    side.push_back(nd->side_length);
-    std::vector<int> nb;
-    for (QuadTreeNode* x : nd->neighbors) nb.push_back(gid[x]);
-    csr_append(&nbr_off, &nbr, nb);
-    csr_append(&orig_off, &orig, nd->src_dof_lists.original_box);
-    csr_append(&act_off, &act, nd->src_dof_lists.active_box);
-    csr_append(&skel_off, &skel, nd->src_dof_lists.skel);
-    csr_append(&red_off, &red, nd->src_dof_lists.redundant);
-    csr_append(&near_off, &near, nd->src_dof_lists.near);
-  }
-  w.i32("level_sizes", level_sizes);
-  w.i32("node_level", lev); w.i32("node_leaf", leaf); w.i32("node_parent", parent);
-  w.i32("node_children", children); w.i32("node_compressed", compressed);
-  w.f64("node_corners", corners); w.f64("node_side", side);
-  w.i32("nbr_off", nbr_off); w.i32("nbr", nbr);
-  w.i32("orig_off", orig_off); w.i32("orig", orig);
-  w.i32("active_off", act_off); w.i32("active", act);
-  w.i32("skel_off", skel_off); w.i32("skel", skel);
-  w.i32("red_off", red_off); w.i32("red", red);
-  w.i32("near_off", near_off); w.i32("near", near);
+  write_tree(w, tree);
   std::vector<int32_t> allskel(tree.root->src_dof_lists.active_box.begin(),
                                tree.root->src_dof_lists.active_box.end());
   w.i32("allskel", allskel);

@@ -96,6 +96,25 @@ def run_reference_id(mats, tols, leaf=64, npp=64):
         return read_result(pout)
 
 
+def run_reference_perturb(geos, sd, leaf=32, npp=128, timeout=600):
+    """The reference's QuadTree::initialize_tree on geos[0], then
+    QuadTree::perturb with geos[1], geos[2], ... in turn; returns the final
+    tree (the result-file fields of a solve run, without the solution)."""
+    exe = ref_binary(leaf, npp)
+    if exe is None:
+        raise FileNotFoundError("reference build missing (make -C oracle ref)")
+    with tempfile.TemporaryDirectory() as td:
+        paths = []
+        for i, geo in enumerate(geos):
+            pth = os.path.join(td, f"p{i}.rsp")
+            write_problem(pth, geo, 0 if sd == 1 else 2, sd, np.zeros(geo.n * sd), 1e-8, leaf,
+                          npp)
+            paths.append(pth)
+        pout = os.path.join(td, "r.rsr")
+        subprocess.run([exe, "--perturb", *paths, pout], check=True, timeout=timeout)
+        return read_result(pout)
+
+
 def csr(res, name, i):
     off = res[name + "_off"]
     return res[name][off[i]:off[i + 1]]

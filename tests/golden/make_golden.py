@@ -58,6 +58,33 @@ def cases():
     return out
 
 
+def subset(geo, keep):
+    """The boundary with only the nodes where `keep` is true."""
+    xy, nv = geo.points.reshape(-1, 2), geo.normals.reshape(-1, 2)
+    return g.Geometry(xy[keep].ravel(), nv[keep].ravel(), geo.weights[keep],
+                      geo.curvatures[keep], geo.hole_centers, geo.hole_radii, int(keep.sum()))
+
+
+def perturb_cases():
+    """(name, sd, leaf, npp, [boundaries]): QuadTree::initialize_tree on the
+    first boundary, then QuadTree::perturb with each later one.  A bump
+    moving along a star moves points between leaves (bursting leaves split);
+    removing every third node of the bump's arc and putting it back empties
+    and refills leaves (sparse subtrees are consolidated, then split again)."""
+    out = []
+    for height, sd, leaf, npp in ((0.05, 1, 32, 128), (0.2, 1, 32, 128), (0.2, 1, 64, 64),
+                                  (0.3, 2, 32, 128)):
+        geos = [g.star_bump(4096, center=float(c), height=height)
+                for c in [0.0] + list(np.linspace(0.3, 3.0, 5))]
+        out.append((f"bump{height:g}_sd{sd}_leaf{leaf}", sd, leaf, npp, geos))
+    base = g.star_bump(4096, center=1.0, height=0.2)
+    t = np.arange(base.n)
+    arc = (t > 400) & (t < 1400)
+    thin = subset(base, ~(arc & (t % 3 != 0)))
+    out.append(("thin_refill_leaf32", 1, 32, 128, [base, thin, base, thin]))
+    return out
+
+
 def save_geometry(d, geo):
     d["points"] = geo.points
     d["normals"] = geo.normals
@@ -107,6 +134,15 @@ def main():
         d[f"A{i}"] = A
     np.savez_compressed(os.path.join(OUT, "id_cases.npz"), **d)
     print("id cases", len(mats), "ranks", ref["ranks"])
+    # perturbed trees: the reference's QuadTree::perturb after each sequence
+    d = {}
+    for name, sd, leaf, npp, geos in perturb_cases():
+        res = refio.run_reference_perturb(geos, sd, leaf, npp)
+        for k in ("level_sizes", "node_level", "node_leaf", "node_parent", "node_children",
+                  "node_corners", "nbr_off", "nbr", "orig_off", "orig"):
+            d[f"{name}/{k}"] = res[k]
+        print("perturb", name, "levels", list(res["level_sizes"]))
+    np.savez_compressed(os.path.join(OUT, "perturb_trees.npz"), **d)
 
 
 if __name__ == "__main__":

@@ -1,9 +1,88 @@
 """Host-side QuadTree::perturb (quadtree.cpp:435-801) through rs_perturb on a
 tree that has not been factored (no GPU needed): after moving a local bump
 along a star-shaped boundary, the updated tree must still be a valid
-quadtree of the new points."""
+quadtree of the new points, and it must equal, bit for bit, the tree the
+reference's own QuadTree::perturb leaves after the same sequence of
+boundaries (tests/golden/perturb_trees.npz, made by the reference built from
+its sources through oracle/ref_dump.cpp --perturb; the live reference too
+where its build is present).
+
+Compared: level sizes, node order, levels, leaf flags, parents, children,
+corners, neighbour lists and the leaves' DOF lists in order.  Interior
+boxes' DOF lists are not compared: the reference remaps original_box on
+leaves only (quadtree.cpp:585-597), so after a perturbation its interior
+lists keep the old numbering, which nothing reads (the factorization builds
+interior active lists from the children, quadtree.cpp:1032-1055).
+"""
+import os
+import sys
+
 import numpy as np
 import pytest
+
+from conftest import GOLDEN
+
+STRUCT_KEYS = ("level_sizes", "node_level", "node_leaf", "node_parent", "node_children",
+               "node_corners", "nbr_off", "nbr")
+
+
+def _leaf_lists(d):
+    return [d["orig"][d["orig_off"][i]:d["orig_off"][i + 1]].tolist()
+            for i in range(len(d["node_level"])) if d["node_leaf"][i]]
+
+
+def _perturb_cases():
+    sys.path.insert(0, os.path.join(GOLDEN))
+    import make_golden
+
+    return make_golden.perturb_cases()
+
+
+def _product_tree(capi, sd, leaf, npp, geos):
+    pde = capi.RS_LAPLACE if sd == 1 else capi.RS_STOKES
+    s = capi.Solver(geos[0], pde, 1e-8, leaf=leaf, npp=npp)
+    s.build_tree()
+    for geo in geos[1:]:
+        s.set_geometry(geo, perturb=True)
+    d = s.tree_dump()
+    s.close()
+    return d
+
+
+def _assert_same_tree(d, r, name):
+    for k in STRUCT_KEYS:
+        assert np.array_equal(d[k], r[k]), (name, k)
+    assert _leaf_lists(d) == _leaf_lists(r), name
+
+
+def test_perturbed_trees_match_the_reference_fixtures(solver_lib):
+    ref = np.load(os.path.join(GOLDEN, "perturb_trees.npz"))
+    for name, sd, leaf, npp, geos in _perturb_cases():
+        r = {k: ref[f"{name}/{k}"] for k in STRUCT_KEYS + ("orig_off", "orig")}
+        d = _product_tree(solver_lib, sd, leaf, npp, geos)
+        _assert_same_tree(d, r, name)
+        # the history matters: a fresh tree of the last boundary differs
+        f = solver_lib.Solver(geos[-1], solver_lib.RS_LAPLACE if sd == 1 else solver_lib.RS_STOKES,
+                              1e-8, leaf=leaf, npp=npp)
+        f.build_tree()
+        fd = f.tree_dump()
+        f.close()
+        assert not (np.array_equal(fd["level_sizes"], d["level_sizes"]) and
+                    np.array_equal(fd["nbr"], d["nbr"])), name
+
+
+def test_perturbed_tree_matches_the_live_reference(solver_lib):
+    refio = pytest.importorskip("refio")
+    if refio.ref_binary(32, 128) is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    from rskel import geometry as G
+
+    rng = np.random.default_rng(21)
+    geos = [G.star_bump(3000, center=float(c), height=float(h))
+            for c, h in zip(rng.uniform(0, 6.28, 4), rng.uniform(0.05, 0.3, 4))]
+    for sd in (1, 2):
+        r = refio.run_reference_perturb(geos, sd, 32, 128)
+        _assert_same_tree(_product_tree(solver_lib, sd, 32, 128, geos), r, f"live sd{sd}")
 
 
 def _check_tree(s, geo, leaf):
