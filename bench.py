@@ -11,10 +11,11 @@ alone between L2 flushes (CUDA events around it); ms_per_step is the mean of
 the K timed steps, the maximum over ranks, and ms_median their median.
 
 Three arms run: plain FP64 (the reference's arithmetic), FP32 factorization
-+ FP64 iterative refinement to a relative residual of 1e-10 (confirmed by a fresh float-float residual), and the same
-with learned sketch sizes (the rank model trained, before timing, on ranks
-the plain FP32 factorization gets on 24 other seeded star and ellipse
-curves).  The headline is the learned refined arm when its solutions are
++ FP64 iterative refinement to a relative residual of 1e-10 (confirmed by a
+fresh float-float residual), and the same with learned sketch sizes (the
+rank model trained, before timing, on the ranks plain FP32 factorizations
+get on 2000 seeded star, rose and ellipse boundaries, Laplace and Stokes;
+rskel/rank_training.py).  The headline is the learned refined arm when its solutions are
 within 1e-8 of the exact discrete solution (the FP64 oracle at tolerance
 1e-12), else the plain refined arm under the same test, else plain FP64.
 Errors against the oracle at the configuration's own tolerance 1e-8 are
@@ -247,33 +248,15 @@ def make_solver(capi, geo, precision, device, model=None):
     return s
 
 
-TRAIN_CURVES, TRAIN_SEED, TRAIN_EPOCHS = 24, 5, 3000
-
-
 def train_rank_model(capi, device):
-    """Rank model for the learned arm: samples (box features, k/n) from plain
-    FP32 factorizations of seeded training curves (none of them the
-    benchmark's star), then full-batch Adam on the GPU.  Not timed."""
-    from rskel import geometry as g
+    """Rank model for the learned arms: (box features, k/n) samples from
+    plain FP32 factorizations of the 2000 seeded training boundaries (random
+    stars, rose curves, ellipses; none of them a benchmark geometry), with
+    the Laplace and the Stokes kernel, then full-batch Adam on the GPU by the
+    library's own kernels.  Not timed."""
+    from rskel import rank_training
 
-    t0 = time.perf_counter()
-    Xs, ys = [], []
-    for geo in g.rank_training_curves(TRAIN_CURVES, TRAIN_SEED):
-        s = make_solver(capi, geo, capi.RS_FP32_REFINE, device)
-        s.factor()
-        X, y = s.rank_samples()
-        Xs.append(X)
-        ys.append(y)
-        s.close()
-    X, y = np.concatenate(Xs), np.concatenate(ys)
-    t1 = time.perf_counter()
-    s = make_solver(capi, g.unit_circle(64), capi.RS_FP32_REFINE, device)
-    w, loss = s.rank_train(X, y, capi.rank_model_init(0), epochs=TRAIN_EPOCHS, lr=3e-3)
-    s.close()
-    info = {"curves": TRAIN_CURVES, "seed": TRAIN_SEED, "samples": int(len(y)),
-            "epochs": TRAIN_EPOCHS, "final_mse": loss, "collect_s": t1 - t0,
-            "train_s": time.perf_counter() - t1}
-    return w, info
+    return rank_training.train_family(device=device)
 
 
 def time_arm(capi, geo, F, precision, steps, warmup, cu, dist, model=None, tune=None):
@@ -367,7 +350,7 @@ def breakdown(st, total_ms):
     return b
 
 
-def other_configs(capi, dist, steps):
+def other_configs(capi, dist, steps, model=None):
     """The other configurations, measured with inputs resident on the device
     (each a few steps; not the headline): a batch of 512 random stars in one
     handle, and Stokes with 16 holes at 262144 DOFs."""
@@ -430,7 +413,57 @@ def other_configs(capi, dist, steps):
             rec["refine_residual"] = st["refine_residual"]
         s.close()
     out["stokes_16_ellipses_262144"] = rec
+    if model is not None:
+        out["stokes_64_ellipses_1048576"] = stokes64(capi, dist, model)
     return out
+
+
+def stokes64(capi, dist, model):
+    """Stokes, unit circle + 64 ellipses, 524288 points (1048576 DOFs), tol
+    1e-8: plain FP64, FP32 factor + FP64 GMRES-IR without and with learned
+    sketch sizes; errors against the oracle's solution at tolerance 1e-12
+    (tests/golden/stokes_64_ellipses_1m_oracle.npz)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location(
+        "make_fullsize", os.path.join(ROOT, "tests", "golden", "make_fullsize.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    geo, F = mk.workload()
+    ref = np.load(mk.OUT)["mu"] if os.path.exists(mk.OUT) else None
+    rec = {"workload": "Stokes DLP, unit circle + 64 ellipses, 524288 points, tol 1e-8",
+           "dofs": 2 * geo.n}
+    for name, prec, w in (("fp64", capi.RS_FP64, None), ("fp32_refine", capi.RS_FP32_REFINE, None),
+                          ("fp32_refine_learned", capi.RS_FP32_REFINE, model)):
+        s = capi.Solver(geo, capi.RS_STOKES, TOL, leaf=LEAF, npp=NPP, precision=prec,
+                        refine_tol=REFINE_TOL, refine_max_iters=10, device=dist.local)
+        if w is not None:
+            s.set_rank_model(w)
+        s.build_tree()
+        ts = []
+        for i in range(2 if prec == capi.RS_FP64 else 3):
+            s.synchronize()
+            s.timer_start()
+            s.factor()
+            mu, _ = s.solve(F)
+            if i > 0:
+                ts.append(s.timer_stop())
+        st = s.stats()
+        r = {"ms_median": statistics.median(ts),
+             "dofs_per_s": 2 * geo.n / (statistics.median(ts) * 1e-3),
+             "id_ms": st["id_ms"]}
+        if ref is not None:
+            r["rel_err_vs_oracle_tol1e-12"] = float(np.linalg.norm(mu - ref) / np.linalg.norm(ref))
+        if prec == capi.RS_FP32_REFINE:
+            r.update(refine_iters=st["refine_iters"], refine_residual=st["refine_residual"],
+                     krylov_steps=st["krylov_steps"], sketch_rows=st["sketch_rows"])
+        if w is not None:
+            r.update(boxes_predicted=st["rank_predicted"], boxes_redone=st["rank_redo"],
+                     boxes_redone_by_judge=st["rank_redo_judge"])
+        rec[name] = r
+        s.close()
+    rec["speedup_learned_vs_fp64"] = rec["fp64"]["ms_median"] / rec["fp32_refine_learned"]["ms_median"]
+    return rec
 
 
 def run_gpu(args):
@@ -505,7 +538,6 @@ def run_gpu(args):
         "data": "synthetic (seeded star curve, exterior point-source data)",
         "config": config(dist.ws),
         "arm": head,
-        "accuracy": acc,
         "plain_fp64": {"value": dist.sum(dofs) / (ms64 * 1e-3), "ms_per_step": ms64,
                        "ms_median": statistics.median(t64),
                        "breakdown_ms": breakdown(st64[-1], statistics.median(t64))},
@@ -540,8 +572,11 @@ def run_gpu(args):
                                    "restatement (OpenMP over boxes, all host cores), median"},
         "clocks": clocks,
         "gpu_launches": launches,
-        "other_configs": other_configs(capi, dist, args.steps) if not args.headline_only else None,
+        "other_configs": (other_configs(capi, dist, args.steps, model)
+                          if not args.headline_only else None),
     }
+    # last, so that the end of the line (what a log tail keeps) holds it
+    line["accuracy"] = acc
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()

@@ -21,8 +21,11 @@
 #include <algorithm>
 #include <cstdio>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "kernels.hpp"
+#include "tcgen05.cuh"
 
 namespace rskel {
 
@@ -122,14 +125,15 @@ size_t id_kernel_smem(int n, bool fp32, bool tile_in_smem) {
   return fp32 ? id_smem_bytes<float>(n, tile_in_smem) : id_smem_bytes<double>(n, tile_in_smem);
 }
 
+template <class Real>
+__device__ void stage_chunk_rows(const IdParams& p, const IdTask& t, IdShared<Real>& S, int c0,
+                                 int cnt, double ox, double oy);
+
 // Fills chunk rows [c0, c0 + cnt) of the virtual ID matrix into S.C (row major).
 template <class Real>
 __device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S, int ld, int c0,
                            int cnt, double ox, double oy) {
-  const int n = t.n, q = t.q;
-  const int sd = p.sd;
-  const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;  // rows per proxy block
-  const double pw = 2.0 * CUDART_PI * t.pr / p.npp;
+  const int n = t.n;
   if (t.dense_off >= 0) {
     const double* A = p.dense + t.dense_off;
     for (int e = threadIdx.x; e < kChunk * n; e += blockDim.x) {
@@ -139,7 +143,28 @@ __device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S
     __syncthreads();
     return;
   }
-  // stage the "other" point of each chunk row
+  stage_chunk_rows<Real>(p, t, S, c0, cnt, ox, oy);
+  __syncthreads();
+  for (TileWalk w(n); w.j < kChunk; w.next()) {  // row i = w.j, column j = w.i
+    const int i = w.j, j = w.i;
+    int kind = S.kind[i];
+    Real val = (Real)0;
+    if (kind == 0 || kind == 2) val = kernel_dofs<Real>(p.pde, S.row, i, S.act, j);
+    else if (kind == 1 || kind == 3) val = kernel_dofs<Real>(p.pde, S.act, j, S.row, i);
+    S.C[(size_t)i * ld + j] = val;
+  }
+  __syncthreads();
+}
+
+// Stages the "other" point of chunk rows [c0, c0 + cnt) of the virtual ID
+// matrix (a row DOF, or a proxy point) and the row's kind in S.row / S.kind.
+template <class Real>
+__device__ void stage_chunk_rows(const IdParams& p, const IdTask& t, IdShared<Real>& S, int c0,
+                                 int cnt, double ox, double oy) {
+  const int q = t.q;
+  const int sd = p.sd;
+  const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;  // rows per proxy block
+  const double pw = 2.0 * CUDART_PI * t.pr / p.npp;
   for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
     int v = c0 + i;
     int kind = -1;
@@ -167,16 +192,6 @@ __device__ void fill_chunk(const IdParams& p, const IdTask& t, IdShared<Real>& S
     }
     S.kind[i] = kind;
   }
-  __syncthreads();
-  for (TileWalk w(n); w.j < kChunk; w.next()) {  // row i = w.j, column j = w.i
-    const int i = w.j, j = w.i;
-    int kind = S.kind[i];
-    Real val = (Real)0;
-    if (kind == 0 || kind == 2) val = kernel_dofs<Real>(p.pde, S.row, i, S.act, j);
-    else if (kind == 1 || kind == 3) val = kernel_dofs<Real>(p.pde, S.act, j, S.row, i);
-    S.C[(size_t)i * ld + j] = val;
-  }
-  __syncthreads();
 }
 
 // Folds the chunk into R: Householder QR of [R; C] with R upper triangular.
@@ -560,24 +575,191 @@ __device__ __forceinline__ int task_ell(const IdParams& p, const IdTask& t) {
 }
 
 // A truncated sketch (mr = ell < m rows) settles the rank only when the rank
-// rule stopped with at least kMinSlack rows to spare; otherwise (no stop
-// within min(n, ell) pivots, or k > ell - kMinSlack) the box is redone.
+// rule stopped with at least `slack` rows to spare; otherwise (no stop
+// within min(n, ell) pivots, or k > ell - slack) the box is redone.  Without
+// the residual judge the slack is kMinSlack rows; with it, one row (the QR
+// stopped before the rows ran out), since the judge's independent test rows
+// then check the interpolation residual that a short sketch can
+// underestimate.
 constexpr int kMinSlack = 8;
-__device__ __forceinline__ bool sketch_too_small(int k, int n, int m, int ell, int full) {
+__device__ __forceinline__ bool sketch_too_small(int k, int n, int m, int ell, int full,
+                                                 bool judged) {
   if (ell >= full || m <= ell) return false;
   if (k == 0) return true;  // no stop: n <= ell would mean full rank, but ell < n + 16 here
-  return k > ell - kMinSlack;
+  return k > ell - (judged ? 1 : kMinSlack);
 }
 
-size_t id_sketch_smem(int n) {
+// Test rows of the residual judge.  A learned pass's truncated sketch (fewer
+// rows than the full n + 16, of a matrix taller than the sketch) is followed
+// by kIdTestRows rows whose signs are independent of the sketch's (rows
+// kTestSignRow + t of the same hash), stored below the sketch.
+constexpr int kTestSignRow = 1 << 12;
+__device__ __forceinline__ int task_test_rows(const IdParams& p, const IdTask& t, int ell, int m) {
+  return (p.redo != nullptr && !p.redo_pass && p.judge_factor > 0.f && ell < sketch_rows(t.n) &&
+          m > ell)
+             ? kIdTestRows
+             : 0;
+}
+__device__ __forceinline__ float sketch_or_test_sign(int r, int ell, int nt, int i) {
+  if (r < ell) return sketch_sign(r, i);
+  return r < ell + nt ? sketch_sign(kTestSignRow + (r - ell), i) : 0.f;
+}
+
+// Residual estimate of an ID (k, perm, Z) from test rows Yt = Omega_t A
+// (nt rows of a row-major tile at Yt, leading dimension ld, columns in A's
+// order) and Z = R11^{-1} R12 (row i of Z at Z + i * ld, column c of Z at
+// offset k + c).  For each redundant column c,
+//   e = Yt(:, perm[k + c]) - Yt(:, perm[0..k)) Z(:, c) = Omega_t (A(:, perm[k+c]) - A(:, skel) Z(:, c)),
+// and E ||Omega_t x||^2 = nt ||x||^2 for +-1 signs, so sqrt(|e|^2 / nt)
+// estimates the interpolation residual of that column (Halko, Martinsson &
+// Tropp 2011, sec. 4.3: a handful of random test vectors bound the residual
+// with high probability).  Returns the squared estimate of the worst column
+// this thread (cstep = the threads sharing the columns) covers.
+__device__ __forceinline__ float judge_cols(const float* Yt, const float* Z, int ld, const int* perm,
+                                            int k, int n, int nt, int c0, int cstep) {
+  float mx = 0.f;
+  for (int c = c0; c < n - k; c += cstep) {
+    float ss = 0.f;
+    for (int t = 0; t < nt; ++t) {
+      const float* y = Yt + (size_t)t * ld;
+      float e = y[perm[k + c]];
+      for (int i = 0; i < k; ++i) e -= y[perm[i]] * Z[(size_t)i * ld + k + c];
+      ss += e * e;
+    }
+    mx = fmaxf(mx, ss);
+  }
+  return mx;
+}
+
+// Redo flag of a judged box: 0 keeps it, 1 = the sketch did not settle the
+// rank (sketch_too_small), 2 = the residual estimate is above the judge's
+// bound.  `worst_sq` is the largest squared column estimate times nt.
+__device__ __forceinline__ int judge_flag(const IdParams& p, float worst_sq, int nt, double thr_r00,
+                                          int ell, int slot) {
+  // thr_r00 = tol |R_00| of the ell-row sketch, and |R_00| estimates
+  // sqrt(ell) ||a_max|| (the largest column of A), so the bound
+  // judge_factor * tol * ||a_max|| is judge_factor * thr_r00 / sqrt(ell)
+  const double est = sqrt((double)worst_sq / nt);
+  const double unit = thr_r00 / sqrt((double)ell);
+  if (p.judge_ratio != nullptr) p.judge_ratio[slot] = unit > 0 ? (float)(est / unit) : -1.f;
+  return est > (double)p.judge_factor * unit ? 2 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core sketch (tcgen05).  Per 64-row chunk of the ID matrix, the
+// sketch update Y += Omega_chunk A_chunk is one tcgen05.mma group: the MMA's
+// M = sketch rows (sketch + test rows, padded to 128 per M tile), N = the
+// box's columns padded to 16, K = the chunk's rows.  Omega is exact in BF16
+// (+-1); the chunk of A is split in three BF16 parts, A = hi + mid + lo to
+// about FP32 precision, and the three products accumulate in one FP32
+// accumulator in tensor memory.  The CUDA cores form the kernel entries
+// (the split and the signs are a few instructions more), write them straight
+// into the operand tiles, and one thread issues the MMAs.
+// ---------------------------------------------------------------------------
+constexpr int kTcOmegaTile = 128 * kChunk * 2;   // bytes of one 128-row BF16 sign tile
+constexpr uint32_t kTcPolls = 1u << 24;          // bound of every wait on the MMA barrier
+
+__host__ __device__ inline int tc_npad(int n) { return (n + 15) & ~15; }
+__host__ __device__ inline int tc_mtiles(int rows) { return (rows + 127) >> 7; }
+// Operand tiles of a box of n columns with `rows` sketch rows: the sign tiles
+// (first, so that any reading of them stays inside the region), then the
+// three split tiles of the chunk.
+__host__ __device__ inline size_t tc_tile_bytes(int n, int rows) {
+  return (size_t)tc_mtiles(rows) * kTcOmegaTile + 3 * (size_t)tc_npad(n) * kChunk * 2;
+}
+__host__ __device__ inline uint32_t tc_tmem_cols(int cols) {
+  uint32_t c = 32;
+  while (c < (uint32_t)cols) c <<= 1;
+  return c;
+}
+
+// Eight sketch signs (bits) of sketch row s for chunk rows 8 grp .. 8 grp + 7.
+__device__ __forceinline__ uint32_t sketch_bits8(int s, int grp) {
+  unsigned x = (unsigned)s * 0x9E3779B1u ^ (unsigned)grp * 0x85EBCA77u ^ 0x6A09E667u;
+  x ^= x >> 15;
+  x *= 0x2C1B3C6Du;
+  x ^= x >> 12;
+  x *= 0x297A2D39u;
+  x ^= x >> 15;
+  return x >> 24;
+}
+
+// v = hi + mid + lo with BF16 parts (each difference is exact in FP32).
+__device__ __forceinline__ void split3(float v, uint16_t& h, uint16_t& m, uint16_t& l) {
+  const __nv_bfloat16 bh = __float2bfloat16_rn(v);
+  const float r1 = v - __bfloat162float(bh);
+  const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(bm);
+  h = __bfloat16_as_ushort(bh);
+  m = __bfloat16_as_ushort(bm);
+  l = __bfloat16_as_ushort(__float2bfloat16_rn(r2));
+}
+
+// Chunk rows [c0, c0 + cnt) (staged in S.row / S.kind) as the MMA operands:
+// B = the chunk's entries, npad x kChunk K-major, in three split tiles at
+// bt, bt + bbytes, bt + 2 bbytes; A = the signs of sketch rows [0, rows)
+// (zero below), mtiles tiles of 128 x kChunk at om.  Each thread forms 8
+// consecutive rows of one column (or 8 signs of one sketch row) and stores
+// one 16-byte core-matrix row per tile; consecutive threads take
+// consecutive columns (rows), so the stores are contiguous.
+__device__ void fill_chunk_tc(const IdParams& p, const IdTask& t, const IdShared<float>& S, int c0,
+                              int cnt, int npad, unsigned char* bt, uint32_t bbytes,
+                              unsigned char* om, int rows, int mtiles) {
+  const int n = t.n;
+  const int items = npad * (kChunk / 8);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int j = it % npad, g = it / npad;
+    uint32_t w[3][4];
+#pragma unroll
+    for (int q = 0; q < 8; q += 2) {
+      uint16_t h[2], md[2], lo[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int i = 8 * g + q + u;
+        float v = 0.f;
+        if (j < n && i < cnt) {
+          const int kind = S.kind[i];
+          if (kind == 0 || kind == 2) v = kernel_dofs<float>(p.pde, S.row, i, S.act, j);
+          else v = kernel_dofs<float>(p.pde, S.act, j, S.row, i);
+        }
+        split3(v, h[u], md[u], lo[u]);
+      }
+      w[0][q >> 1] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+      w[1][q >> 1] = (uint32_t)md[0] | ((uint32_t)md[1] << 16);
+      w[2][q >> 1] = (uint32_t)lo[0] | ((uint32_t)lo[1] << 16);
+    }
+    const uint32_t off = tc::tile_offset(j, 8 * g, npad);
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+      *reinterpret_cast<uint4*>(bt + (size_t)x * bbytes + off) =
+          make_uint4(w[x][0], w[x][1], w[x][2], w[x][3]);
+  }
+  const int orows = mtiles * 128;
+  for (int it = threadIdx.x; it < orows * (kChunk / 8); it += blockDim.x) {
+    const int sr = it % orows, g = it / orows;
+    uint32_t w[4] = {0u, 0u, 0u, 0u};
+    if (sr < rows) {
+      const uint32_t b = sketch_bits8(sr, (c0 >> 3) + g);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)  // BF16 +1 = 0x3F80, -1 = 0xBF80
+        w[q >> 1] |= (uint32_t)(((b >> q) & 1u) ? 0xBF80u : 0x3F80u) << (16 * (q & 1));
+    }
+    *reinterpret_cast<uint4*>(om + (size_t)(sr >> 7) * kTcOmegaTile +
+                              tc::tile_offset(sr & 127, 8 * g, 128)) =
+        make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+size_t id_sketch_smem(int n, bool tc) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const int ld = layout_ld(n, team_size(n));
-  const int ell = sketch_rows(n);
+  const int ell = sketch_rows(n) + kIdTestRows;
   const int lp = (ell + 3) & ~3;
   size_t b = 0;
   b += al(sizeof(float) * (size_t)ell * ld);      // Y
-  b += al(sizeof(float) * (size_t)kChunk * ld);   // C
-  b += al(sizeof(float) * (size_t)kChunk * lp);   // signs
+  // C and the signs, or (tensor cores) the operand tiles in the same bytes
+  const size_t cs = al(sizeof(float) * (size_t)kChunk * ld) + al(sizeof(float) * (size_t)kChunk * lp);
+  b += tc ? std::max(cs, al(tc_tile_bytes(n, ell))) : cs;
   b += al(sizeof(float) * (3 * (size_t)(ell > kChunk ? ell : kChunk) + 3 * 32 * 32));
   b += 2 * al(sizeof(double) * n);
   b += al(sizeof(int) * n);
@@ -592,16 +774,16 @@ size_t id_sketch_smem(int n) {
 // (fixed row, columns across lanes) are both free of bank conflicts.
 __host__ __device__ inline int warp_ld(int n) { return n + (33 - n % 32) % 32; }
 
-size_t id_sketch_y_size(int n) { return (size_t)sketch_rows(n) * warp_ld(n); }
+size_t id_sketch_y_size(int n) { return (size_t)(sketch_rows(n) + kIdTestRows) * warp_ld(n); }
 
 // Shared memory of the sketch-only variant (no Y tile, no QR workspace).
-size_t id_sketch_split_smem(int n) {
+size_t id_sketch_split_smem(int n, bool tc) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const int ld = layout_ld(n, team_size(n));
-  const int lp = (sketch_rows(n) + 3) & ~3;
+  const int lp = (sketch_rows(n) + kIdTestRows + 3) & ~3;
   size_t b = 0;
-  b += al(sizeof(float) * (size_t)kChunk * ld);   // C
-  b += al(sizeof(float) * (size_t)kChunk * lp);   // signs
+  const size_t cs = al(sizeof(float) * (size_t)kChunk * ld) + al(sizeof(float) * (size_t)kChunk * lp);
+  b += tc ? std::max(cs, al(tc_tile_bytes(n, sketch_rows(n) + kIdTestRows))) : cs;
   b += dofs_bytes<float>(n) + dofs_bytes<float>(kChunk);
   b += al(sizeof(int) * kChunk);
   return b;
@@ -610,7 +792,8 @@ size_t id_sketch_split_smem(int n) {
 // kSplit = false: sketch, pivoted QR and Z in one CTA per box.
 // kSplit = true: the sketch only, written to p.sketch_y (row major, leading
 // dimension warp_ld(n)) for id_cpqr_warp_kernel.
-template <int TS, bool kSplit>
+// kTC: the sketch on the tensor cores (tcgen05), the rest unchanged.
+template <int TS, bool kSplit, bool kTC>
 __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   using Real = float;
   const IdTask t = p.tasks[blockIdx.x];
@@ -619,19 +802,35 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   const Layout L = make_layout<TS>(n);
   const int ld = L.ld;
   const int ell = task_ell(p, t);
-  const int lp = (ell + 3) & ~3;
+  const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
+  const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
+  const int nt = task_test_rows(p, t, ell, m);  // judge's test rows below the sketch
+  const int lp = (ell + nt + 3) & ~3;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
   IdShared<Real> S;
   Real* sg;
+  unsigned char* reg;  // S.C and the signs, or (kTC) the tensor cores' operand tiles
+  // the operand tiles share the bytes of S.C and the signs (small matrices
+  // use S.C, sketched ones the tiles)
+  auto union_tiles = [&]() {
+    if constexpr (kTC) {
+      const size_t tb = (tc_tile_bytes(n, ell + nt) + 15) & ~size_t(15);
+      if ((size_t)(sp - reg) < tb) sp = reg + tb;
+    }
+  };
   if constexpr (kSplit) {
     S.R = nullptr;
+    reg = sp;
     S.C = carve<Real>(sp, kChunk * ld);
     sg = carve<Real>(sp, kChunk * lp);
+    union_tiles();
   } else {
-    S.R = carve<Real>(sp, ell * ld);  // holds the sketch Y (or A itself when m <= ell)
+    S.R = carve<Real>(sp, (ell + nt) * ld);  // the sketch Y and test rows (or A itself when m <= ell)
+    reg = sp;
     S.C = carve<Real>(sp, kChunk * ld);
     sg = carve<Real>(sp, kChunk * lp);
+    union_tiles();
     S.v = carve<Real>(sp, 3 * (ell > kChunk ? ell : kChunk) + 3 * 32 * 32);
     S.vn1 = carve<double>(sp, n);
     S.vn2 = carve<double>(sp, n);
@@ -650,8 +849,6 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   for (int j = threadIdx.x; j < n; j += blockDim.x)
     load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], ox, oy, S.act, j);
   __syncthreads();
-  const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
-  const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
   long long clk0 = clock64(), clk_fill = 0, clk_fold = 0;
   int mr;
   if (m <= ell) {
@@ -668,6 +865,104 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
       __syncthreads();
     }
     clk_fill = clock64() - clk0;
+  } else if constexpr (kTC) {
+    mr = ell;
+    // Sketch on the tensor cores: per chunk, the CUDA cores write the
+    // operand tiles, one thread issues 3 splits x 4 K steps of
+    // tcgen05.mma per M tile and commits them to tc_bar; the tiles are
+    // rewritten only after that barrier completes.  Every wait is bounded
+    // and taken by thread 0 alone, which publishes the outcome in tc_ok, so
+    // a give-up leaves the block uniformly (error flag, TMEM freed).
+    __shared__ uint64_t tc_bar;
+    __shared__ uint32_t tc_tmem;
+    __shared__ int tc_ok;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rows = ell + nt;  // sketch rows, then the judge's test rows
+    const int mtiles = tc_mtiles(rows);
+    const int npad = tc_npad(n);
+    unsigned char* om = reg;
+    unsigned char* bt = reg + (size_t)mtiles * kTcOmegaTile;
+    const uint32_t bbytes = (uint32_t)npad * kChunk * 2;
+    const uint32_t ncols = tc_tmem_cols(mtiles * npad);
+    if (warp == 0) {
+      tc::tmem_alloc(&tc_tmem, ncols);
+      tc::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+      tc::mbar_init(&tc_bar, 1);
+      tc::fence_mbar_init();
+      tc_ok = 1;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tc_tmem;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, npad);
+    const uint32_t lbo_a = 128 * 16, lbo_b = (uint32_t)npad * 16;
+    uint32_t phase = 0;
+    for (int c0 = 0; c0 < m; c0 += kChunk) {
+      const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
+      if (c0 > 0) {  // the previous chunk's MMAs have read the tiles
+        if (threadIdx.x == 0 && !tc::mbar_wait(&tc_bar, phase, kTcPolls)) tc_ok = 0;
+        phase ^= 1u;
+        __syncthreads();
+        if (!tc_ok) break;  // block-uniform
+      }
+      stage_chunk_rows<Real>(p, t, S, c0, cnt, ox, oy);
+      __syncthreads();
+      fill_chunk_tc(p, t, S, c0, cnt, npad, bt, bbytes, om, rows, mtiles);
+      tc::fence_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        const uint32_t a0 = tc::smem_u32(om), b0 = tc::smem_u32(bt);
+        for (int mt = 0; mt < mtiles; ++mt)
+          for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int ks = 0; ks < kChunk / 16; ++ks) {
+              const uint64_t ad =
+                  tc::smem_desc(a0 + (uint32_t)mt * kTcOmegaTile + 2u * ks * lbo_a, lbo_a, 128);
+              const uint64_t bd = tc::smem_desc(b0 + (uint32_t)x * bbytes + 2u * ks * lbo_b, lbo_b, 128);
+              tc::mma_bf16(tmem + (uint32_t)(mt * npad), ad, bd, idesc,
+                           (c0 > 0 || x > 0 || ks > 0) ? 1u : 0u);
+            }
+        tc::mma_commit(&tc_bar);
+      }
+    }
+    if (tc_ok) {
+      if (threadIdx.x == 0 && !tc::mbar_wait(&tc_bar, phase, kTcPolls)) tc_ok = 0;
+      __syncthreads();
+    }
+    if (tc_ok) {
+      // Y from tensor memory: warp w reads lanes 32 (w % 4) .. + 31 (sketch
+      // rows), the column half w / 4, eight columns per load
+      tc::fence_after_sync();
+      const int qd = warp & 3, half = warp >> 2, hcols = npad >> 1;
+      for (int mt = 0; mt < mtiles; ++mt) {
+        const int sr = mt * 128 + 32 * qd + lane;
+        for (int j0 = half * hcols; j0 < (half + 1) * hcols; j0 += 8) {
+          float v[8];
+          tc::tmem_ld8(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(mt * npad + j0), v);
+          if (sr < rows)
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+              if (j0 + e < n) {
+                if constexpr (kSplit) Yg[(size_t)sr * wld + j0 + e] = v[e];
+                else S.R[(size_t)sr * ld + j0 + e] = v[e];
+              }
+        }
+      }
+    } else if (threadIdx.x == 0) {
+      // gave up: one more bounded wait for the MMAs in flight, then report
+      tc::mbar_wait(&tc_bar, phase, kTcPolls);
+      if (p.status != nullptr) atomicExch(p.status, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+    if (!tc_ok) return;  // block-uniform
+    clk_fill = clock64() - clk0;
+    clk0 = clock64();
   } else {
     mr = ell;
     const int nrb = lp / 4, ncb = (n + 3) / 4, ntiles = nrb * ncb;
@@ -682,7 +977,7 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
       fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
       for (TileWalk w(lp); w.j < kChunk; w.next()) {
         const int ii = w.j, r = w.i;
-        sg[w.e()] = (r < ell && ii < cnt) ? sketch_sign(r, c0 + ii) : 0.f;
+        sg[w.e()] = ii < cnt ? sketch_or_test_sign(r, ell, nt, c0 + ii) : 0.f;
       }
       __syncthreads();
       const long long c1 = clock64();
@@ -716,7 +1011,7 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
         const int r = r0 + e / 4, c = cc0 + e % 4;
-        if (r < ell && c < n) {
+        if (r < ell + nt && c < n) {
           if constexpr (kSplit) Yg[(size_t)r * wld + c] = acc[q][e];
           else S.R[(size_t)r * ld + c] = acc[q][e];
         }
@@ -732,18 +1027,13 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   clk0 = clock64();
   const int k = mr > 0 ? cpqr_rank<Real, TS>(n, mr, p.tol, L, S) : 0;
   const long long clk_cpqr = clock64() - clk0;
-  if (p.redo != nullptr && !p.redo_pass) {
-    const bool again = sketch_too_small(k, n, m, ell, sketch_rows(n));
-    if (threadIdx.x == 0) p.redo[t.slot] = again ? 1 : 0;
-    if (again) return;  // block-uniform
-  }
-  if (threadIdx.x == 0) p.ranks[t.slot] = k;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];
-  if (k > 0) {
-    const int r = n - k;
+  const bool learned = p.redo != nullptr && !p.redo_pass;
+  int flag = learned && sketch_too_small(k, n, m, ell, sketch_rows(n), nt > 0) ? 1 : 0;  // block-uniform
+  const int r = n - k;
+  if (flag == 0 && k > 0) {
+    // Z = R11^{-1} R12 in place, one team per column of R12
     constexpr int ts = TS;
     const int tt = L.t;
-    Real* T = reinterpret_cast<Real*>(p.fac) + t.fac_off + fac_T(k, r);
     for (int c = L.c0; c < r; c += L.cstep) {
       const int col = k + c;
       for (int row = k - 1; row >= 0; --row) {
@@ -757,7 +1047,37 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
         for (int q2 = tt; q2 < row; q2 += ts) S.R[(size_t)q2 * ld + col] -= zr * S.R[(size_t)q2 * ld + row];
         __syncwarp(team_mask(ts));
       }
-      for (int row = tt; row < k; row += ts) T[row + (size_t)k * c] = S.R[(size_t)row * ld + col];
+    }
+    __syncthreads();
+    if (nt > 0) {
+      // residual judge on the test rows (columns still in A's order: the
+      // pivoted QR moved columns only within its mr rows)
+      float w = judge_cols(S.R + (size_t)mr * ld, S.R, ld, S.perm, k, n, nt, threadIdx.x,
+                           blockDim.x);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+      if ((threadIdx.x & 31) == 0) S.v[threadIdx.x >> 5] = w;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float mx = 0.f;
+        for (int q = 0; q < kWarps; ++q) mx = fmaxf(mx, S.v[q]);
+        S.is[2] = judge_flag(p, mx, nt, S.scal[2], ell, t.slot);
+      }
+      __syncthreads();
+      flag = S.is[2];
+    }
+  }
+  if (learned) {
+    if (threadIdx.x == 0) p.redo[t.slot] = flag;
+    if (flag) return;  // block-uniform
+  }
+  if (threadIdx.x == 0) p.ranks[t.slot] = k;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) p.perm[t.act_off + j] = S.perm[j];
+  if (k > 0) {
+    Real* T = reinterpret_cast<Real*>(p.fac) + t.fac_off + fac_T(k, r);
+    for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
+      const int row = e % k, c = e / k;
+      T[e] = S.R[(size_t)row * ld + k + c];
     }
   }
   if (p.phase_clk != nullptr && threadIdx.x == 0) {
@@ -781,7 +1101,7 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
 size_t id_cpqr_warp_bytes(int n) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const int ell = sketch_rows(n);
-  return al(sizeof(float) * (size_t)ell * warp_ld(n)) + al(sizeof(float) * ell) +
+  return al(sizeof(float) * (size_t)(ell + kIdTestRows) * warp_ld(n)) + al(sizeof(float) * ell) +
          2 * al(sizeof(float) * n) + al(sizeof(int) * n);
 }
 
@@ -800,14 +1120,15 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
   const int prow = p.pde == kStokes ? 2 * p.npp : p.npp;
   const int m = 2 * t.q + (t.use_proxy ? 2 * prow : 0);
   const int mr = m <= ell ? m : ell;
+  const int nt = task_test_rows(p, t, ell, m);  // the judge's test rows follow the sketch
   unsigned char* sp = smem + (size_t)warp * wbytes;
-  float* A = carve<float>(sp, ell * ld);
+  float* A = carve<float>(sp, (ell + nt) * ld);
   float* v = carve<float>(sp, ell);
   float* vn1 = carve<float>(sp, n);
   float* vn2 = carve<float>(sp, n);
   int* perm = carve<int>(sp, n);
   const float* Y = p.sketch_y + t.y_off;
-  for (int e = lane; e < mr * ld; e += 32) A[e] = Y[e];
+  for (int e = lane; e < (mr + nt) * ld; e += 32) A[e] = Y[e];
   for (int j = lane; j < n; j += 32) perm[j] = j;
   __syncwarp();
 #pragma unroll
@@ -914,17 +1235,10 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
     }
     __syncwarp();
   }
-  if (p.redo != nullptr && !p.redo_pass) {
-    const bool again = sketch_too_small(k, n, m, ell, sketch_rows(n));
-    if (lane == 0) p.redo[t.slot] = again ? 1 : 0;
-    if (again) return;  // warp-uniform
-  }
-  if (lane == 0) p.ranks[t.slot] = k;
-  for (int j = lane; j < n; j += 32) p.perm[t.act_off + j] = perm[j];
-  if (k > 0) {
-    // Z = R11^{-1} R12, one lane per column of R12
-    const int r = n - k;
-    float* T = reinterpret_cast<float*>(p.fac) + t.fac_off + fac_T(k, r);
+  const bool learned = p.redo != nullptr && !p.redo_pass;
+  int flag = learned && sketch_too_small(k, n, m, ell, sketch_rows(n), nt > 0) ? 1 : 0;  // warp-uniform
+  if (flag == 0 && k > 0) {
+    // Z = R11^{-1} R12 in place, one lane per column of R12
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       const int col = lane + 32 * c;
@@ -934,8 +1248,32 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
           A[(size_t)row * ld + col] = z;
           for (int q = 0; q < row; ++q) A[(size_t)q * ld + col] -= z * A[(size_t)q * ld + row];
         }
-        for (int row = 0; row < k; ++row) T[row + (size_t)k * (col - k)] = A[(size_t)row * ld + col];
       }
+    }
+    __syncwarp();
+    if (nt > 0) {
+      // residual judge on the test rows (columns in A's order: the pivoted
+      // QR moved columns only within its mr rows)
+      float w = judge_cols(A + (size_t)mr * ld, A, ld, perm, k, n, nt, lane, 32);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+      int f = 0;
+      if (lane == 0) f = judge_flag(p, w, nt, thr, ell, t.slot);
+      flag = __shfl_sync(0xffffffffu, f, 0);
+    }
+  }
+  if (learned) {
+    if (lane == 0) p.redo[t.slot] = flag;
+    if (flag) return;  // warp-uniform
+  }
+  if (lane == 0) p.ranks[t.slot] = k;
+  for (int j = lane; j < n; j += 32) p.perm[t.act_off + j] = perm[j];
+  if (k > 0) {
+    const int r = n - k;
+    float* T = reinterpret_cast<float*>(p.fac) + t.fac_off + fac_T(k, r);
+    for (int e = lane; e < k * r; e += 32) {
+      const int row = e % k, c = e / k;
+      T[e] = A[(size_t)row * ld + k + c];
     }
   }
 }
@@ -946,22 +1284,33 @@ static void launch_id_t(const IdParams& p, int num_tasks, size_t smem, cudaStrea
   id_kernel<Real, TS><<<num_tasks, kThreads, smem, st>>>(p);
 }
 
-template <int TS>
-static void launch_sketch_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
-  set_smem_once<id_sketch_kernel<TS, false>>();
-  id_sketch_kernel<TS, false><<<num_tasks, kThreads, smem, st>>>(p);
+template <int TS, bool kTC>
+static void launch_sketch_tc(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
+  set_smem_once<id_sketch_kernel<TS, false, kTC>>();
+  id_sketch_kernel<TS, false, kTC><<<num_tasks, kThreads, smem, st>>>(p);
   if (p.redo != nullptr) {  // boxes whose predicted sketch was too small
     IdParams q = p;
     q.redo_pass = 1;
-    id_sketch_kernel<TS, false><<<num_tasks, kThreads, smem, st>>>(q);
+    id_sketch_kernel<TS, false, kTC><<<num_tasks, kThreads, smem, st>>>(q);
   }
+}
+template <int TS>
+static void launch_sketch_t(const IdParams& p, int num_tasks, size_t smem, cudaStream_t st) {
+  if (p.tc) launch_sketch_tc<TS, true>(p, num_tasks, smem, st);
+  else launch_sketch_tc<TS, false>(p, num_tasks, smem, st);
 }
 
 // Split FP32 ID: the sketch (one CTA per box), then the warp-per-box QR.
 template <int TS>
 static void launch_split_pass(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
-  set_smem_once<id_sketch_kernel<TS, true>>();
-  id_sketch_kernel<TS, true><<<num_tasks, kThreads, id_sketch_split_smem(nmax), st>>>(p);
+  if (p.tc) {
+    set_smem_once<id_sketch_kernel<TS, true, true>>();
+    id_sketch_kernel<TS, true, true><<<num_tasks, kThreads, id_sketch_split_smem(nmax, true), st>>>(p);
+  } else {
+    set_smem_once<id_sketch_kernel<TS, true, false>>();
+    id_sketch_kernel<TS, true, false>
+        <<<num_tasks, kThreads, id_sketch_split_smem(nmax, false), st>>>(p);
+  }
   const int wbytes = (int)id_cpqr_warp_bytes(nmax);
   int wpc = (int)((size_t)kSmemOptIn / wbytes);
   wpc = wpc < 1 ? 1 : wpc > kWarps ? kWarps : wpc;
@@ -1113,7 +1462,8 @@ int launch_id_wide(const IdParams& p, int num_tasks, int nmax, const WideItem* i
 }
 
 bool id_sketch_ok(int nmax) {
-  return nmax <= 128 && id_sketch_smem(nmax) <= 227 * 1024;
+  return nmax <= 128 && id_sketch_smem(nmax, true) <= 227 * 1024 &&
+         id_sketch_smem(nmax, false) <= 227 * 1024;
 }
 
 
@@ -1133,7 +1483,7 @@ int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32
     return 2 * passes;
   }
   if (fp32 && p.dense == nullptr && id_sketch_ok(nmax)) {
-    const size_t sm = id_sketch_smem(nmax);
+    const size_t sm = id_sketch_smem(nmax, p.tc != 0);
     if (ts == 4) launch_sketch_t<4>(p, num_tasks, sm, st);
     else launch_sketch_t<2>(p, num_tasks, sm, st);
     return passes;

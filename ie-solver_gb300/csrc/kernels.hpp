@@ -32,6 +32,19 @@ struct IdParams {
   // learned sizes in this launch.
   int* redo;
   int redo_pass;
+  // Residual judge of a learned pass (redo != nullptr, redo_pass == 0): a
+  // truncated sketch also forms kIdTestRows test rows with independent
+  // signs, and a box whose estimated interpolation residual (per redundant
+  // column, from the test rows) exceeds judge_factor * tol * (the largest
+  // column norm of its ID matrix) is redone (flag 2).  judge_factor <= 0:
+  // no test rows.  judge_ratio (optional, per slot, filled with NaN by the
+  // caller): the judged boxes' worst estimate over tol * that norm.
+  float judge_factor;
+  float* judge_ratio;
+  // FP32 sketched ID: 1 = the sketch on the tensor cores (tcgen05), 0 = on
+  // the CUDA cores.  status: raised when a tensor-core wait gave up.
+  int tc;
+  int* status;
   // FP32 sketched ID: levels of at least this many boxes run the pivoted QR
   // one warp per box (id_cpqr_warp_kernel), smaller ones one CTA per box
   int split_min_tasks;
@@ -79,6 +92,7 @@ size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem);
 
 // Floats of sketch storage one FP32 task of n columns needs (split ID).
 size_t id_sketch_y_size(int n);
+constexpr int kIdTestRows = 8;  // test rows of the residual judge
 // Shared-memory attribute set-up of the FP64 ID kernels on the current device.
 cudaError_t id_noalloc_prepare();
 int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32,

@@ -159,6 +159,7 @@ struct rs_solver {
   bool rank_model_on = false;
   DevBuf<float> rank_w, rank_feat;
   DevBuf<int> redo, ell_slot;
+  DevBuf<float> judge_ratio;  // trace mode: the residual judge's ratio per slot
   HostBuf<int> h_redo, h_ell;
   std::vector<float> samp_feat, samp_target;
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
@@ -538,11 +539,13 @@ rs_status factor_impl(rs_solver* s) {
   std::vector<int> cand_ids, dc_ids;
   std::vector<int> m_of_slot;
   std::vector<float> feat, feat_s;  // rank-model features per slot, and in sorted order
-  const bool learned = f32 && s->rank_model_on;
+  std::vector<double> slot_work;    // per slot: ID flops, sketch rows, Schur flops
+  const bool model = f32 && s->rank_model_on;
   s->samp_feat.clear();
   s->samp_target.clear();
   s->stats.rank_predicted = 0;
   s->stats.rank_redo = 0;
+  s->stats.rank_redo_judge = 0;
   s->stats.sketch_rows = 0;
   // Contents below these marks are live and survive buffer growth.
   size_t fac_prev = F.fac_used, e_prev = F.e_used, piv_prev = s->piv_used;
@@ -693,6 +696,12 @@ rs_status factor_impl(rs_solver* s) {
     s->stats.max_rows = max_rows;
     const double h_tasks = now_ms();
     if (dct.empty()) continue;
+    // Learned sketch sizes on levels of at least one box per SM: there the
+    // ID is throughput-bound and shorter sketches save work; a level of fewer
+    // boxes runs each box on an SM of its own, so its time is one box's
+    // latency, which a truncated sketch barely shortens and a redone box
+    // doubles.
+    const bool learned = model && (int)idt.size() >= s->num_sms;
     // sort by size for binned launches (slots keep their identity)
     std::vector<size_t> oi(idt.size()), od(dct.size());
     for (size_t i = 0; i < oi.size(); ++i) oi[i] = i;
@@ -846,7 +855,16 @@ rs_status factor_impl(rs_solver* s) {
     ip.sketch_y = y_need ? s->sketch_y.p : nullptr;
     ip.redo = learned && !idt_s.empty() ? s->redo.p : nullptr;
     ip.redo_pass = 0;
+    ip.judge_factor = ip.redo != nullptr ? (float)s->cfg.rank_judge : 0.f;
+    ip.judge_ratio = nullptr;
+    if (s->trace && ip.redo != nullptr) {
+      CU(s->judge_ratio.ensure(idt_s.size()));
+      CU(cudaMemsetAsync(s->judge_ratio.p, 0xff, idt_s.size() * sizeof(float), s->stream));
+      ip.judge_ratio = s->judge_ratio.p;
+    }
     ip.split_min_tasks = s->split_min_tasks;
+    ip.tc = s->cfg.tensor_cores;
+    ip.status = s->status.p + 2;
     ip.phase_clk = nullptr;
     if (s->trace) {
       CU(s->clk.ensure(4 * std::max<size_t>(idt.size(), 1)));
@@ -946,6 +964,24 @@ rs_status factor_impl(rs_solver* s) {
       const double cnt = idt.empty() ? 1.0 : (double)idt.size();
       std::fprintf(stderr, "[rskel]   ID cycles per box avg/max: fill %.0f/%.0f fold %.0f/%.0f cpqr %.0f/%.0f z %.0f/%.0f\n",
                    ph[0] / cnt, mx[0], ph[1] / cnt, mx[1], ph[2] / cnt, mx[2], ph[3] / cnt, mx[3]);
+      if (ip.judge_ratio != nullptr) {
+        // residual judge: estimated residual / (tol |a_max|) of the judged boxes
+        std::vector<float> jr(idt.size());
+        CU(cudaMemcpy(jr.data(), s->judge_ratio.p, jr.size() * sizeof(float),
+                      cudaMemcpyDeviceToHost));
+        std::vector<float> v;
+        for (float x : jr)
+          if (x == x) v.push_back(x);  // NaN: not judged
+        std::sort(v.begin(), v.end());
+        if (!v.empty())
+          std::fprintf(stderr,
+                       "[rskel]   judge: %zu boxes, ratio median %.3g p90 %.3g p99 %.3g max %.3g, "
+                       "%d above %.3g\n",
+                       v.size(), v[v.size() / 2], v[v.size() * 9 / 10], v[v.size() * 99 / 100],
+                       v.back(), (int)(v.end() - std::upper_bound(v.begin(), v.end(),
+                                                                   (float)s->cfg.rank_judge)),
+                       s->cfg.rank_judge);
+      }
       int mmax = 0, nmax = 0;
       double msum = 0;
       for (size_t q = 0; q < idt.size(); ++q) {
@@ -959,34 +995,50 @@ rs_status factor_impl(rs_solver* s) {
                    lv, idt.size(), mmax, idt.empty() ? 0.0 : msum / idt.size(), nmax, dct.size(),
                    ms_id, ms_dc);
     }
-    for (size_t c = 0; c < cand_ids.size(); ++c) {
+    // Per-box bookkeeping after the read-back, independent across boxes:
+    // samples and work counts go to per-slot entries (summed in slot order
+    // below, so the totals do not depend on the thread count).
+    const int nc = (int)cand_ids.size();
+    const size_t sbase = s->samp_target.size();
+    s->samp_feat.resize((sbase + nc) * kRankFeatures);
+    s->samp_target.resize(sbase + nc);
+    slot_work.assign(3 * (size_t)nc, 0.0);  // {id flops, sketch rows, Schur flops}
+    int n_pred = 0, n_redo = 0, n_redo_judge = 0, n_fac = 0, k_max = s->stats.max_rank;
+#pragma omp parallel for schedule(dynamic, 32) if (nc > 96) \
+    reduction(+ : n_pred, n_redo, n_redo_judge, n_fac) reduction(max : k_max)
+    for (int c = 0; c < nc; ++c) {
       const int id = cand_ids[c];
       NodeState& S = s->st[id];
       const int k = s->h_ranks.p[S.slot];
       const int n = (int)S.active.size();
-      s->samp_feat.insert(s->samp_feat.end(), feat.begin() + (size_t)S.slot * kRankFeatures,
-                          feat.begin() + (size_t)(S.slot + 1) * kRankFeatures);
-      s->samp_target.push_back(k > 0 ? (float)k / (float)n : 1.f);
+      std::copy(feat.begin() + (size_t)S.slot * kRankFeatures,
+                feat.begin() + (size_t)(S.slot + 1) * kRankFeatures,
+                s->samp_feat.begin() + (sbase + c) * kRankFeatures);
+      s->samp_target[sbase + c] = k > 0 ? (float)k / (float)n : 1.f;
       const int m = m_of_slot[S.slot];
+      double* wk = slot_work.data() + 3 * (size_t)c;
       if (f32 && n > 128 && n <= kWideMaxN) {
-        s->stats.sketch_rows += std::min(m, n + 16);
-        s->stats.id_flops += sketch_id_flops(m, n, k, n + 16, s->cfg.pde);
+        wk[1] = std::min(m, n + 16);
+        wk[0] = sketch_id_flops(m, n, k, n + 16, s->cfg.pde);
       } else if (f32 && n <= 128) {
         // rows the randomized ID sketched (m when the matrix is no taller)
         const int full = n + 16;
         int ell = full;
         bool again = false;
+        int tests = 0;  // the residual judge's test rows
         if (ip.redo != nullptr) {
-          ++s->stats.rank_predicted;
+          ++n_pred;
           again = s->h_redo.p[S.slot] != 0;
-          s->stats.rank_redo += again;
+          n_redo += again;
+          n_redo_judge += s->h_redo.p[S.slot] == 2;
           ell = std::min(s->h_ell.p[S.slot], full);
+          if (ip.judge_factor > 0.f && ell < full && m > ell) tests = kIdTestRows;
         }
-        s->stats.sketch_rows += std::min(m, ell) + (again ? std::min(m, full) : 0);
-        s->stats.id_flops += sketch_id_flops(m, n, k, ell, s->cfg.pde) +
-                             (again ? sketch_id_flops(m, n, k, full, s->cfg.pde) : 0.0);
+        wk[1] = std::min(m, ell) + tests + (again ? std::min(m, full) : 0);
+        wk[0] = sketch_id_flops(m, n, k, ell, s->cfg.pde) + (tests ? 2.0 * tests * m * n : 0.0) +
+                (again ? sketch_id_flops(m, n, k, full, s->cfg.pde) : 0.0);
       } else {
-        s->stats.id_flops += id_flops(m, n, k, s->cfg.pde);
+        wk[0] = id_flops(m, n, k, s->cfg.pde);
       }
       if (k <= 0) {
         S.e_ld = n;
@@ -997,15 +1049,25 @@ rs_status factor_impl(rs_solver* s) {
       S.k = k;
       S.r = n - k;
       S.perm.assign(s->h_perm.p + (act_off - seg0), s->h_perm.p + (act_off - seg0) + n);
-      S.skel.clear();
-      S.red.clear();
-      for (int i = 0; i < k; ++i) S.skel.push_back(S.active[S.perm[i]]);
-      for (int i = k; i < n; ++i) S.red.push_back(S.active[S.perm[i]]);
+      S.skel.resize(k);
+      S.red.resize(n - k);
+      for (int i = 0; i < k; ++i) S.skel[i] = S.active[S.perm[i]];
+      for (int i = k; i < n; ++i) S.red[i - k] = S.active[S.perm[i]];
       S.e_ld = k;
-      s->stats.max_rank = std::max(s->stats.max_rank, k);
-      s->stats.decouple_flops += dec_flops(k, n - k);
-      ++s->stats.boxes_factored;
+      k_max = std::max(k_max, k);
+      wk[2] = dec_flops(k, n - k);
+      ++n_fac;
     }
+    for (int c = 0; c < nc; ++c) {
+      s->stats.id_flops += slot_work[3 * (size_t)c];
+      s->stats.sketch_rows += slot_work[3 * (size_t)c + 1];
+      s->stats.decouple_flops += slot_work[3 * (size_t)c + 2];
+    }
+    s->stats.rank_predicted += n_pred;
+    s->stats.rank_redo += n_redo;
+    s->stats.rank_redo_judge += n_redo_judge;
+    s->stats.boxes_factored += n_fac;
+    s->stats.max_rank = k_max;
     for (int id : dc_ids) {
       NodeState& S = s->st[id];
       if (S.slot < 0) S.e_ld = (int)S.active.size();
@@ -1878,6 +1940,8 @@ void rs_config_default(rs_config* c) {
   c->refine_solver = 0;
   c->use_graphs = 1;
   c->root_inverse = 1;
+  c->rank_judge = 4.0;
+  c->tensor_cores = 1;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -1892,7 +1956,9 @@ rs_status rs_create(const rs_config* cfg, rs_solver** out) {
   if (cfg->is_strong_admissibility) return RS_ERR_ARG;
   if (cfg->precision != RS_FP64 && cfg->precision != RS_FP32_REFINE) return RS_ERR_ARG;
   if (!(cfg->rank_headroom >= 1.0 && cfg->rank_headroom <= 4.0) || cfg->rank_extra_rows < 0 ||
-      cfg->rank_extra_rows > 128 || cfg->refine_solver < 0 || cfg->refine_solver > 2)
+      cfg->rank_extra_rows > 128 || cfg->refine_solver < 0 || cfg->refine_solver > 2 ||
+      !(cfg->rank_judge >= 0.0 && cfg->rank_judge <= 1e6) || cfg->tensor_cores < 0 ||
+      cfg->tensor_cores > 1)
     return RS_ERR_ARG;
   rs_solver* s = new rs_solver();
   s->cfg = *cfg;
@@ -2212,7 +2278,7 @@ rs_status rs_factor(rs_solver* s) {
     if (!fmm_plan_upload(s->fmm, fhp, s->stream))
       return fail(s, RS_ERR_CUDA, "fast multipole plan failed");
   }
-  CU(cudaMemcpyAsync(s->h_status.p, s->status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+  CU(cudaMemcpyAsync(s->h_status.p, s->status.p, 3 * sizeof(int), cudaMemcpyDeviceToHost,
                      s->stream));
   CU(cudaStreamSynchronize(s->stream));
   float ms = 0;
@@ -2233,6 +2299,7 @@ rs_status rs_factor(rs_solver* s) {
   s->stats.num_compressed = nc;
   s->stats.num_skel_root = s->ns;
   if (s->h_status.p[1] != 0) return fail(s, RS_ERR_CUDA, "grid barrier timed out");
+  if (s->h_status.p[2] != 0) return fail(s, RS_ERR_CUDA, "tensor-core sketch wait gave up");
   if (s->h_status.p[0] != 0) return fail(s, RS_ERR_NUMERIC, "singular or non-finite pivot");
   s->factored = true;
   return RS_OK;

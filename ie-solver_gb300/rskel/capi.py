@@ -45,7 +45,8 @@ class RsConfig(ctypes.Structure):
                 ("fmm_order", ctypes.c_int), ("rank_headroom", ctypes.c_double),
                 ("rank_extra_rows", ctypes.c_int), ("refine_verify", ctypes.c_int),
                 ("refine_solver", ctypes.c_int), ("use_graphs", ctypes.c_int),
-                ("root_inverse", ctypes.c_int)]
+                ("root_inverse", ctypes.c_int), ("rank_judge", ctypes.c_double),
+                ("tensor_cores", ctypes.c_int)]
 
 
 class RsStats(ctypes.Structure):
@@ -64,7 +65,8 @@ class RsStats(ctypes.Structure):
                 ("boxes_factored", ctypes.c_int),
                 ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double),
                 ("rank_predicted", ctypes.c_int), ("rank_redo", ctypes.c_int),
-                ("sketch_rows", ctypes.c_double), ("krylov_steps", ctypes.c_int)]
+                ("sketch_rows", ctypes.c_double), ("krylov_steps", ctypes.c_int),
+                ("rank_redo_judge", ctypes.c_int)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -197,7 +199,7 @@ class Solver:
     def __init__(self, geo, pde, tol, leaf=64, npp=64, precision=RS_FP64, refine_tol=1e-12,
                  refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16, fmm_order=0,
                  rank_headroom=1.25, rank_extra_rows=12, refine_verify=1, refine_solver=0,
-                 use_graphs=1, root_inverse=1):
+                 use_graphs=1, root_inverse=1, rank_judge=4.0, tensor_cores=1):
         self.sd = 2 if pde == RS_STOKES else 1
         self.cfg = default_config(pde=pde, solution_dimension=self.sd, id_tol=tol,
                                   max_leaf_dofs=leaf, num_proxy_points=npp,
@@ -207,7 +209,8 @@ class Solver:
                                   fmm_order=fmm_order, rank_headroom=rank_headroom,
                                   rank_extra_rows=rank_extra_rows, refine_verify=refine_verify,
                                   refine_solver=refine_solver, use_graphs=use_graphs,
-                                  root_inverse=root_inverse)
+                                  root_inverse=root_inverse, rank_judge=rank_judge,
+                                  tensor_cores=tensor_cores)
         h = _vp()
         self._check(lib().rs_create(ctypes.byref(self.cfg), ctypes.byref(h)), None)
         self.h = h

@@ -87,6 +87,16 @@ typedef struct {
                                 pivoting), one product per application; 0 = LU with partial
                                 pivoting and triangular solves (dgetrf/dgetrs, as FP64 and
                                 larger roots always do) */
+  double rank_judge;         /* rank model: residual judge of the truncated sketches.  A box
+                                sketched with the predicted ell rows also forms 8 test rows
+                                with independent signs; its ID is redone with the full sketch
+                                when the residual they estimate, for any redundant column,
+                                exceeds rank_judge * id_tol * (the largest column norm).
+                                Default 4; 0 = off (only the rank-settling rule judges) */
+  int tensor_cores;          /* RS_FP32_REFINE: 1 (default) = the FP32 randomized ID's sketch
+                                Y = Omega A runs on the tensor cores (tcgen05.mma, BF16
+                                operands with A split in three BF16 parts, FP32 accumulation
+                                in tensor memory); 0 = on the CUDA cores (FP32 FMA) */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
@@ -314,6 +324,8 @@ typedef struct {
                                                   randomized-ID sketches of boxes of <= 512 DOFs,
                                                   summed (a redone box counts both sketches) */
   int krylov_steps;                            /* last solve: GMRES steps of GMRES-IR */
+  int rank_redo_judge;                         /* of rank_redo: boxes whose sketch settled the
+                                                  rank but failed the residual judge */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 

@@ -172,3 +172,38 @@ def test_batch_of_512_random_stars_subset_matches_oracle(solver_lib, oracle_lib)
         lo, hi = off[b], off[b + 1]
         assert _rel(sols["fp64"][lo:hi], mu_cfg) <= 10 * 1e-8, b
         assert _rel(sols["fp32"][lo:hi], mu_ex) <= 1e-8, b
+
+
+def _cached_c5():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location(
+        "make_fullsize", os.path.join(GOLDEN, "make_fullsize.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    d = np.load(mk.OUT)
+    geo, F = mk.workload()
+    return geo, F, d["mu"], d["alpha"]
+
+
+def test_stokes_64_ellipses_1m_dofs_matches_cached_oracle(solver_lib, oracle_lib):
+    """FP32 factorization + GMRES-IR on 1048576 DOFs against the oracle's
+    solution at tolerance 1e-12 (cached).  The cached solution is first
+    checked against the equation itself: its relative residual, by the FP64
+    multipole product at order 40 plus U alpha, is below 1e-9."""
+    capi, O = solver_lib, oracle_lib
+    geo, F, mu_o, al_o = _cached_c5()
+    U, P = O.border_matrices(geo, 2)
+    ev = capi.Solver(geo, capi.RS_STOKES, 1e-8, leaf=64, npp=64, fmm_order=40)
+    r = ev.matvec(mu_o[:, None], fast=True)[:, 0] + U @ al_o - F
+    ev.close()
+    assert np.linalg.norm(r) / np.linalg.norm(F) <= 1e-9
+    s = capi.Solver(geo, capi.RS_STOKES, 1e-8, leaf=64, npp=64, precision=capi.RS_FP32_REFINE,
+                    refine_tol=1e-10, refine_max_iters=10)
+    s.factor()
+    mu, al = s.solve(F)
+    st = s.stats()
+    s.close()
+    assert st["refine_residual"] <= 1e-10 and st["krylov_steps"] > 0
+    assert _rel(mu, mu_o) <= 1e-8
+    assert _rel(al, al_o) <= 1e-8

@@ -271,19 +271,41 @@ def test_too_small_predictions_fall_back_to_the_full_sketch(solver_lib):
     s.factor()
     mu0, _ = s.solve(F)
     _, y0 = s.rank_samples()
+    X0, _ = s.rank_samples()
     s0_rows = s.stats()["sketch_rows"]
-    # every prediction ~0: 12-row sketches, so every box of rank > 4 is redone
+    # plain ranks of the boxes whose sketch is predicted: at most 128 DOFs
+    # (feature 0 is n / 128), on levels of at least one ID box per SM (152 on
+    # a GB300; feature 5 is level / 16)
+    n0 = np.rint(X0[:, 0] * 128.0)
+    lv = np.rint(X0[:, 5] * 16.0).astype(int)
+    big = np.bincount(lv)[lv] >= 152
+    k0 = np.rint(y0 * n0)[(n0 <= 128) & big]
+    # every prediction ~0: 12-row sketches
     w = np.zeros(capi.RANK_WEIGHTS, dtype=np.float32)
     w[-1] = -30.0
-    s.set_rank_model(w)
-    s.factor()
-    mu1, _ = s.solve(F)
-    st = s.stats()
-    _, y1 = s.rank_samples()
-    assert st["rank_predicted"] > 100 and st["rank_redo"] >= 0.9 * st["rank_predicted"]
-    assert st["sketch_rows"] > s0_rows
-    # redone boxes get the plain factorization's ranks (boxes not redone may
-    # pick other skeletons, which can change later levels' box lists)
-    assert abs(len(y1) - len(y0)) <= 0.02 * len(y0)
-    assert abs(float(np.mean(y1)) - float(np.mean(y0))) <= 0.02
-    assert np.linalg.norm(mu1 - mu0) / np.linalg.norm(mu0) <= 1e-9
+    for judge in (0.0, 4.0):
+        t = _mixed(capi, geo, rank_judge=judge)
+        t.set_rank_model(w)
+        t.factor()
+        mu1, _ = t.solve(F)
+        st = t.stats()
+        _, y1 = t.rank_samples()
+        assert st["rank_predicted"] > 100
+        if judge == 0.0:
+            # without the residual judge a box needs 8 rows to spare: every box
+            # of rank above 4 is redone
+            assert st["rank_redo"] >= 0.9 * st["rank_predicted"]
+            assert st["rank_redo_judge"] == 0
+        else:
+            # with it, a box whose 12 rows settled its rank (k <= 11) and whose
+            # test rows confirm the residual is kept; every box of plain rank
+            # 12 or more is redone (boxes lists may differ by a few per cent)
+            assert st["rank_redo"] >= 0.98 * np.count_nonzero(k0 >= 12)
+            assert st["rank_redo"] < st["rank_predicted"]
+        assert st["sketch_rows"] > 0.5 * s0_rows
+        # redone boxes get the plain factorization's ranks (boxes not redone may
+        # pick other skeletons, which can change later levels' box lists)
+        assert abs(len(y1) - len(y0)) <= 0.02 * len(y0)
+        assert abs(float(np.mean(y1)) - float(np.mean(y0))) <= 0.02
+        assert np.linalg.norm(mu1 - mu0) / np.linalg.norm(mu0) <= 1e-9
+        t.close()
