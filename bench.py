@@ -263,7 +263,8 @@ def time_arm(capi, geo, F, precision, steps, warmup, cu, dist, model=None, tune=
     s = make_solver(capi, geo, precision, dist.local, model)
     s.build_tree()
     if tune is not None:  # launch shapes from the autotuner, untimed
-        tune["split_min_tasks"], tune["wide_ctas_per_sm"] = s.autotune(reps=3)
+        (tune["split_min_tasks"], tune["wide_ctas_per_sm"],
+         tune["elim_threads"]) = s.autotune(reps=3)
     d_f = cu.malloc(F.nbytes)
     d_mu = cu.malloc(F.nbytes)
     cu.memcpy_htod(d_f, F)

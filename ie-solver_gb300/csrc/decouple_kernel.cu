@@ -101,7 +101,13 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     return;
   }
   Real* fac = reinterpret_cast<Real*>(p.fac) + t.fac_off;
-  for (int e = threadIdx.x; e < k * r; e += blockDim.x) T[e] = fac[fac_T(k, r) + e];
+  // T (k x r, column major in the record) is held transposed, Tt(i, l) =
+  // T(l, i) at Tt[i + r l]: the products below walk i across the threads,
+  // which then read consecutive words
+  for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
+    const int l = e % k, i = e / k;
+    T[i + (size_t)r * l] = fac[fac_T(k, r) + e];
+  }
   __syncthreads();
   const size_t ld = n;
   Real* Mss = M;
@@ -113,7 +119,7 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     for (TileWalk w(r); w.j < k; w.next()) {
       const int i = w.i, j = w.j;
       Real acc = Mrs[i + ld * j];
-      for (int l = 0; l < k; ++l) acc -= T[l + (size_t)k * i] * Mss[l + ld * j];
+      for (int l = 0; l < k; ++l) acc -= T[i + (size_t)r * l] * Mss[l + ld * j];
       Mrs[i + ld * j] = acc;
     }
   __syncthreads();
@@ -123,8 +129,8 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
       const int i = w.i, j = w.j;
       Real a1 = 0, a2 = 0;
       for (int l = 0; l < k; ++l) {
-        a1 += T[l + (size_t)k * i] * Msr[l + ld * j];
-        a2 += Mrs[i + ld * l] * T[l + (size_t)k * j];
+        a1 += T[i + (size_t)r * l] * Msr[l + ld * j];
+        a2 += Mrs[i + ld * l] * T[j + (size_t)r * l];
       }
       Mrr[i + ld * j] = (Mrr[i + ld * j] - a1) - a2;
     }
@@ -134,7 +140,7 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     for (TileWalk w(k); w.j < r; w.next()) {
       const int i = w.i, j = w.j;
       Real acc = Msr[i + ld * j];
-      for (int l = 0; l < k; ++l) acc -= Mss[i + ld * l] * T[l + (size_t)k * j];
+      for (int l = 0; l < k; ++l) acc -= Mss[i + ld * l] * T[j + (size_t)r * l];
       Msr[i + ld * j] = acc;
     }
   __syncthreads();
@@ -239,6 +245,8 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     // record.  The sums run over the DOFs in their own order: in pivot order
     // the Stokes x / y pairs no longer cancel early, and the FP32
     // factorization loses accuracy.
+    // (U_f also goes to T's bytes, free since step 3, for E below)
+    Real* Us = T;
     if (r > 0)
       for (TileWalk w(r); w.j < k; w.next()) {
         const int i = w.i, j = w.j;
@@ -246,6 +254,7 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
         Real acc = 0;
         for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
         Uo[e] = acc;
+        Us[e] = acc;
       }
     if (k > 0)
       for (TileWalk w(k); w.j < r; w.next()) {
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
         const int i = w.i, j = w.j;
         const int e = w.e();
         Real acc = Mss[i + ld * j];
-        for (int l = 0; l < r; ++l) acc -= Msr[i + ld * l] * Uo[l + (size_t)r * j];
+        for (int l = 0; l < r; ++l) acc -= Msr[i + ld * l] * Us[l + (size_t)r * j];
         E_out[e] = acc;
       }
     for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = j;
@@ -314,7 +323,8 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     __syncthreads();
   }
   // 5) U_f = X^{-1} K_r_sn, in place over Mrs (one warp per column).
-  for (int c = warp; c < k; c += kWarps) {
+  const int nwarps = blockDim.x >> 5;
+  for (int c = warp; c < k; c += nwarps) {
     Real* y = Mrs + ld * c;
     if (lane == 0)
       for (int j = 0; j < r; ++j)
@@ -345,7 +355,7 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     }
   __syncthreads();
   // 7) L_f = K_sn_r X^{-1}: solve X^T y = K_sn_r(i,:)^T per row (one warp per row).
-  for (int i = warp; i < k; i += kWarps) {
+  for (int i = warp; i < k; i += nwarps) {
     Real* y = Msr + i;  // stride ld
     for (int j = 0; j < r; ++j) {  // U^T z = b
       const Real yj = y[ld * j] / Mrr[j + ld * j];
@@ -396,15 +406,18 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
 }
 
+// threads: 256 (default) or 128 per box; every loop of the kernel strides
+// by blockDim.x (or its warp count).
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
-                     cudaStream_t st) {
+                     cudaStream_t st, int threads) {
   if (num_tasks <= 0) return;
+  const int nt = threads == 128 ? 128 : kThreads;
   if (fp32) {
     set_smem_once<decouple_kernel<float>>();
-    decouple_kernel<float><<<num_tasks, kThreads, smem, st>>>(p);
+    decouple_kernel<float><<<num_tasks, nt, smem, st>>>(p);
   } else {
     set_smem_once<decouple_kernel<double>>();
-    decouple_kernel<double><<<num_tasks, kThreads, smem, st>>>(p);
+    decouple_kernel<double><<<num_tasks, nt, smem, st>>>(p);
   }
 }
 

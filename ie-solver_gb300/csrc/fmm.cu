@@ -155,7 +155,12 @@ struct FmmArgs {
   const R* charge;  // complex, 2 * (slot + npts * q)
   R* mpole;         // complex, 2 * (k + p * (q + nrhs * box))
   R* local;
+  // near-field source data in slot order, kSrcStride values of R per slot:
+  // Laplace (mode 0) the charge factor b_j = -(w_j / 2pi) nu_j (complex)
+  // then the nrhs densities; Neumann (mode 1) the nrhs real charges
+  const R* src;
 };
+constexpr int kSrcStride = 2 + kMaxRhs;
 
 __device__ __forceinline__ Pos<double> pt_pos(const FmmArgs<double>& a, int s) {
   return {a.rx[s], a.ry[s]};
@@ -190,30 +195,40 @@ __device__ __forceinline__ void st_c(R* a, size_t i, Cx<R> v) {
   a[2 * i + 1] = v.im;
 }
 
-// Complex charges c_j = -(w_j / 2pi) (n_x + i n_y) mu_j in slot order.
+// Complex charges c_j = -(w_j / 2pi) (n_x + i n_y) mu_j in slot order; and
+// the near-field source data (charge factor, densities in R) once per slot.
 template <class R>
 __global__ void charges_kernel(Geo<double> g, const int* slot_pt, int npts, const double* mu,
-                               int nrhs, R* charge) {
+                               int nrhs, R* charge, R* src) {
   const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= (size_t)npts * nrhs) return;
   const int s = (int)(e % npts), q = (int)(e / npts);
   const int pt = slot_pt[s];
-  const double a = -g.w[pt] * (1.0 / (2.0 * CUDART_PI)) * mu[pt + (size_t)npts * q];
-  charge[2 * e] = (R)(a * g.nx[pt]);
-  charge[2 * e + 1] = (R)(a * g.ny[pt]);
+  const double f = -g.w[pt] * (1.0 / (2.0 * CUDART_PI));
+  const double m = mu[pt + (size_t)npts * q];
+  charge[2 * e] = (R)(f * m * g.nx[pt]);
+  charge[2 * e + 1] = (R)(f * m * g.ny[pt]);
+  R* sr = src + (size_t)kSrcStride * s;
+  if (q == 0) {
+    sr[0] = to_r<R>(f * g.nx[pt]);
+    sr[1] = to_r<R>(f * g.ny[pt]);
+  }
+  sr[2 + q] = to_r<R>(m);
 }
 
 // Neumann (adjoint double layer, kernel.cpp:80-91): real charges
 // c_j = (w_j / 2pi) mu_j; (K mu)_i gets Re(nu_i sum_j c_j / (z_i - z_j)).
 template <class R>
 __global__ void neumann_charges_kernel(Geo<double> g, const int* slot_pt, int npts,
-                                       const double* mu, int nrhs, R* charge) {
+                                       const double* mu, int nrhs, R* charge, R* src) {
   const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (e >= (size_t)npts * nrhs) return;
   const int s = (int)(e % npts), q = (int)(e / npts);
   const int pt = slot_pt[s];
-  charge[2 * e] = to_r<R>(g.w[pt] * (1.0 / (2.0 * CUDART_PI)) * mu[pt + (size_t)npts * q]);
+  const R c = to_r<R>(g.w[pt] * (1.0 / (2.0 * CUDART_PI)) * mu[pt + (size_t)npts * q]);
+  charge[2 * e] = c;
   charge[2 * e + 1] = to_r<R>(0.0);
+  src[(size_t)kSrcStride * s + 2 + q] = c;
 }
 
 // Stokes double layer in complex form.  With tau = z_i - z_j, nu_j the
@@ -573,143 +588,106 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
 
 // Evaluation at a leaf's points: L2P + M2P (W list) + P2P (U list), then
 // y = ya * y + yb * (diag mu + phi) (Laplace double layer; for Neumann, phi
-// is Re of the target normal times the Cauchy sum, plus the rank-one sum).  A leaf holds ~30 points on average, so
-// each target is shared by nsplit = blockDim / cnt threads: they split the
-// right-hand sides of L2P / M2P and the sources of P2P (the t-th thread of a
-// target takes every nsplit-th one, starting at t), and their partial
-// sums are added in a fixed order.
+// is Re of the target normal times the Cauchy sum, plus the rank-one sum).
+// One CTA of kEvalWarps warps per leaf, one lane per target: the target's
+// sums for every right-hand side stay in registers; the warps split the
+// work on the same 32 targets (L2P and M2P by right-hand side, P2P by
+// source, round robin) and add their partial sums in a fixed order at the
+// end.  Each source's data (position, charge factor, densities, written once
+// per product by the charges kernel) is read by a whole warp at one
+// address, so no shared-memory staging and no barrier sit in the pair loop.
+// A leaf of more than 32 points takes several passes.
+constexpr int kEvalWarps = 4;
 template <class R>
-__global__ void __launch_bounds__(kEvalThreads, 4) eval_kernel(FmmArgs<R> a, Geo<double> g,
-                                                               const double* mu, double* y,
-                                                               double ya, double yb,
-                                                               const double* r1) {
-  extern __shared__ __align__(16) unsigned char smem[];
+__global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
+    FmmArgs<R> a, Geo<double> g, const double* mu, double* y, double ya, double yb,
+    const double* r1) {
+  __shared__ double part[kEvalWarps - 1][32][kMaxRhs];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int B = a.boxes[blockIdx.x];
   const int s0 = a.pstart[B], cnt = a.pcount[B];
   const int p = a.p, nrhs = a.nrhs;
-  Pos<R>* sp = reinterpret_cast<Pos<R>*>(smem);                 // staged source positions
-  R* sc = reinterpret_cast<R*>(sp + kStage);                    // kStage x kMaxRhs complex
-  double* red = reinterpret_cast<double*>(sc + 2 * kStage * kMaxRhs);  // blockDim x kMaxRhs
   const R isB = rcp(side_of(a, B));
-  const int nsplit = (cnt > 0 && 2 * cnt <= (int)blockDim.x) ? (int)blockDim.x / cnt : 1;
-  const int span = nsplit > 1 ? cnt : (int)blockDim.x;  // targets per pass
-  const int part = threadIdx.x / span, tj = threadIdx.x % span;
-  for (int j0 = 0; j0 < cnt; j0 += span) {
-    const int j = j0 + tj;
-    const bool act = j < cnt && part < nsplit;
+  for (int j0 = 0; j0 < cnt; j0 += 32) {
+    const int j = j0 + lane;
+    const bool act = j < cnt;
+    const int ts = s0 + (act ? j : 0);  // an idle lane shadows the leaf's first point
     R phi[kMaxRhs];
 #pragma unroll
     for (int q = 0; q < kMaxRhs; ++q) phi[q] = (R)0;
-    Pos<R> tp{};
-    // Neumann: every Cauchy sum is multiplied by the target normal
+    const Pos<R> tp = pt_pos(a, ts);
     Cx<R> tnu = {(R)1, (R)0};
-    if (act && a.mode == 1) {
-      const int pt = a.slot_pt[s0 + j];
+    if (a.mode == 1) {
+      const int pt = a.slot_pt[ts];
       tnu = {to_r<R>(g.nx[pt]), to_r<R>(g.ny[pt])};
     }
-    if (act) {
-      tp = pt_pos(a, s0 + j);
-      // L2P
-      const Cx<R> rho = cscale(vec(tp), isB);
+    // L2P (right-hand sides q = wp, wp + kEvalWarps, ...)
+    const Cx<R> rho = cscale(vec(tp), isB);
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) {
+      if (q < nrhs && q % kEvalWarps == wp) {
+        const R* L = a.local + 2 * (size_t)p * (q + nrhs * (size_t)B);
+        Cx<R> h = ld_c(L, p - 1);
+        for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
+        phi[q] += cmul(tnu, h).re;
+      }
+    }
+    // M2P from the W list (the same split)
+    for (int wi = a.w_off[B]; wi < a.w_off[B + 1]; ++wi) {
+      const int C = a.w_idx[wi];
+      const Cx<R> iw = cinv(cadd(vec(tp), box_off(a, C, B)));  // z - c_C
+      const Cx<R> t = cscale(iw, side_of(a, C));
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) {
-        if (q < nrhs && q % nsplit == part) {
-          const R* L = a.local + 2 * (size_t)p * (q + nrhs * (size_t)B);
-          Cx<R> h = ld_c(L, p - 1);
-          for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
-          phi[q] += cmul(tnu, h).re;
-        }
-      }
-      // M2P from the W list
-      for (int wi = a.w_off[B]; wi < a.w_off[B + 1]; ++wi) {
-        const int C = a.w_idx[wi];
-        const Cx<R> iw = cinv(cadd(vec(tp), box_off(a, C, B)));  // z - c_C
-        const Cx<R> t = cscale(iw, side_of(a, C));
-#pragma unroll
-        for (int q = 0; q < kMaxRhs; ++q) {
-          if (q < nrhs && q % nsplit == part) {
-            const R* M = a.mpole + 2 * (size_t)p * (q + nrhs * (size_t)C);
-            Cx<R> h = ld_c(M, p - 1);
-            for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, t), ld_c(M, k));
-            phi[q] += cmul(tnu, cmul(h, iw)).re;
-          }
+        if (q < nrhs && q % kEvalWarps == wp) {
+          const R* M = a.mpole + 2 * (size_t)p * (q + nrhs * (size_t)C);
+          Cx<R> h = ld_c(M, p - 1);
+          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, t), ld_c(M, k));
+          phi[q] += cmul(tnu, cmul(h, iw)).re;
         }
       }
     }
-    // P2P from the U list (sources staged kStage at a time)
+    // P2P from the U list: this warp takes every kEvalWarps-th source
+    int rr = wp;  // the source's position in the U list's concatenation, mod kEvalWarps
     for (int ui = a.u_off[B]; ui < a.u_off[B + 1]; ++ui) {
       const int D = a.u_idx[ui];
-      const int d0 = a.pstart[D], dcnt = a.pcount[D];
+      const int d0 = a.pstart[D], dc = a.pcount[D];
       const auto offD = p2p_off(a, B, D);
-      for (int i0 = 0; i0 < dcnt; i0 += kStage) {
-        const int ic = dcnt - i0 < kStage ? dcnt - i0 : kStage;
-        __syncthreads();
-        for (int e = threadIdx.x; e < ic; e += blockDim.x) sp[e] = pt_pos(a, d0 + i0 + e);
-        // Laplace: a charge is b_j mu_j with b_j = -(w_j / 2pi) nu_j, so the
-        // pair term Re(b_j / tau) is formed once and scaled per right-hand
-        // side; staged as b (kStage complex) then the densities (kStage x
-        // nrhs).  Neumann: real charges.
-        R* sb = sc;
-        R* sdn = sc + 2 * kStage;
+      int sj = d0 + rr;
+      for (; sj < d0 + dc; sj += kEvalWarps) {
+        if (sj == ts) continue;  // self
+        const Cx<R> iv = cmul(tnu, cinv(diff(tp, pt_pos(a, sj), offD)));
+        const R* sr = a.src + (size_t)kSrcStride * sj;
         if (a.mode == 0) {
-          for (int e = threadIdx.x; e < ic; e += blockDim.x) {
-            const int pt = a.slot_pt[d0 + i0 + e];
-            const double f = -g.w[pt] * (1.0 / (2.0 * CUDART_PI));
-            sb[2 * e] = to_r<R>(f * g.nx[pt]);
-            sb[2 * e + 1] = to_r<R>(f * g.ny[pt]);
-          }
-          for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
-            const int i = e % ic, q = e / ic;
-            sdn[i + kStage * q] = to_r<R>(mu[a.slot_pt[d0 + i0 + i] + (size_t)a.npts * q]);
-          }
+          const R t = sr[0] * iv.re - sr[1] * iv.im;
+#pragma unroll
+          for (int q = 0; q < kMaxRhs; ++q)
+            if (q < nrhs) phi[q] += sr[2 + q] * t;
         } else {
-          for (int e = threadIdx.x; e < ic * nrhs; e += blockDim.x) {
-            const int i = e % ic, q = e / ic;
-            sc[i + kStage * q] = a.charge[2 * (d0 + i0 + i + (size_t)a.npts * q)];
-          }
-        }
-        __syncthreads();
-        if (act) {
-          for (int i = part; i < ic; i += nsplit) {
-            if (d0 + i0 + i == s0 + j) continue;  // self
-            const Cx<R> iv = cmul(tnu, cinv(diff(tp, sp[i], offD)));
-            if (a.mode == 0) {
-              const R t = sb[2 * i] * iv.re - sb[2 * i + 1] * iv.im;
 #pragma unroll
-              for (int q = 0; q < kMaxRhs; ++q)
-                if (q < nrhs) phi[q] += sdn[i + kStage * q] * t;
-            } else {
-#pragma unroll
-              for (int q = 0; q < kMaxRhs; ++q)
-                if (q < nrhs) phi[q] += sc[i + kStage * q] * iv.re;
-            }
-          }
+          for (int q = 0; q < kMaxRhs; ++q)
+            if (q < nrhs) phi[q] += sr[2 + q] * iv.re;
         }
       }
+      rr = sj - (d0 + dc);  // carried into the next source box
     }
-    double tot[kMaxRhs];
+    // partial sums of warps 1.. to warp 0, added in warp order
+    __syncthreads();
+    if (wp > 0)
 #pragma unroll
-    for (int q = 0; q < kMaxRhs; ++q) tot[q] = (double)phi[q];
-    if (nsplit > 1) {
-      __syncthreads();
-      if (act)
-#pragma unroll
-        for (int q = 0; q < kMaxRhs; ++q) red[threadIdx.x * kMaxRhs + q] = tot[q];
-      __syncthreads();
-      if (act && part == 0)
-        for (int t = 1; t < nsplit; ++t)
-#pragma unroll
-          for (int q = 0; q < kMaxRhs; ++q) tot[q] += red[(t * span + tj) * kMaxRhs + q];
-    }
-    if (act && part == 0) {
-      const int pt = a.slot_pt[s0 + j];
+      for (int q = 0; q < kMaxRhs; ++q) part[wp - 1][lane][q] = (double)phi[q];
+    __syncthreads();
+    if (wp == 0 && act) {
+      const int pt = a.slot_pt[ts];
       const double diag = (a.mode == 1 ? -0.5 : 0.5) +
                           0.5 * g.kap[pt] * g.w[pt] * (1.0 / (2.0 * CUDART_PI));
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) {
         if (q < nrhs) {
+          double tot = (double)phi[q];
+          for (int w = 1; w < kEvalWarps; ++w) tot += part[w - 1][lane][q];
           const size_t o = pt + (size_t)a.npts * q;
-          const double v = yb * (diag * mu[o] + tot[q] + (a.mode == 1 ? r1[q] : 0.0));
+          const double v = yb * (diag * mu[o] + tot + (a.mode == 1 ? r1[q] : 0.0));
           y[o] = ya == 0.0 ? v : ya * y[o] + v;
         }
       }
@@ -892,6 +870,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
   const int pmax = f.p > f.p32 ? f.p : f.p32;
   cudaError_t e;
   if ((e = f.charge.ensure(2 * (size_t)npts * kMaxRhs)) != cudaSuccess) return e;
+  // (sized in doubles: holds kSrcStride values of R <= 8 bytes per slot)
+  if ((e = f.src.ensure((size_t)npts * kSrcStride)) != cudaSuccess) return e;
   if ((e = f.mpole.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
   if ((e = f.local.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
   if ((e = f.r1.ensure(kMaxRhs)) != cudaSuccess) return e;
@@ -926,6 +906,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
   a.mode = mode;
   R* charge = reinterpret_cast<R*>(f.charge.p);
   a.charge = charge;
+  R* src = reinterpret_cast<R*>(f.src.p);
+  a.src = src;
   a.mpole = reinterpret_cast<R*>(f.mpole.p);
   a.local = reinterpret_cast<R*>(f.local.p);
   const unsigned nleaves = (unsigned)f.leaves_h.size();
@@ -941,9 +923,10 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
     const size_t tot = (size_t)npts * nq;
     const unsigned cg = (unsigned)((tot + 255) / 256);
     if (mode == 0) {
-      charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq, charge);
+      charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq, charge, src);
     } else if (mode == 1) {
-      neumann_charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq, charge);
+      neumann_charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, npts, muq, nq, charge,
+                                                    src);
     } else {
       stokes_charges_kernel<R><<<cg, 256, 0, st>>>(geo, f.slot_pt.p, f.rx.p, f.ry.p, npts, muq,
                                                    nq, charge);
@@ -984,7 +967,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
     if (nleaves && mode == 2)
       stokes_eval_kernel<R><<<nleaves, kEvalThreads, esm, st>>>(a, geo, muq, yq, ya, yb, f.r1.p);
     else if (nleaves)
-      eval_kernel<R><<<nleaves, kEvalThreads, esm, st>>>(a, geo, muq, yq, ya, yb, f.r1.p);
+      eval_warp_kernel<R><<<nleaves, 32 * kEvalWarps, 0, st>>>(a, geo, muq, yq, ya, yb,
+                                                              f.r1.p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -68,6 +68,7 @@ struct FmmPlan {
   size_t v_pairs = 0, u_pairs = 0, w_pairs = 0, x_pairs = 0;
   // work buffers (complex pairs of the variant's number type; sized for FP64)
   DevBuf<double> charge;       // 2 * (slot + npts * rhs)
+  DevBuf<double> src;          // near-field source data, per slot (Laplace, Neumann)
   DevBuf<double> mpole, local; // 2 * (k + p * (rhs + nrhs * box))
   DevBuf<double> r1;           // per right-hand side: the rank-one sums (Neumann, Stokes)
   HostBuf<unsigned char> stage;  // pinned staging of the plan's uploads

@@ -554,14 +554,21 @@ constexpr int kOversample = 16;
 template <int TS>
 constexpr int max_tiles() { return TS == 4 ? 2 : 5; }
 
-__device__ __forceinline__ float sketch_sign(int r, int i) {
-  unsigned x = (unsigned)r * 0x9E3779B1u ^ (unsigned)i * 0x85EBCA77u ^ 0x27D4EB2Fu;
+// The sketch matrix Omega: entry (s, i) (sketch row s, ID-matrix row i) is
+// +-1 from bit i % 8 of a 32-bit integer hash of (s, i / 8), so one hash
+// gives a 16-byte row of eight BF16 signs for the tensor cores; the CUDA-core
+// paths read the same entries one at a time.
+__device__ __forceinline__ uint32_t sketch_bits8(int s, int grp) {
+  unsigned x = (unsigned)s * 0x9E3779B1u ^ (unsigned)grp * 0x85EBCA77u ^ 0x6A09E667u;
   x ^= x >> 15;
   x *= 0x2C1B3C6Du;
   x ^= x >> 12;
   x *= 0x297A2D39u;
   x ^= x >> 15;
-  return (x & 0x80000000u) ? -1.0f : 1.0f;
+  return x >> 24;
+}
+__device__ __forceinline__ float sketch_sign(int s, int i) {
+  return ((sketch_bits8(s, i >> 3) >> (i & 7)) & 1u) ? -1.0f : 1.0f;
 }
 
 __host__ __device__ inline int sketch_rows(int n) { return n + kOversample; }
@@ -591,9 +598,8 @@ __device__ __forceinline__ bool sketch_too_small(int k, int n, int m, int ell, i
 
 // Test rows of the residual judge.  A learned pass's truncated sketch (fewer
 // rows than the full n + 16, of a matrix taller than the sketch) is followed
-// by kIdTestRows rows whose signs are independent of the sketch's (rows
-// kTestSignRow + t of the same hash), stored below the sketch.
-constexpr int kTestSignRow = 1 << 12;
+// by kIdTestRows more rows of Omega (rows ell .. ell + 7, whose signs are
+// independent of the sketch rows'), stored below the sketch.
 __device__ __forceinline__ int task_test_rows(const IdParams& p, const IdTask& t, int ell, int m) {
   return (p.redo != nullptr && !p.redo_pass && p.judge_factor > 0.f && ell < sketch_rows(t.n) &&
           m > ell)
@@ -601,8 +607,7 @@ __device__ __forceinline__ int task_test_rows(const IdParams& p, const IdTask& t
              : 0;
 }
 __device__ __forceinline__ float sketch_or_test_sign(int r, int ell, int nt, int i) {
-  if (r < ell) return sketch_sign(r, i);
-  return r < ell + nt ? sketch_sign(kTestSignRow + (r - ell), i) : 0.f;
+  return r < ell + nt ? sketch_sign(r, i) : 0.f;
 }
 
 // Residual estimate of an ID (k, perm, Z) from test rows Yt = Omega_t A
@@ -671,17 +676,6 @@ __host__ __device__ inline uint32_t tc_tmem_cols(int cols) {
   uint32_t c = 32;
   while (c < (uint32_t)cols) c <<= 1;
   return c;
-}
-
-// Eight sketch signs (bits) of sketch row s for chunk rows 8 grp .. 8 grp + 7.
-__device__ __forceinline__ uint32_t sketch_bits8(int s, int grp) {
-  unsigned x = (unsigned)s * 0x9E3779B1u ^ (unsigned)grp * 0x85EBCA77u ^ 0x6A09E667u;
-  x ^= x >> 15;
-  x *= 0x2C1B3C6Du;
-  x ^= x >> 12;
-  x *= 0x297A2D39u;
-  x ^= x >> 15;
-  return x >> 24;
 }
 
 // v = hi + mid + lo with BF16 parts (each difference is exact in FP32).

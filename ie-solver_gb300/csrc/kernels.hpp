@@ -106,7 +106,7 @@ int launch_id_wide(const IdParams& p, int num_tasks, int nmax, const WideItem* i
 size_t id_wide_tile(int m, int n);  // scratch floats of a wide task (m: rows factored)
 int id_sketch_rows(int n);
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
-                     cudaStream_t st);
+                     cudaStream_t st, int threads = 256);
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st);
 
 // Dense LU with partial pivoting of an n x n column-major matrix (one CTA),

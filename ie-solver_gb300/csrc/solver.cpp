@@ -87,6 +87,7 @@ struct rs_solver {
   // wide ID's CTAs per SM
   int split_min_tasks = 512;
   int wide_ctas_per_sm = 2;
+  int elim_threads = 256;  // threads per box of the Schur eliminations (128 or 256)
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;  // read-back of ranks while eliminations run
   cudaEvent_t ev_c = nullptr;
@@ -934,7 +935,8 @@ rs_status factor_impl(rs_solver* s) {
       DecoupleParams q = dp;
       q.tasks = dt;
       bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
-      launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream);
+      launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream,
+                      s->elim_threads);
       ++s->launches;
     });
     CU(cudaGetLastError());
@@ -1207,7 +1209,8 @@ rs_status factor_impl(rs_solver* s) {
       DecoupleParams q = dp;
       q.tasks = dt;
       bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
-      launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream);
+      launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream,
+                      s->elim_threads);
       ++s->launches;
     });
     CU(cudaGetLastError());
@@ -2287,12 +2290,20 @@ rs_status rs_factor(rs_solver* s) {
   s->stats.t_factor_ms = now_ms() - t0;
   s->stats.id_ms = 0;
   s->stats.decouple_ms = 0;
-  for (int lv : s->timed_levels) {
-    float a = 0, b = 0;
+  s->stats.level_gap_ms = 0;
+  for (size_t q = 0; q < s->timed_levels.size(); ++q) {
+    const int lv = s->timed_levels[q];
+    float a = 0, b = 0, c = 0;
     cudaEventElapsedTime(&a, s->lv_ev[3 * lv], s->lv_ev[3 * lv + 1]);
     cudaEventElapsedTime(&b, s->lv_ev[3 * lv + 1], s->lv_ev[3 * lv + 2]);
     s->stats.id_ms += a;
     s->stats.decouple_ms += b;
+    if (q + 1 < s->timed_levels.size()) {
+      // from this level's Schur end to the next level's ID start: the
+      // stream waits for the host's planning of that level
+      cudaEventElapsedTime(&c, s->lv_ev[3 * lv + 2], s->lv_ev[3 * s->timed_levels[q + 1]]);
+      s->stats.level_gap_ms += c;
+    }
   }
   int nc = 0;
   for (const NodeState& S : s->st) nc += S.compressed;
@@ -2565,7 +2576,8 @@ rs_status rs_get_stats(const rs_solver* s, rs_stats* out) {
   return RS_OK;
 }
 
-rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm) {
+rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm,
+                      int* elim_threads) {
   if (!s || reps < 1) return RS_ERR_ARG;
   // each candidate: the median device time of `reps` factorizations of the
   // handle's geometry; one knob at a time, the other at its current value
@@ -2606,9 +2618,22 @@ rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ct
     }
   }
   s->wide_ctas_per_sm = best_wide;
+  best = 1e300;
+  int best_elim = s->elim_threads;
+  for (int cand : {256, 128}) {
+    s->elim_threads = cand;
+    double ms = 0;
+    RSCHK(time_factor(&ms));
+    if (ms < best) {
+      best = ms;
+      best_elim = cand;
+    }
+  }
+  s->elim_threads = best_elim;
   s->factored = false;  // the last candidate's factors are not the chosen shape's
   if (split_min_tasks) *split_min_tasks = s->split_min_tasks;
   if (wide_ctas_per_sm) *wide_ctas_per_sm = s->wide_ctas_per_sm;
+  if (elim_threads) *elim_threads = s->elim_threads;
   return RS_OK;
 }
 

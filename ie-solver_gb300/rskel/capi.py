@@ -66,7 +66,7 @@ class RsStats(ctypes.Structure):
                 ("residual64_ms", ctypes.c_double), ("residual32_ms", ctypes.c_double),
                 ("rank_predicted", ctypes.c_int), ("rank_redo", ctypes.c_int),
                 ("sketch_rows", ctypes.c_double), ("krylov_steps", ctypes.c_int),
-                ("rank_redo_judge", ctypes.c_int)]
+                ("rank_redo_judge", ctypes.c_int), ("level_gap_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -250,10 +250,12 @@ class Solver:
                                                 _d(arrs[1]), _d(arrs[2]), _d(arrs[3])))
 
     def autotune(self, reps=3):
-        """rs_autotune: returns (split_min_tasks, wide_ctas_per_sm) chosen."""
-        a, b = ctypes.c_int(0), ctypes.c_int(0)
-        self._check(lib().rs_autotune(self.h, reps, ctypes.byref(a), ctypes.byref(b)))
-        return a.value, b.value
+        """rs_autotune: returns (split_min_tasks, wide_ctas_per_sm,
+        elim_threads) chosen."""
+        a, b, c = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        self._check(lib().rs_autotune(self.h, reps, ctypes.byref(a), ctypes.byref(b),
+                                      ctypes.byref(c)))
+        return a.value, b.value, c.value
 
     def _check(self, rc, h="self"):
         if rc != 0:

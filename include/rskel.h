@@ -293,11 +293,13 @@ rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* feat
  * problem and keeps the fastest for this handle's later factorizations:
  * the level size from which the FP32 sketched ID's pivoted QR runs one
  * warp per box instead of one CTA per box (128, 256, 512 (default), 1024,
- * never), then the wide ID's CTAs per SM (1, 2 (default), 4).  Each
- * candidate is the median of `reps` factorizations.  The choices are
- * returned (pointers may be NULL).  The handle must be factored again
- * before solving. */
-rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm);
+ * never), then the wide ID's CTAs per SM (1, 2 (default), 4), then the
+ * threads per box of the Schur eliminations (256 (default), 128: more
+ * boxes resident per SM, fewer threads each).  Each candidate is the median
+ * of `reps` factorizations.  The choices are returned (pointers may be
+ * NULL).  The handle must be factored again before solving. */
+rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm,
+                      int* elim_threads);
 
 /* --- introspection (tree and factorization), for tests and tooling --- */
 typedef struct {
@@ -326,6 +328,10 @@ typedef struct {
   int krylov_steps;                            /* last solve: GMRES steps of GMRES-IR */
   int rank_redo_judge;                         /* of rank_redo: boxes whose sketch settled the
                                                   rank but failed the residual judge */
+  double level_gap_ms;                         /* last rs_factor: device time between one
+                                                  level's last kernel and the next level's
+                                                  first, summed (the device waiting for the
+                                                  host's planning of the next level) */
 } rs_stats;
 rs_status rs_get_stats(const rs_solver* s, rs_stats* out);
 
