@@ -75,6 +75,30 @@ __device__ __forceinline__ DF rcp(DF a) {
   return y + y * e;
 }
 
+// acc += x y for the near field's sums.  For float-float the product's
+// error (an explicit fused multiply-add) and the sum's error (two-sum) are
+// collected in acc.lo without renormalising after every term; acc_norm
+// renormalises (after each source box, so acc.lo stays a few ulps of
+// acc.hi) and is a no-op for the other number types.
+template <class R>
+__device__ __forceinline__ void acc_fma(R& acc, R x, R y) { acc += x * y; }
+__device__ __forceinline__ void acc_fma(DF& acc, DF x, DF y) {
+  const float p = x.hi * y.hi;
+  const float pe = fmaf(x.hi, y.hi, -p) + fmaf(x.hi, y.lo, x.lo * y.hi);
+  const float s = acc.hi + p;
+  const float bb = s - acc.hi;
+  acc.lo += ((acc.hi - (s - bb)) + (p - bb)) + pe;
+  acc.hi = s;
+}
+template <class R>
+__device__ __forceinline__ void acc_norm(R&) {}
+__device__ __forceinline__ void acc_norm(DF& a) { a = df_renorm(a.hi, a.lo); }
+
+// Warp broadcast of lane src's value (float-float: both parts).
+__device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ DF shfl(DF v, int src) { return DF(shfl(v.hi, src), shfl(v.lo, src)); }
+
 template <class R>
 __device__ __forceinline__ R to_r(double v) { return R(v); }
 template <>
@@ -621,55 +645,88 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
       const int pt = a.slot_pt[ts];
       tnu = {to_r<R>(g.nx[pt]), to_r<R>(g.ny[pt])};
     }
-    // L2P (right-hand sides q = wp, wp + kEvalWarps, ...)
+    // L2P (right-hand sides q = wp, wp + kEvalWarps, ...; the loop is kept
+    // rolled and its result added through an unrolled select, which keeps
+    // the kernel's code small)
     const Cx<R> rho = cscale(vec(tp), isB);
+#pragma unroll 1
+    for (int qq = wp; qq < nrhs; qq += kEvalWarps) {
+      const R* L = a.local + 2 * (size_t)p * (qq + nrhs * (size_t)B);
+      Cx<R> h = ld_c(L, p - 1);
+      for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
+      const R v = cmul(tnu, h).re;
 #pragma unroll
-    for (int q = 0; q < kMaxRhs; ++q) {
-      if (q < nrhs && q % kEvalWarps == wp) {
-        const R* L = a.local + 2 * (size_t)p * (q + nrhs * (size_t)B);
-        Cx<R> h = ld_c(L, p - 1);
-        for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
-        phi[q] += cmul(tnu, h).re;
-      }
+      for (int q = 0; q < kMaxRhs; ++q)
+        if (q == qq) phi[q] += v;
     }
-    // M2P from the W list (the same split)
-    for (int wi = a.w_off[B]; wi < a.w_off[B + 1]; ++wi) {
-      const int C = a.w_idx[wi];
-      const Cx<R> iw = cinv(cadd(vec(tp), box_off(a, C, B)));  // z - c_C
-      const Cx<R> t = cscale(iw, side_of(a, C));
-#pragma unroll
-      for (int q = 0; q < kMaxRhs; ++q) {
-        if (q < nrhs && q % kEvalWarps == wp) {
-          const R* M = a.mpole + 2 * (size_t)p * (q + nrhs * (size_t)C);
+    // M2P from the W list (the same split).  Box offsets and sides need FP64
+    // arithmetic (slow on this GPU), so lane l forms them for the list's l-th
+    // box and the warp broadcasts them in turn.
+    for (int wb = a.w_off[B]; wb < a.w_off[B + 1]; wb += 32) {
+      const int nwb = min(32, a.w_off[B + 1] - wb);
+      int Cl = 0;
+      Cx<R> ol = {(R)0, (R)0};
+      R sl = (R)1;
+      if (lane < nwb) {
+        Cl = a.w_idx[wb + lane];
+        ol = box_off(a, Cl, B);
+        sl = side_of(a, Cl);
+      }
+      for (int t = 0; t < nwb; ++t) {
+        const int C = __shfl_sync(0xffffffffu, Cl, t);
+        const Cx<R> oc = {shfl(ol.re, t), shfl(ol.im, t)};
+        const R sc = shfl(sl, t);
+        const Cx<R> iw = cinv(cadd(vec(tp), oc));  // z - c_C
+        const Cx<R> tw = cscale(iw, sc);
+#pragma unroll 1
+        for (int qq = wp; qq < nrhs; qq += kEvalWarps) {
+          const R* M = a.mpole + 2 * (size_t)p * (qq + nrhs * (size_t)C);
           Cx<R> h = ld_c(M, p - 1);
-          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, t), ld_c(M, k));
-          phi[q] += cmul(tnu, cmul(h, iw)).re;
+          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, tw), ld_c(M, k));
+          const R v = cmul(tnu, cmul(h, iw)).re;
+#pragma unroll
+          for (int q = 0; q < kMaxRhs; ++q)
+            if (q == qq) phi[q] += v;
         }
       }
     }
     // P2P from the U list: this warp takes every kEvalWarps-th source
+    // (offsets broadcast as above)
+    using OT = typename OffT<R>::type;
     int rr = wp;  // the source's position in the U list's concatenation, mod kEvalWarps
-    for (int ui = a.u_off[B]; ui < a.u_off[B + 1]; ++ui) {
-      const int D = a.u_idx[ui];
-      const int d0 = a.pstart[D], dc = a.pcount[D];
-      const auto offD = p2p_off(a, B, D);
-      int sj = d0 + rr;
-      for (; sj < d0 + dc; sj += kEvalWarps) {
-        if (sj == ts) continue;  // self
-        const Cx<R> iv = cmul(tnu, cinv(diff(tp, pt_pos(a, sj), offD)));
-        const R* sr = a.src + (size_t)kSrcStride * sj;
-        if (a.mode == 0) {
-          const R t = sr[0] * iv.re - sr[1] * iv.im;
-#pragma unroll
-          for (int q = 0; q < kMaxRhs; ++q)
-            if (q < nrhs) phi[q] += sr[2 + q] * t;
-        } else {
-#pragma unroll
-          for (int q = 0; q < kMaxRhs; ++q)
-            if (q < nrhs) phi[q] += sr[2 + q] * iv.re;
-        }
+    for (int ub = a.u_off[B]; ub < a.u_off[B + 1]; ub += 32) {
+      const int nub = min(32, a.u_off[B + 1] - ub);
+      int Dl = 0;
+      Cx<OT> ol = {OT(0.0), OT(0.0)};
+      if (lane < nub) {
+        Dl = a.u_idx[ub + lane];
+        ol = p2p_off(a, B, Dl);
       }
-      rr = sj - (d0 + dc);  // carried into the next source box
+      for (int t = 0; t < nub; ++t) {
+        const int D = __shfl_sync(0xffffffffu, Dl, t);
+        const Cx<OT> offD = {shfl(ol.re, t), shfl(ol.im, t)};
+        const int d0 = a.pstart[D], dc = a.pcount[D];
+        int sj = d0 + rr;
+        for (; sj < d0 + dc; sj += kEvalWarps) {
+          if (sj == ts) continue;  // self
+          Cx<R> iv = cinv(diff(tp, pt_pos(a, sj), offD));
+          const R* sr = a.src + (size_t)kSrcStride * sj;
+          if (a.mode == 0) {
+            const R tr = sr[0] * iv.re - sr[1] * iv.im;
+#pragma unroll
+            for (int q = 0; q < kMaxRhs; ++q)
+              if (q < nrhs) acc_fma(phi[q], sr[2 + q], tr);
+          } else {
+            iv = cmul(tnu, iv);
+#pragma unroll
+            for (int q = 0; q < kMaxRhs; ++q)
+              if (q < nrhs) acc_fma(phi[q], sr[2 + q], iv.re);
+          }
+        }
+        rr = sj - (d0 + dc);  // carried into the next source box
+#pragma unroll
+        for (int q = 0; q < kMaxRhs; ++q) acc_norm(phi[q]);
+      }
     }
     // partial sums of warps 1.. to warp 0, added in warp order
     __syncthreads();

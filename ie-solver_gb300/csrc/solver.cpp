@@ -109,6 +109,8 @@ struct rs_solver {
   Factor<float> F32;
 
   std::vector<SweepTask> sweeps;
+  std::vector<int> sweep_ids;  // the box of each sweep task
+  size_t sweep_pool = 0;       // pool entries of the sweep tasks' lists
   std::vector<int> sweep_off, sweep_cnt, sweep_nmax;  // per level
   DevBuf<SweepTask> sweep_dev;
   int ns = 0;
@@ -162,7 +164,11 @@ struct rs_solver {
   DevBuf<int> redo, ell_slot;
   DevBuf<float> judge_ratio;  // trace mode: the residual judge's ratio per slot
   HostBuf<int> h_redo, h_ell;
-  std::vector<float> samp_feat, samp_target;
+  // the last factorization's rank samples: the ID boxes in order and their
+  // k / n (features are formed on request from the boxes' kept lists)
+  std::vector<int> samp_box;
+  std::vector<float> samp_target;
+  double samp_tol = 0;
   double host_plan_ms = 0, host_wait_ms = 0, host_post_ms = 0;
 
   // CUDA graph of the factorization's inverse (no holes): the level sweeps
@@ -500,6 +506,19 @@ void launch_binned(const std::vector<Task>& tasks, const Task* dev_tasks, Fits&&
 template <class Real>
 rs_status factor_border(rs_solver* s);
 
+// The stable order of tasks by their size n, by counting sort: the order
+// std::stable_sort by n gives, in time linear in the tasks and the largest n.
+template <class Task>
+void order_by_n(const std::vector<Task>& v, std::vector<size_t>* o, std::vector<int>* cnt) {
+  int nmax = 0;
+  for (const Task& t : v) nmax = std::max(nmax, t.n);
+  cnt->assign((size_t)nmax + 2, 0);
+  for (const Task& t : v) ++(*cnt)[t.n + 1];
+  for (int i = 1; i <= nmax + 1; ++i) (*cnt)[i] += (*cnt)[i - 1];
+  o->resize(v.size());
+  for (size_t i = 0; i < v.size(); ++i) (*o)[(*cnt)[v[i].n]++] = i;
+}
+
 template <class Real>
 rs_status factor_impl(rs_solver* s) {
   constexpr bool f32 = sizeof(Real) == 4;
@@ -541,9 +560,14 @@ rs_status factor_impl(rs_solver* s) {
   std::vector<int> m_of_slot;
   std::vector<float> feat, feat_s;  // rank-model features per slot, and in sorted order
   std::vector<double> slot_work;    // per slot: ID flops, sketch rows, Schur flops
+  std::vector<size_t> oi, od;       // a level's tasks in size order
+  std::vector<int> sort_cnt;
+  std::vector<IdTask> idt_s;
+  std::vector<DecoupleTask> dct_s;
   const bool model = f32 && s->rank_model_on;
-  s->samp_feat.clear();
+  s->samp_box.clear();
   s->samp_target.clear();
+  s->samp_tol = tol;
   s->stats.rank_predicted = 0;
   s->stats.rank_redo = 0;
   s->stats.rank_redo_judge = 0;
@@ -628,6 +652,12 @@ rs_status factor_impl(rs_solver* s) {
       F.e_used += (size_t)n * n;
       s->stats.max_active = std::max(s->stats.max_active, n);
     }
+    // Learned sketch sizes on levels of at least one box per SM: there the
+    // ID is throughput-bound and shorter sketches save work; a level of fewer
+    // boxes runs each box on an SM of its own, so its time is one box's
+    // latency, which a truncated sketch barely shortens and a redone box
+    // doubles.
+    const bool learned = model && nslots >= s->num_sms;
     s->pool.resize(pool_end);
     idt.resize(nslots);
     m_of_slot.resize(nslots);
@@ -664,7 +694,8 @@ rs_status factor_impl(rs_solver* s) {
         t.m_dense = 0;
         const int m = 2 * t.q + (S.use_proxy ? 2 * prow : 0);
         m_of_slot[P.slot] = m;
-        rank_features(s, nd, S, m, tol, feat.data() + (size_t)P.slot * kRankFeatures);
+        if (learned)  // (samples compute theirs on request: rs_rank_samples)
+          rank_features(s, nd, S, m, tol, feat.data() + (size_t)P.slot * kRankFeatures);
         max_rows = std::max(max_rows, m);
         idt[P.slot] = t;
         cand_ids[P.slot] = id;
@@ -697,20 +728,11 @@ rs_status factor_impl(rs_solver* s) {
     s->stats.max_rows = max_rows;
     const double h_tasks = now_ms();
     if (dct.empty()) continue;
-    // Learned sketch sizes on levels of at least one box per SM: there the
-    // ID is throughput-bound and shorter sketches save work; a level of fewer
-    // boxes runs each box on an SM of its own, so its time is one box's
-    // latency, which a truncated sketch barely shortens and a redone box
-    // doubles.
-    const bool learned = model && (int)idt.size() >= s->num_sms;
     // sort by size for binned launches (slots keep their identity)
-    std::vector<size_t> oi(idt.size()), od(dct.size());
-    for (size_t i = 0; i < oi.size(); ++i) oi[i] = i;
-    for (size_t i = 0; i < od.size(); ++i) od[i] = i;
-    std::stable_sort(oi.begin(), oi.end(), [&](size_t a, size_t b) { return idt[a].n < idt[b].n; });
-    std::stable_sort(od.begin(), od.end(), [&](size_t a, size_t b) { return dct[a].n < dct[b].n; });
-    std::vector<IdTask> idt_s(idt.size());
-    std::vector<DecoupleTask> dct_s(dct.size());
+    order_by_n(idt, &oi, &sort_cnt);
+    order_by_n(dct, &od, &sort_cnt);
+    idt_s.resize(idt.size());
+    dct_s.resize(dct.size());
     for (size_t i = 0; i < oi.size(); ++i) idt_s[i] = idt[oi[i]];
     if (learned) {
       feat_s.resize(feat.size());
@@ -1002,7 +1024,7 @@ rs_status factor_impl(rs_solver* s) {
     // below, so the totals do not depend on the thread count).
     const int nc = (int)cand_ids.size();
     const size_t sbase = s->samp_target.size();
-    s->samp_feat.resize((sbase + nc) * kRankFeatures);
+    s->samp_box.resize(sbase + nc);
     s->samp_target.resize(sbase + nc);
     slot_work.assign(3 * (size_t)nc, 0.0);  // {id flops, sketch rows, Schur flops}
     int n_pred = 0, n_redo = 0, n_redo_judge = 0, n_fac = 0, k_max = s->stats.max_rank;
@@ -1013,9 +1035,7 @@ rs_status factor_impl(rs_solver* s) {
       NodeState& S = s->st[id];
       const int k = s->h_ranks.p[S.slot];
       const int n = (int)S.active.size();
-      std::copy(feat.begin() + (size_t)S.slot * kRankFeatures,
-                feat.begin() + (size_t)(S.slot + 1) * kRankFeatures,
-                s->samp_feat.begin() + (sbase + c) * kRankFeatures);
+      s->samp_box[sbase + c] = id;
       s->samp_target[sbase + c] = k > 0 ? (float)k / (float)n : 1.f;
       const int m = m_of_slot[S.slot];
       double* wk = slot_work.data() + 3 * (size_t)c;
@@ -1146,9 +1166,13 @@ rs_status factor_impl(rs_solver* s) {
   s->root_e_off = s->roots_h.empty() ? 0 : s->roots_h[0].a_off;
   // solve plan: compressed boxes per level, skeleton / redundant lists
   s->sweeps.clear();
+  s->sweep_ids.clear();
+  s->sweep_pool = 0;
   s->sweep_off.assign(L, 0);
   s->sweep_cnt.assign(L, 0);
   s->sweep_nmax.assign(L, 0);
+  // (a serial pass for the tasks' pool offsets, then the lists are copied
+  // in parallel: a batch of boundaries has hundreds of thousands of boxes)
   for (int lv = L - 1; lv >= 1; --lv) {
     s->sweep_off[lv] = (int)s->sweeps.size();
     for (int id : s->tree.levels[lv]) {
@@ -1157,16 +1181,27 @@ rs_status factor_impl(rs_solver* s) {
       SweepTask t{};
       t.k = S.k;
       t.r = S.r;
-      t.skel_off = (int)s->pool.size();
-      s->pool.insert(s->pool.end(), S.skel.begin(), S.skel.end());
-      t.red_off = (int)s->pool.size();
-      s->pool.insert(s->pool.end(), S.red.begin(), S.red.end());
+      t.skel_off = (int)(s->pool.size() + s->sweep_pool);
+      t.red_off = t.skel_off + S.k;
+      s->sweep_pool += (size_t)S.k + S.r;
       t.fac_off = S.fac_off;
       t.piv_off = S.piv_off;
       s->sweeps.push_back(t);
+      s->sweep_ids.push_back(id);
       s->sweep_nmax[lv] = std::max(s->sweep_nmax[lv], S.k + S.r);
     }
     s->sweep_cnt[lv] = (int)s->sweeps.size() - s->sweep_off[lv];
+  }
+  {
+    const size_t base = s->pool.size();
+    s->pool.resize(base + s->sweep_pool);
+    const int nsw = (int)s->sweeps.size();
+#pragma omp parallel for schedule(dynamic, 64) if (nsw > 512)
+    for (int i = 0; i < nsw; ++i) {
+      const NodeState& S = s->st[s->sweep_ids[i]];
+      std::copy(S.skel.begin(), S.skel.end(), s->pool.begin() + s->sweeps[i].skel_off);
+      std::copy(S.red.begin(), S.red.end(), s->pool.begin() + s->sweeps[i].red_off);
+    }
   }
   RSCHK(upload_pool(s, seg0));
   CU(s->sweep_dev.ensure(std::max<size_t>(s->sweeps.size(), 1)));
@@ -2685,7 +2720,16 @@ rs_status rs_rank_samples(const rs_solver* s, float* features, float* targets, i
   *count = n;
   const int w = std::min(n, cap);
   if (w > 0) {
-    std::memcpy(features, s->samp_feat.data(), sizeof(float) * kRankFeatures * (size_t)w);
+    // the features of each sample's box, from its lists as the factorization
+    // left them (the same values the planning computes for a rank model)
+    const int prow = (s->cfg.pde == kStokes ? 2 : 1) * s->cfg.num_proxy_points;
+#pragma omp parallel for schedule(dynamic, 64) if (w > 256)
+    for (int i = 0; i < w; ++i) {
+      const int id = s->samp_box[i];
+      const NodeState& S = s->st[id];
+      const int m = 2 * (int)S.rows.size() + (S.use_proxy ? 2 * prow : 0);
+      rank_features(s, s->tree.nodes[id], S, m, s->samp_tol, features + (size_t)i * kRankFeatures);
+    }
     std::memcpy(targets, s->samp_target.data(), sizeof(float) * (size_t)w);
   }
   return RS_OK;
