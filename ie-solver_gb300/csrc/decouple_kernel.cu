@@ -73,11 +73,12 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   const Real* E_in = reinterpret_cast<const Real*>(p.epool);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], 0.0, 0.0, act, j);
-    const BlkRef b = p.blk[t.blk_off + j];
-    bchild[j] = b.child;
-    bidx[j] = b.idx;
-    bld[j] = b.ld;
-    bbase[j] = b.e_base;
+    int c = 0;
+    while (c < 3 && j >= t.cstart[c + 1]) ++c;  // the run of active position j
+    bchild[j] = c;
+    bidx[j] = j - t.cstart[c];
+    bld[j] = t.cld[c];
+    bbase[j] = t.ce[c];
     order[j] = k > 0 ? p.perm[t.perm_off + j] : j;
   }
   __syncthreads();

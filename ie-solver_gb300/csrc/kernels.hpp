@@ -55,7 +55,6 @@ struct DecoupleParams {
   int pde, sd;
   const DecoupleTask* tasks;
   const int* dofs;
-  const BlkRef* blk;
   const int* ranks;
   const int* perm;
   void* fac;       // T in, L/U/X_rr LU out (Real)

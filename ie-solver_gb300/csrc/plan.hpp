@@ -67,28 +67,24 @@ inline int wide_sketch_block(int ell) {
 
 // One elimination (skel_factorization.cpp:77-128) or, for boxes that are not
 // compressed, the assembly of the box's Schur-complemented block.
+// Where entry (a, b) of a box's matrix comes from.  The box's active DOFs
+// are its children's surviving DOFs, child by child (child c's run starts at
+// active position cstart[c]; a leaf is one run with no block).  When DOFs a
+// and b fall in the same run and that child has a Schur-complemented block
+// (ce[c] >= 0), the entry is E[ce[c] + i_a + cld[c] i_b] with i the
+// positions within the run; otherwise it comes from the kernel.
 struct DecoupleTask {
   int n;            // active DOFs
   int act_off;      // active DOFs at dofs[act_off..)
-  int blk_off;      // per-DOF child-block records at blk[blk_off..) (see BlkRef)
   int slot;         // ranks[slot] (k; 0 means "assemble only")
   int perm_off;     // permutation at perm[perm_off..) (n entries)
-  int pad;
   int64_t fac_off;  // T, L, U, X_rr LU at fac[fac_off..)
   int64_t piv_off;  // X_rr pivots at piv[piv_off..)
   int64_t e_off;    // output block E (k x k, or n x n when not compressed)
   int64_t scratch_off;  // >= 0: global-memory tile for large boxes
-};
-
-// Where entry (a, b) of a box's matrix comes from: when two DOFs carry the
-// same `child` tag and e_base >= 0, from that child's Schur-complemented block
-// E[e_base + idx_a + ld * idx_b]; otherwise from the kernel.
-struct BlkRef {
-  int child;     // 0..3, or a unique negative tag for DOFs with no block
-  int idx;       // index within the child's surviving DOF list
-  int ld;        // leading dimension of the child's block
-  int pad;
-  int64_t e_base;  // offset of the child's block in the E pool, -1 = kernel
+  int cstart[4];    // first active position of each child's run (runs in child order)
+  int cld[4];       // leading dimension of each child's block
+  int64_t ce[4];    // offset of each child's block in the E pool, -1 = kernel
 };
 
 // One node of a solve sweep (skel_factorization.cpp:388-426, 507-592).

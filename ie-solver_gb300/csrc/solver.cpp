@@ -102,7 +102,6 @@ struct rs_solver {
   DevBuf<int> dofs, perm, ranks, piv, status;
   DevBuf<IdTask> id_tasks;
   DevBuf<DecoupleTask> dc_tasks;
-  DevBuf<BlkRef> blk;
   HostBuf<int> h_ranks, h_perm, h_status;
   size_t piv_used = 0;
   Factor<double> F64;
@@ -298,6 +297,28 @@ Geo<double> geo_of(const rs_solver* s) {
 // Surviving DOFs of a box after its level: skeleton when compressed.
 const std::vector<int>& surviving(const NodeState& ns) {
   return ns.compressed ? ns.skel : ns.active;
+}
+
+// A box's children's runs in its active list (compute_active's order) and
+// the children's Schur-complemented blocks; a leaf is one run of kernel
+// entries.
+void set_child_runs(const rs_solver* s, const TreeNode& nd, DecoupleTask* d) {
+  if (nd.is_leaf) {
+    for (int c = 0; c < 4; ++c) {
+      d->cstart[c] = c == 0 ? 0 : d->n;
+      d->cld[c] = 0;
+      d->ce[c] = -1;
+    }
+    return;
+  }
+  int o = 0;
+  for (int c = 0; c < 4; ++c) {
+    const NodeState& C = s->st[nd.children[c]];
+    d->cstart[c] = o;
+    d->cld[c] = C.e_ld;
+    d->ce[c] = C.e_ld > 0 ? C.e_off : (int64_t)-1;
+    o += (int)surviving(C).size();
+  }
 }
 
 // QuadTree::remove_inactive_dofs_at_box (quadtree.cpp:1032-1055)
@@ -554,7 +575,6 @@ rs_status factor_impl(rs_solver* s) {
   CU(cudaMemsetAsync(s->status.p, 0, sizeof(int) * 4, s->stream));
   std::vector<IdTask> idt;
   std::vector<DecoupleTask> dct;
-  std::vector<BlkRef> blk;
   std::vector<int> rows;
   std::vector<int> cand_ids, dc_ids;
   std::vector<int> m_of_slot;
@@ -601,7 +621,6 @@ rs_status factor_impl(rs_solver* s) {
     const double h_lists = now_ms();
     idt.clear();
     dct.clear();
-    blk.clear();
     cand_ids.clear();
     dc_ids.clear();
     m_of_slot.clear();
@@ -612,11 +631,11 @@ rs_status factor_impl(rs_solver* s) {
     // pool / block-reference copies, which are independent across boxes.
     struct Slots {
       int kind = 0;  // 0: nothing to do, 1: Schur assembly only, 2: ID + elimination
-      int slot = -1, dci = -1, blk_off = 0;
+      int slot = -1, dci = -1;
       size_t act_off = 0, rows_off = 0;
     };
     std::vector<Slots> pl(nl);
-    size_t pool_end = seg0, blk_end = 0;
+    size_t pool_end = seg0;
     int nslots = 0, ndc = 0;
     for (int q = 0; q < nl; ++q) {
       const int id = lvl[q];
@@ -644,8 +663,6 @@ rs_status factor_impl(rs_solver* s) {
         F.fac_used += fac_reserve(n);
       }
       P.dci = ndc++;
-      P.blk_off = (int)blk_end;
-      blk_end += n;
       S.piv_off = (int64_t)s->piv_used;
       s->piv_used += n;
       S.e_off = (int64_t)F.e_used;
@@ -664,7 +681,6 @@ rs_status factor_impl(rs_solver* s) {
     cand_ids.resize(nslots);
     dct.resize(ndc);
     dc_ids.resize(ndc);
-    blk.resize(blk_end);
     feat.resize((size_t)nslots * kRankFeatures);
     int max_rows = s->stats.max_rows;
 #pragma omp parallel for schedule(dynamic, 16) reduction(max : max_rows) if (nl > 96)
@@ -703,25 +719,13 @@ rs_status factor_impl(rs_solver* s) {
       DecoupleTask d{};
       d.n = n;
       d.act_off = (int)P.act_off;
-      d.blk_off = P.blk_off;
       d.slot = S.slot;
       d.perm_off = (int)P.act_off;
       d.fac_off = S.fac_off;
       d.piv_off = S.piv_off;
       d.e_off = S.e_off;
       d.scratch_off = -1;
-      BlkRef* br = blk.data() + P.blk_off;
-      if (nd.is_leaf) {
-        for (int j = 0; j < n; ++j) br[j] = BlkRef{0, j, 0, 0, -1};
-      } else {
-        int o = 0;
-        for (int c = 0; c < 4; ++c) {
-          const NodeState& C = s->st[nd.children[c]];
-          const std::vector<int>& v = surviving(C);
-          for (int j = 0; j < (int)v.size(); ++j)
-            br[o++] = BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1};
-        }
-      }
+      set_child_runs(s, nd, &d);
       dct[P.dci] = d;
       dc_ids[P.dci] = id;
     }
@@ -836,11 +840,9 @@ rs_status factor_impl(rs_solver* s) {
     if (scratch_need) CU(F.scratch.ensure(scratch_need));
     CU(s->id_tasks.ensure(std::max<size_t>(idt_s.size(), 1)));
     CU(s->dc_tasks.ensure(dct_s.size()));
-    CU(s->blk.ensure(std::max<size_t>(blk.size(), 1)));
     CU(s->ranks.ensure(std::max<size_t>(idt_s.size(), 1)));
     CU(stage_copy(s, s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask)));
     CU(stage_copy(s, s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask)));
-    CU(stage_copy(s, s->blk.p, blk.data(), blk.size() * sizeof(BlkRef)));
     if (!witems.empty()) {
       CU(s->wide_items.ensure(witems.size()));
       CU(s->wide_part.ensure(part_need));
@@ -945,7 +947,6 @@ rs_status factor_impl(rs_solver* s) {
     dp.sd = s->sd;
     dp.tasks = s->dc_tasks.p;
     dp.dofs = s->dofs.p;
-    dp.blk = s->blk.p;
     dp.ranks = s->ranks.p;
     dp.perm = s->perm.p;
     dp.fac = F.fac.p;
@@ -1124,7 +1125,6 @@ rs_status factor_impl(rs_solver* s) {
   s->allskel.clear();
   s->roots_h.clear();
   s->root_nmax = 0;
-  std::vector<BlkRef> rblk;
   std::vector<DecoupleTask> rdt;
   int piv_total = 0;
   for (int r : s->tree.roots) {
@@ -1142,22 +1142,11 @@ rs_status factor_impl(rs_solver* s) {
     DecoupleTask d{};
     d.n = rt.n;
     d.act_off = rt.idx_off;
-    d.blk_off = (int)rblk.size();
     d.slot = -1;
     d.perm_off = rt.idx_off;
     d.e_off = rt.a_off;
     d.scratch_off = -1;
-    const TreeNode& rn = s->tree.nodes[r];
-    if (rn.is_leaf) {
-      for (int j = 0; j < rt.n; ++j) rblk.push_back(BlkRef{0, j, 0, 0, -1});
-    } else {
-      for (int c = 0; c < 4; ++c) {
-        const NodeState& C = s->st[rn.children[c]];
-        const std::vector<int>& v = surviving(C);
-        for (int j = 0; j < (int)v.size(); ++j)
-          rblk.push_back(BlkRef{c, j, C.e_ld, 0, C.e_ld > 0 ? C.e_off : (int64_t)-1});
-      }
-    }
+    set_child_runs(s, s->tree.nodes[r], &d);
     rdt.push_back(d);
     s->roots_h.push_back(rt);
     s->root_nmax = std::max(s->root_nmax, rt.n);
@@ -1221,9 +1210,7 @@ rs_status factor_impl(rs_solver* s) {
         rscratch += (size_t)(d.n + 1) * (d.n + 1) * 2;
       }
     if (rscratch) CU(F.scratch.ensure(rscratch));
-    CU(s->blk.ensure(rblk.size()));
     CU(s->dc_tasks.ensure(rdt.size()));
-    CU(stage_copy(s, s->blk.p, rblk.data(), rblk.size() * sizeof(BlkRef)));
     CU(stage_copy(s, s->dc_tasks.p, rdt.data(), rdt.size() * sizeof(DecoupleTask)));
     DecoupleParams dp{};
     dp.geo = geo_of(s);
@@ -1231,7 +1218,6 @@ rs_status factor_impl(rs_solver* s) {
     dp.sd = s->sd;
     dp.tasks = s->dc_tasks.p;
     dp.dofs = s->dofs.p;
-    dp.blk = s->blk.p;
     dp.ranks = s->ranks.p;
     dp.perm = s->perm.p;
     dp.fac = F.fac.p;
