@@ -29,7 +29,7 @@ __host__ __device__ size_t dec_smem_bytes(int n, bool tile_in_smem) {
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   size_t b = 0;
   if (tile_in_smem) {
-    b += al(sizeof(Real) * (size_t)n * n);        // M
+    b += al(sizeof(Real) * (size_t)n * (n | 1));  // M (leading dimension n | 1)
     b += al(sizeof(Real) * (size_t)(n / 2 + 1) * (n - n / 2 + 1));  // T (k*r <= n^2/4)
   }
   b += dofs_bytes<Real>(n);
@@ -55,11 +55,11 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   unsigned char* sp = smem;
   Real *M, *T;
   if (t.scratch_off < 0) {
-    M = carve<Real>(sp, n * n);
+    M = carve<Real>(sp, n * (n | 1));
     T = carve<Real>(sp, (n / 2 + 1) * (n - n / 2 + 1));
   } else {
     M = reinterpret_cast<Real*>(p.scratch) + t.scratch_off;
-    T = M + (size_t)n * n;
+    T = M + (size_t)n * (n | 1);
   }
   DofSoA<Real> act = carve_dofs<Real>(sp, n);
   int* bchild = carve<int>(sp, n);
@@ -93,12 +93,12 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
       } else {
         val = kernel_dofs<Real>(p.pde, act, ia, act, ib);
       }
-      M[a + (size_t)n * b] = val;
+      M[a + (size_t)(n | 1) * b] = val;
     }
   __syncthreads();
   Real* E_out = reinterpret_cast<Real*>(p.epool) + t.e_off;
   if (k == 0) {
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) E_out[e] = M[e];
+    for (TileWalk w(n); w.j < n; w.next()) E_out[w.e()] = M[w.i + (size_t)(n | 1) * w.j];
     return;
   }
   Real* fac = reinterpret_cast<Real*>(p.fac) + t.fac_off;
@@ -110,7 +110,9 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     T[i + (size_t)r * l] = fac[fac_T(k, r) + e];
   }
   __syncthreads();
-  const size_t ld = n;
+  // an odd leading dimension: walks along a row (threads across columns)
+  // then hit distinct banks
+  const size_t ld = n | 1;
   Real* Mss = M;
   Real* Msr = M + ld * k;
   Real* Mrs = M + k;
