@@ -506,10 +506,14 @@ Factor<float>& factor_of<float>(rs_solver* s) { return s->F32; }
 // up to 64 DOFs, larger boxes whose tiles fit in shared memory, and boxes
 // that need global-memory tiles.  Few launches keep every box of a level in
 // flight at once; the shared-memory request of each launch is its largest box.
+// merge: the first two classes go in one launch (the larger class's
+// configuration serves both).  For a level of fewer boxes than SMs, whose
+// launches each last about one box's latency and run one after the other,
+// that saves a whole launch.
 template <class Task, class Fits, class Launch>
 void launch_binned(const std::vector<Task>& tasks, const Task* dev_tasks, Fits&& fits,
-                   Launch&& fn) {
-  auto cls = [&](int n) { return n <= 64 ? 0 : (fits(n) ? 1 : 2); };
+                   Launch&& fn, bool merge = false) {
+  auto cls = [&](int n) { return !fits(n) ? 2 : (n <= 64 && !merge ? 0 : 1); };
   size_t i = 0;
   while (i < tasks.size()) {
     const int c = cls(tasks[i].n);
@@ -900,6 +904,7 @@ rs_status factor_impl(rs_solver* s) {
     s->timed_levels.push_back(lv);
     auto id_fits = [&](int n) { return id_kernel_smem(n, f32, true) <= kSmemMax; };
     auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
+    const bool small_level = (int)idt_s.size() < s->num_sms;
     auto id_launch = [&](const IdTask* dt, int cnt, int nmax) {
       IdParams q = ip;
       q.tasks = dt;
@@ -910,14 +915,14 @@ rs_status factor_impl(rs_solver* s) {
       // the three ranges: up to 128 columns, wide, wider
       const std::vector<IdTask> lo(idt_s.begin(), idt_s.begin() + w0);
       const std::vector<IdTask> hi(idt_s.begin() + w1, idt_s.end());
-      launch_binned(lo, s->id_tasks.p, id_fits, id_launch);
+      launch_binned(lo, s->id_tasks.p, id_fits, id_launch, small_level);
       IdParams q = ip;
       q.tasks = s->id_tasks.p + w0;
       s->launches += launch_id_wide(q, (int)(w1 - w0), idt_s[w1 - 1].n, s->wide_items.p,
                                     (int)witems.size(), s->wide_part.p, s->stream);
-      launch_binned(hi, s->id_tasks.p + w1, id_fits, id_launch);
+      launch_binned(hi, s->id_tasks.p + w1, id_fits, id_launch, small_level);
     } else {
-      launch_binned(idt_s, s->id_tasks.p, id_fits, id_launch);
+      launch_binned(idt_s, s->id_tasks.p, id_fits, id_launch, small_level);
     }
     CU(cudaGetLastError());
     CU(cudaEventRecord(s->lv_ev[3 * lv + 1], s->stream));
@@ -961,7 +966,7 @@ rs_status factor_impl(rs_solver* s) {
       launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream,
                       s->elim_threads);
       ++s->launches;
-    });
+    }, (int)dct_s.size() < s->num_sms);
     CU(cudaGetLastError());
     CU(cudaEventRecord(s->lv_ev[3 * lv + 2], s->stream));
     const double h1 = now_ms();
