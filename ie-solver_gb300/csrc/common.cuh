@@ -29,6 +29,39 @@ inline void set_smem_once() {
 }
 constexpr int kWarps = kThreads / 32;
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may be
+// scheduled while the previous kernel on its stream still runs, once every
+// CTA of that kernel has called pdl_launch_dependents (or exited); it does
+// its prologue (reads of data written before that kernel) and calls
+// pdl_wait before its first read of the previous kernel's output, which
+// returns once that kernel has completed and its writes are visible.  In a
+// kernel launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launch with programmatic stream serialisation; a plain launch if the
+// attribute is refused.
+template <class... Params, class... Args>
+inline void launch_pdl(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kernel, args...) != cudaSuccess) {
+    (void)cudaGetLastError();
+    kernel<<<grid, block, smem, st>>>(args...);
+  }
+}
+
 // The elements e = threadIdx.x, threadIdx.x + blockDim.x, ... of a
 // column-major rows x cols tile as (i, j) = (e % rows, e / rows), stepped
 // without an integer division per element (a division by a runtime value

@@ -372,6 +372,9 @@ __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  // (programmatic dependent launch: the offsets' powers below overlap the
+  // previous level's kernel; its multipoles are read after pdl_wait)
+  pdl_launch_dependents();
   const int P = a.boxes[blockIdx.x];
   if (a.pcount[P] > 0) return;  // leaf: filled by P2M
   const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
@@ -399,6 +402,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
     }
   }
   __syncthreads();
+  pdl_wait();
   for (int e = threadIdx.x; e < 4 * p * nrhs; e += blockDim.x) {
     const int k = e % p, q = (e / p) % nrhs, c = e / (p * nrhs);
     const int C = a.children[4 * P + c];
@@ -562,6 +566,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  pdl_launch_dependents();  // (as in m2m_kernel)
   const int C = a.boxes[blockIdx.x];
   const int P = a.parent[C];
   if (P < 0) return;
@@ -581,6 +586,7 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
     }
   }
   __syncthreads();
+  pdl_wait();
   for (int e = threadIdx.x; e < p * nrhs; e += blockDim.x) {
     const int l = e % p, q = e / p;
     bv[e] = cmul(ld_c(a.local, l + (size_t)p * (q + nrhs * (size_t)P)), el[l]);
@@ -998,8 +1004,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
       const int cnt = f.level_off[lv + 1] - f.level_off[lv];
       if (!cnt) continue;
       a.boxes = f.lvl_boxes.p + f.level_off[lv];
-      m2m_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (8 * (size_t)p + 4 * (size_t)p * nch + 4),
-                      st>>>(a);
+      launch_pdl(m2m_kernel<R>, dim3(cnt), dim3(kFmmThreads),
+                 sizeof(Cx<R>) * (8 * (size_t)p + 4 * (size_t)p * nch + 4), st, a);
     }
     // interactions and downward pass
     if ((e = cudaMemsetAsync(f.local.p, 0, 2 * sizeof(R) * (size_t)p * nch * nb, st)) !=
@@ -1016,7 +1022,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
       const int cnt = f.level_off[lv + 1] - f.level_off[lv];
       if (!cnt) continue;
       a.boxes = f.lvl_boxes.p + f.level_off[lv];
-      l2l_kernel<R><<<cnt, kFmmThreads, sizeof(Cx<R>) * (2 * (size_t)p + (size_t)p * nch), st>>>(a);
+      launch_pdl(l2l_kernel<R>, dim3(cnt), dim3(kFmmThreads),
+                 sizeof(Cx<R>) * (2 * (size_t)p + (size_t)p * nch), st, a);
     }
     a.boxes = f.leaves.p;
     const size_t esm = sizeof(Pos<R>) * kStage + sizeof(Cx<R>) * kStage * kMaxRhs +

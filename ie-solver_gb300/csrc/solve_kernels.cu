@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   // record and pivots, all written before the solve) while this one works;
   // the reads of x below wait for the previous kernel to complete and its
   // writes to be visible.  Without the launch attribute both are no-ops.
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  pdl_launch_dependents();
   const SweepTask t = p.tasks[blockIdx.x];
   const int k = t.k, r = t.r;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   const int* sk = p.dofs + t.skel_off;
   const int* rd = p.dofs + t.red_off;
   for (int j = threadIdx.x; j < r; j += blockDim.x) piv[j] = p.piv[t.piv_off + j];
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  pdl_wait();
   for (int c0 = 0; c0 < p.nrhs; c0 += kRhsBlock) {
     const int cb = p.nrhs - c0 < kRhsBlock ? p.nrhs - c0 : kRhsBlock;
     if (k > 0)
@@ -183,27 +183,6 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   }
 }
 
-// A sweep launch with programmatic stream serialisation (its prologue may
-// overlap the previous kernel; see sweep_kernel), or a plain launch if the
-// attribute is refused.
-template <class Real>
-static void launch_sweep_pdl(const SweepParams& q, int num_tasks, size_t smem, cudaStream_t st) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)num_tasks);
-  cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, sweep_kernel<Real>, q) != cudaSuccess) {
-    (void)cudaGetLastError();
-    sweep_kernel<Real><<<num_tasks, kThreads, smem, st>>>(q);
-  }
-}
-
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st) {
   if (num_tasks <= 0) return;
   size_t es = fp32 ? sizeof(float) : sizeof(double);
@@ -217,10 +196,10 @@ void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cuda
   if (q.stage_fac) smem += fb;
   if (fp32) {
     set_smem_once<sweep_kernel<float>>();
-    launch_sweep_pdl<float>(q, num_tasks, smem, st);
+    launch_pdl(sweep_kernel<float>, dim3(num_tasks), dim3(kThreads), smem, st, q);
   } else {
     set_smem_once<sweep_kernel<double>>();
-    launch_sweep_pdl<double>(q, num_tasks, smem, st);
+    launch_pdl(sweep_kernel<double>, dim3(num_tasks), dim3(kThreads), smem, st, q);
   }
 }
 
