@@ -325,6 +325,7 @@ __device__ __forceinline__ bool is_g(const FmmArgs<R>& a, int q) {
 template <class R>
 __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  pdl_launch_dependents();  // (the charges are read after pdl_wait below)
   const int b = a.boxes[blockIdx.x];
   const int s0 = a.pstart[b], cnt = a.pcount[b], p = a.p;
   Cx<R>* pw = reinterpret_cast<Cx<R>*>(smem);  // kStage x p
@@ -345,6 +346,7 @@ __global__ void __launch_bounds__(kFmmThreads) p2m_kernel(FmmArgs<R> a) {
       }
     }
     __syncthreads();
+    pdl_wait();
 #pragma unroll
     for (int t = 0; t < kPer; ++t) {
       const int e = threadIdx.x + t * blockDim.x;
@@ -633,6 +635,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     FmmArgs<R> a, Geo<double> g, const double* mu, double* y, double ya, double yb,
     const double* r1) {
   __shared__ double part[kEvalWarps - 1][32][kMaxRhs];
+  pdl_launch_dependents();  // (expansions are read after pdl_wait below)
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int B = a.boxes[blockIdx.x];
   const int s0 = a.pstart[B], cnt = a.pcount[B];
@@ -651,6 +654,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
       const int pt = a.slot_pt[ts];
       tnu = {to_r<R>(g.nx[pt]), to_r<R>(g.ny[pt])};
     }
+    pdl_wait();
     // L2P (right-hand sides q = wp, wp + kEvalWarps, ...; the loop is kept
     // rolled and its result added through an unrolled select, which keeps
     // the kernel's code small)
@@ -998,7 +1002,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
     // upward pass
     a.boxes = f.leaves.p;
     if (nleaves)
-      p2m_kernel<R><<<nleaves, kFmmThreads, sizeof(Cx<R>) * kStage * (size_t)p, st>>>(a);
+      launch_pdl(p2m_kernel<R>, dim3(nleaves), dim3(kFmmThreads),
+                 sizeof(Cx<R>) * kStage * (size_t)p, st, a);
     // levels 0 and 1 have no V, W or X partners: their multipoles are unused
     for (int lv = f.nlevels - 2; lv >= 2; --lv) {
       const int cnt = f.level_off[lv + 1] - f.level_off[lv];
@@ -1031,8 +1036,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
     if (nleaves && mode == 2)
       stokes_eval_kernel<R><<<nleaves, kEvalThreads, esm, st>>>(a, geo, muq, yq, ya, yb, f.r1.p);
     else if (nleaves)
-      eval_warp_kernel<R><<<nleaves, 32 * kEvalWarps, 0, st>>>(a, geo, muq, yq, ya, yb,
-                                                              f.r1.p);
+      launch_pdl(eval_warp_kernel<R>, dim3(nleaves), dim3(32 * kEvalWarps), 0, st, a, geo,
+                 muq, yq, ya, yb, (const double*)f.r1.p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
