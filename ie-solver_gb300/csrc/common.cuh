@@ -170,13 +170,59 @@ template <class Real>
 __device__ __forceinline__ void load_dof(const Geo<double>& g, int sd, int dof, double ox,
                                          double oy, DofSoA<Real>& d, int slot) {
   int p = sd == 1 ? dof : (dof >> 1);
-  d.x[slot] = (Real)(g.x[p] - ox);
-  d.y[slot] = (Real)(g.y[p] - oy);
-  d.nx[slot] = (Real)g.nx[p];
-  d.ny[slot] = (Real)g.ny[p];
-  d.w[slot] = (Real)g.w[p];
-  d.kap[slot] = (Real)g.kap[p];
+  // all six loads before any store: the stores go through generic pointers
+  // that the compiler cannot tell apart from the geometry, so interleaved
+  // they would make six dependent global round trips
+  const double gx = g.x[p], gy = g.y[p], gnx = g.nx[p], gny = g.ny[p], gw = g.w[p];
+  const double gk = g.kap[p];
+  d.x[slot] = (Real)(gx - ox);
+  d.y[slot] = (Real)(gy - oy);
+  d.nx[slot] = (Real)gnx;
+  d.ny[slot] = (Real)gny;
+  d.w[slot] = (Real)gw;
+  d.kap[slot] = (Real)gk;
   d.comp[slot] = dof - p * sd;
+}
+
+// y[i ys] -= a x[i xs] for i < cnt (x and y disjoint), four loads of each
+// ahead of their stores: in a plain loop every load waits behind the
+// previous store, which the compiler cannot prove distinct, so the loop is a
+// chain of shared-memory round trips.  Each element is the same fused
+// multiply-add as in the plain loop.
+template <class T>
+__device__ __forceinline__ void axpy_sub(T* y, int ys, const T* x, int xs, T a, int cnt) {
+  int i = 0;
+  for (; i + 4 <= cnt; i += 4) {
+    const T y0 = y[i * ys], y1 = y[(i + 1) * ys], y2 = y[(i + 2) * ys], y3 = y[(i + 3) * ys];
+    const T x0 = x[i * xs], x1 = x[(i + 1) * xs], x2 = x[(i + 2) * xs], x3 = x[(i + 3) * xs];
+    y[i * ys] = y0 - a * x0;
+    y[(i + 1) * ys] = y1 - a * x1;
+    y[(i + 2) * ys] = y2 - a * x2;
+    y[(i + 3) * ys] = y3 - a * x3;
+  }
+  for (; i < cnt; ++i) y[i * ys] -= a * x[i * xs];
+}
+
+// dst[e] = src[e] for e < n, over `nthreads` threads (this one is `tid`),
+// eight loads in flight per thread before their stores: a plain copy loop
+// through generic pointers keeps each load behind the previous store (the
+// compiler cannot rule out that they alias), one global round trip per
+// element.
+template <class T>
+__device__ __forceinline__ void batched_copy(T* dst, const T* src, int n, int tid, int nthreads) {
+  for (int e0 = tid; e0 < n; e0 += 8 * nthreads) {
+    T v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * nthreads;
+      if (e < n) v[q] = src[e];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int e = e0 + q * nthreads;
+      if (e < n) dst[e] = v[q];
+    }
+  }
 }
 
 // Reciprocal: correctly rounded single-precision reciprocal; for double, a

@@ -44,12 +44,80 @@ size_t decouple_kernel_smem(int n, bool fp32, bool tile_in_smem) {
   return fp32 ? dec_smem_bytes<float>(n, tile_in_smem) : dec_smem_bytes<double>(n, tile_in_smem);
 }
 
+// C = C0 - A B (kSub) or C = A B for an m x n result, over one CTA on 2 x 2
+// register tiles {i, i + hm} x {j, j + hn} (hm = ceil(m / 2), hn =
+// ceil(n / 2)): a step of the sums loads two elements of A and two of B for
+// four independent multiply-adds, and the threads of a warp read
+// consecutive rows of A.  A(i, l) is at A[i + al l], B(l, j) at
+// B[bl l + bj j]; every element's sum runs over l in increasing order, as a
+// loop of one element per thread would run it.  C0 may alias C (a thread
+// reads its own tile before writing it).  The result also goes to C2 when
+// it is given.
+template <bool kSub, class Real>
+__device__ __forceinline__ void cta_gemm(int m, int n, int kk, const Real* A, int al,
+                                         const Real* B, int bl, int bj, const Real* C0, int ld0,
+                                         Real* C, int ldc, Real* C2 = nullptr, int ldc2 = 0) {
+  const int hm = (m + 1) >> 1, hn = (n + 1) >> 1;
+  if (hm == 0 || hn == 0) return;
+  for (TileWalk w(hm); w.j < hn; w.next()) {
+    const int i0 = w.i, j0 = w.j;
+    const bool ri = i0 + hm < m, rj = j0 + hn < n;
+    const int i1 = ri ? i0 + hm : i0, j1 = rj ? j0 + hn : j0;
+    Real c00 = 0, c10 = 0, c01 = 0, c11 = 0;
+    if constexpr (kSub) {
+      c00 = C0[i0 + ld0 * j0];
+      c10 = C0[i1 + ld0 * j0];
+      c01 = C0[i0 + ld0 * j1];
+      c11 = C0[i1 + ld0 * j1];
+    }
+    const Real* a0 = A + i0;
+    const Real* a1 = A + i1;
+    const Real* b0 = B + bj * j0;
+    const Real* b1 = B + bj * j1;
+    for (int l = 0; l < kk; ++l) {
+      const Real x0 = a0[al * l], x1 = a1[al * l];
+      const Real y0 = b0[bl * l], y1 = b1[bl * l];
+      if constexpr (kSub) {
+        c00 -= x0 * y0;
+        c10 -= x1 * y0;
+        c01 -= x0 * y1;
+        c11 -= x1 * y1;
+      } else {
+        c00 += x0 * y0;
+        c10 += x1 * y0;
+        c01 += x0 * y1;
+        c11 += x1 * y1;
+      }
+    }
+    auto put = [&](Real* D, int ld) {
+      D[i0 + ld * j0] = c00;
+      if (ri) D[i1 + ld * j0] = c10;
+      if (rj) D[i0 + ld * j1] = c01;
+      if (ri && rj) D[i1 + ld * j1] = c11;
+    };
+    put(C, ldc);
+    if (C2 != nullptr) put(C2, ldc2);
+  }
+}
+
+
 template <class Real>
 __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   const DecoupleTask t = p.tasks[blockIdx.x];
   const int n = t.n;
   const int k = t.slot >= 0 ? p.ranks[t.slot] : 0;
   const int r = n - k;
+  long long clk[5];
+  clk[0] = clock64();
+  auto stamp = [&](int q) { clk[q] = clock64(); };
+  auto report = [&]() {
+    if (p.phase_clk != nullptr && threadIdx.x == 0) {
+      long long* o = p.phase_clk + 6 * (size_t)blockIdx.x;
+      for (int q = 0; q < 4; ++q) o[q] = clk[q + 1] - clk[q];
+      o[4] = n;
+      o[5] = k;
+    }
+  };
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* sp = smem;
@@ -72,42 +140,76 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
 
   const Real* E_in = reinterpret_cast<const Real*>(p.epool);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    load_dof<Real>(p.geo, p.sd, p.dofs[t.act_off + j], 0.0, 0.0, act, j);
+    const int dof = p.dofs[t.act_off + j];
+    const int oj = k > 0 ? p.perm[t.perm_off + j] : j;
+    load_dof<Real>(p.geo, p.sd, dof, 0.0, 0.0, act, j);
     int c = 0;
     while (c < 3 && j >= t.cstart[c + 1]) ++c;  // the run of active position j
     bchild[j] = c;
     bidx[j] = j - t.cstart[c];
     bld[j] = t.cld[c];
     bbase[j] = t.ce[c];
-    order[j] = k > 0 ? p.perm[t.perm_off + j] : j;
+    order[j] = oj;
   }
   __syncthreads();
   // Assemble Ktilde in skeleton-first order.
-  if (n > 0)
-    for (TileWalk w(n); w.j < n; w.next()) {
-      const int a = w.i, b = w.j;
-      const int ia = order[a], ib = order[b];
-      Real val;
-      if (bchild[ia] == bchild[ib] && bbase[ia] >= 0) {
-        val = E_in[bbase[ia] + bidx[ia] + (int64_t)bld[ia] * bidx[ib]];
-      } else {
-        val = kernel_dofs<Real>(p.pde, act, ia, act, ib);
+  // First the children's E-block entries, four loads in flight per thread
+  // before their stores, then the kernel entries.
+  if (n > 0) {
+    for (TileWalk w(n); w.j < n;) {
+      int dst[4];
+      Real val[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        dst[q] = -1;
+        if (w.j < n) {
+          const int ia = order[w.i], ib = order[w.j];
+          if (bchild[ia] == bchild[ib] && bbase[ia] >= 0) {
+            dst[q] = w.i + (n | 1) * w.j;
+            val[q] = E_in[bbase[ia] + bidx[ia] + (int64_t)bld[ia] * bidx[ib]];
+          }
+          w.next();
+        }
       }
-      M[a + (size_t)(n | 1) * b] = val;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (dst[q] >= 0) M[dst[q]] = val[q];
     }
+    for (TileWalk w(n); w.j < n; w.next()) {
+      const int ia = order[w.i], ib = order[w.j];
+      if (!(bchild[ia] == bchild[ib] && bbase[ia] >= 0))
+        M[w.i + (size_t)(n | 1) * w.j] = kernel_dofs<Real>(p.pde, act, ia, act, ib);
+    }
+  }
   __syncthreads();
+  stamp(1);
   Real* E_out = reinterpret_cast<Real*>(p.epool) + t.e_off;
   if (k == 0) {
     for (TileWalk w(n); w.j < n; w.next()) E_out[w.e()] = M[w.i + (size_t)(n | 1) * w.j];
+    stamp(2);
+    stamp(3);
+    stamp(4);
+    report();
     return;
   }
   Real* fac = reinterpret_cast<Real*>(p.fac) + t.fac_off;
   // T (k x r, column major in the record) is held transposed, Tt(i, l) =
   // T(l, i) at Tt[i + r l]: the products below walk i across the threads,
   // which then read consecutive words
-  for (int e = threadIdx.x; e < k * r; e += blockDim.x) {
-    const int l = e % k, i = e / k;
-    T[i + (size_t)r * l] = fac[fac_T(k, r) + e];
+  {
+    const Real* Tg = fac + fac_T(k, r);
+    const int kr = k * r, nt = blockDim.x;
+    for (int e0 = threadIdx.x; e0 < kr; e0 += 4 * nt) {  // four loads in flight
+      Real v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (e0 + q * nt < kr) v[q] = Tg[e0 + q * nt];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int e = e0 + q * nt;
+        if (e < kr) T[e / k + (size_t)r * (e % k)] = v[q];
+      }
+    }
   }
   __syncthreads();
   // an odd leading dimension: walks along a row (threads across columns)
@@ -118,35 +220,42 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
   Real* Mrs = M + k;
   Real* Mrr = M + k + ld * k;
   // 1) K_r_sn = Mrs - T^T Mss  (r x k), in place
-  if (r > 0)
-    for (TileWalk w(r); w.j < k; w.next()) {
-      const int i = w.i, j = w.j;
-      Real acc = Mrs[i + ld * j];
-      for (int l = 0; l < k; ++l) acc -= T[i + (size_t)r * l] * Mss[l + ld * j];
-      Mrs[i + ld * j] = acc;
-    }
+  cta_gemm<true>(r, k, k, T, r, Mss, 1, (int)ld, Mrs, (int)ld, Mrs, (int)ld);
   __syncthreads();
-  // 2) X_rr = Mrr - T^T Msr - K_r_sn T  (r x r), in place
-  if (r > 0)
-    for (TileWalk w(r); w.j < r; w.next()) {
-      const int i = w.i, j = w.j;
-      Real a1 = 0, a2 = 0;
+  // 2) X_rr = Mrr - T^T Msr - K_r_sn T  (r x r), in place; the two sums are
+  //    kept apart and subtracted in that order
+  if (r > 0) {
+    const int h = (r + 1) >> 1;
+    for (TileWalk w(h); w.j < h; w.next()) {
+      const int i0 = w.i, j0 = w.j;
+      const bool ri = i0 + h < r, rj = j0 + h < r;
+      const int i1 = ri ? i0 + h : i0, j1 = rj ? j0 + h : j0;
+      Real p00 = 0, p10 = 0, p01 = 0, p11 = 0, q00 = 0, q10 = 0, q01 = 0, q11 = 0;
       for (int l = 0; l < k; ++l) {
-        a1 += T[i + (size_t)r * l] * Msr[l + ld * j];
-        a2 += Mrs[i + ld * l] * T[j + (size_t)r * l];
+        const Real t0 = T[i0 + (size_t)r * l], t1 = T[i1 + (size_t)r * l];
+        const Real s0 = Msr[l + ld * j0], s1 = Msr[l + ld * j1];
+        const Real u0 = Mrs[i0 + ld * l], u1 = Mrs[i1 + ld * l];
+        const Real v0 = T[j0 + (size_t)r * l], v1 = T[j1 + (size_t)r * l];
+        p00 += t0 * s0;
+        p10 += t1 * s0;
+        p01 += t0 * s1;
+        p11 += t1 * s1;
+        q00 += u0 * v0;
+        q10 += u1 * v0;
+        q01 += u0 * v1;
+        q11 += u1 * v1;
       }
-      Mrr[i + ld * j] = (Mrr[i + ld * j] - a1) - a2;
+      Mrr[i0 + ld * j0] = (Mrr[i0 + ld * j0] - p00) - q00;
+      if (ri) Mrr[i1 + ld * j0] = (Mrr[i1 + ld * j0] - p10) - q10;
+      if (rj) Mrr[i0 + ld * j1] = (Mrr[i0 + ld * j1] - p01) - q01;
+      if (ri && rj) Mrr[i1 + ld * j1] = (Mrr[i1 + ld * j1] - p11) - q11;
     }
+  }
   __syncthreads();
   // 3) K_sn_r = Msr - Mss T  (k x r), in place
-  if (k > 0)
-    for (TileWalk w(k); w.j < r; w.next()) {
-      const int i = w.i, j = w.j;
-      Real acc = Msr[i + ld * j];
-      for (int l = 0; l < k; ++l) acc -= Mss[i + ld * l] * T[j + (size_t)r * l];
-      Msr[i + ld * j] = acc;
-    }
+  cta_gemm<true>(k, r, k, Mss, (int)ld, T, r, 1, Msr, (int)ld, Msr, (int)ld);
   __syncthreads();
+  stamp(2);
   if (threadIdx.x == 0) scal[0] = 0.0;
   if constexpr (sizeof(Real) == 4) {
     // FP32 factorization: X_rr is inverted explicitly (Gauss-Jordan with
@@ -172,26 +281,29 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
       row_at[i] = i;
     }
     __syncthreads();
+    const int hr = (r + 1) >> 1;
     for (int j = 0; j < r; ++j) {
       const int buf = j & 1;
-      // every warp finds the pivot row itself (no barrier for a broadcast)
-      float best = -1.f;
-      int bi = r, bp = r;
+      const float* cb = colbuf[buf];
+      // every warp finds the pivot row itself (no barrier for a broadcast):
+      // the largest |X(i, j)| over rows not yet pivots, ties to the smallest
+      // position.  Non-negative floats order as their bit patterns, so two
+      // warp reductions give it: the largest value, then the smallest
+      // position holding it.  A NaN's pattern lies above infinity's.
+      unsigned best = 0u, bpos = 0xffffffffu;
       for (int i = lane; i < r; i += 32) {
-        const int ps = pos[i];
-        if (ps < j) continue;
-        const float v = fabsf(colbuf[buf][i]);
-        if (v > best || (v == best && ps < bp)) { best = v; bi = i; bp = ps; }
+        const unsigned ps = (unsigned)pos[i];
+        if (ps < (unsigned)j) continue;
+        const unsigned v = __float_as_uint(fabsf(cb[i]));
+        if (v > best || (v == best && ps < bpos)) {
+          best = v;
+          bpos = ps;
+        }
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        const int op = __shfl_xor_sync(0xffffffffu, bp, o);
-        if (ov > best || (ov == best && op < bp)) { best = ov; bi = oi; bp = op; }
-      }
-      const bool ok = best > 0.f && isfinite(best) && bi < r;
-      const int pr = ok ? bi : row_at[j];  // a singular block: any row, flagged
+      const unsigned wbest = __reduce_max_sync(0xffffffffu, best);
+      const unsigned wpos = __reduce_min_sync(0xffffffffu, best == wbest ? bpos : 0xffffffffu);
+      const bool ok = wbest != 0u && wbest < 0x7f800000u;  // non-zero and finite
+      const int pr = ok ? row_at[wpos] : row_at[j];       // a singular block: any row, flagged
       if (threadIdx.x == 0) {
         piv[j] = pr;
         if (!ok) scal[0] = 1.0;
@@ -210,16 +322,40 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
         row_at[j] = pr;
         pos[pr] = j;
       }
+      // the update on 2 x 2 tiles {i, i + hr} x {c, c + hr}: all four
+      // elements are loaded before any is stored
+      const float* rb = rowbuf[buf];
+      float* cn = colbuf[buf ^ 1];
       if (r > 0)
-        for (TileWalk w(r); w.j < r; w.next()) {
-          const int i = w.i, c = w.j;
-          const Real m = c == j ? (Real)0 : Mrr[i + ld * c];
-          const Real v = i == pr ? rowbuf[buf][c] : m - colbuf[buf][i] * rowbuf[buf][c];
-          Mrr[i + ld * c] = v;
-          if (c == j + 1) colbuf[buf ^ 1][i] = v;
+        for (TileWalk w(hr); w.j < hr; w.next()) {
+          const int i0 = w.i, c0 = w.j;
+          const bool ri = i0 + hr < r, rc = c0 + hr < r;
+          const int i1 = ri ? i0 + hr : i0, c1 = rc ? c0 + hr : c0;
+          const Real a0 = cb[i0], a1 = cb[i1], b0 = rb[c0], b1 = rb[c1];
+          Real m00 = Mrr[i0 + ld * c0], m10 = Mrr[i1 + ld * c0];
+          Real m01 = Mrr[i0 + ld * c1], m11 = Mrr[i1 + ld * c1];
+          if (c0 == j) m00 = m10 = (Real)0;
+          if (c1 == j) m01 = m11 = (Real)0;
+          m00 = i0 == pr ? b0 : m00 - a0 * b0;
+          m10 = i1 == pr ? b0 : m10 - a1 * b0;
+          m01 = i0 == pr ? b1 : m01 - a0 * b1;
+          m11 = i1 == pr ? b1 : m11 - a1 * b1;
+          Mrr[i0 + ld * c0] = m00;
+          if (ri) Mrr[i1 + ld * c0] = m10;
+          if (rc) Mrr[i0 + ld * c1] = m01;
+          if (ri && rc) Mrr[i1 + ld * c1] = m11;
+          if (c0 == j + 1) {
+            cn[i0] = m00;
+            if (ri) cn[i1] = m10;
+          }
+          if (rc && c1 == j + 1) {
+            cn[i0] = m01;
+            if (ri) cn[i1] = m11;
+          }
         }
       __syncthreads();
     }
+    stamp(3);
     int* pinv = bchild;
     for (int j = threadIdx.x; j < r; j += blockDim.x) pinv[j] = j;  // a singular block repeats rows
     __syncthreads();
@@ -250,35 +386,15 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     // factorization loses accuracy.
     // (U_f also goes to T's bytes, free since step 3, for E below)
     Real* Us = T;
-    if (r > 0)
-      for (TileWalk w(r); w.j < k; w.next()) {
-        const int i = w.i, j = w.j;
-        const int e = w.e();
-        Real acc = 0;
-        for (int l = 0; l < r; ++l) acc += Mrr[i + ld * l] * Mrs[l + ld * j];
-        Uo[e] = acc;
-        Us[e] = acc;
-      }
-    if (k > 0)
-      for (TileWalk w(k); w.j < r; w.next()) {
-        const int i = w.i, j = w.j;
-        const int e = w.e();
-        Real acc = 0;
-        for (int l = 0; l < r; ++l) acc += Msr[i + ld * l] * Mrr[l + ld * j];
-        Lo[e] = acc;
-      }
+    cta_gemm<false>(r, k, r, Mrr, (int)ld, Mrs, 1, (int)ld, (const Real*)nullptr, 0, Uo, r, Us, r);
+    cta_gemm<false>(k, r, r, Msr, (int)ld, Mrr, 1, (int)ld, (const Real*)nullptr, 0, Lo, k);
     __syncthreads();  // U_f is read back below (same CTA)
     // E = Mss - K_sn_r U_f  (k x k)
-    if (k > 0)
-      for (TileWalk w(k); w.j < k; w.next()) {
-        const int i = w.i, j = w.j;
-        const int e = w.e();
-        Real acc = Mss[i + ld * j];
-        for (int l = 0; l < r; ++l) acc -= Msr[i + ld * l] * Us[l + (size_t)r * j];
-        E_out[e] = acc;
-      }
+    cta_gemm<true>(k, k, r, Msr, (int)ld, Us, 1, r, Mss, (int)ld, E_out, k);
     for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = j;
     if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
+    stamp(4);
+    report();
     return;
   }
   // 4) LU of X_rr with partial pivoting (dgetrf), in place.
@@ -325,6 +441,7 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
       }
     __syncthreads();
   }
+  stamp(3);
   // 5) U_f = X^{-1} K_r_sn, in place over Mrs (one warp per column).
   const int nwarps = blockDim.x >> 5;
   for (int c = warp; c < k; c += nwarps) {
@@ -407,21 +524,33 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     }
   for (int j = threadIdx.x; j < r; j += blockDim.x) p.piv[t.piv_off + j] = piv[j];
   if (threadIdx.x == 0 && scal[0] != 0.0) atomicExch(p.status, 1);
+  stamp(4);
+  report();
 }
 
-// threads: 256 (default) or 128 per box; every loop of the kernel strides
-// by blockDim.x (or its warp count).
+// threads: 256 or 128 per box, or 0: 128 when the launch holds more boxes
+// than one wave of 256-thread CTAs (every resident slot of every SM), so the
+// boxes run in one wave at twice the CTAs per SM, else 256.  Every loop of
+// the kernel strides by blockDim.x (or its warp count).
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
-                     cudaStream_t st, int threads) {
+                     cudaStream_t st, int threads, int num_sms) {
   if (num_tasks <= 0) return;
-  const int nt = threads == 128 ? 128 : kThreads;
-  if (fp32) {
+  if (fp32)
     set_smem_once<decouple_kernel<float>>();
-    decouple_kernel<float><<<num_tasks, nt, smem, st>>>(p);
-  } else {
+  else
     set_smem_once<decouple_kernel<double>>();
-    decouple_kernel<double><<<num_tasks, nt, smem, st>>>(p);
+  int nt = threads == 128 ? 128 : kThreads;
+  if (threads == 0) {
+    int per_sm = 0;
+    const void* fn = fp32 ? (const void*)decouple_kernel<float> : (const void*)decouple_kernel<double>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem) != cudaSuccess)
+      per_sm = 0;
+    nt = per_sm > 0 && num_tasks > per_sm * num_sms ? 128 : kThreads;
   }
+  if (fp32)
+    decouple_kernel<float><<<num_tasks, nt, smem, st>>>(p);
+  else
+    decouple_kernel<double><<<num_tasks, nt, smem, st>>>(p);
 }
 
 }  // namespace rskel

@@ -629,15 +629,23 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
 // per product by the charges kernel) is read by a whole warp at one
 // address, so no shared-memory staging and no barrier sit in the pair loop.
 // A leaf of more than 32 points takes several passes.
+// kPart 0 does all of it.  kPart 1 does only the near field (P2P) and
+// stores its sums per (slot, right-hand side) in nearsum; kPart 2 does the
+// far field (L2P, M2P), adds nearsum and finishes: the near field can then
+// run beside the tree passes.
 constexpr int kEvalWarps = 4;
-template <class R>
+enum EvalPart : int { kEvalAll = 0, kEvalNear = 1, kEvalFar = 2 };
+template <class R, int kPart>
 __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     FmmArgs<R> a, Geo<double> g, const double* mu, double* y, double ya, double yb,
-    const double* r1) {
+    const double* r1, double* nearsum, int nbox) {
   __shared__ double part[kEvalWarps - 1][32][kMaxRhs];
   pdl_launch_dependents();  // (expansions are read after pdl_wait below)
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  const int B = a.boxes[blockIdx.x];
+  // one leaf per CTA, or (a grid smaller than the leaf count) leaves
+  // blockIdx.x, + gridDim.x, ...
+  for (int li = blockIdx.x; li < nbox; li += gridDim.x) {
+  const int B = a.boxes[li];
   const int s0 = a.pstart[B], cnt = a.pcount[B];
   const int p = a.p, nrhs = a.nrhs;
   const R isB = rcp(side_of(a, B));
@@ -655,6 +663,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
       tnu = {to_r<R>(g.nx[pt]), to_r<R>(g.ny[pt])};
     }
     pdl_wait();
+    if constexpr (kPart != kEvalNear) {
     // L2P (right-hand sides q = wp, wp + kEvalWarps, ...; the loop is kept
     // rolled and its result added through an unrolled select, which keeps
     // the kernel's code small)
@@ -700,6 +709,8 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         }
       }
     }
+    }  // far field
+    if constexpr (kPart != kEvalFar) {
     // P2P from the U list: this warp takes every kEvalWarps-th source
     // (offsets broadcast as above)
     using OT = typename OffT<R>::type;
@@ -738,13 +749,23 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         for (int q = 0; q < kMaxRhs; ++q) acc_norm(phi[q]);
       }
     }
+    }  // near field
     // partial sums of warps 1.. to warp 0, added in warp order
     __syncthreads();
     if (wp > 0)
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) part[wp - 1][lane][q] = (double)phi[q];
     __syncthreads();
-    if (wp == 0 && act) {
+    if (wp == 0 && act && kPart == kEvalNear) {
+#pragma unroll
+      for (int q = 0; q < kMaxRhs; ++q) {
+        if (q < nrhs) {
+          double tot = (double)phi[q];
+          for (int w = 1; w < kEvalWarps; ++w) tot += part[w - 1][lane][q];
+          nearsum[ts + (size_t)a.npts * q] = tot;
+        }
+      }
+    } else if (wp == 0 && act) {
       const int pt = a.slot_pt[ts];
       const double diag = (a.mode == 1 ? -0.5 : 0.5) +
                           0.5 * g.kap[pt] * g.w[pt] * (1.0 / (2.0 * CUDART_PI));
@@ -753,6 +774,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         if (q < nrhs) {
           double tot = (double)phi[q];
           for (int w = 1; w < kEvalWarps; ++w) tot += part[w - 1][lane][q];
+          if (kPart == kEvalFar) tot += nearsum[ts + (size_t)a.npts * q];
           const size_t o = pt + (size_t)a.npts * q;
           const double v = yb * (diag * mu[o] + tot + (a.mode == 1 ? r1[q] : 0.0));
           y[o] = ya == 0.0 ? v : ya * y[o] + v;
@@ -760,6 +782,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
       }
     }
   }
+  }  // leaves
 }
 
 // Stokes evaluation at a leaf's points (channels A, B, G of up to
@@ -923,6 +946,24 @@ __global__ void __launch_bounds__(kEvalThreads, 4) stokes_eval_kernel(FmmArgs<R>
   }
 }
 
+// Grid of the near-field kernel on the side stream: half the CTAs that fit
+// on the GPU at once (at most one per leaf), so that the tree passes'
+// launches find free slots beside it instead of waiting for its CTAs to
+// retire.
+template <class R>
+unsigned near_grid(unsigned nleaves) {
+  static unsigned cap = 0;
+  if (cap == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, eval_warp_kernel<R, kEvalNear>,
+                                                  32 * kEvalWarps, 0);
+    cap = (unsigned)std::max(1, sms * std::max(1, per / 2));
+  }
+  return std::min(nleaves, cap);
+}
+
 template <class R>
 cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* mu, int nrhs,
                     double* y, double ya, double yb, cudaStream_t st) {
@@ -942,6 +983,20 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
   if ((e = f.mpole.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
   if ((e = f.local.ensure(2 * (size_t)pmax * kMaxRhs * nb)) != cudaSuccess) return e;
   if ((e = f.r1.ensure(kMaxRhs)) != cudaSuccess) return e;
+  if (mode != 2) {
+    if ((e = f.nearsum.ensure((size_t)npts * kMaxRhs)) != cudaSuccess) return e;
+    if (f.nearq.st == nullptr) {
+      int lo = 0, hi = 0;
+      if ((e = cudaDeviceGetStreamPriorityRange(&lo, &hi)) != cudaSuccess) return e;
+      // (lo is the numerically greatest value: the lowest priority)
+      if ((e = cudaStreamCreateWithPriority(&f.nearq.st, cudaStreamNonBlocking, lo)) != cudaSuccess)
+        return e;
+      if ((e = cudaEventCreateWithFlags(&f.nearq.charges, cudaEventDisableTiming)) != cudaSuccess)
+        return e;
+      if ((e = cudaEventCreateWithFlags(&f.nearq.near, cudaEventDisableTiming)) != cudaSuccess)
+        return e;
+    }
+  }
   FmmArgs<R> a{};
   a.cx = f.cx.p;
   a.cy = f.cy.p;
@@ -999,6 +1054,17 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
                                                    nq, charge);
     }
     if (mode != 0) rank1_kernel<<<nq, 1024, 0, st>>>(geo, npts, muq, mode, f.r1.p);
+    // the near field on the side stream (Laplace, Neumann), once the charges
+    // kernel's source data are written
+    const bool split = mode != 2 && nleaves > 0 && f.nearq.st != nullptr;
+    if (split) {
+      a.boxes = f.leaves.p;  // the kernel's boxes are the leaves
+      if ((e = cudaEventRecord(f.nearq.charges, st)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(f.nearq.st, f.nearq.charges, 0)) != cudaSuccess) return e;
+      eval_warp_kernel<R, kEvalNear><<<near_grid<R>(nleaves), 32 * kEvalWarps, 0, f.nearq.st>>>(
+          a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
+      if ((e = cudaEventRecord(f.nearq.near, f.nearq.st)) != cudaSuccess) return e;
+    }
     // upward pass
     a.boxes = f.leaves.p;
     if (nleaves)
@@ -1033,11 +1099,17 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
     a.boxes = f.leaves.p;
     const size_t esm = sizeof(Pos<R>) * kStage + sizeof(Cx<R>) * kStage * kMaxRhs +
                        sizeof(double) * kEvalThreads * kMaxRhs;
-    if (nleaves && mode == 2)
+    if (nleaves && mode == 2) {
       stokes_eval_kernel<R><<<nleaves, kEvalThreads, esm, st>>>(a, geo, muq, yq, ya, yb, f.r1.p);
-    else if (nleaves)
-      launch_pdl(eval_warp_kernel<R>, dim3(nleaves), dim3(32 * kEvalWarps), 0, st, a, geo,
-                 muq, yq, ya, yb, (const double*)f.r1.p);
+    } else if (split) {
+      // the far field, after the near field on the side stream
+      if ((e = cudaStreamWaitEvent(st, f.nearq.near, 0)) != cudaSuccess) return e;
+      eval_warp_kernel<R, kEvalFar><<<nleaves, 32 * kEvalWarps, 0, st>>>(
+          a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
+    } else if (nleaves) {
+      launch_pdl(eval_warp_kernel<R, kEvalAll>, dim3(nleaves), dim3(32 * kEvalWarps), 0, st, a,
+                 geo, muq, yq, ya, yb, (const double*)f.r1.p, (double*)nullptr, (int)nleaves);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;

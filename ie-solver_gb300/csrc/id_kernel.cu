@@ -16,8 +16,9 @@
 // pivots and |R_ii| as column-pivoted QR of the full matrix (the column norms
 // it pivots on are invariant under the orthogonal factor), so the pivoted
 // factorization then runs on the small n x n tile only, and stops as soon as
-// the rank is known.  Norms and the rank decision are accumulated in double
-// for both element types.
+// the rank is known.  The norm that decides the rank is accumulated in
+// double for FP64 tiles and as a float pair (about 48 significant bits, on
+// the FP32 pipes) for FP32 tiles.
 #include <algorithm>
 #include <cstdio>
 
@@ -30,6 +31,53 @@
 namespace rskel {
 
 constexpr int kChunk = 64;  // rows per fold
+
+// Sums of squares for the FP32 paths' rank decisions, accumulated as an
+// unevaluated float pair hi + lo (about 48 significant bits) on the FP32
+// pipes: each square exactly by an FMA (p = a a, e = fma(a, a, -p)), each
+// sum exactly by Knuth's two-sum.  The rank is then decided as by an FP64
+// sum, without the FP64 pipe (about 1/60 of the FP32 rate on GB300), whose
+// norm had been the longest link of a pivoted-QR step.  fp_add is
+// commutative bit for bit (two-sum's error term is the exact rounding
+// error, whatever the order), so a butterfly reduction leaves every lane
+// the same pair.
+struct FPair {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FPair fp_add(FPair a, FPair b) {
+  const float s = a.hi + b.hi;
+  const float bv = s - a.hi;
+  const float e = (a.hi - (s - bv)) + (b.hi - bv);
+  const float lo = e + (a.lo + b.lo);
+  const float h = s + lo;
+  return {h, lo - (h - s)};
+}
+
+__device__ __forceinline__ FPair fp_sq(float a) {
+  const float p = a * a;
+  return {p, fmaf(a, a, -p)};
+}
+
+__device__ __forceinline__ FPair fp_warp_sum(FPair v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = fp_add(v, FPair{__shfl_xor_sync(0xffffffffu, v.hi, o),
+                        __shfl_xor_sync(0xffffffffu, v.lo, o)});
+  return v;
+}
+
+// sqrt(hi + lo) to about 46 bits, as a normalised pair (hi is the float
+// nearest the root): the FP32 root of hi and one Newton correction with the
+// pair's residual.  Comparing two normalised pairs lexicographically
+// compares their values.
+__device__ __forceinline__ FPair fp_sqrt(FPair x) {
+  if (!(x.hi > 0.f)) return FPair{0.f, 0.f};
+  const float r0 = sqrtf(x.hi);
+  const float c = (fmaf(-r0, r0, x.hi) + x.lo) / (2.f * r0);
+  const float h = r0 + c;
+  return FPair{h, c - (h - r0)};
+}
 
 // Thread layout inside a CTA: column c of a tile is owned by a team of TS
 // consecutive threads (TS = 8, 4, 2, 1 for n <= 32, 64, 128, > 128); team
@@ -290,7 +338,8 @@ __device__ void fold_chunk(int n, const Layout& L, int step0, IdShared<Real>& S)
 // type; the norm that sets the rank (the pivot column's trailing norm, which
 // is |R_ii|) is accumulated in double.  Returns k.
 template <class Real, int TS>
-__device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Real>& S) {
+__device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Real>& S,
+                         long long* head_clk = nullptr) {
   Real* A = S.R;
   constexpr int ts = TS;
   const int t = L.t, ld = L.ld;
@@ -309,75 +358,127 @@ __device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Re
   Real* v = S.v;
   const int kmax = n < mr ? n : mr;
   for (int i = 0; i < kmax; ++i) {
-    // pivot: first index of the largest partial norm (idamax)
+    const long long t0 = head_clk != nullptr ? clock64() : 0;
+    // Warp 0 alone takes the pivot (first index of the largest partial
+    // norm, idamax), interchanges the columns and forms the reflector of
+    // column i; the other warps wait at the one barrier below.
     if (warp == 0) {
-      Real best = -1;
-      int bi = n;
-      for (int c = i + lane; c < n; c += 32) {
-        const Real val = vn1[c];
-        if (val > best) { best = val; bi = c; }
-      }
+      int bi;  // the same in every lane
+      if constexpr (sizeof(Real) == 4) {
+        // partial norms are >= 0, so their bit patterns order as their
+        // values: the largest by one warp reduction, then its first index
+        unsigned bb = 0u;
+        int li = n;
+        for (int c = i + lane; c < n; c += 32) {
+          const unsigned val = __float_as_uint(vn1[c]);
+          if (li == n || val > bb) { bb = val; li = c; }
+        }
+        const unsigned wb = __reduce_max_sync(0xffffffffu, bb);
+        bi = (int)__reduce_min_sync(0xffffffffu, li < n && bb == wb ? (unsigned)li : (unsigned)n);
+      } else {
+        Real best = -1;
+        bi = n;
+        for (int c = i + lane; c < n; c += 32) {
+          const Real val = vn1[c];
+          if (val > best) { best = val; bi = c; }
+        }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const Real ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        for (int o = 16; o > 0; o >>= 1) {
+          const Real ov = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
       }
-      if (lane == 0) {
-        S.is[1] = bi;
-        if (bi != i) {
+      if (bi != i) {
+        // eight rows per lane loaded before their stores (the tile may be
+        // in global memory)
+        for (int r0 = lane; r0 < mr; r0 += 256) {
+          Real x[8], y[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int r = r0 + 32 * q;
+            if (r < mr) {
+              x[q] = A[(size_t)r * ld + bi];
+              y[q] = A[(size_t)r * ld + i];
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int r = r0 + 32 * q;
+            if (r < mr) {
+              A[(size_t)r * ld + bi] = y[q];
+              A[(size_t)r * ld + i] = x[q];
+            }
+          }
+        }
+        if (lane == 0) {
           int tp = S.perm[bi]; S.perm[bi] = S.perm[i]; S.perm[i] = tp;
           vn1[bi] = vn1[i];
           vn2[bi] = vn2[i];
         }
       }
-    }
-    __syncthreads();
-    const int pvt = S.is[1];
-    if (pvt != i) {
-      for (int r = threadIdx.x; r < mr; r += blockDim.x) {
-        Real tmp = A[(size_t)r * ld + pvt];
-        A[(size_t)r * ld + pvt] = A[(size_t)r * ld + i];
-        A[(size_t)r * ld + i] = tmp;
-      }
-      __syncthreads();
-    }
-    // The reflector of column i, by all of warp 0: its FP64 norm (which sets
-    // the rank) is a chain of mr - i - 1 conversions and FP64 multiply-adds,
-    // on the FP64 pipe's one warp instruction per 16 cycles per SM; over 32
-    // lanes instead of one team it is a few per lane and a shuffle tree.
-    if (warp == 0) {
-      double xs = 0.0;
-      for (int r = i + 1 + lane; r < mr; r += 32) {
-        const double a = (double)A[(size_t)r * ld + i];
-        xs += a * a;
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, o);
+      __syncwarp();
+      // The reflector: its norm |R_ii| sets the rank.  FP32 tiles sum it as
+      // a float pair and compare it with the threshold as pairs (GB300's
+      // FP64 pipe runs at about 1/60 of the FP32 rate; each FP64 warp
+      // instruction in this chain costs tens of cycles); FP64 tiles in
+      // double.
       const double alpha = (double)A[(size_t)i * ld + i];
-      const double nrm = sqrt(alpha * alpha + xs);  // |R_ii|, sets the rank
+      Real nrm;  // |R_ii| rounded to Real
       int stop = 0;
-      if (i == 0) {
-        if (lane == 0) S.scal[2] = fabs(tol * nrm);
-      } else if (nrm < S.scal[2]) {
-        stop = 1;
+      bool below = false;  // some entry below the diagonal is non-zero
+      if constexpr (sizeof(Real) == 4) {
+        FPair xs{0.f, 0.f};
+        for (int r = i + 1 + lane; r < mr; r += 32) xs = fp_add(xs, fp_sq(A[(size_t)r * ld + i]));
+        xs = fp_warp_sum(xs);
+        const FPair nv = fp_sqrt(fp_add(fp_sq((float)alpha), xs));
+        below = xs.hi > 0.f;
+        if (i == 0) {
+          const double td = fabs(tol * ((double)nv.hi + (double)nv.lo));
+          if (lane == 0) {
+            S.scal[2] = td;
+            S.rs[4] = (float)td;
+            S.rs[5] = (float)(td - (double)(float)td);
+          }
+        } else {
+          const float th = S.rs[4], tl = S.rs[5];
+          stop = nv.hi < th || (nv.hi == th && nv.lo < tl) ? 1 : 0;
+        }
+        nrm = nv.hi;
+      } else {
+        double xs = 0.0;
+        for (int r = i + 1 + lane; r < mr; r += 32) {
+          const double a = (double)A[(size_t)r * ld + i];
+          xs += a * a;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, o);
+        const double nd = sqrt(alpha * alpha + xs);
+        below = xs > 0.0;
+        if (i == 0) {
+          if (lane == 0) S.scal[2] = fabs(tol * nd);
+        } else if (nd < S.scal[2]) {
+          stop = 1;
+        }
+        nrm = (Real)nd;
       }
       Real tau = 0, scale = 0, beta = 0;
-      if (!stop && xs > 0.0) {
+      if (!stop && below) {
         const Real a = (Real)alpha;
-        beta = -copysign((Real)nrm, a);
+        beta = -copysign(nrm, a);
         tau = (beta - a) / beta;
         scale = (Real)1 / (a - beta);
       }
       for (int r = i + 1 + lane; r < mr; r += 32) v[r] = A[(size_t)r * ld + i] * scale;
       __syncwarp();
       if (lane == 0) {
-        if (!stop && xs > 0.0) A[(size_t)i * ld + i] = beta;
+        if (!stop && below) A[(size_t)i * ld + i] = beta;
         S.rs[0] = tau;
         S.is[0] = stop;
       }
     }
     __syncthreads();
+    if (head_clk != nullptr) *head_clk += clock64() - t0;
     if (S.is[0] != 0) { k = i; break; }
     const Real tau = S.rs[0];
     for (int c = L.c0; c < n; c += L.cstep) {
@@ -388,7 +489,9 @@ __device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Re
         for (int r = i + 1 + t; r < mr; r += ts) part += v[r] * A[(size_t)r * ld + c];
         part = team_sum<TS>(part);
         const Real tw = tau * (aic + part);
-        for (int r = i + 1 + t; r < mr; r += ts) A[(size_t)r * ld + c] -= tw * v[r];
+        const int r0 = i + 1 + t;
+        if (r0 < mr)
+          axpy_sub(A + (size_t)r0 * ld + c, ts * ld, v + r0, ts, tw, (mr - r0 + ts - 1) / ts);
         aic -= tw;
       }
       // partial norm downdate: vn1 <- sqrt(vn1^2 - a^2), recomputed when the
@@ -517,7 +620,9 @@ __global__ void __launch_bounds__(kThreads) id_kernel(IdParams p) {
         // broadcast within the team (the owner is lane (row % ts) of the team)
         const int base = (threadIdx.x & 31) - tt;
         zr = __shfl_sync(team_mask(ts), zr, base + (row % ts));
-        for (int q2 = tt; q2 < row; q2 += ts) S.R[(size_t)q2 * ld + col] -= zr * S.R[(size_t)q2 * ld + row];
+        if (tt < row)
+          axpy_sub(S.R + (size_t)tt * ld + col, ts * ld, S.R + (size_t)tt * ld + row, ts * ld, zr,
+                   (row - tt + ts - 1) / ts);
         __syncwarp(team_mask(ts));
       }
       for (int row = tt; row < k; row += ts) T[row + (size_t)k * c] = S.R[(size_t)row * ld + col];
@@ -896,14 +1001,15 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
     uint32_t phase = 0;
     for (int c0 = 0; c0 < m; c0 += kChunk) {
       const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
-      if (c0 > 0) {  // the previous chunk's MMAs have read the tiles
-        if (threadIdx.x == 0 && !tc::mbar_wait(&tc_bar, phase, kTcPolls)) tc_ok = 0;
-        phase ^= 1u;
-        __syncthreads();
-        if (!tc_ok) break;  // block-uniform
-      }
+      // the chunk's row points are staged while the previous chunk's MMAs
+      // run (those read only the operand tiles); then the tiles are free
+      // once the MMAs have completed.  The phase moves on only after a wait
+      // that succeeded, so a give-up's last wait is on the MMAs in flight.
       stage_chunk_rows<Real>(p, t, S, c0, cnt, ox, oy);
+      if (c0 > 0 && threadIdx.x == 0 && !tc::mbar_wait(&tc_bar, phase, kTcPolls)) tc_ok = 0;
       __syncthreads();
+      if (!tc_ok) break;  // block-uniform
+      if (c0 > 0) phase ^= 1u;
       fill_chunk_tc(p, t, S, c0, cnt, npad, bt, bbytes, om, rows, mtiles);
       tc::fence_async_smem();
       __syncthreads();
@@ -1019,7 +1125,11 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
     return;
   }
   clk0 = clock64();
-  const int k = mr > 0 ? cpqr_rank<Real, TS>(n, mr, p.tol, L, S) : 0;
+  // (trace: the steps' pivot and reflector time goes to the fold slot,
+  // unused by the tensor-core sketch)
+  const int k = mr > 0 ? cpqr_rank<Real, TS>(n, mr, p.tol, L, S,
+                                             kTC && p.phase_clk != nullptr ? &clk_fold : nullptr)
+                       : 0;
   const long long clk_cpqr = clock64() - clk0;
   const bool learned = p.redo != nullptr && !p.redo_pass;
   int flag = learned && sketch_too_small(k, n, m, ell, sketch_rows(n), nt > 0) ? 1 : 0;  // block-uniform
@@ -1038,7 +1148,9 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
         }
         const int base = (threadIdx.x & 31) - tt;
         zr = __shfl_sync(team_mask(ts), zr, base + (row % ts));
-        for (int q2 = tt; q2 < row; q2 += ts) S.R[(size_t)q2 * ld + col] -= zr * S.R[(size_t)q2 * ld + row];
+        if (tt < row)
+          axpy_sub(S.R + (size_t)tt * ld + col, ts * ld, S.R + (size_t)tt * ld + row, ts * ld, zr,
+                   (row - tt + ts - 1) / ts);
         __syncwarp(team_mask(ts));
       }
     }
@@ -1122,7 +1234,7 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
   float* vn2 = carve<float>(sp, n);
   int* perm = carve<int>(sp, n);
   const float* Y = p.sketch_y + t.y_off;
-  for (int e = lane; e < (mr + nt) * ld; e += 32) A[e] = Y[e];
+  batched_copy(A, Y, (mr + nt) * ld, lane, 32);
   for (int j = lane; j < n; j += 32) perm[j] = j;
   __syncwarp();
 #pragma unroll
@@ -1139,21 +1251,19 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
   const float tol3z = 2.44140625e-4f;
   const int kmax = n < mr ? n : mr;
   int k = 0;
-  double thr = 0.0;
+  double thr = 0.0;   // tol |R_00|, and as a float pair (th, tl) for the steps
+  float th = 0.f, tl = 0.f;
   for (int i = 0; i < kmax; ++i) {
-    // pivot: first index of the largest partial norm
-    float best = -1.f;
-    int bi = n;
+    // pivot: first index of the largest partial norm (norms are >= 0, so
+    // their bit patterns order as their values: two warp reductions)
+    unsigned bb = 0u;
+    int li = n;
     for (int j = i + lane; j < n; j += 32) {
-      const float val = vn1[j];
-      if (val > best) { best = val; bi = j; }
+      const unsigned val = __float_as_uint(vn1[j]);
+      if (li == n || val > bb) { bb = val; li = j; }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-    }
+    const unsigned wb = __reduce_max_sync(0xffffffffu, bb);
+    const int bi = (int)__reduce_min_sync(0xffffffffu, li < n && bb == wb ? (unsigned)li : (unsigned)n);
     if (bi != i) {
       for (int r = lane; r < mr; r += 32) {
         const float a = A[(size_t)r * ld + bi];
@@ -1170,26 +1280,29 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
       __syncwarp();
     }
     // Householder reflector of column i (rows i..mr-1); |R_ii| sets the rank
-    double xs = 0.0;
-    for (int r = i + 1 + lane; r < mr; r += 32) {
-      const double a = (double)A[(size_t)r * ld + i];
-      xs += a * a;
+    FPair xs{0.f, 0.f};
+    for (int r = i + 1 + lane; r < mr; r += 32) xs = fp_add(xs, fp_sq(A[(size_t)r * ld + i]));
+    xs = fp_warp_sum(xs);
+    const float alpha = A[(size_t)i * ld + i];
+    const FPair nv = fp_sqrt(fp_add(fp_sq(alpha), xs));
+    if (i == 0) {
+      thr = fabs(p.tol * ((double)nv.hi + (double)nv.lo));
+      th = (float)thr;
+      tl = (float)(thr - (double)th);
+    } else if (nv.hi < th || (nv.hi == th && nv.lo < tl)) {
+      k = i;
+      break;
     }
-    xs = warp_sum(xs);
-    const double alpha = (double)A[(size_t)i * ld + i];
-    const double nrm = sqrt(alpha * alpha + xs);
-    if (i == 0) thr = fabs(p.tol * nrm);
-    else if (nrm < thr) { k = i; break; }
     float tau = 0.f, scale = 0.f, beta = 0.f;
-    if (xs > 0.0) {
-      const float a = (float)alpha;
-      beta = -copysignf((float)nrm, a);
+    if (xs.hi > 0.f) {
+      const float a = alpha;
+      beta = -copysignf(nv.hi, a);
       tau = (beta - a) / beta;
       scale = 1.f / (a - beta);
     }
     for (int r = i + 1 + lane; r < mr; r += 32) v[r] = A[(size_t)r * ld + i] * scale;
     __syncwarp();
-    if (lane == 0 && xs > 0.0) A[(size_t)i * ld + i] = beta;
+    if (lane == 0 && xs.hi > 0.f) A[(size_t)i * ld + i] = beta;
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       const int j = lane + 32 * c;
@@ -1206,7 +1319,7 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
           }
           for (; r < mr; ++r) w0 += v[r] * A[(size_t)r * ld + j];
           const float tw = tau * ((w0 + w1) + (w2 + w3));
-          for (int q = i + 1; q < mr; ++q) A[(size_t)q * ld + j] -= tw * v[q];
+          axpy_sub(A + (size_t)(i + 1) * ld + j, ld, v + i + 1, 1, tw, mr - i - 1);
           aij -= tw;
         }
         // partial norm downdate (dlaqp2), recomputed when it loses accuracy
@@ -1240,7 +1353,7 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
         for (int row = k - 1; row >= 0; --row) {
           const float z = A[(size_t)row * ld + col] / A[(size_t)row * ld + row];
           A[(size_t)row * ld + col] = z;
-          for (int q = 0; q < row; ++q) A[(size_t)q * ld + col] -= z * A[(size_t)q * ld + row];
+          axpy_sub(A + col, ld, A + row, ld, z, row);
         }
       }
     }

@@ -62,6 +62,9 @@ struct DecoupleParams {
   void* epool;     // E blocks in/out (Real)
   void* scratch;
   int* status;     // non-zero on singular pivot / non-finite value
+  // trace only (else null): per box of the launch, clock cycles of the
+  // assembly, the T products, the X_rr inverse or LU and the rest, then n, k
+  long long* phase_clk;
 };
 
 // Sweep modes (solve_kernels.cu).
@@ -105,7 +108,7 @@ int launch_id_wide(const IdParams& p, int num_tasks, int nmax, const WideItem* i
 size_t id_wide_tile(int m, int n);  // scratch floats of a wide task (m: rows factored)
 int id_sketch_rows(int n);
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
-                     cudaStream_t st, int threads = 256);
+                     cudaStream_t st, int threads, int num_sms);
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st);
 
 // Dense LU with partial pivoting of an n x n column-major matrix (one CTA),

@@ -88,22 +88,19 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   const Real* L = fac + fac_L(k, r);
   const Real* U = fac + fac_U(k, r);
   const Real* X = fac + fac_X(k, r);
-  // The box's factor record (T, L, U, then X_rr) is copied to shared memory
-  // in one coalesced pass: the products and the triangular solves below then
-  // read it without a global round trip per step.  In FP32, X_rr (the
-  // record's largest block, an explicit inverse) stays in place: its product
-  // reads it coalesced, one row per thread and column step, and leaving it
-  // out lets more boxes of a level run at once.  The FP64 LU solve, a chain
-  // of dependent steps, reads it from shared memory.
-  constexpr bool kStageX = sizeof(Real) == 8;
+  // The box's factor record (T, L, U, then X_rr: the LU factors in FP64, the
+  // explicit inverse in FP32) is copied to shared memory in one coalesced
+  // pass, before the wait for the previous level: the copy overlaps that
+  // level's work, and the products and solves below read the record without
+  // a global round trip per step.
   if (p.stage_fac) {
-    const int len = (int)(fac_X(k, r) + (kStageX ? (int64_t)r * r : 0));
+    const int len = (int)(fac_X(k, r) + (int64_t)r * r);
     Real* fsh = carve<Real>(sp, len);
-    for (int e = threadIdx.x; e < len; e += blockDim.x) fsh[e] = fac[e];
+    batched_copy(fsh, fac, len, threadIdx.x, blockDim.x);
     T = fsh + fac_T(k, r);
     L = fsh + fac_L(k, r);
     U = fsh + fac_U(k, r);
-    if (kStageX) X = fsh + fac_X(k, r);
+    X = fsh + fac_X(k, r);
   }
   Real* x = reinterpret_cast<Real*>(p.x);
   const int* sk = p.dofs + t.skel_off;
@@ -189,8 +186,8 @@ void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cuda
   size_t smem = 3 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
                 ((sizeof(int) * nmax + 15) & ~size_t(15)) + 64;
   SweepParams q = p;
-  // FP32 stages T, L, U (3 k r <= 3 n^2 / 4), FP64 the whole record
-  const size_t fe = fp32 ? 3 * (size_t)nmax * nmax / 4 + 8 : (size_t)fac_reserve(nmax);
+  // the whole record: 3 k r + r^2 <= 5 n^2 / 4
+  const size_t fe = (size_t)fac_reserve(nmax);
   const size_t fb = (fe * es + 15) & ~size_t(15);
   q.stage_fac = smem + fb <= (size_t)kSmemOptIn;
   if (q.stage_fac) smem += fb;
@@ -547,6 +544,11 @@ __global__ void __launch_bounds__(kInvG * kInvG) root_inverse_kernel(float* base
 }
 
 // x[idx, c] <- A^{-1} x[idx, c] per root block, with the explicit inverse.
+// The inverse (at most kRootInvMax^2 floats, 64 KB) is staged in shared
+// memory first with many loads in flight: read from global memory inside
+// the product, each thread's row sum was a chain of dependent L2 round
+// trips.  Then one thread per row forms that row for every column of the
+// block, in the same order of terms as before.
 __global__ void __launch_bounds__(kThreads) root_apply_kernel(const float* base,
                                                               const RootTask* tasks,
                                                               const int* dofs, float* x, int ld,
@@ -555,8 +557,10 @@ __global__ void __launch_bounds__(kThreads) root_apply_kernel(const float* base,
   const int n = t.n;
   const float* Ai = base + t.a_off;
   const int* idx = dofs + t.idx_off;
-  __shared__ float sx[kRootInvMax * kRhsBlock];
-  __shared__ float sy[kRootInvMax * kRhsBlock];
+  extern __shared__ __align__(16) float rsm[];
+  float* sA = rsm;                                  // n x n
+  float* sx = rsm + (((size_t)n * n + 3) & ~size_t(3));  // n x kRhsBlock
+  batched_copy(sA, Ai, n * n, threadIdx.x, blockDim.x);
   for (int c0 = 0; c0 < nrhs; c0 += kRhsBlock) {
     const int cb = nrhs - c0 < kRhsBlock ? nrhs - c0 : kRhsBlock;
     for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
@@ -564,16 +568,20 @@ __global__ void __launch_bounds__(kThreads) root_apply_kernel(const float* base,
       sx[e] = x[idx[i] + (size_t)ld * (c0 + c)];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
-      const int i = e % n, c = e / n;
-      float acc = 0.f;
-      for (int l = 0; l < n; ++l) acc += Ai[i + (size_t)n * l] * sx[l + n * c];
-      sy[e] = acc;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
-      const int i = e % n, c = e / n;
-      x[idx[i] + (size_t)ld * (c0 + c)] = sy[e];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      float acc[kRhsBlock];
+#pragma unroll
+      for (int c = 0; c < kRhsBlock; ++c) acc[c] = 0.f;
+      for (int l = 0; l < n; ++l) {
+        const float a = sA[i + (size_t)n * l];
+#pragma unroll
+        for (int c = 0; c < kRhsBlock; ++c)
+          if (c < cb) acc[c] += a * sx[l + n * c];
+      }
+      const int xi = idx[i];
+#pragma unroll
+      for (int c = 0; c < kRhsBlock; ++c)
+        if (c < cb) x[xi + (size_t)ld * (c0 + c)] = acc[c];
     }
     __syncthreads();
   }
@@ -588,7 +596,10 @@ void launch_root_inverse(float* base, const RootTask* tasks, int count, int* sta
 void launch_root_apply(const float* base, const RootTask* tasks, int count, const int* dofs,
                        float* x, int ld, int nrhs, cudaStream_t st) {
   if (count <= 0 || nrhs <= 0) return;
-  root_apply_kernel<<<count, kThreads, 0, st>>>(base, tasks, dofs, x, ld, nrhs);
+  set_smem_once<root_apply_kernel>();
+  const size_t smem = sizeof(float) * ((((size_t)kRootInvMax * kRootInvMax + 3) & ~size_t(3)) +
+                                       (size_t)kRootInvMax * kRhsBlock);
+  root_apply_kernel<<<count, kThreads, smem, st>>>(base, tasks, dofs, x, ld, nrhs);
 }
 
 // ---------------------------------------------------------------------------

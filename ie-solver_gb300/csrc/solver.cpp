@@ -87,7 +87,9 @@ struct rs_solver {
   // wide ID's CTAs per SM
   int split_min_tasks = 512;
   int wide_ctas_per_sm = 2;
-  int elim_threads = 256;  // threads per box of the Schur eliminations (128 or 256)
+  // threads per box of the Schur eliminations: 128, 256, or 0 (per launch:
+  // 128 when 256-thread CTAs would take more than one wave)
+  int elim_threads = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t stream2 = nullptr;  // read-back of ranks while eliminations run
   cudaEvent_t ev_c = nullptr;
@@ -186,6 +188,7 @@ struct rs_solver {
   int launches = 0;
   bool trace = false;  // RSKEL_TRACE=1: per-level timing on stderr
   DevBuf<long long> clk;
+  DevBuf<long long> dclk;  // trace: the eliminations' phase clocks
 };
 
 // ---------------------------------------------------------------------------
@@ -959,12 +962,18 @@ rs_status factor_impl(rs_solver* s) {
     dp.epool = F.epool.p;
     dp.scratch = F.scratch.p;
     dp.status = s->status.p;
+    dp.phase_clk = nullptr;
+    if (s->trace) {
+      CU(s->dclk.ensure(6 * std::max<size_t>(dct_s.size(), 1)));
+      CU(cudaMemsetAsync(s->dclk.p, 0, 6 * dct_s.size() * sizeof(long long), s->stream));
+    }
     launch_binned(dct_s, s->dc_tasks.p, dc_fits, [&](const DecoupleTask* dt, int cnt, int nmax) {
       DecoupleParams q = dp;
       q.tasks = dt;
+      if (s->trace) q.phase_clk = s->dclk.p + 6 * (dt - s->dc_tasks.p);
       bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
       launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream,
-                      s->elim_threads);
+                      s->elim_threads, s->num_sms);
       ++s->launches;
     }, (int)dct_s.size() < s->num_sms);
     CU(cudaGetLastError());
@@ -992,8 +1001,37 @@ rs_status factor_impl(rs_solver* s) {
           mx[z] = std::max(mx[z], (double)clk[4 * q + z]);
         }
       const double cnt = idt.empty() ? 1.0 : (double)idt.size();
-      std::fprintf(stderr, "[rskel]   ID cycles per box avg/max: fill %.0f/%.0f fold %.0f/%.0f cpqr %.0f/%.0f z %.0f/%.0f\n",
+      std::fprintf(stderr, "[rskel]   ID cycles per box avg/max: fill %.0f/%.0f fold|qr-head %.0f/%.0f cpqr %.0f/%.0f z %.0f/%.0f\n",
                    ph[0] / cnt, mx[0], ph[1] / cnt, mx[1], ph[2] / cnt, mx[2], ph[3] / cnt, mx[3]);
+      {
+        // the eliminations: phase cycles per box (average, and the slowest
+        // box's phases with its n and k)
+        const size_t nd = dct_s.size();
+        std::vector<long long> dc(6 * nd);
+        CU(cudaMemcpy(dc.data(), s->dclk.p, dc.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+        double av[4] = {0, 0, 0, 0};
+        size_t worst = 0;
+        long long wt = -1;
+        for (size_t q = 0; q < nd; ++q) {
+          long long tot = 0;
+          for (int z = 0; z < 4; ++z) {
+            av[z] += (double)dc[6 * q + z];
+            tot += dc[6 * q + z];
+          }
+          if (tot > wt) {
+            wt = tot;
+            worst = q;
+          }
+        }
+        const double dn = nd ? (double)nd : 1.0;
+        if (nd)
+          std::fprintf(stderr,
+                       "[rskel]   Schur cycles per box avg: assemble %.0f products %.0f inverse %.0f rest %.0f;"
+                       " slowest (n %lld k %lld): %lld %lld %lld %lld\n",
+                       av[0] / dn, av[1] / dn, av[2] / dn, av[3] / dn, dc[6 * worst + 4],
+                       dc[6 * worst + 5], dc[6 * worst], dc[6 * worst + 1], dc[6 * worst + 2],
+                       dc[6 * worst + 3]);
+      }
       if (ip.judge_ratio != nullptr) {
         // residual judge: estimated residual / (tol |a_max|) of the judged boxes
         std::vector<float> jr(idt.size());
@@ -1236,7 +1274,7 @@ rs_status factor_impl(rs_solver* s) {
       q.tasks = dt;
       bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
       launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream,
-                      s->elim_threads);
+                      s->elim_threads, s->num_sms);
       ++s->launches;
     });
     CU(cudaGetLastError());
@@ -2646,7 +2684,7 @@ rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ct
   s->wide_ctas_per_sm = best_wide;
   best = 1e300;
   int best_elim = s->elim_threads;
-  for (int cand : {256, 128}) {
+  for (int cand : {0, 256, 128}) {
     s->elim_threads = cand;
     double ms = 0;
     RSCHK(time_factor(&ms));

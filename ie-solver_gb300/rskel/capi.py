@@ -92,7 +92,7 @@ def lib():
         L.rs_set_geometry.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.rs_perturb.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
         L.rs_set_geometry_batch.argtypes = [_vp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp]
-        L.rs_autotune.argtypes = [_vp, ctypes.c_int, _ip, _ip]
+        L.rs_autotune.argtypes = [_vp, ctypes.c_int, _ip, _ip, _ip]
         L.rs_build_tree.argtypes = [_vp]
         L.rs_factor.argtypes = [_vp]
         L.rs_solve.argtypes = [_vp, _dp, ctypes.c_int, _dp, _dp]

@@ -294,8 +294,9 @@ rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* feat
  * the level size from which the FP32 sketched ID's pivoted QR runs one
  * warp per box instead of one CTA per box (128, 256, 512 (default), 1024,
  * never), then the wide ID's CTAs per SM (1, 2 (default), 4), then the
- * threads per box of the Schur eliminations (256 (default), 128: more
- * boxes resident per SM, fewer threads each).  Each candidate is the median
+ * threads per box of the Schur eliminations (0 (default): per level, 128
+ * when one wave of 256-thread CTAs does not hold the level's boxes, else
+ * 256; or 256 or 128 for every level).  Each candidate is the median
  * of `reps` factorizations.  The choices are returned (pointers may be
  * NULL).  The handle must be factored again before solving. */
 rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ctas_per_sm,
