@@ -25,7 +25,8 @@ reported too (that oracle carries its own ~1e-8 ID error).
 tree build, factor, solve, and the solutions copied back, every step.
 `roofline` covers the factorization kernel class with the largest CUDA-event
 time per step, against the CUDA-core FMA peak measured live on this GPU
-(lib/libfmapeak.so); `step_breakdown_ms` lists every class.
+(lib/libfmapeak.so), with its DRAM traffic per factorization from ncu;
+`step_breakdown_ms` lists every class.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -527,9 +528,16 @@ def run_gpu(args):
     kms = st["id_ms"] if cls == "id" else st["decouple_ms"]
     achieved = fl / (kms * 1e-3) / 1e12 if kms > 0 else 0.0
     peak = peaks["fp32"] if refined_ok else peaks["fp64"]
-    kname = ({"id": "id_sketch_kernel (FP32 randomized ID)", "schur": "decouple_kernel<float>"}
+    kname = ({"id": "id_sketch_kernel + id_cpqr_warp_kernel (FP32 randomized ID: tcgen05 "
+                    "sketch of the ID matrix, pivoted QR of the sketch on the CUDA cores)",
+              "schur": "decouple_kernel<float>"}
              if refined_ok else
              {"id": "id_kernel<double> (direct CPQR)", "schur": "decouple_kernel<double>"})[cls]
+    # DRAM bytes (read + write) of the ID launches of one factorization of this
+    # workload, from ncu (dram__bytes_read.sum + dram__bytes_write.sum over the
+    # 12 ID launches of a factorization; profiles/id_sketch_star65536.md has
+    # the command): 37.8 MB against 1.18 ms of serialised kernel time
+    traffic = 37.8e6 if refined_ok and cls == "id" else None
     cpu_v = cpu_sample(geo, F, cores, 10) if dist.rank == 0 else 0.0
     line = {
         "metric": METRIC, "value": value, "unit": "DOFs/s", "n_gpus": dist.ws,
@@ -561,12 +569,15 @@ def run_gpu(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp32_fma" if refined_ok else "fp64_fma", "kernel": kname,
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "traffic_unit": "bytes per factorization (the class's launches)",
                      "peak_source": "CUDA-core FMA chains measured now on this GPU "
                                     "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
-                     "work": "algorithmic flops per factorization: ID fill + CPQR to rank + Z, "
-                             "or Schur eliminations (per box: sketch_id_flops, id_flops, dec_flops "
-                             "in solver.cpp)"},
+                     "work": "algorithmic flops per factorization: ID fill + sketch + pivoted QR "
+                             "to the rank + Z, or Schur eliminations (per box: sketch_id_flops, "
+                             "id_flops, dec_flops in solver.cpp), over the class's CUDA-event time",
+                     "note": "latency-bound per box (a chain of dependent QR steps with CTA "
+                             "barriers); the sketch runs on the tensor pipe, 6 % active"},
         "fma_peaks_tflops": peaks,
         "cpu_baseline": {"value": cpu_v, "unit": "DOFs/s", "cores": cores, "kind": "port",
                          "sample": "10 factor + 8-RHS solves of the full workload by the oracle "
