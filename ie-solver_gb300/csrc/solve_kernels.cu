@@ -45,28 +45,6 @@ __device__ void lu_solve_cols(const Real* X, const int* piv, int r, Real* y, int
   }
 }
 
-// x_r <- X_rr^{-1} x_r for cb columns: an LU solve with the FP64 factors
-// (the reference's apply_diag_inv_matrix, skel_factorization.cpp:419-426),
-// a product with the explicit inverse the FP32 factorization stores.
-template <class Real>
-__device__ void diag_solve(const Real* X, const int* piv, int r, Real* xr, Real* xt, int cb) {
-  if constexpr (sizeof(Real) == 4) {
-    if (r > 0)
-      for (TileWalk w(r); w.j < cb; w.next()) {
-        const int i = w.i, c = w.j;
-        const int e = w.e();
-        Real acc = 0;
-        for (int l = 0; l < r; ++l) acc += X[i + (size_t)r * l] * xr[l + r * c];
-        xt[e] = acc;
-      }
-    __syncthreads();
-    for (int e = threadIdx.x; e < r * cb; e += blockDim.x) xr[e] = xt[e];
-  } else {
-    (void)xt;
-    lu_solve_cols<Real>(X, piv, r, xr, r, cb);
-  }
-}
-
 template <class Real>
 __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   // Programmatic dependent launch: the next sweep may be scheduled once every
@@ -81,8 +59,9 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
   unsigned char* sp = smem;
   Real* xs = carve<Real>(sp, k * kRhsBlock);
   Real* xr = carve<Real>(sp, r * kRhsBlock);
-  Real* xt = carve<Real>(sp, r * kRhsBlock);
   int* piv = carve<int>(sp, r);
+  int* sk = carve<int>(sp, k + r);  // the box's skeleton, then redundant, DOF indices
+  int* rd = sk + k;
   const Real* fac = reinterpret_cast<const Real*>(p.fac) + t.fac_off;
   const Real* T = fac + fac_T(k, r);
   const Real* L = fac + fac_L(k, r);
@@ -103,9 +82,12 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
     X = fsh + fac_X(k, r);
   }
   Real* x = reinterpret_cast<Real*>(p.x);
-  const int* sk = p.dofs + t.skel_off;
-  const int* rd = p.dofs + t.red_off;
+  // pivots and the DOF indices before the wait too: after it, the gather of
+  // x is one global round trip instead of two dependent ones
   for (int j = threadIdx.x; j < r; j += blockDim.x) piv[j] = p.piv[t.piv_off + j];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) sk[j] = p.dofs[t.skel_off + j];
+  for (int j = threadIdx.x; j < r; j += blockDim.x) rd[j] = p.dofs[t.red_off + j];
+  __syncthreads();
   pdl_wait();
   for (int c0 = 0; c0 < p.nrhs; c0 += kRhsBlock) {
     const int cb = p.nrhs - c0 < kRhsBlock ? p.nrhs - c0 : kRhsBlock;
@@ -140,13 +122,8 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
           xs[i + k * c] -= acc;
         }
       __syncthreads();
-      if (p.mode == kUpSolve) {
-        diag_solve<Real>(X, piv, r, xr, xt, cb);
-        __syncthreads();
-      }
     } else if (p.mode == kDiagOnly) {
-      diag_solve<Real>(X, piv, r, xr, xt, cb);
-      __syncthreads();
+      // (nothing before the diagonal step)
     } else {  // kDown
       if (r > 0)
         for (TileWalk w(r); w.j < cb; w.next()) {  // x_r -= U x_s
@@ -171,11 +148,34 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
           const int i = w.i, c = w.j;
           x[sk[i] + (size_t)p.ld * (c0 + c)] = xs[i + k * c];
         }
-    if (r > 0)
-      for (TileWalk w(r); w.j < cb; w.next()) {
-        const int i = w.i, c = w.j;
-        x[rd[i] + (size_t)p.ld * (c0 + c)] = xr[i + r * c];
+    // the diagonal step x_r <- X_rr^{-1} x_r (the reference's
+    // apply_diag_inv_matrix, skel_factorization.cpp:419-426): an LU solve with
+    // the FP64 factors, a product with the explicit inverse of the FP32 ones
+    const bool diag = p.mode == kUpSolve || p.mode == kDiagOnly;
+    if constexpr (sizeof(Real) == 4) {
+      // each result straight to x (a thread stores the entries it sums)
+      if (r > 0)
+        for (TileWalk w(r); w.j < cb; w.next()) {
+          const int i = w.i, c = w.j;
+          Real v = xr[i + r * c];
+          if (diag) {
+            Real acc = 0;
+            for (int l = 0; l < r; ++l) acc += X[i + (size_t)r * l] * xr[l + r * c];
+            v = acc;
+          }
+          x[rd[i] + (size_t)p.ld * (c0 + c)] = v;
+        }
+    } else {
+      if (diag) {
+        lu_solve_cols<Real>(X, piv, r, xr, r, cb);
+        __syncthreads();
       }
+      if (r > 0)
+        for (TileWalk w(r); w.j < cb; w.next()) {
+          const int i = w.i, c = w.j;
+          x[rd[i] + (size_t)p.ld * (c0 + c)] = xr[i + r * c];
+        }
+    }
     __syncthreads();
   }
 }
@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(kThreads, 8) sweep_kernel(SweepParams p) {
 void launch_sweep(const SweepParams& p, int num_tasks, int nmax, bool fp32, cudaStream_t st) {
   if (num_tasks <= 0) return;
   size_t es = fp32 ? sizeof(float) : sizeof(double);
-  size_t smem = 3 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
-                ((sizeof(int) * nmax + 15) & ~size_t(15)) + 64;
+  size_t smem = 2 * (((size_t)nmax * kRhsBlock * es + 15) & ~size_t(15)) +
+                2 * ((sizeof(int) * nmax + 15) & ~size_t(15)) + 64;
   SweepParams q = p;
   // the whole record: 3 k r + r^2 <= 5 n^2 / 4
   const size_t fe = (size_t)fac_reserve(nmax);
