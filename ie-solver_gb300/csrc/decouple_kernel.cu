@@ -530,8 +530,11 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
 
 // threads: 256 or 128 per box, or 0: 128 when the launch holds more boxes
 // than one wave of 256-thread CTAs (every resident slot of every SM), so the
-// boxes run in one wave at twice the CTAs per SM, else 256.  Every loop of
-// the kernel strides by blockDim.x (or its warp count).
+// boxes run in one wave at twice the CTAs per SM, else 256.  (512 threads
+// for launches of fewer boxes than SMs made their slowest box no faster: a
+// Gauss-Jordan step is bound by its two barriers and the pivot search, not
+// by the r^2 update.)  Every loop of the kernel strides by blockDim.x (or
+// its warp count).
 void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool fp32,
                      cudaStream_t st, int threads, int num_sms) {
   if (num_tasks <= 0) return;
@@ -545,7 +548,7 @@ void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool f
     const void* fn = fp32 ? (const void*)decouple_kernel<float> : (const void*)decouple_kernel<double>;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem) != cudaSuccess)
       per_sm = 0;
-    nt = per_sm > 0 && num_tasks > per_sm * num_sms ? 128 : kThreads;
+    if (per_sm > 0 && num_tasks > per_sm * num_sms) nt = 128;
   }
   if (fp32)
     decouple_kernel<float><<<num_tasks, nt, smem, st>>>(p);

@@ -942,7 +942,10 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   S.row = carve_dofs<Real>(sp, kChunk);
   S.kind = carve<int>(sp, kChunk);
   const int wld = warp_ld(n);
-  Real* Yg = kSplit ? p.sketch_y + t.y_off : nullptr;
+  // (a row group's partial sketch: blockIdx.y of gridDim.y, stride 0 for one)
+  Real* Yg = kSplit ? p.sketch_y + t.y_off + (int64_t)blockIdx.y * p.y_group_stride : nullptr;
+  const int first = kSplit ? (int)blockIdx.y * kChunk : 0;   // this CTA's first chunk
+  const int cstep = kSplit ? (int)gridDim.y * kChunk : kChunk;  // and its chunk stride
 
   const double ox = t.cx, oy = t.cy;
   for (int j = threadIdx.x; j < n; j += blockDim.x)
@@ -950,7 +953,47 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
   __syncthreads();
   long long clk0 = clock64(), clk_fill = 0, clk_fold = 0;
   int mr;
-  if (m <= ell) {
+  if (!kSplit && p.y_parts > 0) {
+    // the sketch (or the small matrix itself) is the sum of the row groups'
+    // partial sketches, added in group order
+    mr = m <= ell ? m : ell;
+    const int rows = m <= ell ? m : ell + nt;
+    const float* Y0 = p.sketch_y + t.y_off;
+    const int total = rows * n, nth = blockDim.x;
+    for (int e0 = threadIdx.x; e0 < total; e0 += 8 * nth) {
+      // eight entries per thread, all their loads of a group in flight at once
+      float acc[8];
+      int src[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * nth;
+        src[q] = e < total ? (e / n) * wld + e % n : -1;
+        acc[q] = 0.f;
+      }
+      for (int g = 0; g < p.y_parts; ++g) {
+        const float* Yp = Y0 + (int64_t)g * p.y_group_stride;
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = src[q] >= 0 ? Yp[src[q]] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] += v[q];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * nth;
+        if (e < total) S.R[(size_t)(e / n) * ld + e % n] = acc[q];
+      }
+    }
+    __syncthreads();
+    clk_fill = clock64() - clk0;
+  } else if (kSplit && (m <= ell ? blockIdx.y > 0 : first >= m)) {
+    // a row group with no rows: its partial sketch is zero (with m <= ell,
+    // group 0 writes the whole matrix and the others zeros)
+    mr = m <= ell ? m : ell;
+    const int rows = m <= ell ? m : ell + nt;
+    for (int e = threadIdx.x; e < rows * n; e += blockDim.x) Yg[(size_t)(e / n) * wld + e % n] = 0.f;
+    return;
+  } else if (m <= ell) {
     // small matrix: factor A itself
     mr = m;
     for (int c0 = 0; c0 < m; c0 += kChunk) {
@@ -999,17 +1042,17 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
     const uint32_t idesc = tc::idesc_bf16_f32(128, npad);
     const uint32_t lbo_a = 128 * 16, lbo_b = (uint32_t)npad * 16;
     uint32_t phase = 0;
-    for (int c0 = 0; c0 < m; c0 += kChunk) {
+    for (int c0 = first; c0 < m; c0 += cstep) {
       const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
       // the chunk's row points are staged while the previous chunk's MMAs
       // run (those read only the operand tiles); then the tiles are free
       // once the MMAs have completed.  The phase moves on only after a wait
       // that succeeded, so a give-up's last wait is on the MMAs in flight.
       stage_chunk_rows<Real>(p, t, S, c0, cnt, ox, oy);
-      if (c0 > 0 && threadIdx.x == 0 && !tc::mbar_wait(&tc_bar, phase, kTcPolls)) tc_ok = 0;
+      if (c0 > first && threadIdx.x == 0 && !tc::mbar_wait(&tc_bar, phase, kTcPolls)) tc_ok = 0;
       __syncthreads();
       if (!tc_ok) break;  // block-uniform
-      if (c0 > 0) phase ^= 1u;
+      if (c0 > first) phase ^= 1u;
       fill_chunk_tc(p, t, S, c0, cnt, npad, bt, bbytes, om, rows, mtiles);
       tc::fence_async_smem();
       __syncthreads();
@@ -1024,7 +1067,7 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
                   tc::smem_desc(a0 + (uint32_t)mt * kTcOmegaTile + 2u * ks * lbo_a, lbo_a, 128);
               const uint64_t bd = tc::smem_desc(b0 + (uint32_t)x * bbytes + 2u * ks * lbo_b, lbo_b, 128);
               tc::mma_bf16(tmem + (uint32_t)(mt * npad), ad, bd, idesc,
-                           (c0 > 0 || x > 0 || ks > 0) ? 1u : 0u);
+                           (c0 > first || x > 0 || ks > 0) ? 1u : 0u);
             }
         tc::mma_commit(&tc_bar);
       }
@@ -1072,7 +1115,7 @@ __global__ void __launch_bounds__(kThreads) id_sketch_kernel(IdParams p) {
     for (int q = 0; q < kMaxTiles; ++q)
 #pragma unroll
       for (int e = 0; e < 16; ++e) acc[q][e] = 0.f;
-    for (int c0 = 0; c0 < m; c0 += kChunk) {
+    for (int c0 = first; c0 < m; c0 += cstep) {
       const int cnt = m - c0 < kChunk ? m - c0 : kChunk;
       fill_chunk<Real>(p, t, S, ld, c0, cnt, ox, oy);
       for (TileWalk w(lp); w.j < kChunk; w.next()) {
@@ -1431,6 +1474,25 @@ static void launch_split_pass(const IdParams& p, int num_tasks, int nmax, cudaSt
   }
 }
 
+// A level of few boxes: the rows of each box over p.row_groups CTAs, each
+// writing a partial sketch, then one CTA per box sums them and runs the
+// pivoted QR, Z and the outputs.
+template <int TS>
+static void launch_grouped_t(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
+  const dim3 grid(num_tasks, p.row_groups);
+  if (p.tc) {
+    set_smem_once<id_sketch_kernel<TS, true, true>>();
+    id_sketch_kernel<TS, true, true><<<grid, kThreads, id_sketch_split_smem(nmax, true), st>>>(p);
+  } else {
+    set_smem_once<id_sketch_kernel<TS, true, false>>();
+    id_sketch_kernel<TS, true, false>
+        <<<grid, kThreads, id_sketch_split_smem(nmax, false), st>>>(p);
+  }
+  IdParams q = p;
+  q.y_parts = p.row_groups;
+  launch_sketch_t<TS>(q, num_tasks, id_sketch_smem(nmax, p.tc != 0), st);
+}
+
 template <int TS>
 static void launch_split_t(const IdParams& p, int num_tasks, int nmax, cudaStream_t st) {
   launch_split_pass<TS>(p, num_tasks, nmax, st);
@@ -1581,6 +1643,14 @@ int launch_id(const IdParams& p, int num_tasks, int nmax, size_t smem, bool fp32
   if (num_tasks <= 0) return 0;
   const int passes = p.redo != nullptr ? 2 : 1;
   const int ts = team_size(nmax);
+  // A level of few boxes: each box's rows over p.row_groups CTAs (partial
+  // sketches), then the CTA-per-box QR on their sum.
+  if (fp32 && p.dense == nullptr && id_sketch_ok(nmax) && p.sketch_y != nullptr &&
+      p.row_groups > 1 && p.redo == nullptr) {
+    if (ts == 4) launch_grouped_t<4>(p, num_tasks, nmax, st);
+    else launch_grouped_t<2>(p, num_tasks, nmax, st);
+    return 2;
+  }
   // The warp-per-box QR pays off when a level has boxes enough to fill the
   // GPU; small levels keep the lower-latency CTA-per-box QR.
   if (fp32 && p.dense == nullptr && id_sketch_ok(nmax) && p.sketch_y != nullptr &&

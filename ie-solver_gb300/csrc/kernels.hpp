@@ -48,6 +48,14 @@ struct IdParams {
   // FP32 sketched ID: levels of at least this many boxes run the pivoted QR
   // one warp per box (id_cpqr_warp_kernel), smaller ones one CTA per box
   int split_min_tasks;
+  // FP32 sketched ID of a level of few boxes: row_groups >= 2 splits each
+  // box's ID matrix rows (its 64-row chunks, round robin) over that many
+  // CTAs, each writing a partial sketch at sketch_y + y_off + g *
+  // y_group_stride; the CTA-per-box QR then sums the y_parts partial
+  // sketches in order instead of forming the sketch itself.
+  int row_groups;
+  int y_parts;
+  int64_t y_group_stride;
 };
 
 struct DecoupleParams {

@@ -908,6 +908,24 @@ rs_status factor_impl(rs_solver* s) {
     auto id_fits = [&](int n) { return id_kernel_smem(n, f32, true) <= kSmemMax; };
     auto dc_fits = [&](int n) { return decouple_kernel_smem(n, f32, true) <= kSmemMax; };
     const bool small_level = (int)idt_s.size() < s->num_sms;
+    // A level of fewer ID boxes than SMs (no learned sizes there): each box's
+    // ID matrix rows go to several CTAs, about two CTAs per SM in all, at
+    // most one per 64-row chunk.
+    ip.row_groups = 1;
+    ip.y_parts = 0;
+    ip.y_group_stride = (int64_t)y_need;
+    if (f32 && small_level && ip.redo == nullptr && y_need > 0 && s->cfg.id_row_groups != 0 &&
+        s->cfg.id_row_groups != 1) {
+      int chunks = 1;
+      for (const IdTask& t : idt_s)
+        chunks = std::max(chunks, (2 * t.q + (t.use_proxy ? 2 * prow : 0) + 63) / 64);
+      const int want = s->cfg.id_row_groups > 0
+                           ? s->cfg.id_row_groups
+                           : (2 * s->num_sms) / std::max<int>(1, (int)idt_s.size());
+      ip.row_groups = std::max(1, std::min({chunks, want, 16}));
+      if (ip.row_groups > 1) CU(s->sketch_y.ensure((size_t)ip.row_groups * y_need));
+      ip.sketch_y = s->sketch_y.p;
+    }
     auto id_launch = [&](const IdTask* dt, int cnt, int nmax) {
       IdParams q = ip;
       q.tasks = dt;
@@ -2009,6 +2027,7 @@ void rs_config_default(rs_config* c) {
   c->root_inverse = 1;
   c->rank_judge = 4.0;
   c->tensor_cores = 1;
+  c->id_row_groups = -1;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -2025,7 +2044,7 @@ rs_status rs_create(const rs_config* cfg, rs_solver** out) {
   if (!(cfg->rank_headroom >= 1.0 && cfg->rank_headroom <= 4.0) || cfg->rank_extra_rows < 0 ||
       cfg->rank_extra_rows > 128 || cfg->refine_solver < 0 || cfg->refine_solver > 2 ||
       !(cfg->rank_judge >= 0.0 && cfg->rank_judge <= 1e6) || cfg->tensor_cores < 0 ||
-      cfg->tensor_cores > 1)
+      cfg->tensor_cores > 1 || cfg->id_row_groups < -1 || cfg->id_row_groups > 16)
     return RS_ERR_ARG;
   rs_solver* s = new rs_solver();
   s->cfg = *cfg;

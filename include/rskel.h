@@ -97,6 +97,12 @@ typedef struct {
                                 Y = Omega A runs on the tensor cores (tcgen05.mma, BF16
                                 operands with A split in three BF16 parts, FP32 accumulation
                                 in tensor memory); 0 = on the CUDA cores (FP32 FMA) */
+  int id_row_groups;         /* RS_FP32_REFINE, levels with fewer ID boxes than SMs: each
+                                box's ID matrix rows (its 64-row chunks, round robin) are
+                                sketched by this many CTAs, whose partial sketches the pivoted
+                                QR sums in a fixed order.  -1 (default) = about two CTAs per
+                                SM over the level, at most one per chunk and 16 per box;
+                                0 or 1 = one CTA per box; 2..16 = that many */
 } rs_config;
 
 typedef struct rs_solver rs_solver;

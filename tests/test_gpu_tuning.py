@@ -5,6 +5,8 @@
 * With and without the CUDA graph of the factorization's inverse, the
   refined solutions are bit-identical (the graph replays the same
   launches).
+* The small levels' ID sketch split over several CTAs per box gives the
+  ranks of one CTA per box and the same refined solution.
 """
 import numpy as np
 import pytest
@@ -83,3 +85,45 @@ def test_root_inverse_and_root_lu_agree(solver_lib):
         assert s.stats()["refine_residual"] <= 1e-10
         out.append(mu)
     assert np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[1]) <= 1e-9
+
+
+def _levels_ranks(s):
+    """(level, num_skel) of every compressed box, in node order."""
+    out = []
+    for i in range(s.num_nodes()):
+        info, _, _ = s.node_info(i)
+        if info[7]:
+            out.append((int(info[0]), int(info[8])))
+    return out
+
+
+def test_row_groups_sketch_matches_one_cta_per_box(solver_lib):
+    """The small levels' sketch split over several CTAs per box (id_row_groups)
+    sums the same rows of the same signs in another order.  At FP32 ID
+    tolerance 1e-4 (far above the sketch's rounding) the ranks of nearly every
+    box agree with one CTA per box; at the default 1e-6 (where rounding of
+    order 1e-7 |R_00| moves ranks near the threshold) the rank totals agree
+    within 1 % and both refined solutions match to 1e-9."""
+    from rskel import geometry as g
+
+    capi = solver_lib
+    for id_tol in (1e-4, 1e-6):
+        sols, ranks = {}, {}
+        for rg in (0, -1, 5):
+            s, F = _star(capi, g, id_row_groups=rg, fp32_id_tol=id_tol)
+            s.factor()
+            sols[rg], _ = s.solve(F)
+            assert s.stats()["refine_residual"] <= 1e-10
+            ranks[rg] = _levels_ranks(s)
+            s.close()
+        for rg in (-1, 5):
+            a, b = ranks[0], ranks[rg]
+            assert len(a) == len(b) and [x[0] for x in a] == [x[0] for x in b]
+            diff = [abs(x[1] - y[1]) for x, y in zip(a, b)]
+            if id_tol == 1e-4:
+                assert max(diff) <= 1 and sum(d > 0 for d in diff) <= max(2, len(diff) // 50), rg
+            else:
+                ka, kb = sum(x[1] for x in a), sum(x[1] for x in b)
+                assert abs(ka - kb) <= 0.01 * ka, (rg, ka, kb)
+                err = np.linalg.norm(sols[rg] - sols[0]) / np.linalg.norm(sols[0])
+                assert err <= 1e-9, (rg, err)
