@@ -48,6 +48,12 @@ import sys
 import threading
 import time
 
+# OpenMP threads of the host planner (and of the CPU arms) spin between
+# their short parallel regions instead of sleeping (rskel.capi's loader sets
+# the same default; set here before any OpenMP library is loaded)
+if "OMP_WAIT_POLICY" not in os.environ:
+    os.environ.setdefault("GOMP_SPINCOUNT", "100000000")
+
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
