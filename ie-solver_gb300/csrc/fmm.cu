@@ -640,6 +640,10 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     FmmArgs<R> a, Geo<double> g, const double* mu, double* y, double ya, double yb,
     const double* r1, double* nearsum, int nbox) {
   __shared__ double part[kEvalWarps - 1][32][kMaxRhs];
+  // each warp's copy of the expansion it evaluates (one right-hand side of
+  // one box, orders up to 64): the Horner chains below then read shared
+  // memory, not a global load per step
+  __shared__ R wexp[kPart == kEvalNear ? 1 : kEvalWarps][2 * 64];
   pdl_launch_dependents();  // (expansions are read after pdl_wait below)
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   // one leaf per CTA, or (a grid smaller than the leaf count) leaves
@@ -668,11 +672,15 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     // rolled and its result added through an unrolled select, which keeps
     // the kernel's code small)
     const Cx<R> rho = cscale(vec(tp), isB);
+    R* wx = wexp[wp];
 #pragma unroll 1
     for (int qq = wp; qq < nrhs; qq += kEvalWarps) {
       const R* L = a.local + 2 * (size_t)p * (qq + nrhs * (size_t)B);
-      Cx<R> h = ld_c(L, p - 1);
-      for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(L, l));
+      __syncwarp();  // the previous expansion's reads are done
+      for (int e = lane; e < 2 * p; e += 32) wx[e] = L[e];
+      __syncwarp();
+      Cx<R> h = ld_c(wx, p - 1);
+      for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(wx, l));
       const R v = cmul(tnu, h).re;
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q)
@@ -700,8 +708,11 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
 #pragma unroll 1
         for (int qq = wp; qq < nrhs; qq += kEvalWarps) {
           const R* M = a.mpole + 2 * (size_t)p * (qq + nrhs * (size_t)C);
-          Cx<R> h = ld_c(M, p - 1);
-          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, tw), ld_c(M, k));
+          __syncwarp();
+          for (int e = lane; e < 2 * p; e += 32) wx[e] = M[e];
+          __syncwarp();
+          Cx<R> h = ld_c(wx, p - 1);
+          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, tw), ld_c(wx, k));
           const R v = cmul(tnu, cmul(h, iw)).re;
 #pragma unroll
           for (int q = 0; q < kMaxRhs; ++q)
