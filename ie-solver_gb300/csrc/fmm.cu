@@ -640,10 +640,10 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     FmmArgs<R> a, Geo<double> g, const double* mu, double* y, double ya, double yb,
     const double* r1, double* nearsum, int nbox) {
   __shared__ double part[kEvalWarps - 1][32][kMaxRhs];
-  // each warp's copy of the expansion it evaluates (one right-hand side of
+  // each warp's copy of the expansions it evaluates (two right-hand sides of
   // one box, orders up to 64): the Horner chains below then read shared
   // memory, not a global load per step
-  __shared__ R wexp[kPart == kEvalNear ? 1 : kEvalWarps][2 * 64];
+  __shared__ R wexp[kPart == kEvalNear ? 1 : kEvalWarps][4 * 64];
   pdl_launch_dependents();  // (expansions are read after pdl_wait below)
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   // one leaf per CTA, or (a grid smaller than the leaf count) leaves
@@ -668,23 +668,34 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     }
     pdl_wait();
     if constexpr (kPart != kEvalNear) {
-    // L2P (right-hand sides q = wp, wp + kEvalWarps, ...; the loop is kept
-    // rolled and its result added through an unrolled select, which keeps
-    // the kernel's code small)
+    // L2P (right-hand sides q = wp, wp + kEvalWarps, ...; two of them at a
+    // time, whose Horner chains interleave; the loop is kept rolled and its
+    // results added through an unrolled select, which keeps the kernel's
+    // code small)
     const Cx<R> rho = cscale(vec(tp), isB);
     R* wx = wexp[wp];
+    R* wy = wx + 2 * p;
 #pragma unroll 1
-    for (int qq = wp; qq < nrhs; qq += kEvalWarps) {
+    for (int qq = wp; qq < nrhs; qq += 2 * kEvalWarps) {
+      const int q2 = qq + kEvalWarps;
+      const bool two = q2 < nrhs;
       const R* L = a.local + 2 * (size_t)p * (qq + nrhs * (size_t)B);
-      __syncwarp();  // the previous expansion's reads are done
+      __syncwarp();  // the previous expansions' reads are done
       for (int e = lane; e < 2 * p; e += 32) wx[e] = L[e];
+      if (two)
+        for (int e = lane; e < 2 * p; e += 32) wy[e] = L[2 * (size_t)p * kEvalWarps + e];
       __syncwarp();
-      Cx<R> h = ld_c(wx, p - 1);
-      for (int l = p - 2; l >= 0; --l) h = cadd(cmul(h, rho), ld_c(wx, l));
-      const R v = cmul(tnu, h).re;
+      Cx<R> h = ld_c(wx, p - 1), g2 = two ? ld_c(wy, p - 1) : Cx<R>{(R)0, (R)0};
+      for (int l = p - 2; l >= 0; --l) {
+        h = cadd(cmul(h, rho), ld_c(wx, l));
+        if (two) g2 = cadd(cmul(g2, rho), ld_c(wy, l));
+      }
+      const R v = cmul(tnu, h).re, v2 = cmul(tnu, g2).re;
 #pragma unroll
-      for (int q = 0; q < kMaxRhs; ++q)
+      for (int q = 0; q < kMaxRhs; ++q) {
         if (q == qq) phi[q] += v;
+        if (two && q == q2) phi[q] += v2;
+      }
     }
     // M2P from the W list (the same split).  Box offsets and sides need FP64
     // arithmetic (slow on this GPU), so lane l forms them for the list's l-th
@@ -706,17 +717,26 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         const Cx<R> iw = cinv(cadd(vec(tp), oc));  // z - c_C
         const Cx<R> tw = cscale(iw, sc);
 #pragma unroll 1
-        for (int qq = wp; qq < nrhs; qq += kEvalWarps) {
+        for (int qq = wp; qq < nrhs; qq += 2 * kEvalWarps) {
+          const int q2 = qq + kEvalWarps;
+          const bool two = q2 < nrhs;
           const R* M = a.mpole + 2 * (size_t)p * (qq + nrhs * (size_t)C);
           __syncwarp();
           for (int e = lane; e < 2 * p; e += 32) wx[e] = M[e];
+          if (two)
+            for (int e = lane; e < 2 * p; e += 32) wy[e] = M[2 * (size_t)p * kEvalWarps + e];
           __syncwarp();
-          Cx<R> h = ld_c(wx, p - 1);
-          for (int k = p - 2; k >= 0; --k) h = cadd(cmul(h, tw), ld_c(wx, k));
-          const R v = cmul(tnu, cmul(h, iw)).re;
+          Cx<R> h = ld_c(wx, p - 1), g2 = two ? ld_c(wy, p - 1) : Cx<R>{(R)0, (R)0};
+          for (int k = p - 2; k >= 0; --k) {
+            h = cadd(cmul(h, tw), ld_c(wx, k));
+            if (two) g2 = cadd(cmul(g2, tw), ld_c(wy, k));
+          }
+          const R v = cmul(tnu, cmul(h, iw)).re, v2 = cmul(tnu, cmul(g2, iw)).re;
 #pragma unroll
-          for (int q = 0; q < kMaxRhs; ++q)
+          for (int q = 0; q < kMaxRhs; ++q) {
             if (q == qq) phi[q] += v;
+            if (two && q == q2) phi[q] += v2;
+          }
         }
       }
     }
