@@ -282,28 +282,131 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
     }
     __syncthreads();
     const int hr = (r + 1) >> 1;
-    for (int j = 0; j < r; ++j) {
-      const int buf = j & 1;
-      const float* cb = colbuf[buf];
-      // every warp finds the pivot row itself (no barrier for a broadcast):
-      // the largest |X(i, j)| over rows not yet pivots, ties to the smallest
-      // position.  Non-negative floats order as their bit patterns, so two
-      // warp reductions give it: the largest value, then the smallest
-      // position holding it.  A NaN's pattern lies above infinity's.
+    // Pivot search of one step, by every warp (no barrier for a broadcast):
+    // the largest |value| over rows whose position is at least j, ties to the
+    // smallest position.  Non-negative floats order as their bit patterns, so
+    // two warp reductions give it: the largest value, then the smallest
+    // position holding it.  A NaN's pattern lies above infinity's.  val(i)
+    // and pos_of(i) give a row's candidate value and position.
+    auto pivot_search = [&](int j, auto val, auto pos_of, unsigned* wpos_out) -> bool {
       unsigned best = 0u, bpos = 0xffffffffu;
       for (int i = lane; i < r; i += 32) {
-        const unsigned ps = (unsigned)pos[i];
+        const float v = val(i);  // (evaluated for every row: val may store it)
+        const unsigned ps = (unsigned)pos_of(i);
         if (ps < (unsigned)j) continue;
-        const unsigned v = __float_as_uint(fabsf(cb[i]));
-        if (v > best || (v == best && ps < bpos)) {
-          best = v;
+        const unsigned u = __float_as_uint(fabsf(v));
+        if (u > best || (u == best && ps < bpos)) {
+          best = u;
           bpos = ps;
         }
       }
       const unsigned wbest = __reduce_max_sync(0xffffffffu, best);
-      const unsigned wpos = __reduce_min_sync(0xffffffffu, best == wbest ? bpos : 0xffffffffu);
-      const bool ok = wbest != 0u && wbest < 0x7f800000u;  // non-zero and finite
-      const int pr = ok ? row_at[wpos] : row_at[j];       // a singular block: any row, flagged
+      *wpos_out = __reduce_min_sync(0xffffffffu, best == wbest ? bpos : 0xffffffffu);
+      return wbest != 0u && wbest < 0x7f800000u;  // non-zero and finite
+    };
+    // the interchange of positions j and pos[pr] (thread 0)
+    auto interchange = [&](int j, int pr) {
+      const int q = row_at[j], pp = pos[pr];
+      row_at[pp] = q;
+      pos[q] = pp;
+      row_at[j] = pr;
+      pos[pr] = j;
+    };
+    // Steps in pairs (j, j + 1): step j's pivot from column j; column j + 1
+    // as step j leaves it, b'(i) = X(i, j+1) - X(i, j) R1(j+1), formed by
+    // every warp (warp 0 keeps it in colb2), gives step j + 1's pivot among
+    // the positions step j's interchange leaves; both scaled pivot rows R1,
+    // R2 are formed before one barrier, and one pass applies both steps to
+    // every element.  Each element sees the same operations in the same
+    // order as two single steps would apply, so the result is the same.
+    float* colb2 = T;  // (T's bytes are free until U_f is written)
+    float* rb1 = rowbuf[0];
+    float* rb2 = rowbuf[1];
+    int cur = 0;  // colbuf[cur] holds the current column j
+    int j = 0;
+    for (; j + 1 < r; j += 2) {
+      const float* cb = colbuf[cur];
+      float* cn = colbuf[cur ^ 1];  // column j + 2 after both steps
+      unsigned wpos1 = 0, wpos2 = 0;
+      const bool ok1 = pivot_search(j, [&](int i) { return cb[i]; },
+                                    [&](int i) { return pos[i]; }, &wpos1);
+      const int p1 = ok1 ? row_at[wpos1] : row_at[j];  // a singular block: any row, flagged
+      const Real d1 = Mrr[p1 + ld * j];
+      const Real inv1 = d1 != (Real)0 ? (Real)1 / d1 : (Real)0;
+      const Real r1n = Mrr[p1 + ld * (j + 1)] * inv1;  // R1(j + 1)
+      // positions after step j's interchange
+      const int q1 = row_at[j], pp1 = pos[p1];
+      const bool ok2 = pivot_search(
+          j + 1,
+          [&](int i) {
+            const float bv = i == p1 ? r1n : Mrr[i + ld * (j + 1)] - cb[i] * r1n;
+            if (warp == 0) colb2[i] = bv;
+            return bv;
+          },
+          [&](int i) { return i == p1 ? j : (i == q1 ? pp1 : pos[i]); }, &wpos2);
+      const int at_j1 = j + 1 == pp1 ? q1 : row_at[j + 1];
+      const int p2 = ok2 ? ((int)wpos2 == pp1 ? q1 : row_at[wpos2]) : at_j1;
+      const Real d2 = Mrr[p2 + ld * (j + 1)] - cb[p2] * r1n;
+      const Real inv2 = d2 != (Real)0 ? (Real)1 / d2 : (Real)0;
+      if (threadIdx.x == 0) {
+        piv[j] = p1;
+        piv[j + 1] = p2;
+        if (!ok1 || !ok2) scal[0] = 1.0;
+      }
+      const Real ap2 = cb[p2];
+      for (int c = threadIdx.x; c < r; c += blockDim.x) {
+        const Real r1c = c == j ? inv1 : Mrr[p1 + ld * c] * inv1;
+        const Real m2 = (c == j ? (Real)0 : Mrr[p2 + ld * c]) - ap2 * r1c;
+        rb1[c] = r1c;
+        rb2[c] = c == j + 1 ? inv2 : m2 * inv2;
+      }
+      __syncthreads();
+      // (every warp has read pos for this pair by now)
+      if (threadIdx.x == 0) {
+        interchange(j, p1);
+        interchange(j + 1, p2);
+      }
+      if (r > 0)
+        for (TileWalk w(hr); w.j < hr; w.next()) {
+          const int i0 = w.i, c0 = w.j;
+          const bool ri = i0 + hr < r, rc = c0 + hr < r;
+          const int i1 = ri ? i0 + hr : i0, c1 = rc ? c0 + hr : c0;
+          const Real a0 = cb[i0], a1 = cb[i1], e0 = colb2[i0], e1 = colb2[i1];
+          const Real f0 = rb1[c0], f1 = rb1[c1], g0 = rb2[c0], g1 = rb2[c1];
+          Real m[4] = {Mrr[i0 + ld * c0], Mrr[i1 + ld * c0], Mrr[i0 + ld * c1],
+                       Mrr[i1 + ld * c1]};
+          const int ii[4] = {i0, i1, i0, i1}, cc[4] = {c0, c0, c1, c1};
+          const Real aa[4] = {a0, a1, a0, a1}, ee[4] = {e0, e1, e0, e1};
+          const Real ff[4] = {f0, f0, f1, f1}, gg[4] = {g0, g0, g1, g1};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            Real v = cc[q] == j ? (Real)0 : m[q];
+            v = ii[q] == p1 ? ff[q] : v - aa[q] * ff[q];      // step j
+            v = cc[q] == j + 1 ? (Real)0 : v;
+            m[q] = ii[q] == p2 ? gg[q] : v - ee[q] * gg[q];  // step j + 1
+          }
+          Mrr[i0 + ld * c0] = m[0];
+          if (ri) Mrr[i1 + ld * c0] = m[1];
+          if (rc) Mrr[i0 + ld * c1] = m[2];
+          if (ri && rc) Mrr[i1 + ld * c1] = m[3];
+          if (c0 == j + 2) {
+            cn[i0] = m[0];
+            if (ri) cn[i1] = m[1];
+          }
+          if (rc && c1 == j + 2) {
+            cn[i0] = m[2];
+            if (ri) cn[i1] = m[3];
+          }
+        }
+      __syncthreads();
+      cur ^= 1;
+    }
+    if (j < r) {  // the last step of an odd r, alone
+      const float* cb = colbuf[cur];
+      unsigned wpos = 0;
+      const bool ok = pivot_search(j, [&](int i) { return cb[i]; },
+                                   [&](int i) { return pos[i]; }, &wpos);
+      const int pr = ok ? row_at[wpos] : row_at[j];
       if (threadIdx.x == 0) {
         piv[j] = pr;
         if (!ok) scal[0] = 1.0;
@@ -311,27 +414,15 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
       const Real d = Mrr[pr + ld * j];
       const Real inv = d != (Real)0 ? (Real)1 / d : (Real)0;
       for (int c = threadIdx.x; c < r; c += blockDim.x)
-        rowbuf[buf][c] = c == j ? inv : Mrr[pr + ld * c] * inv;
+        rb1[c] = c == j ? inv : Mrr[pr + ld * c] * inv;
       __syncthreads();
-      // (every warp has read pos for this step by now): the interchange of
-      // positions j and pos[pr]
-      if (threadIdx.x == 0) {
-        const int q = row_at[j], pp = pos[pr];
-        row_at[pp] = q;
-        pos[q] = pp;
-        row_at[j] = pr;
-        pos[pr] = j;
-      }
-      // the update on 2 x 2 tiles {i, i + hr} x {c, c + hr}: all four
-      // elements are loaded before any is stored
-      const float* rb = rowbuf[buf];
-      float* cn = colbuf[buf ^ 1];
+      if (threadIdx.x == 0) interchange(j, pr);
       if (r > 0)
         for (TileWalk w(hr); w.j < hr; w.next()) {
           const int i0 = w.i, c0 = w.j;
           const bool ri = i0 + hr < r, rc = c0 + hr < r;
           const int i1 = ri ? i0 + hr : i0, c1 = rc ? c0 + hr : c0;
-          const Real a0 = cb[i0], a1 = cb[i1], b0 = rb[c0], b1 = rb[c1];
+          const Real a0 = cb[i0], a1 = cb[i1], b0 = rb1[c0], b1 = rb1[c1];
           Real m00 = Mrr[i0 + ld * c0], m10 = Mrr[i1 + ld * c0];
           Real m01 = Mrr[i0 + ld * c1], m11 = Mrr[i1 + ld * c1];
           if (c0 == j) m00 = m10 = (Real)0;
@@ -344,14 +435,6 @@ __global__ void __launch_bounds__(kThreads) decouple_kernel(DecoupleParams p) {
           if (ri) Mrr[i1 + ld * c0] = m10;
           if (rc) Mrr[i0 + ld * c1] = m01;
           if (ri && rc) Mrr[i1 + ld * c1] = m11;
-          if (c0 == j + 1) {
-            cn[i0] = m00;
-            if (ri) cn[i1] = m10;
-          }
-          if (rc && c1 == j + 1) {
-            cn[i0] = m01;
-            if (ri) cn[i1] = m11;
-          }
         }
       __syncthreads();
     }
