@@ -627,10 +627,25 @@ void launch_decouple(const DecoupleParams& p, int num_tasks, size_t smem, bool f
     set_smem_once<decouple_kernel<double>>();
   int nt = threads == 128 ? 128 : kThreads;
   if (threads == 0) {
-    int per_sm = 0;
-    const void* fn = fp32 ? (const void*)decouple_kernel<float> : (const void*)decouple_kernel<double>;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem) != cudaSuccess)
-      per_sm = 0;
+    // 256-thread CTAs per SM for this shared-memory size, from a small
+    // per-thread cache (the occupancy query is a driver call per launch)
+    struct Occ {
+      size_t smem;
+      int fp32, per_sm;
+    };
+    static thread_local Occ cache[16];
+    static thread_local int cached = 0;
+    int per_sm = -1;
+    for (int q = 0; q < cached; ++q)
+      if (cache[q].smem == smem && cache[q].fp32 == (int)fp32) per_sm = cache[q].per_sm;
+    if (per_sm < 0) {
+      const void* fn =
+          fp32 ? (const void*)decouple_kernel<float> : (const void*)decouple_kernel<double>;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem) != cudaSuccess)
+        per_sm = 0;
+      cache[cached % 16] = Occ{smem, (int)fp32, per_sm};
+      cached = cached < 16 ? cached + 1 : 16;
+    }
     if (per_sm > 0 && num_tasks > per_sm * num_sms) nt = 128;
   }
   if (fp32)

@@ -104,6 +104,8 @@ struct rs_solver {
   DevBuf<int> dofs, perm, ranks, piv, status;
   DevBuf<IdTask> id_tasks;
   DevBuf<DecoupleTask> dc_tasks;
+  // a level's ID and elimination task records, uploaded together (one copy)
+  DevBuf<unsigned char> lvl_tasks;
   HostBuf<int> h_ranks, h_perm, h_status;
   size_t piv_used = 0;
   Factor<double> F64;
@@ -463,6 +465,26 @@ cudaError_t stage_copy(rs_solver* s, void* dst, const void* src, size_t bytes) {
     off = 0;
   }
   std::memcpy(s->stage.p + off, src, bytes);
+  s->stage_used = off + bytes;
+  return cudaMemcpyAsync(dst, s->stage.p + off, bytes, cudaMemcpyHostToDevice, s->stream);
+}
+
+// Two host arrays to one device buffer, the second at byte offset off2 of
+// it, through the staging ring with one copy.
+cudaError_t stage_copy2(rs_solver* s, void* dst, const void* src1, size_t bytes1,
+                        const void* src2, size_t off2, size_t bytes2) {
+  const size_t bytes = bytes2 ? off2 + bytes2 : bytes1;
+  if (!bytes) return cudaSuccess;
+  size_t off = (s->stage_used + 255) & ~size_t(255);
+  if (off + bytes > s->stage.cap) {
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return e;
+    e = s->stage.ensure(std::max<size_t>(2 * s->stage.cap, bytes + 4096));
+    if (e != cudaSuccess) return e;
+    off = 0;
+  }
+  if (bytes1) std::memcpy(s->stage.p + off, src1, bytes1);
+  if (bytes2) std::memcpy(s->stage.p + off + off2, src2, bytes2);
   s->stage_used = off + bytes;
   return cudaMemcpyAsync(dst, s->stage.p + off, bytes, cudaMemcpyHostToDevice, s->stream);
 }
@@ -845,11 +867,15 @@ rs_status factor_impl(rs_solver* s) {
     e_prev = F.e_used;
     piv_prev = s->piv_used;
     if (scratch_need) CU(F.scratch.ensure(scratch_need));
-    CU(s->id_tasks.ensure(std::max<size_t>(idt_s.size(), 1)));
-    CU(s->dc_tasks.ensure(dct_s.size()));
+    // the level's ID and elimination task records in one buffer, one copy
+    const size_t idt_bytes = idt_s.size() * sizeof(IdTask);
+    const size_t dct_off = (std::max<size_t>(idt_bytes, 1) + 255) & ~size_t(255);
+    CU(s->lvl_tasks.ensure(dct_off + std::max<size_t>(dct_s.size(), 1) * sizeof(DecoupleTask)));
+    IdTask* const d_idt = reinterpret_cast<IdTask*>(s->lvl_tasks.p);
+    DecoupleTask* const d_dct = reinterpret_cast<DecoupleTask*>(s->lvl_tasks.p + dct_off);
     CU(s->ranks.ensure(std::max<size_t>(idt_s.size(), 1)));
-    CU(stage_copy(s, s->id_tasks.p, idt_s.data(), idt_s.size() * sizeof(IdTask)));
-    CU(stage_copy(s, s->dc_tasks.p, dct_s.data(), dct_s.size() * sizeof(DecoupleTask)));
+    CU(stage_copy2(s, s->lvl_tasks.p, idt_s.data(), idt_bytes, dct_s.data(), dct_off,
+                   dct_s.size() * sizeof(DecoupleTask)));
     if (!witems.empty()) {
       CU(s->wide_items.ensure(witems.size()));
       CU(s->wide_part.ensure(part_need));
@@ -862,7 +888,7 @@ rs_status factor_impl(rs_solver* s) {
       CU(s->ell_slot.ensure(idt_s.size()));
       CU(stage_copy(s, s->rank_feat.p, feat_s.data(), feat_s.size() * sizeof(float)));
       CU(cudaMemsetAsync(s->redo.p, 0, idt_s.size() * sizeof(int), s->stream));
-      CU(rank_infer_ell(s->rank_w.p, s->rank_feat.p, s->id_tasks.p, (int)idt_s.size(),
+      CU(rank_infer_ell(s->rank_w.p, s->rank_feat.p, d_idt, (int)idt_s.size(),
                         s->ell_slot.p, (float)s->cfg.rank_headroom, s->cfg.rank_extra_rows,
                         s->stream));
       ++s->launches;
@@ -874,7 +900,7 @@ rs_status factor_impl(rs_solver* s) {
     ip.sd = s->sd;
     ip.npp = s->cfg.num_proxy_points;
     ip.tol = tol;
-    ip.tasks = s->id_tasks.p;
+    ip.tasks = d_idt;
     ip.dofs = s->dofs.p;
     ip.pxy_cos = s->pxy_c.p;
     ip.pxy_sin = s->pxy_s.p;
@@ -936,14 +962,14 @@ rs_status factor_impl(rs_solver* s) {
       // the three ranges: up to 128 columns, wide, wider
       const std::vector<IdTask> lo(idt_s.begin(), idt_s.begin() + w0);
       const std::vector<IdTask> hi(idt_s.begin() + w1, idt_s.end());
-      launch_binned(lo, s->id_tasks.p, id_fits, id_launch, small_level);
+      launch_binned(lo, d_idt, id_fits, id_launch, small_level);
       IdParams q = ip;
-      q.tasks = s->id_tasks.p + w0;
+      q.tasks = d_idt + w0;
       s->launches += launch_id_wide(q, (int)(w1 - w0), idt_s[w1 - 1].n, s->wide_items.p,
                                     (int)witems.size(), s->wide_part.p, s->stream);
-      launch_binned(hi, s->id_tasks.p + w1, id_fits, id_launch, small_level);
+      launch_binned(hi, d_idt + w1, id_fits, id_launch, small_level);
     } else {
-      launch_binned(idt_s, s->id_tasks.p, id_fits, id_launch, small_level);
+      launch_binned(idt_s, d_idt, id_fits, id_launch, small_level);
     }
     CU(cudaGetLastError());
     CU(cudaEventRecord(s->lv_ev[3 * lv + 1], s->stream));
@@ -971,7 +997,7 @@ rs_status factor_impl(rs_solver* s) {
     dp.geo = geo_of(s);
     dp.pde = s->cfg.pde;
     dp.sd = s->sd;
-    dp.tasks = s->dc_tasks.p;
+    dp.tasks = d_dct;
     dp.dofs = s->dofs.p;
     dp.ranks = s->ranks.p;
     dp.perm = s->perm.p;
@@ -985,10 +1011,10 @@ rs_status factor_impl(rs_solver* s) {
       CU(s->dclk.ensure(6 * std::max<size_t>(dct_s.size(), 1)));
       CU(cudaMemsetAsync(s->dclk.p, 0, 6 * dct_s.size() * sizeof(long long), s->stream));
     }
-    launch_binned(dct_s, s->dc_tasks.p, dc_fits, [&](const DecoupleTask* dt, int cnt, int nmax) {
+    launch_binned(dct_s, d_dct, dc_fits, [&](const DecoupleTask* dt, int cnt, int nmax) {
       DecoupleParams q = dp;
       q.tasks = dt;
-      if (s->trace) q.phase_clk = s->dclk.p + 6 * (dt - s->dc_tasks.p);
+      if (s->trace) q.phase_clk = s->dclk.p + 6 * (dt - d_dct);
       bool in_smem = decouple_kernel_smem(nmax, f32, true) <= kSmemMax;
       launch_decouple(q, cnt, decouple_kernel_smem(nmax, f32, in_smem), f32, s->stream,
                       s->elim_threads, s->num_sms);
