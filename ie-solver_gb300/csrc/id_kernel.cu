@@ -357,6 +357,135 @@ __device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Re
   int k = 0;
   Real* v = S.v;
   const int kmax = n < mr ? n : mr;
+  if constexpr (sizeof(Real) == 4) {
+    // FP32 tiles.  Every column's norm below the current row is summed afresh
+    // while its update is applied (one multiply-add per element), so a step's
+    // head, which warp 0 runs while the other warps wait, only picks the
+    // pivot, interchanges the columns and forms the reflector's scalars from
+    // the pivot's norm and its diagonal entry: no reduction over the column
+    // and no reflector vector.  The updates form v(r) = A(r, i) * scale
+    // themselves, the same product the vector held.  A fresh FP32 sum of
+    // squares is accurate to its own size, so |R_ii| near the rank threshold
+    // is as good as the pivot column's own entries (the norm LAPACK's
+    // sgeqp3 forms the same way).
+    float th = 0.f;  // tol |R_00|
+    for (int i = 0; i < kmax; ++i) {
+      const long long t0 = head_clk != nullptr ? clock64() : 0;
+      if (warp == 0) {
+        unsigned bb = 0u;
+        int li = n;
+        for (int c = i + lane; c < n; c += 32) {
+          const unsigned val = __float_as_uint(vn1[c]);
+          if (li == n || val > bb) { bb = val; li = c; }
+        }
+        const unsigned wb = __reduce_max_sync(0xffffffffu, bb);
+        const int bi =
+            (int)__reduce_min_sync(0xffffffffu, li < n && bb == wb ? (unsigned)li : (unsigned)n);
+        const float nrm = vn1[bi];  // |R_ii| (read before the interchange moves vn1[i])
+        if (bi != i) {
+          // eight rows per lane loaded before their stores (the tile may be
+          // in global memory)
+          for (int r0 = lane; r0 < mr; r0 += 256) {
+            Real x[8], y[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int r = r0 + 32 * q;
+              if (r < mr) {
+                x[q] = A[(size_t)r * ld + bi];
+                y[q] = A[(size_t)r * ld + i];
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int r = r0 + 32 * q;
+              if (r < mr) {
+                A[(size_t)r * ld + bi] = y[q];
+                A[(size_t)r * ld + i] = x[q];
+              }
+            }
+          }
+          if (lane == 0) {
+            int tp = S.perm[bi]; S.perm[bi] = S.perm[i]; S.perm[i] = tp;
+            vn1[bi] = vn1[i];
+          }
+        }
+        __syncwarp();
+        const float alpha = A[(size_t)i * ld + i];
+        int stop = 0;
+        if (i == 0) {
+          const double td = fabs(tol * (double)nrm);
+          th = (float)td;
+          if (lane == 0) S.scal[2] = td;
+        } else {
+          stop = nrm < th ? 1 : 0;
+        }
+        const bool below = nrm > fabsf(alpha);  // some entry below the diagonal is non-zero
+        float tau = 0.f, scale = 0.f, beta = 0.f;
+        if (!stop && below) {
+          beta = -copysignf(nrm, alpha);
+          tau = (beta - alpha) / beta;
+          scale = 1.f / (alpha - beta);
+        }
+        if (lane == 0) {
+          if (!stop && below) A[(size_t)i * ld + i] = beta;
+          S.rs[0] = tau;
+          S.rs[1] = scale;
+          S.is[0] = stop;
+        }
+      }
+      __syncthreads();
+      if (head_clk != nullptr) *head_clk += clock64() - t0;
+      if (S.is[0] != 0) { k = i; break; }
+      const float tau = S.rs[0], scale = S.rs[1];
+      for (int c = L.c0; c < n; c += L.cstep) {
+        if (c <= i) continue;
+        float aic = A[(size_t)i * ld + c];
+        float s2 = 0.f;
+        const int r0 = i + 1 + t;
+        if (tau != 0.f) {
+          float part = 0.f;
+          for (int r = r0; r < mr; r += ts) part += (A[(size_t)r * ld + i] * scale) * A[(size_t)r * ld + c];
+          part = team_sum<TS>(part);
+          const float tw = tau * (aic + part);
+          // y(r) -= tw v(r), four rows loaded ahead of their stores, with
+          // the new entries' squares summed
+          int r = r0;
+          for (; r + 3 * ts < mr; r += 4 * ts) {
+            float y[4], x[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              y[q] = A[(size_t)(r + q * ts) * ld + c];
+              x[q] = A[(size_t)(r + q * ts) * ld + i] * scale;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const float yn = y[q] - tw * x[q];
+              A[(size_t)(r + q * ts) * ld + c] = yn;
+              s2 += yn * yn;
+            }
+          }
+          for (; r < mr; r += ts) {
+            const float yn = A[(size_t)r * ld + c] - tw * (A[(size_t)r * ld + i] * scale);
+            A[(size_t)r * ld + c] = yn;
+            s2 += yn * yn;
+          }
+          aic -= tw;
+        } else {
+          for (int r = r0; r < mr; r += ts) {
+            const float a = A[(size_t)r * ld + c];
+            s2 += a * a;
+          }
+        }
+        s2 = team_sum<TS>(s2);
+        if (t == 0) {
+          vn1[c] = sqrtf(s2);
+          A[(size_t)i * ld + c] = aic;
+        }
+      }
+      __syncthreads();
+    }
+    return k;
+  } else {
   for (int i = 0; i < kmax; ++i) {
     const long long t0 = head_clk != nullptr ? clock64() : 0;
     // Warp 0 alone takes the pivot (first index of the largest partial
@@ -516,6 +645,7 @@ __device__ int cpqr_rank(int n, int mr, double tol, const Layout& L, IdShared<Re
     __syncthreads();
   }
   return k;
+  }  // FP64 tiles
 }
 
 template <class Real, int TS>
@@ -1291,14 +1421,18 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
     }
   }
   __syncwarp();
-  const float tol3z = 2.44140625e-4f;
+  // Each column's norm below the current row is summed afresh while its
+  // update is applied (one multiply-add per element, in its own lane), so the
+  // reflector's norm |R_ii|, which sets the rank, is the pivot column's entry
+  // of vn1: no reduction over the column.  A fresh FP32 sum of squares is
+  // accurate to its own size (the norm LAPACK's sgeqp3 forms the same way).
   const int kmax = n < mr ? n : mr;
   int k = 0;
-  double thr = 0.0;   // tol |R_00|, and as a float pair (th, tl) for the steps
-  float th = 0.f, tl = 0.f;
+  double thr = 0.0;  // tol |R_00|
+  float th = 0.f;
   for (int i = 0; i < kmax; ++i) {
-    // pivot: first index of the largest partial norm (norms are >= 0, so
-    // their bit patterns order as their values: two warp reductions)
+    // pivot: first index of the largest norm (norms are >= 0, so their bit
+    // patterns order as their values: two warp reductions)
     unsigned bb = 0u;
     int li = n;
     for (int j = i + lane; j < n; j += 32) {
@@ -1307,6 +1441,8 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
     }
     const unsigned wb = __reduce_max_sync(0xffffffffu, bb);
     const int bi = (int)__reduce_min_sync(0xffffffffu, li < n && bb == wb ? (unsigned)li : (unsigned)n);
+    const float nrm = vn1[bi];  // |R_ii| (read before the interchange moves vn1[i])
+    __syncwarp();
     if (bi != i) {
       for (int r = lane; r < mr; r += 32) {
         const float a = A[(size_t)r * ld + bi];
@@ -1318,39 +1454,33 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
         perm[bi] = perm[i];
         perm[i] = tp;
         vn1[bi] = vn1[i];
-        vn2[bi] = vn2[i];
       }
       __syncwarp();
     }
-    // Householder reflector of column i (rows i..mr-1); |R_ii| sets the rank
-    FPair xs{0.f, 0.f};
-    for (int r = i + 1 + lane; r < mr; r += 32) xs = fp_add(xs, fp_sq(A[(size_t)r * ld + i]));
-    xs = fp_warp_sum(xs);
     const float alpha = A[(size_t)i * ld + i];
-    const FPair nv = fp_sqrt(fp_add(fp_sq(alpha), xs));
     if (i == 0) {
-      thr = fabs(p.tol * ((double)nv.hi + (double)nv.lo));
+      thr = fabs(p.tol * (double)nrm);
       th = (float)thr;
-      tl = (float)(thr - (double)th);
-    } else if (nv.hi < th || (nv.hi == th && nv.lo < tl)) {
+    } else if (nrm < th) {
       k = i;
       break;
     }
+    const bool below = nrm > fabsf(alpha);  // some entry below the diagonal is non-zero
     float tau = 0.f, scale = 0.f, beta = 0.f;
-    if (xs.hi > 0.f) {
-      const float a = alpha;
-      beta = -copysignf(nv.hi, a);
-      tau = (beta - a) / beta;
-      scale = 1.f / (a - beta);
+    if (below) {
+      beta = -copysignf(nrm, alpha);
+      tau = (beta - alpha) / beta;
+      scale = 1.f / (alpha - beta);
     }
     for (int r = i + 1 + lane; r < mr; r += 32) v[r] = A[(size_t)r * ld + i] * scale;
     __syncwarp();
-    if (lane == 0 && xs.hi > 0.f) A[(size_t)i * ld + i] = beta;
+    if (lane == 0 && below) A[(size_t)i * ld + i] = beta;
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       const int j = lane + 32 * c;
       if (j > i && j < n) {
         float aij = A[(size_t)i * ld + j];
+        float s2 = 0.f;
         if (tau != 0.f) {
           float w0 = aij, w1 = 0.f, w2 = 0.f, w3 = 0.f;
           int r = i + 1;
@@ -1362,24 +1492,33 @@ __global__ void __launch_bounds__(kThreads) id_cpqr_warp_kernel(IdParams p, int 
           }
           for (; r < mr; ++r) w0 += v[r] * A[(size_t)r * ld + j];
           const float tw = tau * ((w0 + w1) + (w2 + w3));
-          axpy_sub(A + (size_t)(i + 1) * ld + j, ld, v + i + 1, 1, tw, mr - i - 1);
-          aij -= tw;
-        }
-        // partial norm downdate (dlaqp2), recomputed when it loses accuracy
-        const float v1 = vn1[j];
-        if (v1 != 0.f) {
-          const float v2 = vn2[j];
-          float x = v1 * v1 - aij * aij;
-          x = x < 0.f ? 0.f : x;
-          if (x <= tol3z * v2 * v2) {
-            float s2 = 0.f;
-            for (int q = i + 1; q < mr; ++q) { const float a = A[(size_t)q * ld + j]; s2 += a * a; }
-            vn1[j] = sqrtf(s2);
-            vn2[j] = vn1[j];
-          } else {
-            vn1[j] = sqrtf(x);
+          // y(q) -= tw v(q), four rows loaded ahead of their stores, with the
+          // new entries' squares summed
+          int q = i + 1;
+          for (; q + 3 < mr; q += 4) {
+            float y[4], x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              y[u] = A[(size_t)(q + u) * ld + j];
+              x[u] = v[q + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float yn = y[u] - tw * x[u];
+              A[(size_t)(q + u) * ld + j] = yn;
+              s2 += yn * yn;
+            }
           }
+          for (; q < mr; ++q) {
+            const float yn = A[(size_t)q * ld + j] - tw * v[q];
+            A[(size_t)q * ld + j] = yn;
+            s2 += yn * yn;
+          }
+          aij -= tw;
+        } else {
+          for (int q = i + 1; q < mr; ++q) { const float a = A[(size_t)q * ld + j]; s2 += a * a; }
         }
+        vn1[j] = sqrtf(s2);
         A[(size_t)i * ld + j] = aij;
       }
     }
