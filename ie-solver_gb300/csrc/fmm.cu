@@ -629,12 +629,16 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
 // per product by the charges kernel) is read by a whole warp at one
 // address, so no shared-memory staging and no barrier sit in the pair loop.
 // A leaf of more than 32 points takes several passes.
-// kPart 0 does all of it.  kPart 1 does only the near field (P2P) and
-// stores its sums per (slot, right-hand side) in nearsum; kPart 2 does the
-// far field (L2P, M2P), adds nearsum and finishes: the near field can then
-// run beside the tree passes.
+// kPart 0 does all of it.  With the product split over two streams:
+// kPart 1 does only the near field (P2P) and stores its sums per (slot,
+// right-hand side) in nearsum, as soon as the sources are written; kPart 3
+// does only M2P over the W list and adds its sums to nearsum, as soon as
+// the upward pass is done; kPart 2 does L2P after the downward pass, adds
+// nearsum and finishes.  Only the last is on the product's critical path.
+// The FP32 products, whose passes are short, keep M2P with L2P (kPart 4):
+// there the side stream's M2P finished after the downward pass.
 constexpr int kEvalWarps = 4;
-enum EvalPart : int { kEvalAll = 0, kEvalNear = 1, kEvalFar = 2 };
+enum EvalPart : int { kEvalAll = 0, kEvalNear = 1, kEvalFar = 2, kEvalW = 3, kEvalFarW = 4 };
 template <class R, int kPart>
 __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     FmmArgs<R> a, Geo<double> g, const double* mu, double* y, double ya, double yb,
@@ -667,14 +671,14 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
       tnu = {to_r<R>(g.nx[pt]), to_r<R>(g.ny[pt])};
     }
     pdl_wait();
-    if constexpr (kPart != kEvalNear) {
+    R* wx = wexp[kPart == kEvalNear ? 0 : wp];
+    R* wy = wx + 2 * p;
+    if constexpr (kPart == kEvalAll || kPart == kEvalFar || kPart == kEvalFarW) {
     // L2P (right-hand sides q = wp, wp + kEvalWarps, ...; two of them at a
     // time, whose Horner chains interleave; the loop is kept rolled and its
     // results added through an unrolled select, which keeps the kernel's
     // code small)
     const Cx<R> rho = cscale(vec(tp), isB);
-    R* wx = wexp[wp];
-    R* wy = wx + 2 * p;
 #pragma unroll 1
     for (int qq = wp; qq < nrhs; qq += 2 * kEvalWarps) {
       const int q2 = qq + kEvalWarps;
@@ -697,6 +701,8 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         if (two && q == q2) phi[q] += v2;
       }
     }
+    }  // L2P
+    if constexpr (kPart == kEvalAll || kPart == kEvalW || kPart == kEvalFarW) {
     // M2P from the W list (the same split).  Box offsets and sides need FP64
     // arithmetic (slow on this GPU), so lane l forms them for the list's l-th
     // box and the warp broadcasts them in turn.
@@ -740,8 +746,8 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         }
       }
     }
-    }  // far field
-    if constexpr (kPart != kEvalFar) {
+    }  // M2P
+    if constexpr (kPart == kEvalAll || kPart == kEvalNear) {
     // P2P from the U list: this warp takes every kEvalWarps-th source
     // (offsets broadcast as above)
     using OT = typename OffT<R>::type;
@@ -787,13 +793,14 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) part[wp - 1][lane][q] = (double)phi[q];
     __syncthreads();
-    if (wp == 0 && act && kPart == kEvalNear) {
+    if (wp == 0 && act && (kPart == kEvalNear || kPart == kEvalW)) {
 #pragma unroll
       for (int q = 0; q < kMaxRhs; ++q) {
         if (q < nrhs) {
           double tot = (double)phi[q];
           for (int w = 1; w < kEvalWarps; ++w) tot += part[w - 1][lane][q];
-          nearsum[ts + (size_t)a.npts * q] = tot;
+          double* o = nearsum + ts + (size_t)a.npts * q;
+          *o = kPart == kEvalW ? *o + tot : tot;
         }
       }
     } else if (wp == 0 && act) {
@@ -805,7 +812,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         if (q < nrhs) {
           double tot = (double)phi[q];
           for (int w = 1; w < kEvalWarps; ++w) tot += part[w - 1][lane][q];
-          if (kPart == kEvalFar) tot += nearsum[ts + (size_t)a.npts * q];
+          if (kPart == kEvalFar || kPart == kEvalFarW) tot += nearsum[ts + (size_t)a.npts * q];
           const size_t o = pt + (size_t)a.npts * q;
           const double v = yb * (diag * mu[o] + tot + (a.mode == 1 ? r1[q] : 0.0));
           y[o] = ya == 0.0 ? v : ya * y[o] + v;
@@ -1026,6 +1033,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
         return e;
       if ((e = cudaEventCreateWithFlags(&f.nearq.near, cudaEventDisableTiming)) != cudaSuccess)
         return e;
+      if ((e = cudaEventCreateWithFlags(&f.nearq.mpole, cudaEventDisableTiming)) != cudaSuccess)
+        return e;
     }
   }
   FmmArgs<R> a{};
@@ -1094,7 +1103,9 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
       if ((e = cudaStreamWaitEvent(f.nearq.st, f.nearq.charges, 0)) != cudaSuccess) return e;
       eval_warp_kernel<R, kEvalNear><<<near_grid<R>(nleaves), 32 * kEvalWarps, 0, f.nearq.st>>>(
           a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
-      if ((e = cudaEventRecord(f.nearq.near, f.nearq.st)) != cudaSuccess) return e;
+      if (!std::is_same<R, DF>::value &&
+          (e = cudaEventRecord(f.nearq.near, f.nearq.st)) != cudaSuccess)
+        return e;
     }
     // upward pass
     a.boxes = f.leaves.p;
@@ -1108,6 +1119,16 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
       a.boxes = f.lvl_boxes.p + f.level_off[lv];
       launch_pdl(m2m_kernel<R>, dim3(cnt), dim3(kFmmThreads),
                  sizeof(Cx<R>) * (8 * (size_t)p + 4 * (size_t)p * nch + 4), st, a);
+    }
+    const bool wsplit = split && std::is_same<R, DF>::value;
+    if (wsplit) {
+      // M2P over the W lists on the side stream, once the multipoles are done
+      if ((e = cudaEventRecord(f.nearq.mpole, st)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(f.nearq.st, f.nearq.mpole, 0)) != cudaSuccess) return e;
+      a.boxes = f.leaves.p;
+      eval_warp_kernel<R, kEvalW><<<near_grid<R>(nleaves), 32 * kEvalWarps, 0, f.nearq.st>>>(
+          a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
+      if ((e = cudaEventRecord(f.nearq.near, f.nearq.st)) != cudaSuccess) return e;
     }
     // interactions and downward pass
     if ((e = cudaMemsetAsync(f.local.p, 0, 2 * sizeof(R) * (size_t)p * nch * nb, st)) !=
@@ -1135,8 +1156,12 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
     } else if (split) {
       // the far field, after the near field on the side stream
       if ((e = cudaStreamWaitEvent(st, f.nearq.near, 0)) != cudaSuccess) return e;
-      eval_warp_kernel<R, kEvalFar><<<nleaves, 32 * kEvalWarps, 0, st>>>(
-          a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
+      if (wsplit)
+        eval_warp_kernel<R, kEvalFar><<<nleaves, 32 * kEvalWarps, 0, st>>>(
+            a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
+      else
+        eval_warp_kernel<R, kEvalFarW><<<nleaves, 32 * kEvalWarps, 0, st>>>(
+            a, geo, muq, yq, ya, yb, (const double*)f.r1.p, f.nearsum.p, (int)nleaves);
     } else if (nleaves) {
       launch_pdl(eval_warp_kernel<R, kEvalAll>, dim3(nleaves), dim3(32 * kEvalWarps), 0, st, a,
                  geo, muq, yq, ya, yb, (const double*)f.r1.p, (double*)nullptr, (int)nleaves);

@@ -73,13 +73,14 @@ struct FmmPlan {
   DevBuf<double> r1;           // per right-hand side: the rank-one sums (Neumann, Stokes)
   DevBuf<double> nearsum;      // the near field's sums per (slot, rhs), Laplace and Neumann
   HostBuf<unsigned char> stage;  // pinned staging of the plan's uploads
-  // The near field (P2P) of a Laplace or Neumann product runs on a side
-  // stream of the lowest priority, beside the tree passes (P2M, M2M, M2L,
-  // L2L) on the caller's stream: those are chains of small launches whose
-  // latency leaves most SMs idle.  Created on first use.
+  // The near field (P2P) of a Laplace or Neumann product, and its M2P over
+  // the W lists once the upward pass is done, run on a side stream of the
+  // lowest priority, beside the tree passes (P2M, M2M, M2L, L2L) on the
+  // caller's stream: those are chains of small launches whose latency leaves
+  // most SMs idle.  Created on first use.
   struct SideStream {
     cudaStream_t st = nullptr;
-    cudaEvent_t charges = nullptr, near = nullptr;
+    cudaEvent_t charges = nullptr, near = nullptr, mpole = nullptr;
     SideStream() = default;
     SideStream(const SideStream&) = delete;
     SideStream& operator=(const SideStream&) = delete;
@@ -87,6 +88,7 @@ struct FmmPlan {
       if (st) cudaStreamDestroy(st);
       if (charges) cudaEventDestroy(charges);
       if (near) cudaEventDestroy(near);
+      if (mpole) cudaEventDestroy(mpole);
     }
   } nearq;
 };
