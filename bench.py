@@ -541,9 +541,9 @@ def run_gpu(args):
              {"id": "id_kernel<double> (direct CPQR)", "schur": "decouple_kernel<double>"})[cls]
     # DRAM bytes (read + write) of the ID launches of one factorization of this
     # workload, from ncu (dram__bytes_read.sum + dram__bytes_write.sum over the
-    # 12 ID launches of a factorization; profiles/id_sketch_star65536.md has
-    # the command): 37.8 MB against 1.18 ms of serialised kernel time
-    traffic = 37.8e6 if refined_ok and cls == "id" else None
+    # 18 ID launches of a factorization; profiles/id_sketch_star65536.md has
+    # the command): 50.7 MB against 0.98 ms of serialised kernel time
+    traffic = 50.7e6 if refined_ok and cls == "id" else None
     cpu_v = cpu_sample(geo, F, cores, 10) if dist.rank == 0 else 0.0
     line = {
         "metric": METRIC, "value": value, "unit": "DOFs/s", "n_gpus": dist.ws,
