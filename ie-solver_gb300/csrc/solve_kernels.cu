@@ -543,45 +543,71 @@ __global__ void __launch_bounds__(kInvG * kInvG) root_inverse_kernel(float* base
   if (tid == 0 && s_bad) atomicExch(status, 1);
 }
 
-// x[idx, c] <- A^{-1} x[idx, c] per root block, with the explicit inverse.
-// The inverse (at most kRootInvMax^2 floats, 64 KB) is staged in shared
-// memory first with many loads in flight: read from global memory inside
-// the product, each thread's row sum was a chain of dependent L2 round
-// trips.  Then one thread per row forms that row for every column of the
-// block, in the same order of terms as before.
-__global__ void __launch_bounds__(kThreads) root_apply_kernel(const float* base,
-                                                              const RootTask* tasks,
-                                                              const int* dofs, float* x, int ld,
-                                                              int nrhs) {
+// x[idx, c] <- A^{-1} x[idx, c] per root block, with the explicit inverse:
+// one warp per row of the inverse (rows strided over the CTA's warps), a
+// CTA per root.  Each lane holds its share of its rows (four entries per
+// row, n <= 128) in registers, loaded before the wait for the up sweep, so
+// after it the only global round trips are the gather of x and the stores.
+// Every row's sum runs over l in the same order for every launch.
+constexpr int kRootApplyWarps = 32;
+constexpr int kRootRowsPerWarp = kRootInvMax / kRootApplyWarps;
+
+__global__ void __launch_bounds__(32 * kRootApplyWarps) root_apply_kernel(
+    const float* base, const RootTask* tasks, const int* dofs, float* x, int ld, int nrhs) {
+  pdl_launch_dependents();
   const RootTask t = tasks[blockIdx.x];
   const int n = t.n;
   const float* Ai = base + t.a_off;
   const int* idx = dofs + t.idx_off;
-  extern __shared__ __align__(16) float rsm[];
-  float* sA = rsm;                                  // n x n
-  float* sx = rsm + (((size_t)n * n + 3) & ~size_t(3));  // n x kRhsBlock
-  batched_copy(sA, Ai, n * n, threadIdx.x, blockDim.x);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ float sx[kRootInvMax * kRhsBlock];
+  __shared__ int sidx[kRootInvMax];
+  float a[kRootRowsPerWarp][4];
+#pragma unroll
+  for (int q = 0; q < kRootRowsPerWarp; ++q) {
+    const int i = warp + kRootApplyWarps * q;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int l = lane + 32 * h;
+      a[q][h] = i < n && l < n ? Ai[i + (size_t)n * l] : 0.f;
+    }
+  }
+  for (int e = threadIdx.x; e < n; e += blockDim.x) sidx[e] = idx[e];
+  __syncthreads();
+  pdl_wait();
   for (int c0 = 0; c0 < nrhs; c0 += kRhsBlock) {
     const int cb = nrhs - c0 < kRhsBlock ? nrhs - c0 : kRhsBlock;
     for (int e = threadIdx.x; e < n * cb; e += blockDim.x) {
       const int i = e % n, c = e / n;
-      sx[e] = x[idx[i] + (size_t)ld * (c0 + c)];
+      sx[i + n * c] = x[sidx[i] + (size_t)ld * (c0 + c)];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < kRootRowsPerWarp; ++q) {
+      const int i = warp + kRootApplyWarps * q;
+      if (i >= n) break;
       float acc[kRhsBlock];
 #pragma unroll
       for (int c = 0; c < kRhsBlock; ++c) acc[c] = 0.f;
-      for (int l = 0; l < n; ++l) {
-        const float a = sA[i + (size_t)n * l];
 #pragma unroll
-        for (int c = 0; c < kRhsBlock; ++c)
-          if (c < cb) acc[c] += a * sx[l + n * c];
+      for (int h = 0; h < 4; ++h) {
+        const int l = lane + 32 * h;
+        if (l < n)
+#pragma unroll
+          for (int c = 0; c < kRhsBlock; ++c)
+            if (c < cb) acc[c] += a[q][h] * sx[l + n * c];
       }
-      const int xi = idx[i];
 #pragma unroll
       for (int c = 0; c < kRhsBlock; ++c)
-        if (c < cb) x[xi + (size_t)ld * (c0 + c)] = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+      if (lane < cb) {
+        float v = acc[0];
+#pragma unroll
+        for (int c = 1; c < kRhsBlock; ++c)
+          if (lane == c) v = acc[c];
+        x[sidx[i] + (size_t)ld * (c0 + lane)] = v;
+      }
     }
     __syncthreads();
   }
@@ -596,10 +622,8 @@ void launch_root_inverse(float* base, const RootTask* tasks, int count, int* sta
 void launch_root_apply(const float* base, const RootTask* tasks, int count, const int* dofs,
                        float* x, int ld, int nrhs, cudaStream_t st) {
   if (count <= 0 || nrhs <= 0) return;
-  set_smem_once<root_apply_kernel>();
-  const size_t smem = sizeof(float) * ((((size_t)kRootInvMax * kRootInvMax + 3) & ~size_t(3)) +
-                                       (size_t)kRootInvMax * kRhsBlock);
-  root_apply_kernel<<<count, kThreads, smem, st>>>(base, tasks, dofs, x, ld, nrhs);
+  launch_pdl(root_apply_kernel, dim3(count), dim3(32 * kRootApplyWarps), 0, st, base, tasks, dofs,
+             x, ld, nrhs);
 }
 
 // ---------------------------------------------------------------------------
