@@ -171,6 +171,7 @@ struct FmmArgs {
   const double *rx, *ry;                  // FP64 variant
   const float *rxh, *rxl, *ryh, *ryl;     // float and float-float variants
   const R* binom;
+  int bs;  // row stride of binom: twice the order it was built for (at least a.p)
   const int *pstart, *pcount, *parent, *slot_pt, *children;
   const int *v_off, *v_idx, *w_off, *w_idx, *x_off, *x_idx, *u_off, *u_idx;
   const int* boxes;
@@ -379,7 +380,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2m_kernel(FmmArgs<R> a) {
   pdl_launch_dependents();
   const int P = a.boxes[blockIdx.x];
   if (a.pcount[P] > 0) return;  // leaf: filled by P2M
-  const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
+  const int p = a.p, nrhs = a.nrhs, P2 = a.bs;
   Cx<R>* dl = reinterpret_cast<Cx<R>*>(smem);  // 4 x p: d_c^l
   Cx<R>* gk = dl + 4 * p;                      // 4 x p: g_c^k
   Cx<R>* av = gk + 4 * p;                      // 4 x nrhs x p: M_k(c) g_c^k
@@ -447,7 +448,7 @@ template <class R>
 __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = a.boxes[blockIdx.x];
-  const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
+  const int p = a.p, nrhs = a.nrhs, P2 = a.bs;
   Cx<R>* av = reinterpret_cast<Cx<R>*>(smem);  // p x nrhs scaled source coefficients
   Cx<R>* vp = av + (size_t)p * nrhs;           // p: (-1)^l (s_B/d)^l / d
   Cx<R>* pw = vp + p;                          // kStage x p powers for P2L
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(kFmmThreads) m2l_kernel(FmmArgs<R> a) {
       if (e >= p * nrhs) break;
       const int l = e % p, q = e / p;
       Cx<R> s = {(R)0, (R)0};
-      const R* brow = a.binom + (size_t)l;  // C(k + l, l) = binom[(k + l) * P2 + l]
+      const R* brow = a.binom + (size_t)l;  // C(k + l, l) = binom[(k + l) * bs + l]
       for (int k = 0; k < p; ++k) {
         const R bk = brow[(size_t)(k + l) * P2];
         s.re += bk * av[k + p * q].re;
@@ -572,7 +573,7 @@ __global__ void __launch_bounds__(kFmmThreads) l2l_kernel(FmmArgs<R> a) {
   const int C = a.boxes[blockIdx.x];
   const int P = a.parent[C];
   if (P < 0) return;
-  const int p = a.p, nrhs = a.nrhs, P2 = 2 * p;
+  const int p = a.p, nrhs = a.nrhs, P2 = a.bs;
   Cx<R>* el = reinterpret_cast<Cx<R>*>(smem);  // p: e^l
   Cx<R>* hm = el + p;                          // p: (2e)^-m
   Cx<R>* bv = hm + p;                          // nrhs x p: L_l(P) e^l
@@ -1008,7 +1009,8 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
   constexpr bool f32 = std::is_same<R, float>::value;
   const int p = f32 ? f.p32 : f.p;
   const int npts = f.npts, nb = f.nbox;
-  if (p < 2 || p * kMaxRhs > 4 * kFmmThreads) return cudaErrorInvalidValue;
+  if (p < 2 || p * kMaxRhs > 4 * kFmmThreads || (f32 && p > f.p32_tab))
+    return cudaErrorInvalidValue;
   set_smem_once<p2m_kernel<R>>();
   set_smem_once<m2m_kernel<R>>();
   set_smem_once<m2l_kernel<R>>();
@@ -1047,6 +1049,7 @@ cudaError_t apply_t(FmmPlan& f, int mode, const Geo<double>& geo, const double* 
   a.rxl = f.rxl.p;
   a.ryh = f.ryh.p;
   a.ryl = f.ryl.p;
+  a.bs = f32 ? 2 * f.p32_tab : 2 * f.p;
   if constexpr (f32) a.binom = f.binom32.p;
   else if constexpr (std::is_same<R, DF>::value) a.binom = reinterpret_cast<const DF*>(f.binom_df.p);
   else a.binom = f.binom.p;

@@ -39,7 +39,8 @@ enum FmmArith : int { kFmmF64 = 0, kFmmF32 = 1, kFmmDF = 2 };
 
 struct FmmPlan {
   int p = 0;          // expansion order, FP64 and float-float variants
-  int p32 = 0;        // expansion order, FP32 variant
+  int p32 = 0;        // expansion order, FP32 variant (fmm_set_order32)
+  int p32_tab = 0;    // order binom32 was built for: the largest p32
   int nbox = 0;
   int npts = 0;
   int nlevels = 0;
@@ -125,6 +126,10 @@ cudaError_t fmm_apply(FmmPlan& f, int pde, const Geo<double>& geo, const double*
 // Sets the order of the FP64 and float-float variants (2..64; the plan's
 // lists do not depend on it).  Synchronous: call between products.
 bool fmm_set_order(FmmPlan& f, int p, cudaStream_t st);
+// Sets the order of the FP32 variant, 2 .. the order the plan was built
+// with (its binomial table serves every lower order).  Takes effect with the
+// next fmm_apply; nothing is synchronised.
+bool fmm_set_order32(FmmPlan& f, int p);
 // Kernels one fmm_apply launches.
 int fmm_launches(const FmmPlan& f, int pde, int nrhs);
 

@@ -83,6 +83,12 @@ void pascal(int P2, std::vector<double>* t) {
 
 }  // namespace
 
+bool fmm_set_order32(FmmPlan& f, int p) {
+  if (p < 2 || p > f.p32_tab) return false;
+  f.p32 = p;
+  return true;
+}
+
 bool fmm_set_order(FmmPlan& f, int p, cudaStream_t st) {
   if (p < 2 || p > 64) return false;
   std::vector<double> binom;
@@ -269,6 +275,7 @@ bool fmm_plan_upload(FmmPlan& f, FmmHostPlan& h, cudaStream_t st) {
   f.built = false;
   if (!h.ok) return false;
   f.p32 = h.p32;
+  f.p32_tab = h.p32;
   f.nbox = h.nbox;
   f.npts = h.npts;
   f.nlevels = h.nlevels;

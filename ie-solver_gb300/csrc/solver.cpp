@@ -1605,7 +1605,8 @@ namespace {
 // configuration, or matched to the refinement tolerance: on the 65536-point
 // star the product's relative error is about 10^(-0.36 p - 2.1) (order 20:
 // 1.2e-9, 28: 1.8e-12, 32: 6.5e-14), and the residual needs it ten times
-// below refine_tol.  FP32 order 16 for the correction products.
+// below refine_tol.  FP32 products of corrections at order 16 at most (the
+// plan's FP32 table), lower for the later, smaller corrections.
 // The Stokes product also evaluates derivatives of the expansions (about
 // 30x the Laplace error at the same order on the 16-hole, 131072-point
 // geometry), so it takes four more terms.
@@ -1624,6 +1625,15 @@ int auto_fmm_order(double refine_tol, int pde) {
 // correction only while this bound stays below half the tolerance, and
 // sums the bounds.
 double fmm32_error(int pde) { return pde == kStokes ? 8e-7 : 6e-8; }
+// Below order kFmmOrder32 the FP32 product's error grows with the
+// truncation of the expansions: by about 10^0.36 per order dropped (the
+// slope of the multipole error over the orders, measured on the 65536-point
+// star; the same geometric rate bounds well-separated interactions).
+double fmm32_order_factor(int p) { return std::pow(10.0, 0.36 * (kFmmOrder32 - p)); }
+constexpr int kFmmOrder32Min = 4;
+int fmm32_fixed(const rs_solver* s) {
+  return s->cfg.fmm_order32 > 0 ? s->cfg.fmm_order32 : kFmmOrder32;
+}
 // Relative residual the inner GMRES of GMRES-IR aims for (its FP32
 // products and preconditioner are good to about 1e-7).
 constexpr double kGmresInnerTol = 1e-6;
@@ -1669,8 +1679,9 @@ rs_status residual(rs_solver* s, const double* f, const double* mu, const double
 // variant (the full residual uses the float-float variant) (the correction is ~1e-6 of the solution, so FP32 accuracy of the
 // product leaves the residual exact to ~1e-13 of the data).
 rs_status residual_update(rs_solver* s, const double* x, const double* xa, int nrhs, double* r,
-                          double* rg, double* g) {
+                          double* rg, double* g, int p32) {
   const int D = s->D;
+  if (!fmm_set_order32(s->fmm, p32)) return fail(s, RS_ERR_ARG, "bad FP32 multipole order");
   CU(fmm_apply(s->fmm, s->cfg.pde, geo_of(s), x, nrhs, r, 1.0, -1.0, kFmmF32, s->stream));
   s->launches += fmm_launches(s->fmm, s->cfg.pde, nrhs);
   if (s->nb > 0) {
@@ -1696,7 +1707,8 @@ rs_status apply_neg_op(rs_solver* s, const double* z, int nrhs, double* y) {
   const int D = s->D, nb = s->nb;
   const size_t nd = (size_t)D * nrhs;
   CU(cudaMemsetAsync(y, 0, (nd + (size_t)nb * nrhs) * 8, s->stream));
-  return residual_update(s, z, nb ? z + nd : nullptr, nrhs, y, nb ? y + nd : nullptr, s->g64.p);
+  return residual_update(s, z, nb ? z + nd : nullptr, nrhs, y, nb ? y + nd : nullptr, s->g64.p,
+                         fmm32_fixed(s));
 }
 
 // z = M^{-1} v with the FP32 factorization (block vectors; the alpha block
@@ -1924,6 +1936,7 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
   for (it = 0; it < max_it; ++it) {
     const double before = prev;
     bool upd = false;
+    int p32 = fmm32_fixed(s);  // order of this step's FP32 product
     if (krylov) {
       CU(s->kb.ensure(kbl));
       CU(s->x64.ensure(kbl));
@@ -1946,7 +1959,15 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
       // residual recurrence with the FP32 product of the correction (x ~
       // prev relative to the data) only while its error, eps32 * prev, is
       // below half the tolerance; otherwise a fresh float-float residual
-      upd = recur && it > 0 && eps32 * prev <= 0.5 * s->cfg.refine_tol;
+      upd = recur && it > 0 &&
+            eps32 * fmm32_order_factor(fmm32_fixed(s)) * prev <= 0.5 * s->cfg.refine_tol;
+      // the correction's product at the lowest order whose error bound stays
+      // within refine_tol / 8 (or within what order 16 gives)
+      if (upd && s->cfg.fmm_order32 == 0) {
+        const double budget = std::max(eps32 * prev, 0.125 * s->cfg.refine_tol);
+        while (p32 > kFmmOrder32Min && eps32 * fmm32_order_factor(p32 - 1) * prev <= budget)
+          --p32;
+      }
       if (upd) {
         launch_f2d(F.x.p, s->x64.p, nd, s->stream);
         launch_axpby(mu, s->x64.p, 1.0, 1.0, nd, s->stream);
@@ -1955,8 +1976,8 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
           launch_axpby(a64, s->xa64.p, 1.0, 1.0, (size_t)nb * nrhs, s->stream);
         }
         s->launches += 4;
-        rec_err += eps32 * prev;
-        RSCHK(residual_update(s, s->x64.p, s->xa64.p, nrhs, s->r64.p, rg, s->g64.p));
+        rec_err += eps32 * fmm32_order_factor(p32) * prev;
+        RSCHK(residual_update(s, s->x64.p, s->xa64.p, nrhs, s->r64.p, rg, s->g64.p, p32));
         RSCHK(measure(&s->stats.residual32_ms));
       } else {
         launch_add_f2d(mu, F.x.p, nd, s->stream);
@@ -1968,8 +1989,8 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
     }
     prev = worst;
     if (s->trace)
-      std::fprintf(stderr, "[rskel] refine %d: %s, %s residual %.3e\n", it,
-                   krylov ? "GMRES" : "stationary", upd ? "recurrence" : "fresh", worst);
+      std::fprintf(stderr, "[rskel] refine %d: %s, %s residual %.3e (FP32 order %d)\n", it,
+                   krylov ? "GMRES" : "stationary", upd ? "recurrence" : "fresh", worst, p32);
     if (it == 0 && recur) {
       // The multipole errors scale with |mu| while the tolerance is relative
       // to |f|: on an ill-conditioned system (|mu| >> |f|) the float-float
@@ -2054,6 +2075,7 @@ void rs_config_default(rs_config* c) {
   c->rank_judge = 4.0;
   c->tensor_cores = 1;
   c->id_row_groups = -1;
+  c->fmm_order32 = 0;
 }
 
 rs_status rs_create(const rs_config* cfg, rs_solver** out) {
@@ -2070,7 +2092,8 @@ rs_status rs_create(const rs_config* cfg, rs_solver** out) {
   if (!(cfg->rank_headroom >= 1.0 && cfg->rank_headroom <= 4.0) || cfg->rank_extra_rows < 0 ||
       cfg->rank_extra_rows > 128 || cfg->refine_solver < 0 || cfg->refine_solver > 2 ||
       !(cfg->rank_judge >= 0.0 && cfg->rank_judge <= 1e6) || cfg->tensor_cores < 0 ||
-      cfg->tensor_cores > 1 || cfg->id_row_groups < -1 || cfg->id_row_groups > 16)
+      cfg->tensor_cores > 1 || cfg->id_row_groups < -1 || cfg->id_row_groups > 16 ||
+      cfg->fmm_order32 < 0 || cfg->fmm_order32 == 1 || cfg->fmm_order32 > 16)
     return RS_ERR_ARG;
   rs_solver* s = new rs_solver();
   s->cfg = *cfg;
@@ -2529,6 +2552,7 @@ rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int
   CU(dx.ensure(nd));
   CU(dy.ensure(nd));
   CU(cudaMemcpyAsync(dx.p, x, nd * 8, cudaMemcpyHostToDevice, s->stream));
+  if (!fmm_set_order32(s->fmm, fmm32_fixed(s))) return fail(s, RS_ERR_ARG, "bad FP32 multipole order");
   CU(fmm_apply(s->fmm, s->cfg.pde, geo_of(s), dx.p, nrhs, dy.p, 0.0, 1.0, arith, s->stream));
   CU(cudaMemcpyAsync(y, dy.p, nd * 8, cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));

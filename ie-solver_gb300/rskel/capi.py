@@ -47,7 +47,7 @@ class RsConfig(ctypes.Structure):
                 ("refine_solver", ctypes.c_int), ("use_graphs", ctypes.c_int),
                 ("root_inverse", ctypes.c_int), ("rank_judge", ctypes.c_double),
                 ("tensor_cores", ctypes.c_int),
-                ("id_row_groups", ctypes.c_int)]
+                ("id_row_groups", ctypes.c_int), ("fmm_order32", ctypes.c_int)]
 
 
 class RsStats(ctypes.Structure):
@@ -215,7 +215,7 @@ class Solver:
                  refine_max_iters=10, fp32_id_tol=1e-6, device=0, min_dofs=16, fmm_order=0,
                  rank_headroom=1.25, rank_extra_rows=12, refine_verify=1, refine_solver=0,
                  use_graphs=1, root_inverse=1, rank_judge=4.0, tensor_cores=1,
-                 id_row_groups=-1):
+                 id_row_groups=-1, fmm_order32=0):
         self.sd = 2 if pde == RS_STOKES else 1
         self.cfg = default_config(pde=pde, solution_dimension=self.sd, id_tol=tol,
                                   max_leaf_dofs=leaf, num_proxy_points=npp,
@@ -226,7 +226,8 @@ class Solver:
                                   rank_extra_rows=rank_extra_rows, refine_verify=refine_verify,
                                   refine_solver=refine_solver, use_graphs=use_graphs,
                                   root_inverse=root_inverse, rank_judge=rank_judge,
-                                  tensor_cores=tensor_cores, id_row_groups=id_row_groups)
+                                  tensor_cores=tensor_cores, id_row_groups=id_row_groups,
+                                  fmm_order32=fmm_order32)
         h = _vp()
         self._check(lib().rs_create(ctypes.byref(self.cfg), ctypes.byref(h)), None)
         self.h = h

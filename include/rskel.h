@@ -103,6 +103,14 @@ typedef struct {
                                 QR sums in a fixed order.  -1 (default) = about two CTAs per
                                 SM over the level, at most one per chunk and 16 per box;
                                 0 or 1 = one CTA per box; 2..16 = that many */
+  int fmm_order32;           /* RS_FP32_REFINE: multipole order of the FP32 products of
+                                refinement corrections.  0 (default) = chosen per correction
+                                from the accuracy it needs: the product's error, about
+                                10^(-0.36 p) relative to the correction, times the residual the
+                                correction came from, is kept below refine_tol / 8 (and never
+                                asked below what order 16 gives), so the later, smaller
+                                corrections take orders down to 4; GMRES-IR's products stay at
+                                16.  2..16 = that order for every FP32 product */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
@@ -186,7 +194,7 @@ rs_status rs_matvec(rs_solver* s, const double* x, int nrhs, double* y);
  * (pairs of floats, ~48-bit significands, on the FP32 pipes), the variant of
  * the refinement's full residual; both at order rs_config.fmm_order.
  * arith = 1: the FP32 variant used for products with refinement corrections
- * (~1e-7 relative).  No reference counterpart: the reference applies K only
+ * (~1e-7 relative at order 16; at rs_config.fmm_order32 when that is set).  No reference counterpart: the reference applies K only
  * densely in its tests (ie_solver_test.cpp:87-95). */
 rs_status rs_matvec_fast(rs_solver* s, const double* x, int nrhs, double* y, int arith);
 

@@ -6,7 +6,10 @@ Tolerances: FP64 and float-float variants, max |y_fmm - y_dense| <= 1e-10
 max |y_dense| per column at the default order (31; measured ~1e-13 on the
 65536-point star); lower orders must be no more accurate than higher ones.
 FP32 variant (used only for products with refinement corrections): <= 2e-6
-of max |y_dense|.
+of max |y_dense|.  Below order 16 (the refinement's later corrections) the
+FP32 product must stay within the error bound the refinement assumes for
+it: eps16 * 10^(0.36 (16 - p)), eps16 = 6e-8 (Laplace, Neumann) or 8e-7
+(Stokes), on rough vectors such as refinement corrections.
 """
 import numpy as np
 import pytest
@@ -105,3 +108,24 @@ def test_neumann_fmm_matches_dense(solver_lib):
         assert _rel(s.matvec(x, fast=True), z) <= 1e-10
         assert _rel(s.matvec(x, fast=True, arith=2), z) <= 1e-10
         assert _rel(s.matvec(x, fast=True, fp32=True), z) <= 2e-6
+
+
+@pytest.mark.parametrize("pde", [0, 1, 2])
+def test_fmm_fp32_lower_orders_within_the_refinement_bound(pde, solver_lib):
+    from rskel import geometry as G
+    capi = solver_lib
+    geo = (G.circle_with_ellipses(16384, 4, np.random.default_rng(2)) if pde == capi.RS_STOKES
+           else G.star(16384))
+    eps16 = 8e-7 if pde == capi.RS_STOKES else 6e-8
+    errs = []
+    z = None
+    for p in (4, 6, 8, 10, 12, 14, 16):
+        s = capi.Solver(geo, pde, 1e-8, fmm_order32=p)
+        x = np.random.default_rng(11).standard_normal((s.D, 3))
+        if z is None:
+            z = s.matvec(x)
+        e = _rel(s.matvec(x, fast=True, fp32=True), z)
+        assert e <= eps16 * 10.0 ** (0.36 * (16 - p)), (p, e)
+        errs.append(e)
+        s.close()
+    assert errs[0] > errs[3] > errs[6], errs
