@@ -25,6 +25,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/rskel.h"
@@ -60,6 +61,47 @@ struct Factor {
   DevBuf<Real> Sinv, Mt;  // bordered system: S^{-1} and the product's output
   size_t fac_used = 0, e_used = 0;
 };
+
+// An allocator whose value-less construct leaves elements uninitialised:
+// the DOF pool of a large batch grows by tens of MB per level, and every
+// element it gains is written by the list copies right after, so the zero
+// fill of a plain resize was pure cost (about 5 ms per level on the
+// 512-boundary batch).
+template <class T>
+struct DefaultInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = DefaultInitAlloc<U>;
+  };
+  DefaultInitAlloc() = default;
+  template <class U>
+  DefaultInitAlloc(const DefaultInitAlloc<U>&) {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+};
+
+// memcpy split over the OpenMP team when large (the uploads of a large
+// batch's level are tens of MB); a plain memcpy below 4 MB.
+void copy_in(void* dst, const void* src, size_t bytes) {
+  constexpr size_t kPar = size_t(4) << 20, kChunkBytes = size_t(1) << 20;
+  if (bytes < kPar) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  const long nch = (long)((bytes + kChunkBytes - 1) / kChunkBytes);
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nch; ++c) {
+    const size_t o = (size_t)c * kChunkBytes;
+    std::memcpy(static_cast<char*>(dst) + o, static_cast<const char*>(src) + o,
+                std::min(kChunkBytes, bytes - o));
+  }
+}
 
 double now_ms() {
   return std::chrono::duration<double, std::milli>(
@@ -100,7 +142,7 @@ struct rs_solver {
   DevBuf<double> gx, gy, gnx, gny, gw, gk, pxy_c, pxy_s;
   bool geo_on_dev = false;
 
-  std::vector<int> pool;  // host mirror of the device DOF pool
+  std::vector<int, DefaultInitAlloc<int>> pool;  // host mirror of the device DOF pool
   DevBuf<int> dofs, perm, ranks, piv, status;
   DevBuf<IdTask> id_tasks;
   DevBuf<DecoupleTask> dc_tasks;
@@ -464,7 +506,7 @@ cudaError_t stage_copy(rs_solver* s, void* dst, const void* src, size_t bytes) {
     if (e != cudaSuccess) return e;
     off = 0;
   }
-  std::memcpy(s->stage.p + off, src, bytes);
+  copy_in(s->stage.p + off, src, bytes);
   s->stage_used = off + bytes;
   return cudaMemcpyAsync(dst, s->stage.p + off, bytes, cudaMemcpyHostToDevice, s->stream);
 }
@@ -483,8 +525,8 @@ cudaError_t stage_copy2(rs_solver* s, void* dst, const void* src1, size_t bytes1
     if (e != cudaSuccess) return e;
     off = 0;
   }
-  if (bytes1) std::memcpy(s->stage.p + off, src1, bytes1);
-  if (bytes2) std::memcpy(s->stage.p + off + off2, src2, bytes2);
+  if (bytes1) copy_in(s->stage.p + off, src1, bytes1);
+  if (bytes2) copy_in(s->stage.p + off + off2, src2, bytes2);
   s->stage_used = off + bytes;
   return cudaMemcpyAsync(dst, s->stage.p + off, bytes, cudaMemcpyHostToDevice, s->stream);
 }
