@@ -704,9 +704,14 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
     }
     }  // L2P
     if constexpr (kPart == kEvalAll || kPart == kEvalW || kPart == kEvalFarW) {
-    // M2P from the W list (the same split).  Box offsets and sides need FP64
+    // M2P from the W list (the same split by right-hand side; with fewer
+    // right-hand sides than warps, the warps of one right-hand side take
+    // every G-th box of the list).  Box offsets and sides need FP64
     // arithmetic (slow on this GPU), so lane l forms them for the list's l-th
     // box and the warp broadcasts them in turn.
+    const int nr = nrhs < kEvalWarps ? nrhs : kEvalWarps;
+    const int G = kEvalWarps / nr, grp = wp / nr, rq = wp % nr;
+    if (grp < G)
     for (int wb = a.w_off[B]; wb < a.w_off[B + 1]; wb += 32) {
       const int nwb = min(32, a.w_off[B + 1] - wb);
       int Cl = 0;
@@ -718,13 +723,14 @@ __global__ void __launch_bounds__(32 * kEvalWarps) eval_warp_kernel(
         sl = side_of(a, Cl);
       }
       for (int t = 0; t < nwb; ++t) {
+        if ((wb + t) % G != grp) continue;  // (warp-uniform)
         const int C = __shfl_sync(0xffffffffu, Cl, t);
         const Cx<R> oc = {shfl(ol.re, t), shfl(ol.im, t)};
         const R sc = shfl(sl, t);
         const Cx<R> iw = cinv(cadd(vec(tp), oc));  // z - c_C
         const Cx<R> tw = cscale(iw, sc);
 #pragma unroll 1
-        for (int qq = wp; qq < nrhs; qq += 2 * kEvalWarps) {
+        for (int qq = rq; qq < nrhs; qq += 2 * kEvalWarps) {
           const int q2 = qq + kEvalWarps;
           const bool two = q2 < nrhs;
           const R* M = a.mpole + 2 * (size_t)p * (qq + nrhs * (size_t)C);
