@@ -2004,9 +2004,13 @@ rs_status solve_device_impl(rs_solver* s, const double* f, int nrhs, double* mu,
       upd = recur && it > 0 &&
             eps32 * fmm32_order_factor(fmm32_fixed(s)) * prev <= 0.5 * s->cfg.refine_tol;
       // the correction's product at the lowest order whose error bound stays
-      // within refine_tol / 8 (or within what order 16 gives)
+      // within a quarter of the recurrence's remaining slack (half the
+      // tolerance less the bounds already summed), or within what order 16
+      // gives: once the slack is spent, every product is at order 16, so
+      // the lower orders never make the bound call for a confirming residual
       if (upd && s->cfg.fmm_order32 == 0) {
-        const double budget = std::max(eps32 * prev, 0.125 * s->cfg.refine_tol);
+        const double slack = 0.5 * s->cfg.refine_tol - rec_err;
+        const double budget = std::max(eps32 * prev, 0.25 * slack);
         while (p32 > kFmmOrder32Min && eps32 * fmm32_order_factor(p32 - 1) * prev <= budget)
           --p32;
       }

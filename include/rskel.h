@@ -107,10 +107,11 @@ typedef struct {
                                 refinement corrections.  0 (default) = chosen per correction
                                 from the accuracy it needs: the product's error, about
                                 10^(-0.36 p) relative to the correction, times the residual the
-                                correction came from, is kept below refine_tol / 8 (and never
-                                asked below what order 16 gives), so the later, smaller
-                                corrections take orders down to 4; GMRES-IR's products stay at
-                                16.  2..16 = that order for every FP32 product */
+                                correction came from, is kept below a quarter of what the
+                                residual recurrence's error bound has left of refine_tol / 2
+                                (and never asked below what order 16 gives), so the later,
+                                smaller corrections take orders down to 4; GMRES-IR's products
+                                stay at 16.  2..16 = that order for every FP32 product */
 } rs_config;
 
 typedef struct rs_solver rs_solver;
