@@ -35,6 +35,7 @@ def test_config_defaults_are_the_reference_defaults(solver_lib):
     # fields beyond the reference's configuration
     assert c.precision == solver_lib.RS_FP64 and c.refine_verify == 1 and c.refine_solver == 0
     assert c.use_graphs == 1 and c.root_inverse == 1
+    assert c.fmm_order32 == 0 and c.tensor_cores == 1 and c.id_row_groups == -1
 
 
 def test_geometry_checks_leave_the_handle_unchanged(solver_lib):
@@ -66,6 +67,13 @@ def test_argument_validation(solver_lib):
     assert lib.rs_create(ctypes.byref(bad), ctypes.byref(h)) == 1
     bad = solver_lib.default_config(is_strong_admissibility=1)
     assert lib.rs_create(ctypes.byref(bad), ctypes.byref(h)) == 1
+    # the FP32 correction products' multipole order: 0 (chosen per correction) or 2..16
+    for o32, ok in ((0, True), (1, False), (2, True), (16, True), (17, False), (-1, False)):
+        cfg = solver_lib.default_config(fmm_order32=o32)
+        rc = lib.rs_create(ctypes.byref(cfg), ctypes.byref(h))
+        assert (rc == 0) == ok, (o32, rc)
+        if rc == 0:
+            lib.rs_destroy(h)
     geo = g.unit_circle(64)
     s = solver_lib.Solver(geo, solver_lib.RS_LAPLACE, 1e-6)
     with pytest.raises(solver_lib.RsError) as e:
