@@ -2759,20 +2759,47 @@ rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ct
                       int* elim_threads) {
   if (!s || reps < 1) return RS_ERR_ARG;
   // each candidate: the median device time of `reps` factorizations of the
-  // handle's geometry; one knob at a time, the other at its current value
+  // handle's geometry; one knob at a time, the other at its current value.
+  // An FP32 factorization is timed with one refined solve of fixed smooth
+  // data (1 + x/2 - y/4 at every point and component): the launch shapes
+  // change the factorization's rounding, and with it the number of
+  // refinement steps a solve takes, which can cost more than a faster
+  // factorization saves.
+  rs_status rc = rs_factor(s);  // warm-up (plans, buffers, first launches)
+  if (rc != RS_OK) return rc;
+  const bool with_solve = s->fp32;
+  DevBuf<double> df, dmu, dal;
+  if (with_solve) {
+    std::vector<double> f(s->D);
+    for (int i = 0; i < s->D; ++i) {
+      const int pt = i / s->sd;
+      f[i] = 1.0 + 0.5 * s->pts[2 * pt] - 0.25 * s->pts[2 * pt + 1];
+    }
+    CU(df.ensure(s->D));
+    CU(dmu.ensure(s->D));
+    CU(dal.ensure(std::max(s->nb, 1)));
+    CU(cudaMemcpy(df.p, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   auto time_factor = [&](double* ms) -> rs_status {
     std::vector<double> t;
     for (int r = 0; r < reps; ++r) {
-      rs_status rc = rs_factor(s);
-      if (rc != RS_OK) return rc;
-      t.push_back(s->stats.dev_factor_ms);
+      rs_status rc2 = rs_factor(s);
+      if (rc2 != RS_OK) return rc2;
+      double m = s->stats.dev_factor_ms;
+      if (with_solve) {
+        rc2 = rs_solve_device(s, df.p, 1, dmu.p, dal.p);
+        if (rc2 != RS_OK) return rc2;
+        CU(cudaStreamSynchronize(s->stream));
+        float sm = 0;
+        CU(cudaEventElapsedTime(&sm, s->ev_f0, s->ev_f1));
+        m += sm;
+      }
+      t.push_back(m);
     }
     std::sort(t.begin(), t.end());
     *ms = t[t.size() / 2];
     return RS_OK;
   };
-  rs_status rc = rs_factor(s);  // warm-up (plans, buffers, first launches)
-  if (rc != RS_OK) return rc;
   double best = 1e300;
   int best_split = s->split_min_tasks;
   for (int cand : {1, 32, 128, 256, 512, 1024, 1 << 30}) {

@@ -304,8 +304,11 @@ rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* feat
                            const float* targets, int count, float* grad, float* loss);
 
 /* Autotuner (no reference counterpart): times factorizations of the
- * handle's current geometry over the launch shapes that depend on the
- * problem and keeps the fastest for this handle's later factorizations:
+ * handle's current geometry (RS_FP32_REFINE: each with one refined solve of
+ * fixed smooth data, since the launch shapes change the factorization's
+ * rounding and so the solve's refinement steps) over the launch shapes that
+ * depend on the problem and keeps the fastest for this handle's later
+ * factorizations:
  * the level size from which the FP32 sketched ID's pivoted QR runs one
  * warp per box instead of one CTA per box (128, 256, 512 (default), 1024,
  * never), then the wide ID's CTAs per SM (1, 2 (default), 4), then the
