@@ -115,3 +115,31 @@ def test_no_cpu_fallback_without_gpu(solver_lib):
     with pytest.raises(solver_lib.RsError) as e:
         s.factor()
     assert e.value.code == 4  # RS_ERR_NO_DEVICE
+
+
+def test_ctypes_structs_match_the_header(solver_lib, tmp_path):
+    """The Python binding's rs_config and rs_stats mirrors have the header's
+    layout: every field at the C compiler's offset, and the same size."""
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "rskel.h"', "int main(void) {"]
+    for st, cname in ((solver_lib.RsConfig, "rs_config"), (solver_lib.RsStats, "rs_stats")):
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in st._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = str(tmp_path / "layout")
+    res = subprocess.run(["gcc", "-I", inc, str(src), "-o", exe], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for st, cname in ((solver_lib.RsConfig, "rs_config"), (solver_lib.RsStats, "rs_stats")):
+        assert got[(cname, "size")] == ctypes.sizeof(st), cname
+        for f, _ in st._fields_:
+            assert got[(cname, f)] == getattr(st, f).offset, (cname, f)
