@@ -2760,24 +2760,42 @@ rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ct
   if (!s || reps < 1) return RS_ERR_ARG;
   // each candidate: the median device time of `reps` factorizations of the
   // handle's geometry; one knob at a time, the other at its current value.
-  // An FP32 factorization is timed with one refined solve of fixed smooth
-  // data (1 + x/2 - y/4 at every point and component): the launch shapes
-  // change the factorization's rounding, and with it the number of
-  // refinement steps a solve takes, which can cost more than a faster
-  // factorization saves.
+  // An FP32 factorization is timed with one refined solve after it: the
+  // launch shapes change the factorization's rounding, and with it the
+  // number of refinement steps a solve takes, which can cost more than a
+  // faster factorization saves.  The data are kTuneRhs columns of the
+  // potential of a point source, log |x - c_q|, at points c_q on the circle
+  // of 1.25 times the half-diagonal of the geometry's bounding box around
+  // its centre, outside the geometry (the same in every component for
+  // Stokes): close enough to the boundary to show the factorization's
+  // accuracy, as a solve's own data do.
   rs_status rc = rs_factor(s);  // warm-up (plans, buffers, first launches)
   if (rc != RS_OK) return rc;
   const bool with_solve = s->fp32;
+  constexpr int kTuneRhs = 8;
   DevBuf<double> df, dmu, dal;
   if (with_solve) {
-    std::vector<double> f(s->D);
-    for (int i = 0; i < s->D; ++i) {
-      const int pt = i / s->sd;
-      f[i] = 1.0 + 0.5 * s->pts[2 * pt] - 0.25 * s->pts[2 * pt + 1];
+    double x0 = s->pts[0], x1 = x0, y0 = s->pts[1], y1 = y0;
+    for (int p = 0; p < s->n; ++p) {
+      x0 = std::min(x0, s->pts[2 * p]);
+      x1 = std::max(x1, s->pts[2 * p]);
+      y0 = std::min(y0, s->pts[2 * p + 1]);
+      y1 = std::max(y1, s->pts[2 * p + 1]);
     }
-    CU(df.ensure(s->D));
-    CU(dmu.ensure(s->D));
-    CU(dal.ensure(std::max(s->nb, 1)));
+    const double cx = 0.5 * (x0 + x1), cy = 0.5 * (y0 + y1);
+    const double rad = 1.25 * std::max(0.5 * std::hypot(x1 - x0, y1 - y0), 1e-300);
+    std::vector<double> f((size_t)s->D * kTuneRhs);
+    for (int q = 0; q < kTuneRhs; ++q) {
+      const double a = 0.3 + 2.0 * 3.14159265358979323846 * q / kTuneRhs;
+      const double sx = cx + rad * std::cos(a), sy = cy + rad * std::sin(a);
+      for (int i = 0; i < s->D; ++i) {
+        const int pt = i / s->sd;
+        f[i + (size_t)s->D * q] = std::log(std::hypot(s->pts[2 * pt] - sx, s->pts[2 * pt + 1] - sy));
+      }
+    }
+    CU(df.ensure(f.size()));
+    CU(dmu.ensure(f.size()));
+    CU(dal.ensure(std::max<size_t>((size_t)s->nb * kTuneRhs, 1)));
     CU(cudaMemcpy(df.p, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   auto time_factor = [&](double* ms) -> rs_status {
@@ -2787,7 +2805,7 @@ rs_status rs_autotune(rs_solver* s, int reps, int* split_min_tasks, int* wide_ct
       if (rc2 != RS_OK) return rc2;
       double m = s->stats.dev_factor_ms;
       if (with_solve) {
-        rc2 = rs_solve_device(s, df.p, 1, dmu.p, dal.p);
+        rc2 = rs_solve_device(s, df.p, kTuneRhs, dmu.p, dal.p);
         if (rc2 != RS_OK) return rc2;
         CU(cudaStreamSynchronize(s->stream));
         float sm = 0;

@@ -305,8 +305,9 @@ rs_status rs_rank_gradient(rs_solver* s, const float* weights, const float* feat
 
 /* Autotuner (no reference counterpart): times factorizations of the
  * handle's current geometry (RS_FP32_REFINE: each with one refined solve of
- * fixed smooth data, since the launch shapes change the factorization's
- * rounding and so the solve's refinement steps) over the launch shapes that
+ * eight columns of point-source potentials from outside the geometry, since
+ * the launch shapes change the factorization's rounding and so the solve's
+ * refinement steps) over the launch shapes that
  * depend on the problem and keeps the fastest for this handle's later
  * factorizations:
  * the level size from which the FP32 sketched ID's pivoted QR runs one
